@@ -1,0 +1,190 @@
+/*
+ * montjoie_gb300 - C ABI of the GB300 matrix-free acoustic operator and
+ * leap-frog time loop.
+ *
+ * Drop-in boundary for one hot path of Montjoie (marcdurufle33/Montjoie): the
+ * matrix-free stiffness product of the scalar acoustic (Laplace) equation on
+ * mass-lumped Gauss-Lobatto Q_r hexahedra, and the order-2 leap-frog
+ * (ModifiedEquationIterator) that drives it.  Plain pointers and sizes only;
+ * every call returns MJ_OK (0) or an error code and never aborts; the text of
+ * the last error of the calling thread is returned by mj_last_error().
+ *
+ * Array conventions (the reference's):
+ *  - Nodle: n_elt x (r+1)^3 int32 global dof numbers, row e in the reference
+ *    local order NumDofs3D (vertices, edges, faces, interior;
+ *    MONTJOIE/src/Quadrature/HexahedronQuadrature.cxx:51-171);
+ *  - stiffness factors: n_elt x (r+1)^3 x 6 doubles, the symmetric 3x3
+ *    B = (J w) DF^-1 mu DF^-T of every quadrature point (= dof) in local order,
+ *    entries xx, xy, xz, yy, yz, zz (Glob_matMass_Bh,
+ *    MONTJOIE/src/Elliptic/Helmholtz/VarHelmholtz.cxx:95-123);
+ *  - 1-D rule: Gauss-Lobatto points on [0,1] and G[a*(r+1)+b] = phi_a'(x_b)
+ *    (Globatto::ComputeGradPhi, MONTJOIE/src/Quadrature/GaussLobatto.cxx:175-191).
+ * All vectors are contiguous arrays of n_dof doubles (Seldon Vector<double>
+ * storage, GetData()).
+ */
+#ifndef MONTJOIE_GB300_H
+#define MONTJOIE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------- */
+#define MJ_OK 0
+#define MJ_ERR_ARG 1         /* invalid argument (size, range, null pointer) */
+#define MJ_ERR_CUDA 2        /* a CUDA call failed (text in mj_last_error) */
+#define MJ_ERR_STATE 3       /* call out of order (e.g. advance before init) */
+#define MJ_ERR_NONFINITE 4   /* non-finite value met (divergence guard) */
+#define MJ_ERR_GEOMETRY 5    /* non-positive Jacobian (degenerate element) */
+#define MJ_ERR_NOMEM 6       /* device allocation failed */
+
+/* ---- precision of an operator ---------------------------------------- */
+#define MJ_FP64 0   /* plain form: FP64 everywhere */
+#define MJ_FP32 1   /* chosen form: FP32 state, factors and contractions,
+                       FP64 setup, mass inversion and diagnostics */
+
+typedef struct mj_op mj_op;
+typedef struct mj_lf mj_lf;
+
+/* Returns the message of the last failed call on this thread ("" if none). */
+const char* mj_last_error(void);
+
+/* Library version string. */
+const char* mj_version(void);
+
+/* ---- operator -------------------------------------------------------- */
+
+typedef struct {
+  int order;          /* r >= 1, r <= 8 */
+  int n_elt;          /* number of hexahedra */
+  int n_dof;          /* number of global dofs */
+  const int32_t* nodle;   /* n_elt x (r+1)^3, host memory */
+} mj_mesh_desc;
+
+typedef struct {
+  const double* factors;   /* n_elt x (r+1)^3 x 6, host memory */
+  const double* gradphi;   /* (r+1)^2 derivative matrix, or NULL: built from the GL rule */
+} mj_geom_desc;
+
+/* Creates the operator y <- beta*y + alpha*A*x on the current CUDA device.
+ * Replaces the construction of FemMatrixFreeClass<double, LaplaceEquation<Dimension3> >
+ * (MONTJOIE/src/Computation/FemMatrixFreeClass.hxx:74-300; its data is the
+ * problem's Nodle and Glob_matMass_Bh). precision: MJ_FP64 or MJ_FP32. */
+int mj_op_create(const mj_mesh_desc* mesh, const mj_geom_desc* geom, int precision, mj_op** out);
+
+/* Releases every device buffer of the operator. NULL is accepted. */
+int mj_op_destroy(mj_op* op);
+
+/* y <- beta*y + alpha*A*x with HOST vectors of n_dof doubles (y is not read when
+ * beta == 0).  Replaces VirtualMatrix<double>::MltAddVector(alpha, x, beta, y)
+ * (SELDON/matrix/Matrix_Base.hxx:41-140) as implemented by
+ * FemMatrixFreeClass_Base<T>::MltAddVector (MONTJOIE/src/Computation/FemMatrixFreeClass.cxx:953-1166)
+ * and MltAddScalarH1 (MONTJOIE/src/Computation/ProdMatVectScalarH1.cxx:679-727).
+ * Synchronous. */
+int mj_op_mltadd(mj_op* op, double alpha, const double* x, double beta, double* y);
+
+/* Same product on DEVICE vectors of n_dof elements in the operator's precision
+ * (double for MJ_FP64, float for MJ_FP32), ordered on `stream`
+ * (a cudaStream_t, NULL = legacy default stream).  Asynchronous. */
+int mj_op_mltadd_device(mj_op* op, double alpha, const void* x, double beta, void* y, void* stream);
+
+/* Sizes and layout facts of an operator. */
+int mj_op_info(const mj_op* op, int* order, int* n_elt, int* n_dof, int* precision,
+               size_t* device_bytes);
+
+/* Number of kernels this library launched on the calling process since load. */
+uint64_t mj_kernel_launches(void);
+
+/* ---- leap-frog time loop -------------------------------------------- */
+
+typedef struct {
+  double dt;                 /* time step */
+  const double* mass;        /* lumped mass D (n_dof), host */
+  const double* inv_mass;    /* 1/D as the scheme uses it (n_dof), host; NULL -> 1/D */
+  int n_src;                 /* sparse spatial source F: n_src (index, value) pairs */
+  const int32_t* src_idx;
+  const double* src_val;
+  int n_pulse;               /* pulse p(t_n + dt) of step n = 0..n_pulse-1, host; */
+  const double* pulse;       /* steps past n_pulse get no source */
+  const double* norm_weight; /* per-dof weight M_i = sum of J*w over the points on
+                                dof i (n_dof), or NULL: no norm diagnostics */
+  int n_rec;                 /* receivers: n_rec x n_rec_w (dof, weight) pairs */
+  int n_rec_w;
+  const int32_t* rec_idx;
+  const double* rec_w;
+} mj_lf_desc;
+
+/* Binds a leap-frog integrator to an operator (copies the descriptor's arrays
+ * to the device).  Replaces ModifiedEquationIterator<double> of order 2
+ * (MONTJOIE/src/Instationary/ModifiedEquation.hxx:78-114) with its
+ * VirtualOdeSystem operators ApplyOperatorKh/Dh/DhMinusdtSh, SolveOperatorDhPlusdtSh
+ * and AddScalarTimeSource (MONTJOIE/src/Instationary/TimeSchemes.hxx:35-151). */
+int mj_lf_create(mj_op* op, const mj_lf_desc* desc, mj_lf** out);
+int mj_lf_destroy(mj_lf* lf);
+
+/* Initial conditions U^0 = u0, U^1 = U^0 + dt*(du0 + dt/2 * D^-1(-A U^0))
+ * (ModifiedEquationIterator::SetInitialConditionS,
+ *  MONTJOIE/src/Instationary/ModifiedEquation.cxx:92-124).  Host vectors;
+ * du0 may be NULL (zero).  Resets the step counter to 0. */
+int mj_lf_init(mj_lf* lf, const double* u0, const double* du0);
+
+/* Advances nsteps steps (Advance, ModifiedEquation.cxx:290-345).  Before each
+ * step the iterate U^n is handed to the diagnostics, as GiveIterate is
+ * (ModifiedEquation.cxx:40-47): norms[s] (if not NULL, nsteps entries) gets
+ * sum_i M_i u_i^2 (GetNormeSolution, VarInstationary.cxx:2696-2745) and
+ * traces[k*trace_stride + s] (if not NULL) the receiver values.  Host outputs. */
+int mj_lf_advance(mj_lf* lf, int nsteps, double* norms, double* traces, int trace_stride);
+
+/* Copies U^n (the current iterate) and U^{n+1} to host vectors (either may be NULL). */
+int mj_lf_get_state(mj_lf* lf, double* u_n, double* u_np1);
+
+/* Whole run of RunSecondOrderScheme (ModifiedEquation.cxx:16-53): init from
+ * host u0/du0, nsteps steps with diagnostics of U^0..U^{nsteps-1}, then the
+ * final iterate U^{nsteps} (GiveFinalIterate) into u_final and, when norms /
+ * traces are given, its diagnostics in entry nsteps (norms: nsteps+1 entries,
+ * trace_stride >= nsteps+1).  Host buffers; synchronous. */
+int mj_lf_run(mj_lf* lf, const double* u0, const double* du0, int nsteps, double* u_final,
+              double* norms, double* traces, int trace_stride);
+
+/* Device-side access for callers that keep the state resident: pointers to the
+ * current U^n and U^{n+1} buffers (operator precision) and the step counter. */
+int mj_lf_device_state(mj_lf* lf, void** u_n, void** u_np1, int* step);
+
+/* Sets the CUDA stream (cudaStream_t) used by the integrator's launches. */
+int mj_lf_set_stream(mj_lf* lf, void* stream);
+
+/* ---- setup helpers (geometry, numbering, mass) ------------------------ */
+
+/* Global numbering of a conforming hexahedral mesh of order r: vertices,
+ * edges, faces and interiors get shared dofs with consistent orientation
+ * (the role of MeshNumbering/NumberMap, MONTJOIE/src/Mesh/NumberMap.cxx).
+ * hexes: n_elt x 8 vertex indices in reference-cube order; nodle_out:
+ * n_elt x (r+1)^3 in reference local order.  Dofs are numbered in the order
+ * elements first touch them.  *n_dof receives the count. */
+int mj_number_hex_mesh(int order, int n_elt, int n_vert, const int32_t* hexes, int32_t* nodle_out,
+                       int* n_dof);
+
+/* FP64 geometry on the device: per quadrature point J*w and the stiffness
+ * factors B = (J w) DF^-1 mu_e DF^-T of straight-sided (trilinear) hexahedra
+ * (VarGeometryProblem.cxx:685-759, VarHelmholtz.cxx:54-131).  verts:
+ * n_elt x 8 x 3 host; mu: n_elt host.  factors_out (n_elt x Q x 6) and
+ * jw_out (n_elt x Q) are host buffers (either may be NULL); positions_out
+ * (n_elt x Q x 3, may be NULL) gets the physical points.  Returns
+ * MJ_ERR_GEOMETRY when a Jacobian is not positive. */
+int mj_geometry(int order, int n_elt, const double* verts, const double* mu, double* factors_out,
+                double* jw_out, double* positions_out);
+
+/* Lumped mass D_i = sum rho_e J w over the points on dof i (TimeAcoustic.cxx:889-965)
+ * accumulated on the host in element order (the reference's assembly order,
+ * so sums round alike).  rho may be NULL (1). */
+int mj_lumped_mass(int order, int n_elt, int n_dof, const int32_t* nodle, const double* jw,
+                   const double* rho, double* mass_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MONTJOIE_GB300_H */

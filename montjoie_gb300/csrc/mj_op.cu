@@ -1,0 +1,647 @@
+// Operator (MltAdd) and leap-frog integrator behind the C ABI.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "mj_common.cuh"
+#include "mj_kernels.cuh"
+
+namespace mj {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+std::atomic<uint64_t>& launch_counter() {
+  static std::atomic<uint64_t> c{0};
+  return c;
+}
+
+int sm_count() {
+  int dev = 0, n = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 1;
+  return n > 0 ? n : 1;
+}
+
+__global__ void k_norm_final(const double* __restrict__ partial, int nparts, double* __restrict__ out,
+                             int* __restrict__ nonfinite_flag) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0.0;
+    for (int b = 0; b < nparts; b++) s += partial[b];
+    *out = s;
+    if (!isfinite(s)) *nonfinite_flag = 1;
+  }
+}
+
+// Elements per tile for each n = r+1 (threads per CTA = E*n*n).
+static int tile_elems(int n) {
+  switch (n) {
+    case 2: return 32;   // 128 threads
+    case 3: return 14;   // 126
+    case 4: return 8;    // 128
+    case 5: return 5;    // 125
+    case 6: return 4;    // 144
+    case 7: return 3;    // 147
+    case 8: return 2;    // 128
+    case 9: return 2;    // 162
+    default: return 1;
+  }
+}
+
+}  // namespace mj
+
+using namespace mj;
+
+struct mj_op {
+  int order = 0, n = 0, Q = 0, n_elt = 0, n_dof = 0, precision = MJ_FP64;
+  int E = 1, n_tiles = 0;
+  size_t r_len = 0;  // length of R (tile-layout points)
+  DevBuf nodle_t, fac_t, R, ptr, pos;
+  std::vector<int> h_ptr, h_pos;  // CSR incidences (host copy, for integrators)
+  double gradphi[kMaxN * kMaxN];
+  DevBuf xbuf, ybuf;              // staging for host-vector MltAdd
+  cudaStream_t stream = nullptr;
+  int grid_k1 = 1;
+  size_t device_bytes() const {
+    return nodle_t.bytes + fac_t.bytes + R.bytes + ptr.bytes + pos.bytes + xbuf.bytes + ybuf.bytes;
+  }
+};
+
+struct mj_lf {
+  mj_op* op = nullptr;
+  double dt = 0;
+  int n_dof = 0;
+  DevBuf ptr, pos;       // CSR with source entries appended
+  DevBuf src_val;        // op precision
+  DevBuf mass, minv;     // op precision (FP64: D and 1/D; FP32: unused / dt^2/D)
+  DevBuf inv_mass64;     // FP64 1/D for the initial step
+  DevBuf norm_w;         // FP64 weights, or empty
+  DevBuf rec_idx, rec_w; // receivers
+  DevBuf ua, ub;         // state: U^n (cur) and U^{n+1} (next)
+  DevBuf du0, tmp;       // staging
+  DevBuf partial, norms_d, traces_d, flag;
+  std::vector<double> pulse;
+  int n_src = 0, n_rec = 0, n_rec_w = 0;
+  int step = 0;
+  bool initialised = false;
+  bool cur_is_a = true;
+  cudaStream_t stream = nullptr;
+  int norm_blocks = 0;
+  void* cur() { return cur_is_a ? ua.ptr : ub.ptr; }
+  void* next() { return cur_is_a ? ub.ptr : ua.ptr; }
+};
+
+namespace {
+
+template <typename Real, int N>
+void launch_k1_n(mj_op* op, const void* x, cudaStream_t s) {
+  GMatrix<Real, N> G;
+  for (int a = 0; a < N * N; a++) G.g[a] = Real(op->gradphi[a]);
+  constexpr int NN = N * N;
+  switch (op->E) {
+#define MJ_K1_CASE(EV)                                                                          \
+  case EV:                                                                                      \
+    k_local_stiffness<Real, N, EV><<<op->grid_k1, EV * NN, 0, s>>>(                             \
+        static_cast<const Real*>(x), op->nodle_t.as<int>(), op->fac_t.as<Real>(),               \
+        op->R.as<Real>(), op->n_tiles, G);                                                      \
+    break;
+    MJ_K1_CASE(1) MJ_K1_CASE(2) MJ_K1_CASE(3) MJ_K1_CASE(4) MJ_K1_CASE(5)
+    MJ_K1_CASE(8) MJ_K1_CASE(14) MJ_K1_CASE(32)
+#undef MJ_K1_CASE
+    default: break;
+  }
+  count_launch();
+}
+
+template <typename Real>
+void launch_k1(mj_op* op, const void* x, cudaStream_t s) {
+  switch (op->n) {
+    case 2: launch_k1_n<Real, 2>(op, x, s); break;
+    case 3: launch_k1_n<Real, 3>(op, x, s); break;
+    case 4: launch_k1_n<Real, 4>(op, x, s); break;
+    case 5: launch_k1_n<Real, 5>(op, x, s); break;
+    case 6: launch_k1_n<Real, 6>(op, x, s); break;
+    case 7: launch_k1_n<Real, 7>(op, x, s); break;
+    case 8: launch_k1_n<Real, 8>(op, x, s); break;
+    case 9: launch_k1_n<Real, 9>(op, x, s); break;
+  }
+}
+
+// Occupancy-sized persistent grid for K1.
+template <typename Real, int N>
+int k1_grid_n(int E, int n_tiles) {
+  int per_sm = 1;
+  constexpr int NN = N * N;
+  switch (E) {
+#define MJ_OCC(EV)                                                                              \
+  case EV:                                                                                      \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_local_stiffness<Real, N, EV>,      \
+                                                  EV * NN, 0);                                  \
+    break;
+    MJ_OCC(1) MJ_OCC(2) MJ_OCC(3) MJ_OCC(4) MJ_OCC(5) MJ_OCC(8) MJ_OCC(14) MJ_OCC(32)
+#undef MJ_OCC
+  }
+  if (per_sm < 1) per_sm = 1;
+  long g = (long)per_sm * sm_count();
+  return (int)std::max(1L, std::min<long>(g, n_tiles));
+}
+
+template <typename Real>
+int k1_grid(int n, int E, int n_tiles) {
+  switch (n) {
+    case 2: return k1_grid_n<Real, 2>(E, n_tiles);
+    case 3: return k1_grid_n<Real, 3>(E, n_tiles);
+    case 4: return k1_grid_n<Real, 4>(E, n_tiles);
+    case 5: return k1_grid_n<Real, 5>(E, n_tiles);
+    case 6: return k1_grid_n<Real, 6>(E, n_tiles);
+    case 7: return k1_grid_n<Real, 7>(E, n_tiles);
+    case 8: return k1_grid_n<Real, 8>(E, n_tiles);
+    case 9: return k1_grid_n<Real, 9>(E, n_tiles);
+  }
+  return 1;
+}
+
+int stream_grid(int n) {
+  long g = (n + 255) / 256;
+  return (int)std::max(1L, std::min<long>(g, (long)sm_count() * 16));
+}
+
+template <typename Real>
+int mltadd_impl(mj_op* op, double alpha, const void* x, double beta, void* y, cudaStream_t s) {
+  launch_k1<Real>(op, x, s);
+  k_gather_mltadd<Real><<<stream_grid(op->n_dof), 256, 0, s>>>(
+      op->R.as<Real>(), op->ptr.as<int>(), op->pos.as<int>(), Real(alpha), Real(beta),
+      static_cast<Real*>(y), op->n_dof);
+  count_launch();
+  MJ_CUDA(cudaGetLastError());
+  return MJ_OK;
+}
+
+template <typename Real>
+__global__ void k_cast_from_f64(const double* __restrict__ a, Real* __restrict__ b, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = Real(a[i]);
+}
+template <typename Real>
+__global__ void k_cast_to_f64(const Real* __restrict__ a, double* __restrict__ b, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = double(a[i]);
+}
+
+// Copies a host double vector into a device vector of the operator precision.
+int upload_vec(mj_op* op, const double* h, void* d, DevBuf& stage, cudaStream_t s) {
+  const int n = op->n_dof;
+  if (op->precision == MJ_FP64) {
+    MJ_CUDA(cudaMemcpyAsync(d, h, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    return MJ_OK;
+  }
+  if (stage.bytes < sizeof(double) * n) MJ_CUDA(stage.alloc(sizeof(double) * n));
+  MJ_CUDA(cudaMemcpyAsync(stage.ptr, h, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  k_cast_from_f64<float><<<stream_grid(n), 256, 0, s>>>(stage.as<double>(), static_cast<float*>(d), n);
+  count_launch();
+  MJ_CUDA(cudaGetLastError());
+  return MJ_OK;
+}
+
+int download_vec(mj_op* op, const void* d, double* h, DevBuf& stage, cudaStream_t s) {
+  const int n = op->n_dof;
+  if (op->precision == MJ_FP64) {
+    MJ_CUDA(cudaMemcpyAsync(h, d, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    return MJ_OK;
+  }
+  if (stage.bytes < sizeof(double) * n) MJ_CUDA(stage.alloc(sizeof(double) * n));
+  k_cast_to_f64<float><<<stream_grid(n), 256, 0, s>>>(static_cast<const float*>(d), stage.as<double>(), n);
+  count_launch();
+  MJ_CUDA(cudaGetLastError());
+  MJ_CUDA(cudaMemcpyAsync(h, stage.ptr, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  return MJ_OK;
+}
+
+size_t elem_size(int precision) { return precision == MJ_FP64 ? sizeof(double) : sizeof(float); }
+
+}  // namespace
+
+extern "C" {
+
+const char* mj_last_error(void) { return g_last_error.c_str(); }
+
+const char* mj_version(void) { return "montjoie_gb300 0.1 (sm_103a)"; }
+
+uint64_t mj_kernel_launches(void) { return launch_counter().load(); }
+
+int mj_op_create(const mj_mesh_desc* mesh, const mj_geom_desc* geom, int precision, mj_op** out) {
+  MJ_CHECK_ARG(mesh && geom && out, "mj_op_create: null argument");
+  *out = nullptr;
+  const int r = mesh->order;
+  MJ_CHECK_ARG(r >= 1 && r <= kMaxOrder, "mj_op_create: order must be in [1, 8]");
+  MJ_CHECK_ARG(mesh->n_elt > 0 && mesh->n_dof > 0, "mj_op_create: empty mesh");
+  MJ_CHECK_ARG(mesh->nodle && geom->factors, "mj_op_create: nodle and factors are required");
+  MJ_CHECK_ARG(precision == MJ_FP64 || precision == MJ_FP32, "mj_op_create: precision must be MJ_FP64 or MJ_FP32");
+  const int n = r + 1, Q = n * n * n, NN = n * n;
+  const long long total_pts = (long long)mesh->n_elt * Q;
+  MJ_CHECK_ARG(total_pts < (1LL << 31) - 1, "mj_op_create: n_elt*(r+1)^3 exceeds int32 indexing");
+
+  std::unique_ptr<mj_op> op(new mj_op());
+  op->order = r; op->n = n; op->Q = Q; op->n_elt = mesh->n_elt; op->n_dof = mesh->n_dof;
+  op->precision = precision;
+  op->E = tile_elems(n);
+  op->n_tiles = (mesh->n_elt + op->E - 1) / op->E;
+  op->r_len = (size_t)op->n_tiles * op->E * Q;
+  MJ_CHECK_ARG(op->r_len < (size_t)INT32_MAX, "mj_op_create: mesh too large for int32 incidences");
+
+  // derivative matrix
+  if (geom->gradphi) {
+    for (int a = 0; a < NN; a++) op->gradphi[a] = geom->gradphi[a];
+  } else {
+    double pts[kMaxN], wts[kMaxN];
+    gauss_lobatto(r, pts, wts);
+    gl_derivative_matrix(r, pts, op->gradphi);
+  }
+  for (int a = 0; a < NN; a++)
+    MJ_CHECK_ARG(std::isfinite(op->gradphi[a]), "mj_op_create: non-finite derivative matrix");
+
+  const std::vector<int> num = hex_local_numbering(r);
+  const int E = op->E;
+  const size_t TQ = (size_t)E * Q;
+  // tile-layout connectivity and factors, and CSR incidences
+  std::vector<int> nodle_t(op->r_len, 0);
+  std::vector<int> count(op->n_dof + 1, 0);
+  for (long long t = 0; t < total_pts; t++) {
+    const int d = mesh->nodle[t];
+    MJ_CHECK_ARG(d >= 0 && d < mesh->n_dof, "mj_op_create: Nodle entry out of [0, n_dof)");
+    count[d + 1]++;
+  }
+  for (int d = 0; d < op->n_dof; d++)
+    MJ_CHECK_ARG(count[d + 1] > 0, "mj_op_create: a dof belongs to no element");
+  op->h_ptr.assign(op->n_dof + 1, 0);
+  for (int d = 0; d < op->n_dof; d++) op->h_ptr[d + 1] = op->h_ptr[d] + count[d + 1];
+  op->h_pos.assign((size_t)total_pts, 0);
+  std::vector<int> fill(op->h_ptr.begin(), op->h_ptr.end() - 1);
+
+  const size_t esz = elem_size(precision);
+  std::vector<unsigned char> fac_bytes(op->r_len * 6 * esz, 0);
+  double* fac64 = reinterpret_cast<double*>(fac_bytes.data());
+  float* fac32 = reinterpret_cast<float*>(fac_bytes.data());
+  // Iterate R positions in increasing order so each dof's incidences are sorted.
+  for (int tile = 0; tile < op->n_tiles; tile++)
+    for (int k = 0; k < n; k++)
+      for (int el = 0; el < E; el++) {
+        const int e = tile * E + el;
+        for (int j = 0; j < n; j++)
+          for (int i = 0; i < n; i++) {
+            const size_t rp = (((size_t)tile * n + k) * E + el) * NN + j * n + i;
+            if (e >= mesh->n_elt) continue;  // padding: nodle 0, factors 0, no incidence
+            const int ql = num[(i * n + j) * n + k];
+            const size_t src = (size_t)e * Q + ql;
+            const int d = mesh->nodle[src];
+            nodle_t[rp] = d;
+            op->h_pos[fill[d]++] = (int)rp;
+            for (int c = 0; c < 6; c++) {
+              const double v = geom->factors[src * 6 + c];
+              if (!std::isfinite(v)) {
+                set_error("mj_op_create: non-finite stiffness factor");
+                return MJ_ERR_NONFINITE;
+              }
+              const size_t fp = (size_t)tile * 6 * TQ + c * TQ + (rp - (size_t)tile * TQ);
+              if (precision == MJ_FP64) fac64[fp] = v;
+              else fac32[fp] = (float)v;
+            }
+          }
+      }
+
+  MJ_CUDA(op->nodle_t.alloc(sizeof(int) * op->r_len));
+  MJ_CUDA(op->fac_t.alloc(fac_bytes.size()));
+  MJ_CUDA(op->R.alloc(esz * op->r_len));
+  MJ_CUDA(op->ptr.alloc(sizeof(int) * (op->n_dof + 1)));
+  MJ_CUDA(op->pos.alloc(sizeof(int) * op->h_pos.size()));
+  MJ_CUDA(cudaMemcpy(op->nodle_t.ptr, nodle_t.data(), sizeof(int) * op->r_len, cudaMemcpyHostToDevice));
+  MJ_CUDA(cudaMemcpy(op->fac_t.ptr, fac_bytes.data(), fac_bytes.size(), cudaMemcpyHostToDevice));
+  MJ_CUDA(cudaMemcpy(op->ptr.ptr, op->h_ptr.data(), sizeof(int) * (op->n_dof + 1), cudaMemcpyHostToDevice));
+  MJ_CUDA(cudaMemcpy(op->pos.ptr, op->h_pos.data(), sizeof(int) * op->h_pos.size(), cudaMemcpyHostToDevice));
+  MJ_CUDA(cudaMemset(op->R.ptr, 0, esz * op->r_len));
+  op->grid_k1 = (precision == MJ_FP64) ? k1_grid<double>(n, E, op->n_tiles) : k1_grid<float>(n, E, op->n_tiles);
+  MJ_CUDA(cudaGetLastError());
+  *out = op.release();
+  return MJ_OK;
+}
+
+int mj_op_destroy(mj_op* op) {
+  delete op;
+  return MJ_OK;
+}
+
+int mj_op_info(const mj_op* op, int* order, int* n_elt, int* n_dof, int* precision, size_t* device_bytes) {
+  MJ_CHECK_ARG(op, "mj_op_info: null operator");
+  if (order) *order = op->order;
+  if (n_elt) *n_elt = op->n_elt;
+  if (n_dof) *n_dof = op->n_dof;
+  if (precision) *precision = op->precision;
+  if (device_bytes) *device_bytes = op->device_bytes();
+  return MJ_OK;
+}
+
+int mj_op_mltadd_device(mj_op* op, double alpha, const void* x, double beta, void* y, void* stream) {
+  MJ_CHECK_ARG(op && x && y, "mj_op_mltadd_device: null argument");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  return op->precision == MJ_FP64 ? mltadd_impl<double>(op, alpha, x, beta, y, s)
+                                  : mltadd_impl<float>(op, alpha, x, beta, y, s);
+}
+
+int mj_op_mltadd(mj_op* op, double alpha, const double* x, double beta, double* y) {
+  MJ_CHECK_ARG(op && x && y, "mj_op_mltadd: null argument");
+  const size_t esz = elem_size(op->precision);
+  const int n = op->n_dof;
+  if (op->xbuf.bytes < esz * n) MJ_CUDA(op->xbuf.alloc(esz * n));
+  if (op->ybuf.bytes < esz * n) MJ_CUDA(op->ybuf.alloc(esz * n));
+  DevBuf stage;
+  cudaStream_t s = op->stream;
+  int rc = upload_vec(op, x, op->xbuf.ptr, stage, s);
+  if (rc) return rc;
+  if (beta != 0.0) {
+    rc = upload_vec(op, y, op->ybuf.ptr, stage, s);
+    if (rc) return rc;
+  }
+  rc = mj_op_mltadd_device(op, alpha, op->xbuf.ptr, beta, op->ybuf.ptr, s);
+  if (rc) return rc;
+  rc = download_vec(op, op->ybuf.ptr, y, stage, s);
+  if (rc) return rc;
+  MJ_CUDA(cudaStreamSynchronize(s));
+  return MJ_OK;
+}
+
+// ------------------------------------------------------------------ leap-frog
+
+int mj_lf_create(mj_op* op, const mj_lf_desc* desc, mj_lf** out) {
+  MJ_CHECK_ARG(op && desc && out, "mj_lf_create: null argument");
+  *out = nullptr;
+  MJ_CHECK_ARG(desc->dt > 0 && std::isfinite(desc->dt), "mj_lf_create: dt must be positive");
+  MJ_CHECK_ARG(desc->mass, "mj_lf_create: mass is required");
+  MJ_CHECK_ARG(desc->n_src >= 0 && (desc->n_src == 0 || (desc->src_idx && desc->src_val)),
+               "mj_lf_create: bad source arrays");
+  MJ_CHECK_ARG(desc->n_pulse >= 0 && (desc->n_pulse == 0 || desc->pulse), "mj_lf_create: bad pulse array");
+  MJ_CHECK_ARG(desc->n_rec >= 0 && (desc->n_rec == 0 || (desc->rec_idx && desc->rec_w && desc->n_rec_w > 0)),
+               "mj_lf_create: bad receiver arrays");
+  const int n = op->n_dof;
+  std::unique_ptr<mj_lf> lf(new mj_lf());
+  lf->op = op; lf->dt = desc->dt; lf->n_dof = n; lf->stream = op->stream;
+  const size_t esz = elem_size(op->precision);
+
+  std::vector<double> invD(n);
+  for (int i = 0; i < n; i++) {
+    MJ_CHECK_ARG(std::isfinite(desc->mass[i]) && desc->mass[i] > 0, "mj_lf_create: mass must be positive");
+    invD[i] = desc->inv_mass ? desc->inv_mass[i] : 1.0 / desc->mass[i];
+  }
+  // CSR with the source entries appended after each dof's element entries
+  std::vector<int> src_of(n, -1);
+  for (int s = 0; s < desc->n_src; s++) {
+    const int d = desc->src_idx[s];
+    MJ_CHECK_ARG(d >= 0 && d < n, "mj_lf_create: source index out of range");
+    MJ_CHECK_ARG(src_of[d] < 0, "mj_lf_create: duplicate source index");
+    src_of[d] = s;
+  }
+  std::vector<int> ptr(n + 1, 0), pos;
+  pos.reserve(op->h_pos.size() + desc->n_src);
+  for (int d = 0; d < n; d++) {
+    for (int q = op->h_ptr[d]; q < op->h_ptr[d + 1]; q++) pos.push_back(op->h_pos[q]);
+    if (src_of[d] >= 0) pos.push_back(-src_of[d] - 1);
+    ptr[d + 1] = (int)pos.size();
+  }
+  MJ_CUDA(lf->ptr.alloc(sizeof(int) * (n + 1)));
+  MJ_CUDA(lf->pos.alloc(sizeof(int) * pos.size()));
+  MJ_CUDA(cudaMemcpy(lf->ptr.ptr, ptr.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
+  MJ_CUDA(cudaMemcpy(lf->pos.ptr, pos.data(), sizeof(int) * pos.size(), cudaMemcpyHostToDevice));
+  lf->n_src = desc->n_src;
+  MJ_CUDA(lf->src_val.alloc(esz * std::max(1, desc->n_src)));
+  MJ_CUDA(lf->inv_mass64.alloc(sizeof(double) * n));
+  MJ_CUDA(cudaMemcpy(lf->inv_mass64.ptr, invD.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+  if (op->precision == MJ_FP64) {
+    if (desc->n_src)
+      MJ_CUDA(cudaMemcpy(lf->src_val.ptr, desc->src_val, sizeof(double) * desc->n_src, cudaMemcpyHostToDevice));
+    MJ_CUDA(lf->mass.alloc(sizeof(double) * n));
+    MJ_CUDA(lf->minv.alloc(sizeof(double) * n));
+    MJ_CUDA(cudaMemcpy(lf->mass.ptr, desc->mass, sizeof(double) * n, cudaMemcpyHostToDevice));
+    MJ_CUDA(cudaMemcpy(lf->minv.ptr, invD.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+  } else {
+    std::vector<float> sv(std::max(1, desc->n_src)), m(n);
+    for (int s = 0; s < desc->n_src; s++) sv[s] = (float)desc->src_val[s];
+    for (int i = 0; i < n; i++) m[i] = (float)(desc->dt * desc->dt * invD[i]);
+    MJ_CUDA(cudaMemcpy(lf->src_val.ptr, sv.data(), sizeof(float) * sv.size(), cudaMemcpyHostToDevice));
+    MJ_CUDA(lf->minv.alloc(sizeof(float) * n));
+    MJ_CUDA(cudaMemcpy(lf->minv.ptr, m.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+  }
+  lf->pulse.assign(desc->pulse, desc->pulse + desc->n_pulse);
+  if (desc->norm_weight) {
+    MJ_CUDA(lf->norm_w.alloc(sizeof(double) * n));
+    MJ_CUDA(cudaMemcpy(lf->norm_w.ptr, desc->norm_weight, sizeof(double) * n, cudaMemcpyHostToDevice));
+  }
+  lf->n_rec = desc->n_rec;
+  lf->n_rec_w = desc->n_rec_w;
+  if (desc->n_rec) {
+    const size_t m = (size_t)desc->n_rec * desc->n_rec_w;
+    for (size_t t = 0; t < m; t++)
+      MJ_CHECK_ARG(desc->rec_idx[t] >= 0 && desc->rec_idx[t] < n, "mj_lf_create: receiver dof out of range");
+    MJ_CUDA(lf->rec_idx.alloc(sizeof(int) * m));
+    MJ_CUDA(lf->rec_w.alloc(sizeof(double) * m));
+    MJ_CUDA(cudaMemcpy(lf->rec_idx.ptr, desc->rec_idx, sizeof(int) * m, cudaMemcpyHostToDevice));
+    MJ_CUDA(cudaMemcpy(lf->rec_w.ptr, desc->rec_w, sizeof(double) * m, cudaMemcpyHostToDevice));
+  }
+  MJ_CUDA(lf->ua.alloc(esz * n));
+  MJ_CUDA(lf->ub.alloc(esz * n));
+  lf->norm_blocks = std::min(stream_grid(n), 1024);
+  MJ_CUDA(lf->partial.alloc(sizeof(double) * lf->norm_blocks));
+  MJ_CUDA(lf->flag.alloc(sizeof(int)));
+  MJ_CUDA(cudaMemset(lf->flag.ptr, 0, sizeof(int)));
+  *out = lf.release();
+  return MJ_OK;
+}
+
+int mj_lf_destroy(mj_lf* lf) {
+  delete lf;
+  return MJ_OK;
+}
+
+int mj_lf_set_stream(mj_lf* lf, void* stream) {
+  MJ_CHECK_ARG(lf, "mj_lf_set_stream: null integrator");
+  lf->stream = static_cast<cudaStream_t>(stream);
+  return MJ_OK;
+}
+
+namespace {
+
+template <typename Real>
+int lf_init_impl(mj_lf* lf, const double* u0, const double* du0) {
+  mj_op* op = lf->op;
+  cudaStream_t s = lf->stream;
+  const int n = lf->n_dof;
+  DevBuf stage;
+  int rc = upload_vec(op, u0, lf->ua.ptr, stage, s);
+  if (rc) return rc;
+  const Real* du0_d = nullptr;
+  if (du0) {
+    if (lf->du0.bytes < sizeof(Real) * n) MJ_CUDA(lf->du0.alloc(sizeof(Real) * n));
+    rc = upload_vec(op, du0, lf->du0.ptr, stage, s);
+    if (rc) return rc;
+    du0_d = lf->du0.as<Real>();
+  }
+  launch_k1<Real>(op, lf->ua.ptr, s);
+  k_gather_init<Real><<<stream_grid(n), 256, 0, s>>>(op->R.as<Real>(), lf->ptr.as<int>(), lf->pos.as<int>(),
+                                                      lf->ua.as<Real>(), du0_d, lf->inv_mass64.as<double>(),
+                                                      lf->dt, lf->ub.as<Real>(), n);
+  count_launch();
+  MJ_CUDA(cudaGetLastError());
+  lf->cur_is_a = true;
+  lf->step = 0;
+  lf->initialised = true;
+  MJ_CUDA(cudaMemsetAsync(lf->flag.ptr, 0, sizeof(int), s));
+  MJ_CUDA(cudaStreamSynchronize(s));
+  return MJ_OK;
+}
+
+template <typename Real>
+int lf_diag(mj_lf* lf, double* norms_d, int norm_col, double* traces_d, int stride, int col) {
+  cudaStream_t s = lf->stream;
+  const int n = lf->n_dof;
+  const Real* u = static_cast<const Real*>(lf->cur());
+  if (norms_d && lf->norm_w.ptr) {
+    k_norm_partial<Real><<<lf->norm_blocks, 256, 0, s>>>(u, lf->norm_w.as<double>(), n, lf->partial.as<double>());
+    k_norm_final<<<1, 32, 0, s>>>(lf->partial.as<double>(), lf->norm_blocks, norms_d + norm_col, lf->flag.as<int>());
+    count_launch(2);
+  }
+  if (traces_d && lf->n_rec) {
+    const int threads = 128, blocks = (lf->n_rec * 32 + threads - 1) / threads;
+    k_receivers<Real><<<blocks, threads, 0, s>>>(u, lf->rec_idx.as<int>(), lf->rec_w.as<double>(), lf->n_rec,
+                                                 lf->n_rec_w, traces_d, stride, col);
+    count_launch();
+  }
+  MJ_CUDA(cudaGetLastError());
+  return MJ_OK;
+}
+
+template <typename Real>
+int lf_step(mj_lf* lf) {
+  mj_op* op = lf->op;
+  cudaStream_t s = lf->stream;
+  const int n = lf->n_dof;
+  const double p = (lf->step < (int)lf->pulse.size()) ? lf->pulse[lf->step] : 0.0;
+  // U1 = next (u^{n+1}), U0 = cur (u^n); the result u^{n+2} overwrites U0.
+  launch_k1<Real>(op, lf->next(), s);
+  const double dt2 = lf->dt * lf->dt;
+  if (op->precision == MJ_FP64) {
+    k_gather_leapfrog<Real, true><<<stream_grid(n), 256, 0, s>>>(
+        op->R.as<Real>(), lf->ptr.as<int>(), lf->pos.as<int>(), lf->src_val.as<Real>(), Real(p),
+        static_cast<Real*>(lf->cur()), static_cast<const Real*>(lf->next()), lf->mass.as<Real>(),
+        lf->minv.as<Real>(), Real(dt2), n);
+  } else {
+    k_gather_leapfrog<Real, false><<<stream_grid(n), 256, 0, s>>>(
+        op->R.as<Real>(), lf->ptr.as<int>(), lf->pos.as<int>(), lf->src_val.as<Real>(), Real(p),
+        static_cast<Real*>(lf->cur()), static_cast<const Real*>(lf->next()), nullptr,
+        lf->minv.as<Real>(), Real(dt2), n);
+  }
+  count_launch();
+  MJ_CUDA(cudaGetLastError());
+  lf->cur_is_a = !lf->cur_is_a;  // new cur = old next; new next = overwritten old cur
+  lf->step++;
+  return MJ_OK;
+}
+
+template <typename Real>
+int lf_advance_impl(mj_lf* lf, int nsteps, double* norms, double* traces, int stride, bool final_diag) {
+  const int cols = nsteps + (final_diag ? 1 : 0);
+  double* nd = nullptr;
+  double* td = nullptr;
+  if (norms && lf->norm_w.ptr) {
+    if (lf->norms_d.bytes < sizeof(double) * cols) MJ_CUDA(lf->norms_d.alloc(sizeof(double) * cols));
+    nd = lf->norms_d.as<double>();
+  }
+  if (traces && lf->n_rec) {
+    MJ_CHECK_ARG(stride >= cols, "mj_lf_advance: trace_stride smaller than the number of recorded iterates");
+    const size_t b = sizeof(double) * (size_t)lf->n_rec * cols;
+    if (lf->traces_d.bytes < b) MJ_CUDA(lf->traces_d.alloc(b));
+    td = lf->traces_d.as<double>();
+  }
+  for (int s = 0; s < nsteps; s++) {
+    int rc = lf_diag<Real>(lf, nd, s, td, cols, s);
+    if (rc) return rc;
+    rc = lf_step<Real>(lf);
+    if (rc) return rc;
+  }
+  if (final_diag) {
+    int rc = lf_diag<Real>(lf, nd, nsteps, td, cols, nsteps);
+    if (rc) return rc;
+  }
+  cudaStream_t s = lf->stream;
+  if (nd) MJ_CUDA(cudaMemcpyAsync(norms, nd, sizeof(double) * cols, cudaMemcpyDeviceToHost, s));
+  if (td)
+    for (int k = 0; k < lf->n_rec; k++)
+      MJ_CUDA(cudaMemcpyAsync(traces + (size_t)k * stride, td + (size_t)k * cols, sizeof(double) * cols,
+                              cudaMemcpyDeviceToHost, s));
+  int flag = 0;
+  MJ_CUDA(cudaMemcpyAsync(&flag, lf->flag.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MJ_CUDA(cudaStreamSynchronize(s));
+  if (flag) {
+    set_error("mj_lf_advance: non-finite norm (unstable run?)");
+    return MJ_ERR_NONFINITE;
+  }
+  return MJ_OK;
+}
+
+}  // namespace
+
+int mj_lf_init(mj_lf* lf, const double* u0, const double* du0) {
+  MJ_CHECK_ARG(lf && u0, "mj_lf_init: null argument");
+  return lf->op->precision == MJ_FP64 ? lf_init_impl<double>(lf, u0, du0) : lf_init_impl<float>(lf, u0, du0);
+}
+
+int mj_lf_advance(mj_lf* lf, int nsteps, double* norms, double* traces, int trace_stride) {
+  MJ_CHECK_ARG(lf, "mj_lf_advance: null integrator");
+  MJ_CHECK_ARG(nsteps >= 0, "mj_lf_advance: negative step count");
+  if (!lf->initialised) {
+    set_error("mj_lf_advance: mj_lf_init must be called first");
+    return MJ_ERR_STATE;
+  }
+  return lf->op->precision == MJ_FP64 ? lf_advance_impl<double>(lf, nsteps, norms, traces, trace_stride, false)
+                                      : lf_advance_impl<float>(lf, nsteps, norms, traces, trace_stride, false);
+}
+
+int mj_lf_get_state(mj_lf* lf, double* u_n, double* u_np1) {
+  MJ_CHECK_ARG(lf, "mj_lf_get_state: null integrator");
+  if (!lf->initialised) {
+    set_error("mj_lf_get_state: mj_lf_init must be called first");
+    return MJ_ERR_STATE;
+  }
+  DevBuf stage;
+  int rc;
+  if (u_n && (rc = download_vec(lf->op, lf->cur(), u_n, stage, lf->stream))) return rc;
+  if (u_np1 && (rc = download_vec(lf->op, lf->next(), u_np1, stage, lf->stream))) return rc;
+  MJ_CUDA(cudaStreamSynchronize(lf->stream));
+  return MJ_OK;
+}
+
+int mj_lf_run(mj_lf* lf, const double* u0, const double* du0, int nsteps, double* u_final, double* norms,
+              double* traces, int trace_stride) {
+  MJ_CHECK_ARG(lf && u0, "mj_lf_run: null argument");
+  MJ_CHECK_ARG(nsteps >= 0, "mj_lf_run: negative step count");
+  int rc = mj_lf_init(lf, u0, du0);
+  if (rc) return rc;
+  rc = lf->op->precision == MJ_FP64 ? lf_advance_impl<double>(lf, nsteps, norms, traces, trace_stride, true)
+                                    : lf_advance_impl<float>(lf, nsteps, norms, traces, trace_stride, true);
+  if (rc) return rc;
+  if (u_final) return mj_lf_get_state(lf, u_final, nullptr);
+  return MJ_OK;
+}
+
+int mj_lf_device_state(mj_lf* lf, void** u_n, void** u_np1, int* step) {
+  MJ_CHECK_ARG(lf, "mj_lf_device_state: null integrator");
+  if (u_n) *u_n = lf->cur();
+  if (u_np1) *u_np1 = lf->next();
+  if (step) *step = lf->step;
+  return MJ_OK;
+}
+
+}  // extern "C"

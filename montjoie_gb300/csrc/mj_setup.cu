@@ -1,0 +1,387 @@
+// One-time setup: 1-D Gauss-Lobatto rule, local and global hexahedral
+// numbering, FP64 geometry on the device, lumped mass.
+#include <cuda_runtime.h>
+
+#include <array>
+#include <cmath>
+#include <cstring>
+#include <unordered_map>
+#include <vector>
+
+#include "mj_common.cuh"
+
+namespace mj {
+
+namespace {
+const int kCorner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+const int kEdge[12][2] = {{0, 1}, {1, 2}, {3, 2}, {0, 3}, {0, 4}, {1, 5}, {2, 6}, {3, 7}, {4, 5}, {5, 6}, {7, 6}, {4, 7}};
+}  // namespace
+
+std::vector<int> hex_local_numbering(int r) {
+  const int n = r + 1;
+  std::vector<int> num(n * n * n, -1);
+  auto at = [&](int i, int j, int k) -> int& { return num[(i * n + j) * n + k]; };
+  int node = 0;
+  for (int v = 0; v < 8; v++) at(kCorner[v][0] * r, kCorner[v][1] * r, kCorner[v][2] * r) = node++;
+  for (int e = 0; e < 12; e++) {
+    const int* a = kCorner[kEdge[e][0]];
+    const int* b = kCorner[kEdge[e][1]];
+    for (int l = 1; l < r; l++) {
+      // point at parameter l from corner a towards corner b
+      at(a[0] * r + l * (b[0] - a[0]), a[1] * r + l * (b[1] - a[1]), a[2] * r + l * (b[2] - a[2])) = node++;
+    }
+  }
+  for (int p = 1; p < r; p++) for (int q = 1; q < r; q++) at(0, p, q) = node++;
+  for (int p = 1; p < r; p++) for (int q = 1; q < r; q++) at(p, 0, q) = node++;
+  for (int p = 1; p < r; p++) for (int q = 1; q < r; q++) at(p, q, 0) = node++;
+  for (int p = 1; p < r; p++) for (int q = 1; q < r; q++) at(p, q, r) = node++;
+  for (int p = 1; p < r; p++) for (int q = 1; q < r; q++) at(p, r, q) = node++;
+  for (int p = 1; p < r; p++) for (int q = 1; q < r; q++) at(r, p, q) = node++;
+  for (int p = 1; p < r; p++)
+    for (int q = 1; q < r; q++)
+      for (int s = 1; s < r; s++) at(p, q, s) = node++;
+  return num;
+}
+
+// Legendre polynomial P_r and derivative on [-1,1].
+static void legendre_pd(int r, double x, double& p, double& dp) {
+  double p0 = 1.0, p1 = x, d0 = 0.0, d1 = 1.0;
+  if (r == 0) { p = 1.0; dp = 0.0; return; }
+  for (int k = 1; k < r; k++) {
+    const double p2 = ((2.0 * k + 1.0) * x * p1 - k * p0) / (k + 1.0);
+    const double d2 = d0 + (2.0 * k + 1.0) * p1;
+    p0 = p1; p1 = p2; d0 = d1; d1 = d2;
+  }
+  p = p1; dp = d1;
+}
+
+void gauss_lobatto(int r, double* pts, double* wts) {
+  // Interior nodes: roots of P_r' (Newton on P_r', second derivative from the
+  // Legendre equation), weights 1/(r(r+1) P_r(x)^2) on [0,1].
+  const double pi = 3.14159265358979323846;
+  std::vector<double> x(r + 1);
+  for (int i = 0; i <= r; i++) x[i] = -std::cos(pi * i / r);
+  for (int i = 1; i < r; i++)
+    for (int it = 0; it < 100; it++) {
+      double p, dp;
+      legendre_pd(r, x[i], p, dp);
+      const double d2 = (2.0 * x[i] * dp - r * (r + 1.0) * p) / (1.0 - x[i] * x[i]);
+      const double step = dp / d2;
+      x[i] -= step;
+      if (std::fabs(step) < 1e-17) break;
+    }
+  for (int i = 0; i <= r; i++) {
+    double p, dp;
+    legendre_pd(r, x[i], p, dp);
+    pts[i] = 0.5 * (x[i] + 1.0);
+    wts[i] = 1.0 / (r * (r + 1.0) * p * p);
+  }
+  pts[0] = 0.0;
+  pts[r] = 1.0;
+}
+
+void gl_derivative_matrix(int r, const double* pts, double* g) {
+  const int n = r + 1;
+  std::vector<double> c(n);
+  for (int i = 0; i < n; i++) {
+    double prod = 1.0;
+    for (int j = 0; j < n; j++)
+      if (j != i) prod *= pts[i] - pts[j];
+    c[i] = 1.0 / prod;
+  }
+  for (int b = 0; b < n; b++) {
+    double sum = 0.0;
+    for (int a = 0; a < n; a++)
+      if (a != b) {
+        g[a * n + b] = c[a] / (c[b] * (pts[b] - pts[a]));
+        sum += g[a * n + b];
+      }
+    g[b * n + b] = -sum;
+    if (std::fabs(g[b * n + b]) <= 1e3 * 2.220446049250313e-16) g[b * n + b] = 0.0;
+  }
+}
+
+// ------------------------------------------------------------ geometry kernel
+
+struct GeomParams {
+  int n, Q;
+  double pts[kMaxN];
+  double wts[kMaxN];
+};
+
+__constant__ unsigned char c_coord[kMaxN * kMaxN * kMaxN * 3];  // local index -> (i,j,k)
+
+__global__ void k_geometry(const double* __restrict__ verts, const double* __restrict__ mu, int n_elt,
+                           const GeomParams P, double* __restrict__ fac, double* __restrict__ jw,
+                           double* __restrict__ xq, int* __restrict__ bad) {
+  const long long total = (long long)n_elt * P.Q;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int e = (int)(t / P.Q);
+    const int q = (int)(t - (long long)e * P.Q);
+    const int ci = c_coord[3 * q], cj = c_coord[3 * q + 1], ck = c_coord[3 * q + 2];
+    const double x = P.pts[ci], y = P.pts[cj], z = P.pts[ck];
+    const double w = P.wts[ci] * P.wts[cj] * P.wts[ck];
+    const double* v = verts + (size_t)e * 24;
+    double F[3] = {0, 0, 0}, DF[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    const double cx[2] = {1.0 - x, x}, cy[2] = {1.0 - y, y}, cz[2] = {1.0 - z, z};
+    const double dd[2] = {-1.0, 1.0};
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      const int a = (c == 1 || c == 2 || c == 5 || c == 6), b = (c == 2 || c == 3 || c == 6 || c == 7), g = (c >= 4);
+      const double N = cx[a] * cy[b] * cz[g];
+      const double Nx = dd[a] * cy[b] * cz[g], Ny = cx[a] * dd[b] * cz[g], Nz = cx[a] * cy[b] * dd[g];
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        const double vc = v[c * 3 + d];
+        F[d] += N * vc;
+        DF[d][0] += Nx * vc;
+        DF[d][1] += Ny * vc;
+        DF[d][2] += Nz * vc;
+      }
+    }
+    const double c00 = DF[1][1] * DF[2][2] - DF[1][2] * DF[2][1];
+    const double c01 = DF[1][2] * DF[2][0] - DF[1][0] * DF[2][2];
+    const double c02 = DF[1][0] * DF[2][1] - DF[1][1] * DF[2][0];
+    const double J = DF[0][0] * c00 + DF[0][1] * c01 + DF[0][2] * c02;
+    if (!(J > 0.0)) atomicAdd(bad, 1);
+    const double iJ = 1.0 / J;
+    double inv[3][3];
+    inv[0][0] = c00 * iJ;
+    inv[1][0] = c01 * iJ;
+    inv[2][0] = c02 * iJ;
+    inv[0][1] = (DF[0][2] * DF[2][1] - DF[0][1] * DF[2][2]) * iJ;
+    inv[1][1] = (DF[0][0] * DF[2][2] - DF[0][2] * DF[2][0]) * iJ;
+    inv[2][1] = (DF[0][1] * DF[2][0] - DF[0][0] * DF[2][1]) * iJ;
+    inv[0][2] = (DF[0][1] * DF[1][2] - DF[0][2] * DF[1][1]) * iJ;
+    inv[1][2] = (DF[0][2] * DF[1][0] - DF[0][0] * DF[1][2]) * iJ;
+    inv[2][2] = (DF[0][0] * DF[1][1] - DF[0][1] * DF[1][0]) * iJ;
+    const double jwq = J * w;
+    if (jw) jw[t] = jwq;
+    if (xq) { xq[3 * t] = F[0]; xq[3 * t + 1] = F[1]; xq[3 * t + 2] = F[2]; }
+    if (fac) {
+      const double s = jwq * mu[e];
+      const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+      for (int c = 0; c < 6; c++) {
+        const int a = ia[c], b = ib[c];
+        fac[6 * t + c] = s * (inv[a][0] * inv[b][0] + inv[a][1] * inv[b][1] + inv[a][2] * inv[b][2]);
+      }
+    }
+  }
+}
+
+}  // namespace mj
+
+using namespace mj;
+
+namespace {
+
+struct EdgeKey {
+  int a, b;
+  bool operator==(const EdgeKey& o) const { return a == o.a && b == o.b; }
+};
+struct EdgeHash {
+  size_t operator()(const EdgeKey& k) const { return std::hash<long long>()(((long long)k.a << 32) ^ (unsigned)k.b); }
+};
+struct FaceKey {
+  int a, b, c;  // origin corner, first-axis neighbour, second-axis neighbour (canonical)
+  bool operator==(const FaceKey& o) const { return a == o.a && b == o.b && c == o.c; }
+};
+struct FaceHash {
+  size_t operator()(const FaceKey& k) const {
+    size_t h = std::hash<long long>()(((long long)k.a << 32) ^ (unsigned)k.b);
+    return h ^ (std::hash<int>()(k.c) * 0x9e3779b97f4a7c15ULL);
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+int mj_number_hex_mesh(int order, int n_elt, int n_vert, const int32_t* hexes, int32_t* nodle_out, int* n_dof) {
+  MJ_CHECK_ARG(order >= 1 && order <= kMaxOrder, "mj_number_hex_mesh: order must be in [1, 8]");
+  MJ_CHECK_ARG(n_elt > 0 && n_vert > 0 && hexes && nodle_out && n_dof, "mj_number_hex_mesh: bad argument");
+  const int r = order, n = r + 1, Q = n * n * n, m = r - 1;
+  const std::vector<int> num = hex_local_numbering(r);
+  for (long long t = 0; t < 8LL * n_elt; t++)
+    MJ_CHECK_ARG(hexes[t] >= 0 && hexes[t] < n_vert, "mj_number_hex_mesh: vertex index out of range");
+  std::vector<int> vdof(n_vert, -1);
+  std::unordered_map<EdgeKey, int, EdgeHash> edges;
+  std::unordered_map<FaceKey, int, FaceHash> faces;
+  edges.reserve((size_t)n_elt * 3 + 16);
+  faces.reserve((size_t)n_elt * 3 + 16);
+  long long next = 0;
+  for (int e = 0; e < n_elt; e++) {
+    const int32_t* hv = hexes + 8LL * e;
+    auto gvert = [&](int ci, int cj, int ck) {  // global vertex at corner (ci,cj,ck) in {0,1}^3
+      for (int c = 0; c < 8; c++)
+        if (kCorner[c][0] == ci && kCorner[c][1] == cj && kCorner[c][2] == ck) return (int)hv[c];
+      return -1;
+    };
+    int32_t* out = nodle_out + (size_t)e * Q;
+    int interior_base = -1;
+    // Traverse the element's nodes in local-numbering order so dofs are
+    // numbered in first-touch order (vertices, edges, faces, interior).
+    std::vector<int> order_of(Q);
+    for (int i = 0; i < n; i++)
+      for (int j = 0; j < n; j++)
+        for (int k = 0; k < n; k++) order_of[num[(i * n + j) * n + k]] = (i * n + j) * n + k;
+    for (int ql = 0; ql < Q; ql++) {
+      const int lin = order_of[ql];
+      const int i = lin / (n * n), j = (lin / n) % n, k = lin % n;
+      const int c[3] = {i, j, k};
+      int nb = 0;
+      for (int d = 0; d < 3; d++) nb += (c[d] == 0 || c[d] == r);
+      int dof = -1;
+      if (nb == 3) {
+        const int g = gvert(i / r, j / r, k / r);
+        if (vdof[g] < 0) vdof[g] = (int)next++;
+        dof = vdof[g];
+      } else if (nb == 2) {
+        int ax = 0;
+        for (int d = 0; d < 3; d++)
+          if (c[d] != 0 && c[d] != r) ax = d;
+        int lo[3] = {c[0] / r, c[1] / r, c[2] / r}, hi[3] = {c[0] / r, c[1] / r, c[2] / r};
+        lo[ax] = 0;
+        hi[ax] = 1;
+        const int ga = gvert(lo[0], lo[1], lo[2]), gb = gvert(hi[0], hi[1], hi[2]);
+        const int l = c[ax];
+        EdgeKey key{std::min(ga, gb), std::max(ga, gb)};
+        const int lc = (ga < gb) ? l : r - l;
+        auto it = edges.find(key);
+        int base;
+        if (it == edges.end()) {
+          base = (int)next;
+          next += m;
+          edges.emplace(key, base);
+        } else {
+          base = it->second;
+        }
+        dof = base + (lc - 1);
+      } else if (nb == 1) {
+        int fx = 0;
+        for (int d = 0; d < 3; d++)
+          if (c[d] == 0 || c[d] == r) fx = d;
+        const int pa = (fx == 0) ? 1 : 0, qa = (fx == 2) ? 1 : 2;  // the two varying axes
+        const int side = c[fx] / r;
+        auto corner = [&](int sp, int sq) {
+          int cc[3];
+          cc[fx] = side;
+          cc[pa] = sp;
+          cc[qa] = sq;
+          return gvert(cc[0], cc[1], cc[2]);
+        };
+        const int g[2][2] = {{corner(0, 0), corner(0, 1)}, {corner(1, 0), corner(1, 1)}};
+        // canonical frame: origin = smallest vertex; first axis towards its
+        // smaller neighbour.
+        int os = 0, oq = 0;
+        for (int a = 0; a < 2; a++)
+          for (int b = 0; b < 2; b++)
+            if (g[a][b] < g[os][oq]) { os = a; oq = b; }
+        const int nP = g[1 - os][oq], nQ = g[os][1 - oq];
+        const bool swap = nQ < nP;  // first canonical axis is q
+        int p = c[pa], q = c[qa];
+        if (os) p = r - p;
+        if (oq) q = r - q;
+        int u = swap ? q : p, v = swap ? p : q;
+        FaceKey key{g[os][oq], swap ? nQ : nP, swap ? nP : nQ};
+        auto it = faces.find(key);
+        int base;
+        if (it == faces.end()) {
+          base = (int)next;
+          next += (long long)m * m;
+          faces.emplace(key, base);
+        } else {
+          base = it->second;
+        }
+        dof = base + (u - 1) * m + (v - 1);
+      } else {
+        if (interior_base < 0) {
+          interior_base = (int)next;
+          next += (long long)m * m * m;
+        }
+        dof = interior_base + ((i - 1) * m + (j - 1)) * m + (k - 1);
+      }
+      if (next > INT32_MAX) {
+        set_error("mj_number_hex_mesh: too many dofs for int32");
+        return MJ_ERR_ARG;
+      }
+      out[ql] = dof;
+    }
+  }
+  *n_dof = (int)next;
+  return MJ_OK;
+}
+
+int mj_geometry(int order, int n_elt, const double* verts, const double* mu, double* factors_out, double* jw_out,
+                double* positions_out) {
+  MJ_CHECK_ARG(order >= 1 && order <= kMaxOrder, "mj_geometry: order must be in [1, 8]");
+  MJ_CHECK_ARG(n_elt > 0 && verts, "mj_geometry: bad argument");
+  MJ_CHECK_ARG(!factors_out || mu, "mj_geometry: factors need mu");
+  const int r = order, n = r + 1, Q = n * n * n;
+  GeomParams P{};
+  P.n = n;
+  P.Q = Q;
+  gauss_lobatto(r, P.pts, P.wts);
+  const std::vector<int> num = hex_local_numbering(r);
+  std::vector<unsigned char> coord(Q * 3);
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++)
+      for (int k = 0; k < n; k++) {
+        const int q = num[(i * n + j) * n + k];
+        coord[3 * q] = (unsigned char)i;
+        coord[3 * q + 1] = (unsigned char)j;
+        coord[3 * q + 2] = (unsigned char)k;
+      }
+  MJ_CUDA(cudaMemcpyToSymbol(c_coord, coord.data(), coord.size()));
+  const size_t pts = (size_t)n_elt * Q;
+  DevBuf dv, dmu, dfac, djw, dxq, dbad;
+  MJ_CUDA(dv.alloc(sizeof(double) * 24 * n_elt));
+  MJ_CUDA(cudaMemcpy(dv.ptr, verts, sizeof(double) * 24 * n_elt, cudaMemcpyHostToDevice));
+  if (factors_out) {
+    MJ_CUDA(dmu.alloc(sizeof(double) * n_elt));
+    MJ_CUDA(cudaMemcpy(dmu.ptr, mu, sizeof(double) * n_elt, cudaMemcpyHostToDevice));
+    MJ_CUDA(dfac.alloc(sizeof(double) * 6 * pts));
+  }
+  if (jw_out) MJ_CUDA(djw.alloc(sizeof(double) * pts));
+  if (positions_out) MJ_CUDA(dxq.alloc(sizeof(double) * 3 * pts));
+  MJ_CUDA(dbad.alloc(sizeof(int)));
+  MJ_CUDA(cudaMemset(dbad.ptr, 0, sizeof(int)));
+  const int blocks = (int)std::min<size_t>((pts + 255) / 256, (size_t)sm_count() * 32);
+  k_geometry<<<blocks, 256>>>(dv.as<double>(), dmu.as<double>(), n_elt, P, dfac.as<double>(), djw.as<double>(),
+                              dxq.as<double>(), dbad.as<int>());
+  count_launch();
+  MJ_CUDA(cudaGetLastError());
+  int bad = 0;
+  MJ_CUDA(cudaMemcpy(&bad, dbad.ptr, sizeof(int), cudaMemcpyDeviceToHost));
+  if (factors_out) MJ_CUDA(cudaMemcpy(factors_out, dfac.ptr, sizeof(double) * 6 * pts, cudaMemcpyDeviceToHost));
+  if (jw_out) MJ_CUDA(cudaMemcpy(jw_out, djw.ptr, sizeof(double) * pts, cudaMemcpyDeviceToHost));
+  if (positions_out) MJ_CUDA(cudaMemcpy(positions_out, dxq.ptr, sizeof(double) * 3 * pts, cudaMemcpyDeviceToHost));
+  if (bad) {
+    set_error("mj_geometry: " + std::to_string(bad) + " quadrature points with non-positive Jacobian");
+    return MJ_ERR_GEOMETRY;
+  }
+  return MJ_OK;
+}
+
+int mj_lumped_mass(int order, int n_elt, int n_dof, const int32_t* nodle, const double* jw, const double* rho,
+                   double* mass_out) {
+  MJ_CHECK_ARG(order >= 1 && order <= kMaxOrder, "mj_lumped_mass: order must be in [1, 8]");
+  MJ_CHECK_ARG(n_elt > 0 && n_dof > 0 && nodle && jw && mass_out, "mj_lumped_mass: bad argument");
+  const int Q = (order + 1) * (order + 1) * (order + 1);
+  // Element-loop accumulation in the reference's order (AddMatrixWithBC over
+  // elements, then points), so sums round identically.
+  std::memset(mass_out, 0, sizeof(double) * n_dof);
+  for (int e = 0; e < n_elt; e++) {
+    const double re = rho ? rho[e] : 1.0;
+    for (int q = 0; q < Q; q++) {
+      const int d = nodle[(size_t)e * Q + q];
+      MJ_CHECK_ARG(d >= 0 && d < n_dof, "mj_lumped_mass: Nodle entry out of range");
+      mass_out[d] += re * jw[(size_t)e * Q + q];
+    }
+  }
+  return MJ_OK;
+}
+
+}  // extern "C"

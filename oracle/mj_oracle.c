@@ -1,0 +1,483 @@
+/*
+ * ORACLE - test infrastructure only.  Never linked into the product library.
+ *
+ * A plain-C, FP64 restatement of the reference's hot path for the scalar
+ * acoustic wave equation on mass-lumped Gauss-Lobatto Q_r hexahedra
+ * (Montjoie, marcdurufle33/Montjoie).  Each function cites the reference
+ * file:line it restates.  Parity is pinned by tests/golden fixtures produced
+ * by the reference itself (oracle/ref_dump.cc, tests/golden/make_golden.py).
+ *
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
+ * this library, always as the checker or the CPU baseline.
+ *
+ * Conventions (all from the reference):
+ *  - reference cube [0,1]^3, GL weights summing to 1
+ *    (MONTJOIE/src/Quadrature/GaussLobatto.cxx:27-45);
+ *  - G[a*n+b] = phi_a'(xi_b) (Globatto::ComputeGradPhi, GaussLobatto.cxx:175-191);
+ *  - local dof / quadrature index of (i,j,k) is num[(i*n+j)*n+k]
+ *    (HexahedronQuadrature.cxx:51-171), i along x;
+ *  - stiffness factor per point B = (J w) DF^-1 mu DF^-T, stored as the six
+ *    entries xx,xy,xz,yy,yz,zz (VarHelmholtz.cxx:95-123).
+ */
+#define _GNU_SOURCE
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define OC_MAXN 32   /* largest 1-D rule (the degree-24 pulse interpolation) */
+#define OC_MAXE 10   /* largest element order + 1 */
+
+/* ---------------------------------------------------------------- 1-D rule */
+
+/* Legendre P_r and its derivative at x in [-1,1] (three-term recurrence). */
+static void legendre(int r, double x, double* p, double* dp) {
+  double p0 = 1.0, p1 = x, dp0 = 0.0, dp1 = 1.0;
+  if (r == 0) { *p = 1.0; *dp = 0.0; return; }
+  for (int k = 1; k < r; k++) {
+    double p2 = ((2.0 * k + 1.0) * x * p1 - k * p0) / (k + 1.0);
+    double dp2 = dp0 + (2.0 * k + 1.0) * p1;
+    p0 = p1; p1 = p2; dp0 = dp1; dp1 = dp2;
+  }
+  *p = p1; *dp = dp1;
+}
+
+/* Gauss-Lobatto points and weights on [0,1], r+1 points
+ * (ComputeGaussLobatto, MONTJOIE/src/Quadrature/GaussJacobi.cxx:178-181):
+ * interior points are the roots of P_r', found by Newton iteration on
+ * (1-x^2) P_r'(x) from Chebyshev-Lobatto guesses; weights 2/(r(r+1)P_r^2)
+ * on [-1,1], halved on [0,1]. */
+void oc_gauss_lobatto(int r, double* pts, double* wts) {
+  int n = r + 1;
+  double x[OC_MAXN];
+  for (int i = 0; i < n; i++) x[i] = -cos(M_PI * i / r);
+  for (int i = 1; i < r; i++) {
+    for (int it = 0; it < 100; it++) {
+      /* f = P_r'(x); f' = P_r''(x) = (2x P_r' - r(r+1) P_r)/(1-x^2) */
+      double p, dp;
+      legendre(r, x[i], &p, &dp);
+      double d2p = (2.0 * x[i] * dp - r * (r + 1.0) * p) / (1.0 - x[i] * x[i]);
+      double dx = dp / d2p;
+      x[i] -= dx;
+      if (fabs(dx) < 1e-17) break;
+    }
+  }
+  for (int i = 0; i < n; i++) {
+    double p, dp;
+    legendre(r, x[i], &p, &dp);
+    pts[i] = 0.5 * (x[i] + 1.0);
+    wts[i] = 1.0 / (r * (r + 1.0) * p * p);
+  }
+  pts[0] = 0.0; pts[r] = 1.0;
+}
+
+/* Derivative matrix G[a*n+b] = phi_a'(x_b) of the Lagrange basis on the
+ * points, with the reference's barycentric formula and diagonal
+ * (Globatto::ComputeGradPhi, GaussLobatto.cxx:175-191): off-diagonal
+ * c_a / (c_b (x_b - x_a)), c_i = 1/prod_{j!=i}(x_i-x_j)
+ * (ComputeFactorPhi, GaussLobatto.cxx:95-106); diagonal = minus the sum of
+ * the others, zeroed when below 1e3*eps. */
+void oc_grad_matrix(int r, const double* pts, double* G) {
+  int n = r + 1;
+  double c[OC_MAXN];
+  for (int i = 0; i < n; i++) {
+    c[i] = 1.0;
+    for (int j = 0; j < n; j++)
+      if (j != i) c[i] *= pts[i] - pts[j];
+    c[i] = 1.0 / c[i];
+  }
+  for (int b = 0; b < n; b++) {
+    double sum = 0.0;
+    for (int a = 0; a < n; a++)
+      if (a != b) {
+        G[a * n + b] = c[a] / (c[b] * (pts[b] - pts[a]));
+        sum += G[a * n + b];
+      }
+    G[b * n + b] = -sum;
+    if (fabs(G[b * n + b]) <= 1e3 * 2.220446049250313e-16) G[b * n + b] = 0.0;
+  }
+}
+
+/* Lagrange basis values phi_a(x) on the points (product formula). */
+static void lagrange_values(int n, const double* pts, double x, double* phi) {
+  for (int a = 0; a < n; a++) {
+    double v = 1.0;
+    for (int b = 0; b < n; b++)
+      if (b != a) v *= (x - pts[b]) / (pts[a] - pts[b]);
+    phi[a] = v;
+  }
+}
+
+/* ----------------------------------------------------- local hex numbering */
+
+/* NumDofs3D of a Q_r hexahedron (HexahedronQuadrature::ConstructHexahedralNumbering,
+ * MONTJOIE/src/Quadrature/HexahedronQuadrature.cxx:51-171): the 8 vertices,
+ * then the r-1 nodes of the 12 edges (edge list GetEdgeCube, :41-47), the
+ * (r-1)^2 nodes of faces x=0, y=0, z=0, z=1, y=1, x=1, then the interior. */
+void oc_hex_numbering(int r, int* num) {
+  int n = r + 1;
+#define NUM(i, j, k) num[((i) * n + (j)) * n + (k)]
+  for (int t = 0; t < n * n * n; t++) num[t] = -1;
+  static const int corner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                                   {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+  static const int edge[12][2] = {{0, 1}, {1, 2}, {3, 2}, {0, 3}, {0, 4}, {1, 5},
+                                  {2, 6}, {3, 7}, {4, 5}, {5, 6}, {7, 6}, {4, 7}};
+  int node = 0;
+  for (int v = 0; v < 8; v++) NUM(corner[v][0] * r, corner[v][1] * r, corner[v][2] * r) = node++;
+  for (int e = 0; e < 12; e++) {
+    const int* a = corner[edge[e][0]];
+    const int* b = corner[edge[e][1]];
+    for (int l = 1; l < r; l++)
+      NUM((l * b[0] * r + (r - l) * a[0] * r) / r, (l * b[1] * r + (r - l) * a[1] * r) / r,
+          (l * b[2] * r + (r - l) * a[2] * r) / r) = node++;
+  }
+  for (int i = 1; i < r; i++) for (int j = 1; j < r; j++) NUM(0, i, j) = node++;
+  for (int i = 1; i < r; i++) for (int j = 1; j < r; j++) NUM(i, 0, j) = node++;
+  for (int i = 1; i < r; i++) for (int j = 1; j < r; j++) NUM(i, j, 0) = node++;
+  for (int i = 1; i < r; i++) for (int j = 1; j < r; j++) NUM(i, j, r) = node++;
+  for (int i = 1; i < r; i++) for (int j = 1; j < r; j++) NUM(i, r, j) = node++;
+  for (int i = 1; i < r; i++) for (int j = 1; j < r; j++) NUM(r, i, j) = node++;
+  for (int i = 1; i < r; i++) for (int j = 1; j < r; j++) for (int k = 1; k < r; k++) NUM(i, j, k) = node++;
+#undef NUM
+}
+
+/* ------------------------------------------------------------ geometry */
+
+/* Trilinear map of a hexahedron and its Jacobian matrix DF[d][a] = dF_d/dxi_a
+ * at reference point (x,y,z) (straight-sided hexahedron, vertex order of the
+ * reference cube). */
+static void trilinear(const double* v, double x, double y, double z, double* F, double DF[3][3]) {
+  const double cx[2] = {1.0 - x, x}, cy[2] = {1.0 - y, y}, cz[2] = {1.0 - z, z};
+  const double dx[2] = {-1.0, 1.0};
+  static const int corner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                                   {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+  for (int d = 0; d < 3; d++) {
+    F[d] = 0.0;
+    for (int a = 0; a < 3; a++) DF[d][a] = 0.0;
+  }
+  for (int c = 0; c < 8; c++) {
+    int a = corner[c][0], b = corner[c][1], g = corner[c][2];
+    double N = cx[a] * cy[b] * cz[g];
+    double Nx = dx[a] * cy[b] * cz[g], Ny = cx[a] * dx[b] * cz[g], Nz = cx[a] * cy[b] * dx[g];
+    for (int d = 0; d < 3; d++) {
+      F[d] += N * v[c * 3 + d];
+      DF[d][0] += Nx * v[c * 3 + d];
+      DF[d][1] += Ny * v[c * 3 + d];
+      DF[d][2] += Nz * v[c * 3 + d];
+    }
+  }
+}
+
+/* Geometric factors of every quadrature point
+ * (VarGeometryProblem::ComputeLocalMassMatrix, VarGeometryProblem.cxx:685-759,
+ *  then HelmholtzEquation_Base::ComputeMassMatrixGen, VarHelmholtz.cxx:54-131):
+ *   jw = det(DF) * w,   B = jw * DF^-1 * mu * DF^-T   (mu isotropic scalar),
+ *   xq = F(xi) physical position of the point.
+ * verts: ne x 8 x 3; mu: ne; outputs bh: ne x Q x 6, jw: ne x Q, xq: ne x Q x 3
+ * (any of the outputs may be NULL). Returns the number of non-positive
+ * Jacobians met. */
+int oc_geometry(int r, int ne, const double* verts, const double* mu, const int* num,
+                double* bh, double* jw, double* xq) {
+  int n = r + 1, Q = n * n * n, bad = 0;
+  double pts[OC_MAXN], wts[OC_MAXN];
+  oc_gauss_lobatto(r, pts, wts);
+#pragma omp parallel for reduction(+ : bad)
+  for (int e = 0; e < ne; e++) {
+    const double* v = verts + (size_t)e * 24;
+    for (int i = 0; i < n; i++)
+      for (int j = 0; j < n; j++)
+        for (int k = 0; k < n; k++) {
+          int q = num[(i * n + j) * n + k];
+          double F[3], DF[3][3];
+          trilinear(v, pts[i], pts[j], pts[k], F, DF);
+          double J = DF[0][0] * (DF[1][1] * DF[2][2] - DF[1][2] * DF[2][1]) -
+                     DF[0][1] * (DF[1][0] * DF[2][2] - DF[1][2] * DF[2][0]) +
+                     DF[0][2] * (DF[1][0] * DF[2][1] - DF[1][1] * DF[2][0]);
+          if (J <= 0.0) bad++;
+          double inv[3][3];
+          inv[0][0] = (DF[1][1] * DF[2][2] - DF[1][2] * DF[2][1]) / J;
+          inv[0][1] = (DF[0][2] * DF[2][1] - DF[0][1] * DF[2][2]) / J;
+          inv[0][2] = (DF[0][1] * DF[1][2] - DF[0][2] * DF[1][1]) / J;
+          inv[1][0] = (DF[1][2] * DF[2][0] - DF[1][0] * DF[2][2]) / J;
+          inv[1][1] = (DF[0][0] * DF[2][2] - DF[0][2] * DF[2][0]) / J;
+          inv[1][2] = (DF[0][2] * DF[1][0] - DF[0][0] * DF[1][2]) / J;
+          inv[2][0] = (DF[1][0] * DF[2][1] - DF[1][1] * DF[2][0]) / J;
+          inv[2][1] = (DF[0][1] * DF[2][0] - DF[0][0] * DF[2][1]) / J;
+          inv[2][2] = (DF[0][0] * DF[1][1] - DF[0][1] * DF[1][0]) / J;
+          double w = wts[i] * wts[j] * wts[k];
+          double jwq = J * w;
+          size_t o = (size_t)e * Q + q;
+          if (jw) jw[o] = jwq;
+          if (xq) { xq[3 * o] = F[0]; xq[3 * o + 1] = F[1]; xq[3 * o + 2] = F[2]; }
+          if (bh) {
+            double s = jwq * mu[e];
+            static const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
+            for (int t = 0; t < 6; t++) {
+              int a = ia[t], b = ib[t];
+              bh[6 * o + t] = s * (inv[a][0] * inv[b][0] + inv[a][1] * inv[b][1] + inv[a][2] * inv[b][2]);
+            }
+          }
+        }
+  }
+  return bad;
+}
+
+/* Lumped mass D_i = sum over (e,j) with Nodle(e,j) = i of rho_e * jw(e,j)
+ * (ContinuousMassMatrixAcoustic::Init, TimeAcoustic.cxx:889-965). */
+void oc_lumped_mass(int ne, int Q, int ndof, const int* nodle, const double* jw,
+                    const double* rho, double* D) {
+  memset(D, 0, sizeof(double) * (size_t)ndof);
+  for (int e = 0; e < ne; e++)
+    for (int j = 0; j < Q; j++) D[nodle[(size_t)e * Q + j]] += (rho ? rho[e] : 1.0) * jw[(size_t)e * Q + j];
+}
+
+/* ------------------------------------------------------------ operator */
+
+/* One element of MltAdd_ElementH1_Scalar (ProdMatVectScalarH1.cxx:256-668) for
+ * Laplace with variable coefficients: gather (NumberMap::GetLocalUnknownVector,
+ * NumberMap.cxx:661-699), gradient Vh = Rh^T Uh (HexahedronLobatto.cxx:257-281,
+ * Rh entries built in HexahedronGauss.cxx:244-368: dphi_{ijk}/dx at (l,j,k) is
+ * G[i][l], etc.), Vh(q) = B(q) Vh(q) (ProdMatVectScalarH1.cxx:468-481), Uh = Rh Vh
+ * (HexahedronLobatto.cxx:220-244), scatter-add alpha*Uh
+ * (NumberMap::AddLocalUnknownVector, NumberMap.cxx:745-777). */
+static void element_apply(int n, const int* num, const double* G, const int* nodle_e,
+                          const double* bh_e, double alpha, const double* x, double* y) {
+  double U[OC_MAXE * OC_MAXE * OC_MAXE];
+  double V[3][OC_MAXE * OC_MAXE * OC_MAXE];
+#define IX(i, j, k) (((i) * n + (j)) * n + (k))
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++)
+      for (int k = 0; k < n; k++) U[IX(i, j, k)] = x[nodle_e[num[IX(i, j, k)]]];
+  for (int l = 0; l < n; l++)
+    for (int m = 0; m < n; m++)
+      for (int p = 0; p < n; p++) {
+        double gx = 0.0, gy = 0.0, gz = 0.0;
+        for (int a = 0; a < n; a++) {
+          gx += G[a * n + l] * U[IX(a, m, p)];
+          gy += G[a * n + m] * U[IX(l, a, p)];
+          gz += G[a * n + p] * U[IX(l, m, a)];
+        }
+        const double* b = bh_e + 6 * num[IX(l, m, p)];
+        V[0][IX(l, m, p)] = b[0] * gx + b[1] * gy + b[2] * gz;
+        V[1][IX(l, m, p)] = b[1] * gx + b[3] * gy + b[4] * gz;
+        V[2][IX(l, m, p)] = b[2] * gx + b[4] * gy + b[5] * gz;
+      }
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++)
+      for (int k = 0; k < n; k++) {
+        double s = 0.0;
+        for (int a = 0; a < n; a++) {
+          s += G[i * n + a] * V[0][IX(a, j, k)];
+          s += G[j * n + a] * V[1][IX(i, a, k)];
+          s += G[k * n + a] * V[2][IX(i, j, a)];
+        }
+        y[nodle_e[num[IX(i, j, k)]]] += alpha * s;
+      }
+#undef IX
+}
+
+/* y = beta*y + alpha*A*x, A the positive stiffness operator
+ * (MltAddScalarH1, ProdMatVectScalarH1.cxx:679-727; beta scaling at :690-693).
+ * Serial element loop, or, when color_ptr is given, a loop over colours whose
+ * elements share no dof (parallel inside a colour). */
+void oc_stiffness_mltadd(int r, int ne, int ndof, const int* nodle, const int* num,
+                         const double* G, const double* bh, double alpha, const double* x,
+                         double beta, double* y, int ncolors, const int* color_ptr,
+                         const int* color_elems) {
+  int n = r + 1, Q = n * n * n;
+  if (beta == 0.0) memset(y, 0, sizeof(double) * (size_t)ndof);
+  else if (beta != 1.0)
+    for (int i = 0; i < ndof; i++) y[i] *= beta;
+  if (ncolors <= 0 || !color_ptr) {
+    for (int e = 0; e < ne; e++)
+      element_apply(n, num, G, nodle + (size_t)e * Q, bh + (size_t)e * Q * 6, alpha, x, y);
+    return;
+  }
+  for (int c = 0; c < ncolors; c++) {
+#pragma omp parallel for schedule(static)
+    for (int t = color_ptr[c]; t < color_ptr[c + 1]; t++) {
+      int e = color_elems[t];
+      element_apply(n, num, G, nodle + (size_t)e * Q, bh + (size_t)e * Q * 6, alpha, x, y);
+    }
+  }
+}
+
+/* ------------------------------------------------------------ sources */
+
+/* Primitive of the Ricker wavelet (TimeRickerSource::Evaluate,
+ * MONTJOIE/src/Source/TimeSource.cxx:33-50). */
+static double ricker_primitive(double f0, double t) {
+  double T0 = 1.0 / f0;
+  if (t <= -0.9 * T0 || t >= 2.9 * T0) return 0.0;
+  double tmp = f0 * t - 1.0;
+  return -tmp * exp(-tmp * tmp * M_PI * M_PI) / f0;
+}
+
+/* Pulse p(t_n + dt), n = 0..nsteps-1, as the time loop sees it
+ * (TimeSourceHyperbolic::Init/GenerateValues/EvaluateDerivative,
+ * TimeSource.cxx:798-880, with nb_deriv = 1 and order_interpolation = 24):
+ * the primitive is sampled at 25 GL points of the window [t0, t0 + 0.5/f0],
+ * differentiated with the GL derivative matrix, and the derivative is
+ * interpolated; the window jumps forward when t > t1 + eps_time.  No pulse
+ * at or after tlimit = 2.5/f0 (AddScalarSourceAtTime, VarInstationary.cxx:2392-2396). */
+void oc_ricker_pulse(double f0, double t_init, double dt, int nsteps, double eps_time,
+                     double tlimit, double* pulse) {
+  enum { R = 24, N = 25 };
+  double pts[N], wts[N], G[N * N], val[N], der[N], phi[N];
+  oc_gauss_lobatto(R, pts, wts);
+  oc_grad_matrix(R, pts, G);
+  double t0 = t_init, t1 = t_init + 0.5 / f0;
+  int have = 0;
+  for (int s = 0; s < nsteps; s++) {
+    double t = t_init + s * dt + dt;
+    if (t > t1 + eps_time && t1 > t0) {
+      while (t > t1 + eps_time) {
+        double tn = t1 + (t1 - t0);
+        t0 = t1; t1 = tn;
+      }
+      have = 0;
+    }
+    if (!have) {
+      for (int i = 0; i < N; i++) val[i] = ricker_primitive(f0, (1.0 - pts[i]) * t0 + pts[i] * t1);
+      for (int j = 0; j < N; j++) {
+        double acc = 0.0;
+        for (int k = 0; k < N; k++) acc += G[k * N + j] * val[k];
+        der[j] = acc * (1.0 / (t1 - t0));
+      }
+      have = 1;
+    }
+    lagrange_values(N, pts, (t - t0) / (t1 - t0), phi);
+    double p = 0.0;
+    for (int i = 0; i < N; i++) p += phi[i] * der[i];
+    pulse[s] = (t >= tlimit) ? 0.0 : p;
+  }
+}
+
+/* Gaussian amplitude g(x) = beta exp(-alpha r^2) for r < R, alpha = -ln(1e-6)/R^2,
+ * beta = sqrt(alpha/pi) (GaussianSource, MONTJOIE/src/Source/SourceSpatiale.cxx:33-90);
+ * F_i = sum over points (e,j) of jw * g(x_q) (lumped quadrature). */
+void oc_gaussian_source(int ne, int Q, int ndof, const int* nodle, const double* jw,
+                        const double* xq, const double* center, double radius, double* F) {
+  double alpha = -log(1e-6) / (radius * radius), beta = sqrt(alpha / M_PI);
+  memset(F, 0, sizeof(double) * (size_t)ndof);
+  for (int e = 0; e < ne; e++)
+    for (int j = 0; j < Q; j++) {
+      size_t o = (size_t)e * Q + j;
+      double dx = xq[3 * o] - center[0], dy = xq[3 * o + 1] - center[1], dz = xq[3 * o + 2] - center[2];
+      double rr = sqrt(dx * dx + dy * dy + dz * dz);
+      if (rr < radius) F[nodle[o]] += jw[o] * beta * exp(-alpha * rr * rr);
+    }
+}
+
+/* "Norme solution" sum_e sum_j jw(e,j) u(Nodle(e,j))^2, no square root
+ * (VarInstationary_Fem::GetNormeSolution, VarInstationary.cxx:2696-2745). */
+double oc_norm(int ne, int Q, const int* nodle, const double* jw, const double* u) {
+  double s = 0.0;
+  for (size_t o = 0; o < (size_t)ne * Q; o++) s += jw[o] * u[nodle[o]] * u[nodle[o]];
+  return s;
+}
+
+/* ------------------------------------------------------------ leap-frog */
+
+/* Order-2 leap-frog (ModifiedEquationIterator, MONTJOIE/src/Instationary/ModifiedEquation.cxx):
+ * start U0 = u0, U1 = U0 + dt*(du0 + dt/2 * invD*(-A U0)) (SetInitialConditionS :92-124;
+ * no damping, no source), then for n = 0..nsteps-1 (Advance :290-345):
+ *   Ah = -A U1;  Ah += p_n F;  Ah = dt^2 Ah - D U0;  Ah += 2 D U1;
+ *   U0 <- U1;   U1 <- invD Ah.
+ * On return u0 = U^{nsteps} (the iterate handed to GiveFinalIterate) and
+ * u1 = U^{nsteps+1}.  norms (nsteps+1 entries, may be NULL) receives the
+ * norm of the iterate given at each loop index and at the end; traces
+ * (nrec x (nsteps+1), may be NULL) receives sum_t W[k][t] u[idx[k][t]] of the
+ * same iterates, with Q weights per receiver. */
+void oc_leapfrog(int r, int ne, int ndof, const int* nodle, const int* num, const double* G,
+                 const double* bh, const double* D, const double* invD, int nsrc,
+                 const int* src_idx, const double* src_val, const double* pulse, double dt,
+                 int nsteps, double* u0, const double* du0, double* u1, const double* jw,
+                 double* norms, int nrec, const int* rec_idx, const double* rec_w, double* traces,
+                 int ncolors, const int* color_ptr, const int* color_elems) {
+  int n = r + 1, Q = n * n * n;
+  double dt2 = dt * dt;
+  double* ah = (double*)malloc(sizeof(double) * (size_t)ndof);
+  /* SetInitialConditionS */
+  oc_stiffness_mltadd(r, ne, ndof, nodle, num, G, bh, -1.0, u0, 0.0, ah, ncolors, color_ptr, color_elems);
+  for (int i = 0; i < ndof; i++) {
+    double v = ah[i] * invD[i];
+    v *= 0.5 * dt;
+    v += du0 ? du0[i] : 0.0;
+    v *= dt;
+    u1[i] = v + u0[i];
+  }
+  for (int s = 0; s <= nsteps; s++) {
+    if (norms) norms[s] = oc_norm(ne, Q, nodle, jw, u0);
+    if (traces)
+      for (int k = 0; k < nrec; k++) {
+        double acc = 0.0;
+        for (int t = 0; t < Q; t++) acc += rec_w[(size_t)k * Q + t] * u0[rec_idx[(size_t)k * Q + t]];
+        traces[(size_t)k * (nsteps + 1) + s] = acc;
+      }
+    if (s == nsteps) break;
+    oc_stiffness_mltadd(r, ne, ndof, nodle, num, G, bh, -1.0, u1, 0.0, ah, ncolors, color_ptr, color_elems);
+    double p = pulse ? pulse[s] : 0.0;
+    if (p != 0.0)
+      for (int t = 0; t < nsrc; t++) ah[src_idx[t]] += p * src_val[t];
+    for (int i = 0; i < ndof; i++) {
+      double a = dt2 * ah[i] - D[i] * u0[i];
+      a += 2.0 * D[i] * u1[i];
+      u0[i] = u1[i];
+      u1[i] = a * invD[i];
+    }
+  }
+  free(ah);
+}
+
+/* ------------------------------------------------------------ receivers */
+
+/* Interpolation weights of a point inside element e: invert the trilinear
+ * map by Newton iteration, then tensor Lagrange values at the local dofs
+ * (the role of SismoPoint interpolation, MONTJOIE/src/Output/GridInterpolation.cxx:836).
+ * w: Q weights in local dof order. Returns 0 when the point maps inside
+ * [0,1]^3 (within tol), 1 otherwise. */
+int oc_point_weights(int r, const double* verts_e, const int* num, const double* p, double* w,
+                     double* xi_out) {
+  int n = r + 1;
+  double pts[OC_MAXN], wts[OC_MAXN];
+  oc_gauss_lobatto(r, pts, wts);
+  double xi[3] = {0.5, 0.5, 0.5};
+  for (int it = 0; it < 50; it++) {
+    double F[3], DF[3][3];
+    trilinear(verts_e, xi[0], xi[1], xi[2], F, DF);
+    double res[3] = {p[0] - F[0], p[1] - F[1], p[2] - F[2]};
+    double J = DF[0][0] * (DF[1][1] * DF[2][2] - DF[1][2] * DF[2][1]) -
+               DF[0][1] * (DF[1][0] * DF[2][2] - DF[1][2] * DF[2][0]) +
+               DF[0][2] * (DF[1][0] * DF[2][1] - DF[1][1] * DF[2][0]);
+    double inv[3][3];
+    inv[0][0] = (DF[1][1] * DF[2][2] - DF[1][2] * DF[2][1]) / J;
+    inv[0][1] = (DF[0][2] * DF[2][1] - DF[0][1] * DF[2][2]) / J;
+    inv[0][2] = (DF[0][1] * DF[1][2] - DF[0][2] * DF[1][1]) / J;
+    inv[1][0] = (DF[1][2] * DF[2][0] - DF[1][0] * DF[2][2]) / J;
+    inv[1][1] = (DF[0][0] * DF[2][2] - DF[0][2] * DF[2][0]) / J;
+    inv[1][2] = (DF[0][2] * DF[1][0] - DF[0][0] * DF[1][2]) / J;
+    inv[2][0] = (DF[1][0] * DF[2][1] - DF[1][1] * DF[2][0]) / J;
+    inv[2][1] = (DF[0][1] * DF[2][0] - DF[0][0] * DF[2][1]) / J;
+    inv[2][2] = (DF[0][0] * DF[1][1] - DF[0][1] * DF[1][0]) / J;
+    double step = 0.0;
+    for (int a = 0; a < 3; a++) {
+      double d = inv[a][0] * res[0] + inv[a][1] * res[1] + inv[a][2] * res[2];
+      xi[a] += d;
+      step += fabs(d);
+    }
+    if (step < 1e-15) break;
+  }
+  double px[OC_MAXN], py[OC_MAXN], pz[OC_MAXN];
+  lagrange_values(n, pts, xi[0], px);
+  lagrange_values(n, pts, xi[1], py);
+  lagrange_values(n, pts, xi[2], pz);
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++)
+      for (int k = 0; k < n; k++) w[num[(i * n + j) * n + k]] = px[i] * py[j] * pz[k];
+  if (xi_out) { xi_out[0] = xi[0]; xi_out[1] = xi[1]; xi_out[2] = xi[2]; }
+  const double tol = 1e-10;
+  for (int a = 0; a < 3; a++)
+    if (xi[a] < -tol || xi[a] > 1.0 + tol) return 1;
+  return 0;
+}

@@ -1,0 +1,290 @@
+"""ORACLE - test infrastructure only (the product never imports this module).
+
+ctypes bindings to ``oracle/_build/liboracle.so`` (the plain-C FP64
+restatement of the reference's acoustic hot path, ``oracle/mj_oracle.c``) plus
+small numpy helpers.  Used by ``tests/``, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py`` as the checker, never as the measured path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+REF_DUMP = os.path.join(HERE, "_ref", "ref_dump")
+
+_lib = None
+
+_D = ctypes.POINTER(ctypes.c_double)
+_I = ctypes.POINTER(ctypes.c_int)
+
+
+def build(quiet: bool = True) -> str:
+    """Compile the C restatement (gcc) if needed; returns the library path."""
+    src = os.path.join(HERE, "mj_oracle.c")
+    if not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+        os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
+        subprocess.run(["gcc", "-std=c11", "-O2", "-fPIC", "-shared", "-fopenmp", "-o", LIB_PATH, src, "-lm"],
+                       check=True, capture_output=quiet)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB_PATH)
+        L.oc_gauss_lobatto.argtypes = [ctypes.c_int, _D, _D]
+        L.oc_grad_matrix.argtypes = [ctypes.c_int, _D, _D]
+        L.oc_hex_numbering.argtypes = [ctypes.c_int, _I]
+        L.oc_geometry.argtypes = [ctypes.c_int, ctypes.c_int, _D, _D, _I, _D, _D, _D]
+        L.oc_geometry.restype = ctypes.c_int
+        L.oc_lumped_mass.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _D, _D, _D]
+        L.oc_stiffness_mltadd.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _I, _D, _D,
+                                          ctypes.c_double, _D, ctypes.c_double, _D, ctypes.c_int, _I, _I]
+        L.oc_ricker_pulse.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                      ctypes.c_double, ctypes.c_double, _D]
+        L.oc_gaussian_source.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _D, _D, _D,
+                                         ctypes.c_double, _D]
+        L.oc_norm.argtypes = [ctypes.c_int, ctypes.c_int, _I, _D, _D]
+        L.oc_norm.restype = ctypes.c_double
+        L.oc_leapfrog.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _I, _D, _D, _D, _D,
+                                  ctypes.c_int, _I, _D, _D, ctypes.c_double, ctypes.c_int, _D, _D, _D,
+                                  _D, _D, ctypes.c_int, _I, _D, _D, ctypes.c_int, _I, _I]
+        L.oc_point_weights.argtypes = [ctypes.c_int, _D, _I, _D, _D, _D]
+        L.oc_point_weights.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _p(a, t=_D):
+    if a is None:
+        return ctypes.cast(None, t)
+    return a.ctypes.data_as(t)
+
+
+def f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+# ---------------------------------------------------------------- 1-D / local
+
+def gauss_lobatto(r: int):
+    pts, wts = np.zeros(r + 1), np.zeros(r + 1)
+    lib().oc_gauss_lobatto(r, _p(pts), _p(wts))
+    return pts, wts
+
+
+def grad_matrix(r: int):
+    pts, _ = gauss_lobatto(r)
+    G = np.zeros((r + 1) * (r + 1))
+    lib().oc_grad_matrix(r, _p(pts), _p(G))
+    return G.reshape(r + 1, r + 1)
+
+
+def hex_numbering(r: int):
+    num = np.zeros((r + 1) ** 3, dtype=np.int32)
+    lib().oc_hex_numbering(r, _p(num, _I))
+    return num
+
+
+# ---------------------------------------------------------------- setup
+
+def structured_nodle(n: int, r: int) -> np.ndarray:
+    """Lattice numbering of an n^3 structured cube: dof (I,J,K), I along x,
+    numbered (K*(rn+1)+J)*(rn+1)+I; rows in the reference local order."""
+    m = r * n + 1
+    num = hex_numbering(r).reshape(r + 1, r + 1, r + 1)
+    e = np.arange(n)
+    ez, ey, ex = np.meshgrid(e, e, e, indexing="ij")
+    ex, ey, ez = ex.ravel(), ey.ravel(), ez.ravel()
+    ii, jj, kk = np.meshgrid(np.arange(r + 1), np.arange(r + 1), np.arange(r + 1), indexing="ij")
+    nodle = np.zeros((n ** 3, (r + 1) ** 3), dtype=np.int32)
+    I = ex[:, None] * r + ii.ravel()[None, :]
+    J = ey[:, None] * r + jj.ravel()[None, :]
+    K = ez[:, None] * r + kk.ravel()[None, :]
+    nodle[:, num.ravel()] = ((K * m + J) * m + I)
+    return nodle
+
+
+def structured_colors(n: int):
+    """8-colouring of an n^3 structured cube (parity of the element indices)."""
+    e = np.arange(n)
+    ez, ey, ex = np.meshgrid(e, e, e, indexing="ij")
+    col = ((ex % 2) + 2 * (ey % 2) + 4 * (ez % 2)).ravel()
+    order = np.argsort(col, kind="stable").astype(np.int32)
+    ptr = np.searchsorted(col[order], np.arange(9)).astype(np.int32)
+    return ptr, order
+
+
+def geometry(r: int, verts_e: np.ndarray, mu: np.ndarray):
+    """Per-point stiffness factors (ne,Q,6), J*w (ne,Q) and positions (ne,Q,3)."""
+    ne = verts_e.shape[0]
+    Q = (r + 1) ** 3
+    num = hex_numbering(r)
+    bh, jw, xq = np.zeros((ne, Q, 6)), np.zeros((ne, Q)), np.zeros((ne, Q, 3))
+    bad = lib().oc_geometry(r, ne, _p(f64(verts_e)), _p(f64(mu)), _p(num, _I), _p(bh), _p(jw), _p(xq))
+    if bad:
+        raise ValueError(f"{bad} non-positive Jacobians")
+    return bh, jw, xq
+
+
+def lumped_mass(nodle, jw, ndof, rho=None):
+    ne, Q = nodle.shape
+    D = np.zeros(ndof)
+    lib().oc_lumped_mass(ne, Q, ndof, _p(i32(nodle), _I), _p(f64(jw)),
+                         _p(None if rho is None else f64(rho)), _p(D))
+    return D
+
+
+def stiffness_mltadd(r, nodle, bh, alpha, x, beta, y, colors=None):
+    """y <- beta*y + alpha*A*x in place (FP64)."""
+    ne, Q = nodle.shape
+    G = grad_matrix(r).ravel().copy()
+    num = hex_numbering(r)
+    assert y.dtype == np.float64 and y.flags.c_contiguous
+    ptr, elems = (None, None) if colors is None else colors
+    nc = 0 if colors is None else len(ptr) - 1
+    lib().oc_stiffness_mltadd(r, ne, y.size, _p(i32(nodle), _I), _p(num, _I), _p(G), _p(f64(bh)),
+                              float(alpha), _p(f64(x)), float(beta), _p(y), nc,
+                              _p(None if ptr is None else i32(ptr), _I),
+                              _p(None if elems is None else i32(elems), _I))
+    return y
+
+
+def ricker_pulse(f0, t_init, dt, nsteps, eps_time, tlimit=None):
+    if tlimit is None:
+        tlimit = 2.5 / f0
+    out = np.zeros(nsteps)
+    lib().oc_ricker_pulse(float(f0), float(t_init), float(dt), int(nsteps), float(eps_time), float(tlimit), _p(out))
+    return out
+
+
+def gaussian_source(nodle, jw, xq, ndof, center, radius):
+    ne, Q = nodle.shape
+    F = np.zeros(ndof)
+    lib().oc_gaussian_source(ne, Q, ndof, _p(i32(nodle), _I), _p(f64(jw)), _p(f64(xq)),
+                             _p(f64(center)), float(radius), _p(F))
+    return F
+
+
+def norm(nodle, jw, u):
+    ne, Q = nodle.shape
+    return lib().oc_norm(ne, Q, _p(i32(nodle), _I), _p(f64(jw)), _p(f64(u)))
+
+
+def point_weights(r, verts_e, p):
+    Q = (r + 1) ** 3
+    w = np.zeros(Q)
+    xi = np.zeros(3)
+    out = lib().oc_point_weights(r, _p(f64(verts_e)), _p(hex_numbering(r), _I), _p(f64(p)), _p(w), _p(xi))
+    return w, xi, out == 0
+
+
+def leapfrog(r, nodle, bh, D, invD, src_idx, src_val, pulse, dt, nsteps, u0, u1=None, du0=None,
+             jw=None, rec_idx=None, rec_w=None, colors=None):
+    """Run the reference's order-2 leap-frog on the CPU. Returns (u_N, u_{N+1}, norms, traces)."""
+    ne, Q = nodle.shape
+    ndof = D.size
+    G = grad_matrix(r).ravel().copy()
+    num = hex_numbering(r)
+    u0 = f64(u0).copy()
+    u1 = np.zeros(ndof)
+    norms = np.zeros(nsteps + 1) if jw is not None else None
+    nrec = 0 if rec_idx is None else rec_idx.shape[0]
+    traces = np.zeros((nrec, nsteps + 1)) if nrec else None
+    ptr, elems = (None, None) if colors is None else colors
+    nc = 0 if colors is None else len(ptr) - 1
+    lib().oc_leapfrog(r, ne, ndof, _p(i32(nodle), _I), _p(num, _I), _p(G), _p(f64(bh)), _p(f64(D)), _p(f64(invD)),
+                      int(len(src_idx)), _p(i32(src_idx), _I), _p(f64(src_val)), _p(f64(pulse)), float(dt),
+                      int(nsteps), _p(u0), _p(None if du0 is None else f64(du0)), _p(u1),
+                      _p(None if jw is None else f64(jw)), _p(norms), nrec,
+                      _p(None if rec_idx is None else i32(rec_idx), _I), _p(None if rec_w is None else f64(rec_w)),
+                      _p(traces), nc, _p(None if ptr is None else i32(ptr), _I),
+                      _p(None if elems is None else i32(elems), _I))
+    return u0, u1, norms, traces
+
+
+def power_iteration_lambda_max(r, nodle, bh, invD, iters=200, seed=0, colors=None):
+    """Largest eigenvalue of D^-1 A by power iteration (the reference needs
+    ARPACK/SLEPc for TimeStep = AUTO; an explicit dt is passed instead)."""
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(-1.0, 1.0, invD.size)
+    y = np.zeros_like(x)
+    lam = 0.0
+    for _ in range(iters):
+        stiffness_mltadd(r, nodle, bh, 1.0, x, 0.0, y, colors)
+        y *= invD
+        lam = float(np.linalg.norm(y) / np.linalg.norm(x))
+        x = y / np.linalg.norm(y)
+    return lam
+
+
+# ---------------------------------------------------------------- reference runs
+
+def run_reference(deck: str, outdir: str, x=None, y0=None, alpha=1.0, beta=0.0, snaps=(), norms=True,
+                  timeout=3600):
+    """Run the reference's own solver (oracle/_ref/ref_dump) on a deck and load its dumps."""
+    os.makedirs(outdir, exist_ok=True)
+    cmd = [REF_DUMP, deck, outdir]
+    if x is not None:
+        f64(x).tofile(os.path.join(outdir, "in_x.f64"))
+        cmd += ["--x", os.path.join(outdir, "in_x.f64"), "--alpha", repr(float(alpha)), "--beta", repr(float(beta))]
+        if y0 is not None:
+            f64(y0).tofile(os.path.join(outdir, "in_y0.f64"))
+            cmd += ["--y0", os.path.join(outdir, "in_y0.f64")]
+    if snaps:
+        cmd += ["--snaps", ",".join(str(s) for s in snaps)]
+    if not norms:
+        cmd += ["--no-norms"]
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    res = subprocess.run(cmd, cwd=outdir, capture_output=True, text=True, timeout=timeout, env=env)
+    if res.returncode != 0:
+        raise RuntimeError(f"reference run failed ({res.returncode}):\n{res.stdout[-3000:]}\n{res.stderr[-3000:]}")
+    return load_dump(outdir)
+
+
+def load_dump(outdir: str) -> dict:
+    meta = {}
+    with open(os.path.join(outdir, "meta.txt")) as f:
+        for line in f:
+            k, v = line.split()
+            meta[k] = float(v) if any(c in v for c in ".eE") else int(v)
+    out = {"meta": meta}
+    ne, Q, ndof, r = meta["n_elt"], meta["nq"], meta["n_dof"], meta["order"]
+    shapes = {
+        "nodle.i32": (ne, Q), "verts.f64": (ne, 8, 3), "elem_ref.i32": (ne,), "affine.i32": (ne,),
+        "variable.i32": (ne,), "bh.f64": (ne, Q, 6), "jw.f64": (ne, Q), "massD.f64": (ndof,),
+        "invD.f64": (ndof,), "src_idx.i32": (-1,), "src_val.f64": (-1,), "pulse.f64": (-1,),
+        "points1d.f64": (r + 1,), "weights1d.f64": (r + 1,), "gradphi.f64": (r + 1, r + 1),
+        "numdofs3d.i32": ((r + 1) ** 3,), "kh_y.f64": (ndof,), "kh_ax.f64": (ndof,),
+        "norms.f64": (-1,), "times.f64": (-1,), "u_final.f64": (ndof,),
+    }
+    for name, shp in shapes.items():
+        p = os.path.join(outdir, name)
+        if os.path.exists(p):
+            dt = np.int32 if name.endswith(".i32") else np.float64
+            out[name.split(".")[0]] = np.fromfile(p, dtype=dt).reshape(shp)
+    # The final iterate reaches the GiveIterate hook twice (GiveFinalIterate
+    # forwards to GiveIterate): keep one record per iterate.
+    if "times" in out and len(out["times"]) >= 2 and out["times"][-1] == out["times"][-2]:
+        out["times"] = out["times"][:-1]
+        out["norms"] = out["norms"][:-1]
+    snaps = {}
+    for fn in sorted(os.listdir(outdir)):
+        if fn.startswith("u_") and fn[2:8].isdigit():
+            snaps[int(fn[2:8])] = np.fromfile(os.path.join(outdir, fn), dtype=np.float64)
+    out["snaps"] = snaps
+    run = os.path.join(outdir, "run.txt")
+    if os.path.exists(run):
+        with open(run) as f:
+            out["run"] = {l.split()[0]: float(l.split()[1]) for l in f if l.strip()}
+    return out
