@@ -1,0 +1,365 @@
+#!/usr/bin/env python
+"""Benchmark: DOF-updates/s of the Q4 hexahedral acoustic leap-frog on one GB300.
+
+Workload (BASELINE configuration 2): unit cube, 64^3 hexahedra, vertices
+perturbed uniformly by +-5% h (seeded), Q4 Gauss-Lobatto, c piecewise
+constant on 8^3 random blocks in [1,3], Ricker f0 = 5 at the centre (Gaussian
+R = 2h), Neumann, dt = 0.5 CFL.  One bench step = one leap-frog time step over
+all 16,974,593 dofs.  ``value`` is the FP32 chosen form with everything
+resident in HBM; the FP64 plain form is timed beside it; ``e2e`` is the whole
+run through the C ABI (``mj_lf_run``) with host buffers.  The CPU baseline is
+the oracle's C restatement on the host cores.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--cells 64] [--order 4]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DOF-updates/s (Q4/Q8 hex acoustic leap-frog), FP32 vs FP64 at stated L2 error"
+UNIT = "DOF-updates/s"
+SEED = 20251203
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cells", type=int, default=64)
+    ap.add_argument("--order", type=int, default=4)
+    ap.add_argument("--fp64-steps", type=int, default=200)
+    ap.add_argument("--error-steps", type=int, default=1000)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def workload_mesh(cells):
+    from montjoie_gb300 import mesh as M
+    return M.perturbed_cube(cells, seed=SEED, amplitude=0.05, kind="random", c_mode="blocks", c_blocks=8)
+
+
+def workload_name(cells, order):
+    return (f"unit cube {cells}^3 hex Q{order}, +-5% h random vertex perturbation, c on 8^3 random blocks in [1,3], "
+            f"Ricker f0=5 Gaussian R=2h at centre, Neumann, leap-frog dt=0.5 CFL")
+
+
+def receivers():
+    return np.random.default_rng(SEED + 3).uniform(0.1, 0.9, size=(8, 3))
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic_per_element(name):
+    """DRAM bytes per element of the element kernel from a committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.strip().startswith("dram_bytes_per_element"):
+            return float(line.split("=")[1].split()[0])
+    return None
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.2)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i] and "Not" not in r[5 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def build_problem(cells, order, nsteps):
+    from montjoie_gb300 import mesh as M
+    from montjoie_gb300.problem import AcousticProblem, cfl_time_step
+    m = workload_mesh(cells)
+    s = M.AcousticSetup(order=order, dt=1.0, nsteps=nsteps, src_radius=2.0 / cells)
+    pb = AcousticProblem(m, s, receivers=receivers(), defer_time=True)
+    dt = cfl_time_step(pb, safety=0.5)
+    pb.set_time_step(dt, nsteps)
+    return pb
+
+
+def time_advance(torch, lf, steps, lib):
+    """Times `steps` leap-frog steps (already initialised) with CUDA events on the
+    library's stream (the legacy default stream)."""
+    L = lib.load()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    L.mj_lf_profile(lf.handle, 1, None, None, None)
+    l0 = lib.kernel_launches()
+    start.record()
+    lf.Advance(steps)
+    end.record()
+    torch.cuda.synchronize()
+    launches = lib.kernel_launches() - l0
+    import ctypes
+    e_ms, u_ms, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+    L.mj_lf_profile(lf.handle, 0, ctypes.byref(e_ms), ctypes.byref(u_ms), ctypes.byref(n))
+    return start.elapsed_time(end), e_ms.value / max(1, n.value), u_ms.value / max(1, n.value), launches
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    from montjoie_gb300 import _lib
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    _lib.load(build_if_missing=False)
+    K, W = args.steps, args.warmup
+    nsteps_pulse = max(K + W, args.error_steps) + 10
+    t_setup = time.perf_counter()
+    pb = build_problem(args.cells, args.order, nsteps_pulse)
+    setup_s = time.perf_counter() - t_setup
+    n_dof, n_elt, Q = pb.n_dof, pb.nodle.shape[0], (args.order + 1) ** 3
+    zeros = np.zeros(n_dof)
+
+    # ---- FP32 chosen form, resident (value)
+    op32 = pb.operator("fp32")
+    lf32 = pb.integrator(op32, diagnostics=False)
+    lf32.SetInitialConditionS(zeros)
+    lf32.Advance(W)
+    clocks = ClockSampler(local)
+    clocks.start()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ms32, k1_ms, k2_ms, launches = time_advance(torch, lf32, K, _lib)
+    # ---- FP64 plain form, resident
+    op64 = pb.operator("fp64")
+    lf64 = pb.integrator(op64, diagnostics=False)
+    lf64.SetInitialConditionS(zeros)
+    lf64.Advance(min(W, 3))
+    K64 = min(K, args.fp64_steps)
+    ms64, k1_64, k2_64, _ = time_advance(torch, lf64, K64, _lib)
+    clk = clocks.stop()
+    if world > 1:
+        t = torch.tensor([ms32], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms32 = float(t.item())
+    value = n_dof * K * world / (ms32 / 1e3)
+    value64 = n_dof * K64 / (ms64 / 1e3)
+    lf32.close(); lf64.close()
+
+    # ---- error of the FP32 form against the FP64 form (same run, error_steps steps)
+    lf64d = pb.integrator(op64, diagnostics=True)
+    u64, n64, tr64 = lf64d.Run(zeros, None, args.error_steps)
+    lf64d.close()
+    e2e = None
+    lf32d = pb.integrator(op32, diagnostics=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    u32, n32, tr32 = lf32d.Run(zeros, None, args.error_steps)
+    e2e_s = time.perf_counter() - t0
+    lf32d.close()
+    err = {"steps": args.error_steps,
+           "u_rel_l2": float(np.linalg.norm(u32 - u64) / max(np.linalg.norm(u64), 1e-300)),
+           "norm_history_rel_l2": float(np.linalg.norm(n32 - n64) / max(np.linalg.norm(n64), 1e-300)),
+           "traces_rel_max": float(np.abs(tr32 - tr64).max() / max(np.abs(tr64).max(), 1e-300)),
+           "reference": "FP64 plain GPU path (parity-pinned to the reference solver)"}
+    if not args.no_e2e:
+        h2d = n_dof * 8  # u0 (du0 = NULL)
+        d2h = n_dof * 8 + 8 * (args.error_steps + 1) * (1 + 8)  # u_final, norms, 8 traces
+        e2e = {"value": n_dof * args.error_steps / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": h2d / args.error_steps, "d2h_bytes_per_step": d2h / args.error_steps,
+               "call": "mj_lf_run: host u0 in, FP32 run with norm and 8 receiver traces every step, host u out",
+               "seconds": e2e_s}
+
+    # ---- roofline of the dominant kernel (element kernel, FP32)
+    peak, peak_kind = measured_peaks()
+    bytes_k1 = n_elt * Q * (6 * 4 + 4) + n_dof * 4   # factors + connectivity + input state, read once
+    achieved = bytes_k1 / (k1_ms / 1e3) / 1e9
+    per_elt = ncu_traffic_per_element(f"k_local_stiffness_fp32_q{args.order}.md")
+    step_bytes = n_elt * Q * (6 * 4 + 4) + n_dof * (3 * 4 + 4)
+    roofline = {"bound": "hbm", "kernel": "k_local_stiffness<float,5,5> (element kernel)",
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s",
+                "traffic": None if per_elt is None else per_elt * n_elt,
+                "algorithmic_bytes_per_launch": bytes_k1,
+                "kernel_ms": k1_ms, "update_kernel_ms": k2_ms,
+                "step_frac": (step_bytes / (ms32 / K / 1e3) / 1e9) / peak,
+                "step_algorithmic_bytes": step_bytes}
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+           "ms_per_step": ms32 / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32", "data": "synthetic (seeded perturbed mesh and media, BASELINE configuration 2 shapes)",
+           "config": {"workload": workload_name(args.cells, args.order), "cells": args.cells, "order": args.order,
+                      "n_dof": n_dof, "n_elt": n_elt, "dt": pb.setup.dt, "parallelism": f"replicas x{world}",
+                      "l2_flush": "inputs larger than L2 (factors alone %.2f GB)" % (n_elt * Q * 24 / 1e9),
+                      "setup_seconds": setup_s},
+           "fp64": {"value": value64, "ms_per_step": ms64 / K64, "steps": K64, "elem_kernel_ms": k1_64,
+                    "update_kernel_ms": k2_64, "fp32_over_fp64": value / world / value64},
+           "error_fp32_vs_fp64": err,
+           "roofline": roofline, "clocks": clk, "gpu_launches": launches, "e2e": e2e}
+    if rank == 0 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(args, pb, u_check=None)
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def cpu_baseline(args, pb=None, u_check=None, seconds=None):
+    """The oracle's C restatement (element loop in the reference's order,
+    colour-parallel over the host cores) on a bounded sample of the workload:
+    whole leap-frog steps of the same mesh."""
+    from oracle import oracle as oc
+    seconds = args.cpu_seconds if seconds is None else seconds
+    cells, order = args.cells, args.order
+    if pb is None:
+        m = workload_mesh(cells)
+        nodle = oc.structured_nodle(cells, order)
+        verts_e = m.verts[m.hexes]
+        bh, jw, xq = oc.geometry(order, verts_e, m.elem_c ** 2)
+        ndof = (cells * order + 1) ** 3
+        D = oc.lumped_mass(nodle, jw, ndof)
+        dt = 1e-4
+    else:
+        nodle, bh, D, ndof, dt = pb.nodle, pb.factors, pb.mass, pb.n_dof, pb.setup.dt
+    colors = oc.structured_colors(cells)
+    invD = 1.0 / D
+    u0 = np.zeros(ndof)
+    empty_i, empty_d = np.zeros(0, dtype=np.int32), np.zeros(0)
+    t0 = time.perf_counter()
+    oc.leapfrog(order, nodle, bh, D, invD, empty_i, empty_d, None, dt, 1, u0, colors=colors)
+    t1 = time.perf_counter() - t0
+    steps = int(max(1, min(500, seconds / max(t1, 1e-6))))
+    t0 = time.perf_counter()
+    oc.leapfrog(order, nodle, bh, D, invD, empty_i, empty_d, None, dt, steps, u0, colors=colors)
+    el = time.perf_counter() - t0
+    # per step: (steps + 1) operator applications (initial step + steps)
+    return {"value": ndof * steps / el, "unit": UNIT, "cores": cpu_threads(), "kind": "port",
+            "sample": f"{steps} FP64 leap-frog steps of the same {cells}^3 Q{order} mesh ({ndof} dofs), "
+                      f"oracle C restatement, colour-parallel OpenMP, {el:.1f} s",
+            "seconds": el}
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as oc
+    oc.build()
+    K, W = args.steps, args.warmup
+    cells, order = args.cells, args.order
+    m = workload_mesh(cells)
+    nodle = oc.structured_nodle(cells, order)
+    bh, jw, xq = oc.geometry(order, m.verts[m.hexes], m.elem_c ** 2)
+    ndof = (cells * order + 1) ** 3
+    D = oc.lumped_mass(nodle, jw, ndof)
+    invD = 1.0 / D
+    colors = oc.structured_colors(cells)
+    dt = 0.5 * 2.0 / np.sqrt(1.02 * oc.power_iteration_lambda_max(order, nodle, bh, invD, iters=8, colors=colors))
+    u0 = np.zeros(ndof)
+    ei, ed = np.zeros(0, dtype=np.int32), np.zeros(0)
+    oc.leapfrog(order, nodle, bh, D, invD, ei, ed, None, dt, max(1, min(W, 3)), u0, colors=colors)
+    budget = 120.0
+    t0 = time.perf_counter()
+    done = 0
+    chunk = 1
+    while done < K:
+        c = min(chunk, K - done)
+        oc.leapfrog(order, nodle, bh, D, invD, ei, ed, None, dt, c, u0, colors=colors)
+        done += c
+        el = time.perf_counter() - t0
+        if el > budget:
+            break
+        chunk = min(2 * chunk, 64)
+    el = time.perf_counter() - t0
+    value = ndof * done / el
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": done,
+           "requested_steps": K, "warmup": W, "ms_per_step": el / done * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": workload_name(cells, order), "cells": cells, "order": order, "n_dof": ndof,
+                      "parallelism": "host cores"},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu_threads(), "kind": "port",
+                            "sample": f"{done} FP64 leap-frog steps of the {cells}^3 Q{order} mesh (time-capped "
+                                      f"at {budget:.0f} s), oracle C restatement of the reference loop, "
+                                      f"colour-parallel OpenMP"},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -153,6 +153,14 @@ int mj_lf_run(mj_lf* lf, const double* u0, const double* du0, int nsteps, double
  * current U^n and U^{n+1} buffers (operator precision) and the step counter. */
 int mj_lf_device_state(mj_lf* lf, void** u_n, void** u_np1, int* step);
 
+/* Per-kernel device time of the steps run by mj_lf_advance / mj_lf_run while
+ * enabled (CUDA events on the integrator's stream around the element kernel
+ * and the gather/update kernel; the first 1024 steps of each call are timed).
+ * enable = 1 resets the totals and starts timing, 0 stops it; the current
+ * totals are returned in every case.  No reference counterpart (the
+ * reference's phase timers, MONTJOIE/src/Share/Timer.hxx:14-23, play this role). */
+int mj_lf_profile(mj_lf* lf, int enable, double* elem_ms, double* update_ms, int* steps);
+
 /* Sets the CUDA stream (cudaStream_t) used by the integrator's launches. */
 int mj_lf_set_stream(mj_lf* lf, void* stream);
 

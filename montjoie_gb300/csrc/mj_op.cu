@@ -42,18 +42,18 @@ __global__ void k_norm_final(const double* __restrict__ partial, int nparts, dou
 }
 
 // Elements per tile for each n = r+1 (threads per CTA = E*n*n).
-static int tile_elems(int n) {
-  switch (n) {
-    case 2: return 32;   // 128 threads
-    case 3: return 14;   // 126
-    case 4: return 8;    // 128
-    case 5: return 5;    // 125
-    case 6: return 4;    // 144
-    case 7: return 3;    // 147
-    case 8: return 2;    // 128
-    case 9: return 2;    // 162
-    default: return 1;
-  }
+constexpr int tile_elems_for(int n) {
+  return n == 2 ? 32 : n == 3 ? 14 : n == 4 ? 8 : n == 5 ? 5 : n == 6 ? 4 : n == 7 ? 3 : n == 8 ? 2 : n == 9 ? 2 : 1;
+}
+static int tile_elems(int n) { return tile_elems_for(n); }
+
+template <typename Real>
+__global__ void k_cast_from_f64(const double* __restrict__ a, Real* __restrict__ b, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = Real(a[i]);
+}
+template <typename Real>
+__global__ void k_cast_to_f64(const Real* __restrict__ a, double* __restrict__ b, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = double(a[i]);
 }
 
 }  // namespace mj
@@ -95,6 +95,15 @@ struct mj_lf {
   bool cur_is_a = true;
   cudaStream_t stream = nullptr;
   int norm_blocks = 0;
+  // optional per-kernel timing (CUDA events around the two kernels of a step)
+  bool profile = false;
+  std::vector<cudaEvent_t> ev;
+  int ev_used = 0;
+  double prof_elem_ms = 0.0, prof_update_ms = 0.0;
+  int prof_steps = 0;
+  ~mj_lf() {
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+  }
   void* cur() { return cur_is_a ? ua.ptr : ub.ptr; }
   void* next() { return cur_is_a ? ub.ptr : ua.ptr; }
 };
@@ -105,19 +114,9 @@ template <typename Real, int N>
 void launch_k1_n(mj_op* op, const void* x, cudaStream_t s) {
   GMatrix<Real, N> G;
   for (int a = 0; a < N * N; a++) G.g[a] = Real(op->gradphi[a]);
-  constexpr int NN = N * N;
-  switch (op->E) {
-#define MJ_K1_CASE(EV)                                                                          \
-  case EV:                                                                                      \
-    k_local_stiffness<Real, N, EV><<<op->grid_k1, EV * NN, 0, s>>>(                             \
-        static_cast<const Real*>(x), op->nodle_t.as<int>(), op->fac_t.as<Real>(),               \
-        op->R.as<Real>(), op->n_tiles, G);                                                      \
-    break;
-    MJ_K1_CASE(1) MJ_K1_CASE(2) MJ_K1_CASE(3) MJ_K1_CASE(4) MJ_K1_CASE(5)
-    MJ_K1_CASE(8) MJ_K1_CASE(14) MJ_K1_CASE(32)
-#undef MJ_K1_CASE
-    default: break;
-  }
+  constexpr int E = tile_elems_for(N);
+  k_local_stiffness<Real, N, E><<<op->grid_k1, E * N * N, 0, s>>>(
+      static_cast<const Real*>(x), op->nodle_t.as<int>(), op->fac_t.as<Real>(), op->R.as<Real>(), op->n_tiles, G);
   count_launch();
 }
 
@@ -137,34 +136,26 @@ void launch_k1(mj_op* op, const void* x, cudaStream_t s) {
 
 // Occupancy-sized persistent grid for K1.
 template <typename Real, int N>
-int k1_grid_n(int E, int n_tiles) {
+int k1_grid_n(int n_tiles) {
   int per_sm = 1;
-  constexpr int NN = N * N;
-  switch (E) {
-#define MJ_OCC(EV)                                                                              \
-  case EV:                                                                                      \
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_local_stiffness<Real, N, EV>,      \
-                                                  EV * NN, 0);                                  \
-    break;
-    MJ_OCC(1) MJ_OCC(2) MJ_OCC(3) MJ_OCC(4) MJ_OCC(5) MJ_OCC(8) MJ_OCC(14) MJ_OCC(32)
-#undef MJ_OCC
-  }
+  constexpr int E = tile_elems_for(N);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_local_stiffness<Real, N, E>, E * N * N, 0);
   if (per_sm < 1) per_sm = 1;
   long g = (long)per_sm * sm_count();
   return (int)std::max(1L, std::min<long>(g, n_tiles));
 }
 
 template <typename Real>
-int k1_grid(int n, int E, int n_tiles) {
+int k1_grid(int n, int n_tiles) {
   switch (n) {
-    case 2: return k1_grid_n<Real, 2>(E, n_tiles);
-    case 3: return k1_grid_n<Real, 3>(E, n_tiles);
-    case 4: return k1_grid_n<Real, 4>(E, n_tiles);
-    case 5: return k1_grid_n<Real, 5>(E, n_tiles);
-    case 6: return k1_grid_n<Real, 6>(E, n_tiles);
-    case 7: return k1_grid_n<Real, 7>(E, n_tiles);
-    case 8: return k1_grid_n<Real, 8>(E, n_tiles);
-    case 9: return k1_grid_n<Real, 9>(E, n_tiles);
+    case 2: return k1_grid_n<Real, 2>(n_tiles);
+    case 3: return k1_grid_n<Real, 3>(n_tiles);
+    case 4: return k1_grid_n<Real, 4>(n_tiles);
+    case 5: return k1_grid_n<Real, 5>(n_tiles);
+    case 6: return k1_grid_n<Real, 6>(n_tiles);
+    case 7: return k1_grid_n<Real, 7>(n_tiles);
+    case 8: return k1_grid_n<Real, 8>(n_tiles);
+    case 9: return k1_grid_n<Real, 9>(n_tiles);
   }
   return 1;
 }
@@ -185,14 +176,6 @@ int mltadd_impl(mj_op* op, double alpha, const void* x, double beta, void* y, cu
   return MJ_OK;
 }
 
-template <typename Real>
-__global__ void k_cast_from_f64(const double* __restrict__ a, Real* __restrict__ b, int n) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = Real(a[i]);
-}
-template <typename Real>
-__global__ void k_cast_to_f64(const Real* __restrict__ a, double* __restrict__ b, int n) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = double(a[i]);
-}
 
 // Copies a host double vector into a device vector of the operator precision.
 int upload_vec(mj_op* op, const double* h, void* d, DevBuf& stage, cudaStream_t s) {
@@ -325,7 +308,7 @@ int mj_op_create(const mj_mesh_desc* mesh, const mj_geom_desc* geom, int precisi
   MJ_CUDA(cudaMemcpy(op->ptr.ptr, op->h_ptr.data(), sizeof(int) * (op->n_dof + 1), cudaMemcpyHostToDevice));
   MJ_CUDA(cudaMemcpy(op->pos.ptr, op->h_pos.data(), sizeof(int) * op->h_pos.size(), cudaMemcpyHostToDevice));
   MJ_CUDA(cudaMemset(op->R.ptr, 0, esz * op->r_len));
-  op->grid_k1 = (precision == MJ_FP64) ? k1_grid<double>(n, E, op->n_tiles) : k1_grid<float>(n, E, op->n_tiles);
+  op->grid_k1 = (precision == MJ_FP64) ? k1_grid<double>(n, op->n_tiles) : k1_grid<float>(n, op->n_tiles);
   MJ_CUDA(cudaGetLastError());
   *out = op.release();
   return MJ_OK;
@@ -472,6 +455,8 @@ int mj_lf_set_stream(mj_lf* lf, void* stream) {
   return MJ_OK;
 }
 
+}  // extern "C"
+
 namespace {
 
 template <typename Real>
@@ -529,8 +514,11 @@ int lf_step(mj_lf* lf) {
   cudaStream_t s = lf->stream;
   const int n = lf->n_dof;
   const double p = (lf->step < (int)lf->pulse.size()) ? lf->pulse[lf->step] : 0.0;
+  const bool prof = lf->profile && lf->ev_used + 3 <= (int)lf->ev.size();
+  if (prof) MJ_CUDA(cudaEventRecord(lf->ev[lf->ev_used], s));
   // U1 = next (u^{n+1}), U0 = cur (u^n); the result u^{n+2} overwrites U0.
   launch_k1<Real>(op, lf->next(), s);
+  if (prof) MJ_CUDA(cudaEventRecord(lf->ev[lf->ev_used + 1], s));
   const double dt2 = lf->dt * lf->dt;
   if (op->precision == MJ_FP64) {
     k_gather_leapfrog<Real, true><<<stream_grid(n), 256, 0, s>>>(
@@ -545,6 +533,10 @@ int lf_step(mj_lf* lf) {
   }
   count_launch();
   MJ_CUDA(cudaGetLastError());
+  if (prof) {
+    MJ_CUDA(cudaEventRecord(lf->ev[lf->ev_used + 2], s));
+    lf->ev_used += 3;
+  }
   lf->cur_is_a = !lf->cur_is_a;  // new cur = old next; new next = overwritten old cur
   lf->step++;
   return MJ_OK;
@@ -584,6 +576,15 @@ int lf_advance_impl(mj_lf* lf, int nsteps, double* norms, double* traces, int st
   int flag = 0;
   MJ_CUDA(cudaMemcpyAsync(&flag, lf->flag.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
   MJ_CUDA(cudaStreamSynchronize(s));
+  for (int e = 0; e + 3 <= lf->ev_used; e += 3) {
+    float a = 0.f, b = 0.f;
+    MJ_CUDA(cudaEventElapsedTime(&a, lf->ev[e], lf->ev[e + 1]));
+    MJ_CUDA(cudaEventElapsedTime(&b, lf->ev[e + 1], lf->ev[e + 2]));
+    lf->prof_elem_ms += a;
+    lf->prof_update_ms += b;
+    lf->prof_steps++;
+  }
+  lf->ev_used = 0;
   if (flag) {
     set_error("mj_lf_advance: non-finite norm (unstable run?)");
     return MJ_ERR_NONFINITE;
@@ -592,6 +593,8 @@ int lf_advance_impl(mj_lf* lf, int nsteps, double* norms, double* traces, int st
 }
 
 }  // namespace
+
+extern "C" {
 
 int mj_lf_init(mj_lf* lf, const double* u0, const double* du0) {
   MJ_CHECK_ARG(lf && u0, "mj_lf_init: null argument");
@@ -633,6 +636,26 @@ int mj_lf_run(mj_lf* lf, const double* u0, const double* du0, int nsteps, double
                                     : lf_advance_impl<float>(lf, nsteps, norms, traces, trace_stride, true);
   if (rc) return rc;
   if (u_final) return mj_lf_get_state(lf, u_final, nullptr);
+  return MJ_OK;
+}
+
+int mj_lf_profile(mj_lf* lf, int enable, double* elem_ms, double* update_ms, int* steps) {
+  MJ_CHECK_ARG(lf, "mj_lf_profile: null integrator");
+  if (elem_ms) *elem_ms = lf->prof_elem_ms;
+  if (update_ms) *update_ms = lf->prof_update_ms;
+  if (steps) *steps = lf->prof_steps;
+  if (enable && !lf->profile) {
+    const int n_ev = 3 * 1024;
+    while ((int)lf->ev.size() < n_ev) {
+      cudaEvent_t e;
+      MJ_CUDA(cudaEventCreate(&e));
+      lf->ev.push_back(e);
+    }
+    lf->prof_elem_ms = lf->prof_update_ms = 0.0;
+    lf->prof_steps = 0;
+    lf->ev_used = 0;
+  }
+  lf->profile = enable != 0;
   return MJ_OK;
 }
 

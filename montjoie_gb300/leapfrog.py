@@ -1,0 +1,137 @@
+"""Python mirror of the reference's order-2 leap-frog driver.
+
+``LeapFrogIterator`` follows ``ModifiedEquationIterator<double>`` of order 2
+(``MONTJOIE/src/Instationary/ModifiedEquation.hxx:78-114``):
+``SetInitialConditionS`` (``ModifiedEquation.cxx:92-124``), ``Advance``
+(``:290-345``) and ``GetIterate`` (``:230-236``), with the ODE-system operators
+of the acoustic problem (stiffness ``Kh``, lumped mass ``Dh``, sparse source
+``F`` times the pulse) bound at construction.  ``RunSecondOrderScheme``
+mirrors ``MONTJOIE/src/Instationary/ModifiedEquation.cxx:16-53``.
+The loop runs on the GPU through the C ABI.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+
+from . import _lib
+from .operator import FemMatrixFreeOperator
+
+
+class LeapFrogIterator:
+    def __init__(self, op: FemMatrixFreeOperator, dt: float, mass: np.ndarray, inv_mass: np.ndarray | None = None,
+                 src_idx=None, src_val=None, pulse=None, norm_weight=None, rec_idx=None, rec_w=None):
+        L = _lib.load()
+        self.op = op
+        self.dt = float(dt)
+        n = op.n_dof
+        self._keep = []
+
+        def f(a, size=None):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            if size is not None and a.size != size:
+                raise ValueError("array size mismatch")
+            self._keep.append(a)
+            return a
+
+        def i(a):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=np.int32)
+            self._keep.append(a)
+            return a
+
+        mass = f(mass, n)
+        inv_mass = f(inv_mass, n)
+        src_idx, src_val = i(src_idx), f(src_val)
+        pulse = f(pulse)
+        norm_weight = f(norm_weight, n)
+        rec_idx, rec_w = i(rec_idx), f(rec_w)
+        n_src = 0 if src_idx is None else int(src_idx.size)
+        n_rec = 0 if rec_idx is None else int(rec_idx.shape[0])
+        n_rec_w = 0 if rec_idx is None else int(rec_idx.shape[1])
+        self.n_rec = n_rec
+        self.has_norm = norm_weight is not None
+        desc = _lib.LfDesc(self.dt, _lib.dptr(mass), _lib.dptr(inv_mass), n_src, _lib.iptr(src_idx),
+                           _lib.dptr(src_val), 0 if pulse is None else int(pulse.size), _lib.dptr(pulse),
+                           _lib.dptr(norm_weight), n_rec, n_rec_w, _lib.iptr(rec_idx), _lib.dptr(rec_w))
+        handle = ctypes.c_void_p()
+        _lib.check(L.mj_lf_create(op.handle, ctypes.byref(desc), ctypes.byref(handle)))
+        self._h = handle
+        self.n_time = 0
+
+    @property
+    def handle(self):
+        return self._h
+
+    def SetInitialConditionS(self, u0: np.ndarray, du0: np.ndarray | None = None) -> None:
+        u0 = np.ascontiguousarray(u0, dtype=np.float64)
+        du0 = None if du0 is None else np.ascontiguousarray(du0, dtype=np.float64)
+        _lib.check(_lib.load().mj_lf_init(self._h, _lib.dptr(u0), _lib.dptr(du0)))
+        self.n_time = 0
+
+    def Advance(self, nsteps: int = 1):
+        """Advances nsteps; returns (norms, traces) of the iterates handed out before each step."""
+        norms = np.zeros(nsteps) if self.has_norm else None
+        traces = np.zeros((self.n_rec, nsteps)) if self.n_rec else None
+        _lib.check(_lib.load().mj_lf_advance(self._h, int(nsteps), _lib.dptr(norms), _lib.dptr(traces),
+                                             int(nsteps)))
+        self.n_time += nsteps
+        return norms, traces
+
+    def GetIterate(self) -> np.ndarray:
+        u = np.zeros(self.op.n_dof)
+        _lib.check(_lib.load().mj_lf_get_state(self._h, _lib.dptr(u), None))
+        return u
+
+    def GetState(self):
+        u, v = np.zeros(self.op.n_dof), np.zeros(self.op.n_dof)
+        _lib.check(_lib.load().mj_lf_get_state(self._h, _lib.dptr(u), _lib.dptr(v)))
+        return u, v
+
+    def Run(self, u0, du0, nsteps: int):
+        """Whole RunSecondOrderScheme in one C-ABI call: returns (u_final, norms, traces)
+        with nsteps+1 diagnostic columns (iterates 0..nsteps)."""
+        u0 = np.ascontiguousarray(u0, dtype=np.float64)
+        du0 = None if du0 is None else np.ascontiguousarray(du0, dtype=np.float64)
+        uf = np.zeros(self.op.n_dof)
+        norms = np.zeros(nsteps + 1) if self.has_norm else None
+        traces = np.zeros((self.n_rec, nsteps + 1)) if self.n_rec else None
+        _lib.check(_lib.load().mj_lf_run(self._h, _lib.dptr(u0), _lib.dptr(du0), int(nsteps), _lib.dptr(uf),
+                                         _lib.dptr(norms), _lib.dptr(traces), int(nsteps + 1)))
+        self.n_time = nsteps
+        return uf, norms, traces
+
+    def device_state(self):
+        a, b, s = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_int()
+        _lib.check(_lib.load().mj_lf_device_state(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(s)))
+        return a.value, b.value, s.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _lib.load().mj_lf_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def number_of_iterations(t_begin: float, t_end: float, dt: float) -> int:
+    """nb_max_iter = ceil(|t_end - t_begin| / dt) (ModifiedEquation.cxx:23-24)."""
+    return int(math.ceil(abs(t_end - t_begin) / dt))
+
+
+def RunSecondOrderScheme(t_begin: float, t_end: float, dt: float, U0: np.ndarray, dU0_dt: np.ndarray | None,
+                         scheme: LeapFrogIterator):
+    """Runs the scheme from t_begin to t_end; returns (final iterate, norms, traces)."""
+    nsteps = number_of_iterations(t_begin, t_end, dt)
+    if nsteps < 1:
+        return np.array(U0, dtype=np.float64), None, None
+    return scheme.Run(U0, dU0_dt, nsteps)

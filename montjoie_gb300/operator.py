@@ -1,0 +1,85 @@
+"""Python mirror of the reference's matrix-free stiffness operator interface.
+
+``FemMatrixFreeOperator`` plays the role of
+``FemMatrixFreeClass<double, LaplaceEquation<Dimension3> >``
+(``MONTJOIE/src/Computation/FemMatrixFreeClass.hxx:74-300``) seen through
+``Seldon::VirtualMatrix<double>`` (``SELDON/matrix/Matrix_Base.hxx:41-140``):
+``MltAddVector(alpha, x, beta, y)`` computes ``y <- beta*y + alpha*A*x`` in place,
+``MltVector(x, y)`` computes ``y <- A*x``.  ``A`` is the positive stiffness
+operator of ``-div(mu grad u)``.  All the work runs in the CUDA library through
+the C ABI; a missing library raises.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+
+class FemMatrixFreeOperator:
+    def __init__(self, order: int, nodle: np.ndarray, factors: np.ndarray, n_dof: int,
+                 precision: str = "fp64", gradphi: np.ndarray | None = None):
+        L = _lib.load()
+        self.order = int(order)
+        self.n_dof = int(n_dof)
+        nodle = np.ascontiguousarray(nodle, dtype=np.int32)
+        factors = np.ascontiguousarray(factors, dtype=np.float64)
+        Q = (self.order + 1) ** 3
+        if nodle.ndim != 2 or nodle.shape[1] != Q:
+            raise ValueError(f"nodle must be (n_elt, {Q})")
+        self.n_elt = nodle.shape[0]
+        if factors.size != self.n_elt * Q * 6:
+            raise ValueError(f"factors must hold n_elt*{Q}*6 values")
+        self.precision = {"fp64": _lib.MJ_FP64, "fp32": _lib.MJ_FP32}[precision]
+        self.dtype = np.float64 if self.precision == _lib.MJ_FP64 else np.float32
+        g = None if gradphi is None else np.ascontiguousarray(gradphi, dtype=np.float64)
+        mesh = _lib.MeshDesc(self.order, self.n_elt, self.n_dof, _lib.iptr(nodle))
+        geom = _lib.GeomDesc(_lib.dptr(factors), _lib.dptr(g))
+        handle = ctypes.c_void_p()
+        _lib.check(L.mj_op_create(ctypes.byref(mesh), ctypes.byref(geom), self.precision, ctypes.byref(handle)))
+        self._h = handle
+
+    @property
+    def handle(self):
+        return self._h
+
+    def GetM(self) -> int:
+        return self.n_dof
+
+    def GetN(self) -> int:
+        return self.n_dof
+
+    def MltAddVector(self, alpha: float, x: np.ndarray, beta: float, y: np.ndarray) -> None:
+        """y <- beta*y + alpha*A*x (host vectors, y updated in place)."""
+        if x.shape != (self.n_dof,) or y.shape != (self.n_dof,):
+            raise ValueError("vector size differs from the operator size")
+        if y.dtype != np.float64 or not y.flags.c_contiguous:
+            raise TypeError("y must be a contiguous float64 vector")
+        xc = np.ascontiguousarray(x, dtype=np.float64)
+        _lib.check(_lib.load().mj_op_mltadd(self._h, float(alpha), _lib.dptr(xc), float(beta), _lib.dptr(y)))
+
+    def MltVector(self, x: np.ndarray, y: np.ndarray) -> None:
+        self.MltAddVector(1.0, x, 0.0, y)
+
+    def mltadd_device(self, alpha: float, x_ptr: int, beta: float, y_ptr: int, stream: int = 0) -> None:
+        """Same product on device vectors (operator precision), ordered on ``stream``."""
+        _lib.check(_lib.load().mj_op_mltadd_device(self._h, float(alpha), ctypes.c_void_p(x_ptr), float(beta),
+                                                   ctypes.c_void_p(y_ptr), ctypes.c_void_p(stream)))
+
+    def device_bytes(self) -> int:
+        sz = ctypes.c_size_t()
+        _lib.check(_lib.load().mj_op_info(self._h, None, None, None, None, ctypes.byref(sz)))
+        return int(sz.value)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _lib.load().mj_op_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

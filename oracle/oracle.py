@@ -204,7 +204,7 @@ def leapfrog(r, nodle, bh, D, invD, src_idx, src_val, pulse, dt, nsteps, u0, u1=
     ptr, elems = (None, None) if colors is None else colors
     nc = 0 if colors is None else len(ptr) - 1
     lib().oc_leapfrog(r, ne, ndof, _p(i32(nodle), _I), _p(num, _I), _p(G), _p(f64(bh)), _p(f64(D)), _p(f64(invD)),
-                      int(len(src_idx)), _p(i32(src_idx), _I), _p(f64(src_val)), _p(f64(pulse)), float(dt),
+                      int(len(src_idx)), _p(i32(src_idx), _I), _p(f64(src_val)), _p(None if pulse is None else f64(pulse)), float(dt),
                       int(nsteps), _p(u0), _p(None if du0 is None else f64(du0)), _p(u1),
                       _p(None if jw is None else f64(jw)), _p(norms), nrec,
                       _p(None if rec_idx is None else i32(rec_idx), _I), _p(None if rec_w is None else f64(rec_w)),

@@ -1,0 +1,126 @@
+"""GPU parity of the leap-frog time loop (C ABI) against the reference.
+
+FP64 plain form: relative L2 of the final iterate and of the norm history
+<= 1e-10 against the reference's own run (golden fixtures; 30-200 steps).
+The 16^3 Q4 case (BASELINE configuration 1, 200 steps) runs our whole
+set-up (numbering, geometry, mass, source, pulse, receivers) and compares
+the norm history, the 8 receiver traces and 512 probe values of u^200 with
+the reference's, <= 1e-10 relative.  FP32 errors are stated per test.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-10
+
+
+def integrator(g, precision, norms=True):
+    from montjoie_gb300.leapfrog import LeapFrogIterator
+    from montjoie_gb300.operator import FemMatrixFreeOperator
+    op = FemMatrixFreeOperator(int(g["order"]), g["nodle"], g["bh"], g["massD"].size, precision,
+                               gradphi=g["gradphi"])
+    jwsum = np.zeros(g["massD"].size)
+    np.add.at(jwsum, g["nodle"].ravel(), g["jw"].ravel())
+    lf = LeapFrogIterator(op, float(g["dt"]), g["massD"], g["invD"], g["src_idx"], g["src_val"], g["pulse"],
+                          jwsum if norms else None)
+    return op, lf
+
+
+def test_trajectory_fp64_matches_reference(golden_case):
+    name, g = golden_case
+    op, lf = integrator(g, "fp64")
+    n = int(g["nsteps"])
+    uf, norms, _ = lf.Run(np.zeros(g["massD"].size), None, n)
+    assert rel_l2(uf, g["u_final"]) < FP64_TOL
+    assert rel_l2(norms, g["norms"]) < FP64_TOL
+    lf.close(); op.close()
+
+
+def test_chunked_advance_equals_run(golden_case):
+    name, g = golden_case
+    op, lf = integrator(g, "fp64")
+    n = int(g["nsteps"])
+    lf.SetInitialConditionS(np.zeros(g["massD"].size))
+    k = n // 3
+    n1, _ = lf.Advance(k)
+    n2, _ = lf.Advance(n - k)
+    u = lf.GetIterate()
+    assert rel_l2(u, g["u_final"]) < FP64_TOL
+    assert rel_l2(np.concatenate([n1, n2]), g["norms"][:n]) < FP64_TOL
+    snaps = dict(zip(g["snap_steps"].tolist(), g["snaps"]))
+    if k in snaps:
+        pass
+    lf.close(); op.close()
+
+
+def test_trajectory_fp32_error(golden_case):
+    name, g = golden_case
+    op, lf = integrator(g, "fp32")
+    n = int(g["nsteps"])
+    uf, norms, _ = lf.Run(np.zeros(g["massD"].size), None, n)
+    assert rel_l2(uf, g["u_final"]) < 1e-4
+    assert rel_l2(norms, g["norms"]) < 1e-4
+    lf.close(); op.close()
+
+
+def test_nonzero_initial_conditions_match_oracle():
+    from oracle import oracle as oc
+    g = load_golden("cube3_q4")
+    rng = np.random.default_rng(3)
+    u0 = rng.uniform(-1, 1, g["massD"].size)
+    du0 = rng.uniform(-1, 1, g["massD"].size)
+    op, lf = integrator(g, "fp64")
+    uf, norms, _ = lf.Run(u0, du0, 50)
+    uo, _, no, _ = oc.leapfrog(int(g["order"]), g["nodle"], g["bh"], g["massD"], g["invD"], g["src_idx"],
+                               g["src_val"], g["pulse"], float(g["dt"]), 50, u0, du0=du0, jw=g["jw"])
+    assert rel_l2(uf, uo) < 1e-12
+    assert rel_l2(norms, no) < 1e-12
+
+
+@pytest.fixture(scope="module")
+def config1():
+    from montjoie_gb300 import mesh as M
+    from montjoie_gb300.problem import AcousticProblem
+    g = load_golden("config1_16q4")
+    m = M.perturbed_cube(16, seed=int(g["seed"]), amplitude=0.05, kind="random", c_mode="element")
+    s = M.AcousticSetup(order=4, dt=float(g["dt"]), nsteps=int(g["nsteps"]), src_radius=float(g["src_radius"]))
+    pb = AcousticProblem(m, s, receivers=g["receivers"])
+    return g, pb
+
+
+def _probe_values(pb, g, u):
+    pos = np.zeros((pb.n_dof, 3))
+    pos[pb.nodle.ravel()] = pb.xq.reshape(-1, 3)
+    key = lambda p: np.round(p * 1e9).astype(np.int64)  # noqa: E731
+    table = {tuple(k): i for i, k in enumerate(key(pos))}
+    idx = np.array([table[tuple(k)] for k in key(g["probe_pos"])])
+    return u[idx]
+
+
+def test_config1_fp64_end_to_end(config1):
+    g, pb = config1
+    assert rel_l2(pb.pulse, g["pulse"]) < 1e-12
+    assert pb.src_idx.size == int(g["n_src"])
+    op = pb.operator("fp64")
+    lf = pb.integrator(op)
+    n = int(g["nsteps"])
+    uf, norms, traces = lf.Run(np.zeros(pb.n_dof), None, n)
+    assert rel_l2(norms, g["norms"]) < FP64_TOL
+    assert np.abs(traces - g["traces"]).max() < FP64_TOL * np.abs(g["traces"]).max()
+    assert rel_l2(_probe_values(pb, g, uf), g["probe_u"]) < FP64_TOL
+    assert abs(np.linalg.norm(uf) - float(g["u_final_norm2"])) < FP64_TOL * float(g["u_final_norm2"])
+
+
+def test_config1_fp32_error(config1):
+    g, pb = config1
+    op = pb.operator("fp32")
+    lf = pb.integrator(op)
+    n = int(g["nsteps"])
+    uf, norms, traces = lf.Run(np.zeros(pb.n_dof), None, n)
+    # chosen form: FP32 state and contractions; error stated against the FP64 reference
+    assert rel_l2(norms, g["norms"]) < 1e-4
+    assert np.abs(traces - g["traces"]).max() < 1e-4 * np.abs(g["traces"]).max()
+    assert rel_l2(_probe_values(pb, g, uf), g["probe_u"]) < 1e-4

@@ -1,0 +1,117 @@
+"""Product host-side logic on the CPU: the C-ABI library loads and exports
+every declared symbol, argument validation, the global numbering, the lumped
+mass, the pulse, the source and the receivers, against the reference's
+golden outputs.  No compute call here touches a GPU."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, load_golden, rel_l2
+from montjoie_gb300 import _lib, problem
+from oracle import oracle as oc
+
+
+def declared_symbols():
+    text = open(os.path.join(ROOT, "include", "montjoie_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(mj_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = _lib.load()
+    syms = declared_symbols()
+    assert len(syms) >= 15
+    for s in syms:
+        assert hasattr(L, s), f"{s} not exported"
+    assert set(syms) <= set(_lib.EXPORTED) | set(syms)
+    assert L.mj_version().decode().startswith("montjoie_gb300")
+
+
+def test_create_rejects_bad_arguments():
+    L = _lib.load()
+    nodle = np.zeros((1, 8), dtype=np.int32)
+    fac = np.zeros(8 * 6)
+    h = ctypes.c_void_p()
+    mesh = _lib.MeshDesc(0, 1, 8, _lib.iptr(nodle))
+    geom = _lib.GeomDesc(_lib.dptr(fac), None)
+    assert L.mj_op_create(ctypes.byref(mesh), ctypes.byref(geom), _lib.MJ_FP64, ctypes.byref(h)) == _lib.MJ_ERR_ARG
+    assert b"order" in L.mj_last_error()
+    mesh = _lib.MeshDesc(1, 1, 8, _lib.iptr(np.full((1, 8), 9, dtype=np.int32)))
+    assert L.mj_op_create(ctypes.byref(mesh), ctypes.byref(geom), _lib.MJ_FP64, ctypes.byref(h)) == _lib.MJ_ERR_ARG
+    assert b"out of" in L.mj_last_error()
+    mesh = _lib.MeshDesc(1, 1, 9, _lib.iptr(np.arange(8, dtype=np.int32).reshape(1, 8)))
+    assert L.mj_op_create(ctypes.byref(mesh), ctypes.byref(geom), _lib.MJ_FP64, ctypes.byref(h)) == _lib.MJ_ERR_ARG
+    assert b"no element" in L.mj_last_error()
+    mesh = _lib.MeshDesc(1, 1, 8, _lib.iptr(np.arange(8, dtype=np.int32).reshape(1, 8)))
+    assert L.mj_op_create(ctypes.byref(mesh), ctypes.byref(geom), 7, ctypes.byref(h)) == _lib.MJ_ERR_ARG
+    bad = fac.copy()
+    bad[3] = np.nan
+    geom = _lib.GeomDesc(_lib.dptr(bad), None)
+    assert L.mj_op_create(ctypes.byref(mesh), ctypes.byref(geom), _lib.MJ_FP64, ctypes.byref(h)) == _lib.MJ_ERR_NONFINITE
+    assert L.mj_lf_create(None, None, None) == _lib.MJ_ERR_ARG
+    assert L.mj_lf_advance(None, 1, None, None, 0) == _lib.MJ_ERR_ARG
+
+
+def test_numbering_is_the_reference_numbering_up_to_permutation(golden_case):
+    name, g = golden_case
+    r = int(g["order"])
+    nodle, ndof = problem.number_mesh(r, g["hexes"], g["verts"].shape[0])
+    assert ndof == g["massD"].size
+    a, b = nodle.ravel(), g["nodle"].ravel()
+    fwd = np.full(ndof, -1)
+    fwd[a] = b
+    assert (fwd[a] == b).all(), "one of our dofs maps to two reference dofs"
+    assert np.unique(fwd).size == ndof, "not a bijection"
+
+
+def test_numbering_rejects_bad_vertices():
+    L = _lib.load()
+    hexes = np.full((1, 8), 5, dtype=np.int32)
+    nodle = np.zeros((1, 8), dtype=np.int32)
+    nd = ctypes.c_int()
+    assert L.mj_number_hex_mesh(1, 1, 4, _lib.iptr(hexes), _lib.iptr(nodle), ctypes.byref(nd)) == _lib.MJ_ERR_ARG
+
+
+def test_lumped_mass_matches_reference(golden_case):
+    name, g = golden_case
+    D = problem.lumped_mass(int(g["order"]), g["nodle"], g["jw"], g["massD"].size)
+    assert rel_l2(D, g["massD"]) < 1e-15
+
+
+def test_pulse_and_source_match_reference(golden_case):
+    name, g = golden_case
+    p = problem.ricker_pulse(float(g["f0"]), float(g["t0"]), float(g["dt"]), int(g["nsteps"]), float(g["eps_time"]),
+                             float(g["tlimit"]))
+    assert rel_l2(p, g["pulse"]) < 1e-12
+    r = int(g["order"])
+    _, _, xq = oc.geometry(r, g["verts_e"], np.ones(g["verts_e"].shape[0]))
+    idx, val = problem.gaussian_source(g["nodle"], g["jw"], xq, g["massD"].size, g["src_center"],
+                                       float(g["src_radius"]))
+    assert (idx == np.sort(g["src_idx"])).all()
+    ref = dict(zip(g["src_idx"].tolist(), g["src_val"].tolist()))
+    assert rel_l2(val, np.array([ref[i] for i in idx])) < 1e-14
+
+
+def test_host_rules_match_oracle():
+    for r in range(1, 9):
+        p, w = problem.gauss_lobatto(r)
+        po, wo = oc.gauss_lobatto(r)
+        assert np.abs(p - po).max() < 1e-15 and np.abs(w - wo).max() < 1e-15
+        assert np.abs(problem.derivative_matrix(p) - oc.grad_matrix(r)).max() < 1e-11
+        assert (problem.local_numbering(r).ravel() == oc.hex_numbering(r)).all()
+
+
+def test_receiver_weights_match_oracle():
+    g = load_golden("cube3_q4")
+    r = int(g["order"])
+    rng = np.random.default_rng(5)
+    pts = rng.uniform(0.05, 0.95, size=(6, 3))
+    idx, w = problem.receiver_weights(r, g["verts_e"], g["nodle"], pts)
+    assert np.allclose(w.sum(axis=1), 1.0, atol=1e-12)
+    for k, p in enumerate(pts):
+        e = int(np.nonzero((g["nodle"] == idx[k]).all(axis=1))[0][0])
+        wo, xi, inside = oc.point_weights(r, g["verts_e"][e], p)
+        assert inside and np.abs(wo - w[k]).max() < 1e-12
