@@ -65,6 +65,8 @@ struct mj_op {
   int E = 1, n_tiles = 0;
   size_t r_len = 0;  // length of R (tile-layout points)
   DevBuf nodle_t, fac_t, R, ptr, pos;
+  DevBuf err;                     // device error flag (bounded-wait timeouts)
+  int TS = 0;                     // padded points per tile
   std::vector<int> h_ptr, h_pos;  // CSR incidences (host copy, for integrators)
   double gradphi[kMaxN * kMaxN];
   DevBuf xbuf, ybuf;              // staging for host-vector MltAdd
@@ -112,11 +114,10 @@ namespace {
 
 template <typename Real, int N>
 void launch_k1_n(mj_op* op, const void* x, cudaStream_t s) {
-  GMatrix<Real, N> G;
-  for (int a = 0; a < N * N; a++) G.g[a] = Real(op->gradphi[a]);
   constexpr int E = tile_elems_for(N);
-  k_local_stiffness<Real, N, E><<<op->grid_k1, E * N * N, 0, s>>>(
-      static_cast<const Real*>(x), op->nodle_t.as<int>(), op->fac_t.as<Real>(), op->R.as<Real>(), op->n_tiles, G);
+  k_local_stiffness<Real, N, E><<<op->grid_k1, E * N * N, K1Smem<Real, N, E>::total, s>>>(
+      static_cast<const Real*>(x), op->nodle_t.as<int>(), op->fac_t.as<Real>(), op->R.as<Real>(), op->n_tiles,
+      op->err.as<int>());
   count_launch();
 }
 
@@ -139,7 +140,9 @@ template <typename Real, int N>
 int k1_grid_n(int n_tiles) {
   int per_sm = 1;
   constexpr int E = tile_elems_for(N);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_local_stiffness<Real, N, E>, E * N * N, 0);
+  const size_t smem = K1Smem<Real, N, E>::total;
+  cudaFuncSetAttribute(k_local_stiffness<Real, N, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_local_stiffness<Real, N, E>, E * N * N, smem);
   if (per_sm < 1) per_sm = 1;
   long g = (long)per_sm * sm_count();
   return (int)std::max(1L, std::min<long>(g, n_tiles));
@@ -235,7 +238,8 @@ int mj_op_create(const mj_mesh_desc* mesh, const mj_geom_desc* geom, int precisi
   op->precision = precision;
   op->E = tile_elems(n);
   op->n_tiles = (mesh->n_elt + op->E - 1) / op->E;
-  op->r_len = (size_t)op->n_tiles * op->E * Q;
+  op->TS = tile_stride(op->E * Q);
+  op->r_len = (size_t)op->n_tiles * op->TS;
   MJ_CHECK_ARG(op->r_len < (size_t)INT32_MAX, "mj_op_create: mesh too large for int32 incidences");
 
   // derivative matrix
@@ -251,7 +255,7 @@ int mj_op_create(const mj_mesh_desc* mesh, const mj_geom_desc* geom, int precisi
 
   const std::vector<int> num = hex_local_numbering(r);
   const int E = op->E;
-  const size_t TQ = (size_t)E * Q;
+  const size_t TS = (size_t)op->TS;
   // tile-layout connectivity and factors, and CSR incidences
   std::vector<int> nodle_t(op->r_len, 0);
   std::vector<int> count(op->n_dof + 1, 0);
@@ -278,7 +282,7 @@ int mj_op_create(const mj_mesh_desc* mesh, const mj_geom_desc* geom, int precisi
         const int e = tile * E + el;
         for (int j = 0; j < n; j++)
           for (int i = 0; i < n; i++) {
-            const size_t rp = (((size_t)tile * n + k) * E + el) * NN + j * n + i;
+            const size_t rp = (size_t)tile * TS + ((size_t)k * E + el) * NN + j * n + i;
             if (e >= mesh->n_elt) continue;  // padding: nodle 0, factors 0, no incidence
             const int ql = num[(i * n + j) * n + k];
             const size_t src = (size_t)e * Q + ql;
@@ -291,7 +295,7 @@ int mj_op_create(const mj_mesh_desc* mesh, const mj_geom_desc* geom, int precisi
                 set_error("mj_op_create: non-finite stiffness factor");
                 return MJ_ERR_NONFINITE;
               }
-              const size_t fp = (size_t)tile * 6 * TQ + c * TQ + (rp - (size_t)tile * TQ);
+              const size_t fp = (size_t)tile * 6 * TS + c * TS + (rp - (size_t)tile * TS);
               if (precision == MJ_FP64) fac64[fp] = v;
               else fac32[fp] = (float)v;
             }
@@ -308,6 +312,15 @@ int mj_op_create(const mj_mesh_desc* mesh, const mj_geom_desc* geom, int precisi
   MJ_CUDA(cudaMemcpy(op->ptr.ptr, op->h_ptr.data(), sizeof(int) * (op->n_dof + 1), cudaMemcpyHostToDevice));
   MJ_CUDA(cudaMemcpy(op->pos.ptr, op->h_pos.data(), sizeof(int) * op->h_pos.size(), cudaMemcpyHostToDevice));
   MJ_CUDA(cudaMemset(op->R.ptr, 0, esz * op->r_len));
+  {
+    // derivative matrix of this order into the constant-memory slot n
+    std::vector<double> g64(op->gradphi, op->gradphi + NN);
+    std::vector<float> g32(g64.begin(), g64.end());
+    MJ_CUDA(cudaMemcpyToSymbol(c_gmat64, g64.data(), sizeof(double) * NN, sizeof(double) * kMaxNK * kMaxNK * n));
+    MJ_CUDA(cudaMemcpyToSymbol(c_gmat32, g32.data(), sizeof(float) * NN, sizeof(float) * kMaxNK * kMaxNK * n));
+  }
+  MJ_CUDA(op->err.alloc(sizeof(int)));
+  MJ_CUDA(cudaMemset(op->err.ptr, 0, sizeof(int)));
   op->grid_k1 = (precision == MJ_FP64) ? k1_grid<double>(n, op->n_tiles) : k1_grid<float>(n, op->n_tiles);
   MJ_CUDA(cudaGetLastError());
   *out = op.release();
