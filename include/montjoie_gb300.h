@@ -191,6 +191,32 @@ int mj_geometry(int order, int n_elt, const double* verts, const double* mu, dou
 int mj_lumped_mass(int order, int n_elt, int n_dof, const int32_t* nodle, const double* jw,
                    const double* rho, double* mass_out);
 
+/* ---- allocation-free product ------------------------------------------ */
+
+/* Largest n_elt*(order+1)^3 accepted by mj_stiffness_mltadd_static. */
+#define MJ_STATIC_SCRATCH_POINTS 4194304
+
+/* y <- beta*y + alpha*A*x in FP64 without allocating any memory.
+ * No counterpart in the reference: it serves callers that must not let a
+ * library allocate GPU memory.  Examples are a solver whose device memory is
+ * carved out of one arena owned by another allocator, or a time loop that
+ * stages every buffer up front and must not call cudaMalloc/cudaFree later,
+ * because those calls can synchronise the device and fragment the arena.
+ * All arrays are DEVICE pointers the caller owns, in the reference layout:
+ * nodle (n_elt x (r+1)^3 int32), factors (n_elt x (r+1)^3 x 6), x and y
+ * (n_dof doubles).  The element-local scratch is a fixed array of
+ * MJ_STATIC_SCRATCH_POINTS doubles (32 MiB) inside the library.  Every GPU
+ * that loads the library holds it until the process exits.  Larger meshes are
+ * rejected with MJ_ERR_ARG.  The first call on a device looks up that array's
+ * device address, so make the first call on each device before any stream
+ * capture.  All calls share the one array, so calls that overlap on the GPU
+ * (other streams or host threads) race; serialise them.  The work is ordered
+ * on `stream` (a cudaStream_t, NULL = legacy default stream) and the call
+ * returns once it is done.  The scatter uses atomic additions, so the result
+ * equals mj_op_mltadd's up to rounding order. */
+int mj_stiffness_mltadd_static(int order, int n_elt, int n_dof, const int32_t* nodle, const double* factors,
+                               double alpha, const double* x, double beta, double* y, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

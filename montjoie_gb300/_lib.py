@@ -26,7 +26,7 @@ EXPORTED = [
     "mj_last_error", "mj_version", "mj_op_create", "mj_op_destroy", "mj_op_mltadd", "mj_op_mltadd_device",
     "mj_op_info", "mj_kernel_launches", "mj_lf_create", "mj_lf_destroy", "mj_lf_init", "mj_lf_advance",
     "mj_lf_get_state", "mj_lf_run", "mj_lf_device_state", "mj_lf_profile", "mj_lf_set_stream", "mj_number_hex_mesh",
-    "mj_geometry", "mj_lumped_mass",
+    "mj_geometry", "mj_lumped_mass", "mj_stiffness_mltadd_static",
 ]
 
 _D = ctypes.POINTER(ctypes.c_double)
@@ -98,6 +98,8 @@ def load(build_if_missing: bool = True):
     L.mj_number_hex_mesh.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _I, ctypes.POINTER(ctypes.c_int)]
     L.mj_geometry.argtypes = [ctypes.c_int, ctypes.c_int, _D, _D, _D, _D, _D]
     L.mj_lumped_mass.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _D, _D, _D]
+    L.mj_stiffness_mltadd_static.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP, ctypes.c_double,
+                                             _VP, ctypes.c_double, _VP, _VP]
     _lib = L
     return _lib
 
