@@ -164,6 +164,53 @@ int mj_lf_profile(mj_lf* lf, int enable, double* elem_ms, double* update_ms, int
 /* Sets the CUDA stream (cudaStream_t) used by the integrator's launches. */
 int mj_lf_set_stream(mj_lf* lf, void* stream);
 
+/* ---- many sources on one mesh ------------------------------------------ */
+
+typedef struct mj_lfb mj_lfb;
+
+typedef struct {
+  double dt;                 /* time step */
+  int n_rhs;                 /* S independent runs (one per source), multiple of 8, <= 4096 */
+  const double* mass;        /* lumped mass D (n_dof), host */
+  const double* inv_mass;    /* 1/D (n_dof), host; NULL -> 1/D */
+  int n_src;                 /* sparse sources: entry t adds pulse * src_val[t] at dof */
+  const int32_t* src_idx;    /* src_idx[t] of run src_rhs[t] */
+  const int32_t* src_rhs;
+  const double* src_val;
+  int n_pulse;               /* pulse p(t_n + dt) shared by all runs, host */
+  const double* pulse;
+  int n_rec;                 /* receivers sampled for every run: n_rec x n_rec_w (dof, weight) */
+  int n_rec_w;
+  const int32_t* rec_idx;
+  const double* rec_w;
+} mj_lfb_desc;
+
+/* Binds S leap-frog runs that share the mesh (and the operator, which must be
+ * MJ_FP32) but have their own sources and states; the state lives on the
+ * device as an n_dof x S array (row-major: the S values of a dof together).
+ * Each run is the order-2 ModifiedEquationIterator of mj_lf_create
+ * (MONTJOIE/src/Instationary/ModifiedEquation.cxx:92-124,290-345); the
+ * reference runs them one after the other.  The element-kernel variant is
+ * chosen by timing the candidates on this operator. */
+int mj_lfb_create(mj_op* op, const mj_lfb_desc* desc, mj_lfb** out);
+int mj_lfb_destroy(mj_lfb* b);
+
+/* U^0 = u0, U^1 from SetInitialConditionS for every run; u0, du0: n_dof x S
+ * host arrays (row-major), NULL = zero. */
+int mj_lfb_init(mj_lfb* b, const double* u0, const double* du0);
+
+/* Advances nsteps steps of every run.  use_graph != 0 replays a captured
+ * CUDA graph of 20 steps (two kernels per step) when no traces are asked.
+ * traces (or NULL): receiver k of run s before step j of this call at
+ * traces[(k*S + s)*trace_stride + j]. */
+int mj_lfb_advance(mj_lfb* b, int nsteps, double* traces, int trace_stride, int use_graph);
+
+/* Copies U^n and U^{n+1} (n_dof x S row-major, either may be NULL) to the host. */
+int mj_lfb_get_state(mj_lfb* b, double* u_n, double* u_np1);
+
+/* Tuned variant and progress: runs, elements per CTA, lanes (runs per pass), grid, steps done. */
+int mj_lfb_info(const mj_lfb* b, int* n_rhs, int* tile_elems, int* lanes, int* grid, int* step);
+
 /* ---- setup helpers (geometry, numbering, mass) ------------------------ */
 
 /* Global numbering of a conforming hexahedral mesh of order r: vertices,

@@ -27,6 +27,7 @@ EXPORTED = [
     "mj_op_info", "mj_kernel_launches", "mj_lf_create", "mj_lf_destroy", "mj_lf_init", "mj_lf_advance",
     "mj_lf_get_state", "mj_lf_run", "mj_lf_device_state", "mj_lf_profile", "mj_lf_set_stream", "mj_number_hex_mesh",
     "mj_geometry", "mj_lumped_mass", "mj_stiffness_mltadd_static",
+    "mj_lfb_create", "mj_lfb_destroy", "mj_lfb_init", "mj_lfb_advance", "mj_lfb_get_state", "mj_lfb_info",
 ]
 
 _D = ctypes.POINTER(ctypes.c_double)
@@ -48,6 +49,15 @@ class LfDesc(ctypes.Structure):
         ("n_src", ctypes.c_int), ("src_idx", _I), ("src_val", _D),
         ("n_pulse", ctypes.c_int), ("pulse", _D),
         ("norm_weight", _D),
+        ("n_rec", ctypes.c_int), ("n_rec_w", ctypes.c_int), ("rec_idx", _I), ("rec_w", _D),
+    ]
+
+
+class LfbDesc(ctypes.Structure):
+    _fields_ = [
+        ("dt", ctypes.c_double), ("n_rhs", ctypes.c_int), ("mass", _D), ("inv_mass", _D),
+        ("n_src", ctypes.c_int), ("src_idx", _I), ("src_rhs", _I), ("src_val", _D),
+        ("n_pulse", ctypes.c_int), ("pulse", _D),
         ("n_rec", ctypes.c_int), ("n_rec_w", ctypes.c_int), ("rec_idx", _I), ("rec_w", _D),
     ]
 
@@ -98,6 +108,12 @@ def load(build_if_missing: bool = True):
     L.mj_number_hex_mesh.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _I, ctypes.POINTER(ctypes.c_int)]
     L.mj_geometry.argtypes = [ctypes.c_int, ctypes.c_int, _D, _D, _D, _D, _D]
     L.mj_lumped_mass.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _D, _D, _D]
+    L.mj_lfb_create.argtypes = [_VP, ctypes.POINTER(LfbDesc), ctypes.POINTER(_VP)]
+    L.mj_lfb_destroy.argtypes = [_VP]
+    L.mj_lfb_init.argtypes = [_VP, _D, _D]
+    L.mj_lfb_advance.argtypes = [_VP, ctypes.c_int, _D, ctypes.c_int, ctypes.c_int]
+    L.mj_lfb_get_state.argtypes = [_VP, _D, _D]
+    L.mj_lfb_info.argtypes = [_VP] + [ctypes.POINTER(ctypes.c_int)] * 5
     L.mj_stiffness_mltadd_static.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP, ctypes.c_double,
                                              _VP, ctypes.c_double, _VP, _VP]
     _lib = L

@@ -1,0 +1,495 @@
+// Many right-hand sides on one mesh: S independent leap-frog runs (one per
+// source) advanced together, FP32, state stored [dof][S] so every dof row of
+// S values moves as one contiguous block.  The factors and connectivity are
+// streamed once per step for all S runs.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <memory>
+#include <vector>
+
+#include "mj_internal.cuh"
+#include "mj_k1.cuh"
+
+namespace mj {
+namespace {
+
+// ---- element kernel variants for many right-hand sides (FP32) -----------
+
+template <int N, int E, int L>
+int rhs_prepare_one(int* ctas) {
+  using P = K1Plan<float, N, E, L>;
+  int dev = 0, optin = 0;
+  MJ_CUDA(cudaGetDevice(&dev));
+  MJ_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  if ((int)P::total > optin || P::threads > 1024) {
+    set_error("many-RHS element kernel variant does not fit");
+    return MJ_ERR_ARG;
+  }
+  MJ_CUDA(cudaFuncSetAttribute(k_local_stiffness_rhs<N, E, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)P::total));
+  MJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas, k_local_stiffness_rhs<N, E, L>, P::threads, P::total));
+  if (*ctas < 1) {
+    set_error("many-RHS element kernel variant cannot be resident");
+    return MJ_ERR_ARG;
+  }
+  return MJ_OK;
+}
+
+template <int N, int E, int L>
+void rhs_launch_one(int grid, const float* x, const int* nodle_e, const float* fac_e, float* R, int n_tiles, int S,
+                    int* err, cudaStream_t s) {
+  using P = K1Plan<float, N, E, L>;
+  k_local_stiffness_rhs<N, E, L><<<grid, P::threads, P::total, s>>>(x, nodle_e, fac_e, R, n_tiles, S, err);
+}
+
+#define MJ_RHS_VARIANTS(X)                                                                                     \
+  X(2, 4, 32) X(2, 8, 16) X(3, 2, 32) X(3, 4, 16) X(4, 1, 32) X(4, 2, 16) X(5, 1, 32) X(5, 1, 16) X(5, 2, 8) \
+  X(6, 1, 16) X(6, 1, 8) X(7, 1, 16) X(7, 1, 8) X(8, 1, 8) X(9, 1, 8)
+
+int rhs_prepare(int n, int E, int L, int* ctas) {
+#define MJ_X(NV, EV, LV) \
+  if (n == NV && E == EV && L == LV) return rhs_prepare_one<NV, EV, LV>(ctas);
+  MJ_RHS_VARIANTS(MJ_X)
+#undef MJ_X
+  set_error("no many-RHS element kernel variant for this order");
+  return MJ_ERR_ARG;
+}
+
+void rhs_launch(int n, int E, int L, int grid, const float* x, const int* nodle_e, const float* fac_e, float* R,
+                int n_tiles, int S, int* err, cudaStream_t s) {
+#define MJ_X(NV, EV, LV)                                                             \
+  if (n == NV && E == EV && L == LV) {                                               \
+    rhs_launch_one<NV, EV, LV>(grid, x, nodle_e, fac_e, R, n_tiles, S, err, s);      \
+    return;                                                                          \
+  }
+  MJ_RHS_VARIANTS(MJ_X)
+#undef MJ_X
+}
+
+// ---- per-(dof, rhs) kernels ------------------------------------------------
+
+// Gather + sources + leap-frog, thread per (dof d, right-hand side s):
+//   Ah = -(A U1)[d][s] + p * F_s[d];  U[d][s] <- 2 U1 - U0 + (dt^2/D_d) Ah
+// Source entries are CSR entries with pos < 0: slot -pos-1 of (src_val,
+// src_rhs) applies to right-hand side src_rhs only.  The pulse of the step
+// is pulse[ctr[q]]; block 0 writes ctr[1-q] = ctr[q] + 1 for the next step
+// (two counters, so a captured sequence of steps needs no host update).
+__global__ void k_gather_leapfrog_rhs(const float* __restrict__ R, const int* __restrict__ ptr,
+                                      const int* __restrict__ pos, const float* __restrict__ src_val,
+                                      const int* __restrict__ src_rhs, const double* __restrict__ pulse, int n_pulse,
+                                      int* __restrict__ ctr, int q, float* __restrict__ u0,
+                                      const float* __restrict__ u1, const float* __restrict__ m, int n_dof, int S) {
+  const int step = ctr[q];
+  const float p = (step < n_pulse) ? (float)pulse[step] : 0.f;
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctr[1 - q] = step + 1;
+  const long long total = (long long)n_dof * S;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int d = (int)(t / S);
+    const int s = (int)(t - (long long)d * S);
+    float y = 0.f;
+    const int q1 = __ldg(ptr + d + 1);
+    for (int e = __ldg(ptr + d); e < q1; e++) {
+      const int ps = __ldg(pos + e);
+      if (ps >= 0) y += __ldg(R + (size_t)ps * S + s);
+      else if (__ldg(src_rhs + (-ps - 1)) == s) y += -p * __ldg(src_val + (-ps - 1));
+    }
+    u0[t] = 2.f * __ldg(u1 + t) - u0[t] + __ldg(m + d) * (-y);
+  }
+}
+
+// First step U1 = U0 + dt (dU0 + dt/2 D^-1 (-A U0)) for every right-hand side.
+// du0 and u1 may be the same array (each thread reads its entry before writing it).
+__global__ void k_gather_init_rhs(const float* __restrict__ R, const int* __restrict__ ptr,
+                                  const int* __restrict__ pos, const float* __restrict__ u0, const float* du0,
+                                  const double* __restrict__ inv_mass, double dt, float* u1, int n_dof, int S) {
+  const long long total = (long long)n_dof * S;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int d = (int)(t / S);
+    const int s = (int)(t - (long long)d * S);
+    float y = 0.f;
+    for (int e = ptr[d]; e < ptr[d + 1]; e++) {
+      const int ps = pos[e];
+      if (ps >= 0) y += R[(size_t)ps * S + s];
+    }
+    double v = double(-y) * inv_mass[d];
+    v *= 0.5 * dt;
+    v += du0 ? double(du0[t]) : 0.0;
+    v *= dt;
+    u1[t] = float(v + double(u0[t]));
+  }
+}
+
+// Receiver k, right-hand side s: sum_t W[k][t] U[idx[k][t]][s], FP64 sum;
+// written to out[(k*S + s)*stride + col].
+__global__ void k_receivers_rhs(const float* __restrict__ u, const int* __restrict__ idx,
+                                const double* __restrict__ w, int n_rec, int n_w, int S,
+                                double* __restrict__ out, int stride, int col) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_rec * S) return;
+  const int k = t / S, s = t - k * S;
+  double acc = 0.0;
+  for (int a = 0; a < n_w; a++) acc += w[(size_t)k * n_w + a] * double(u[(size_t)idx[(size_t)k * n_w + a] * S + s]);
+  out[(size_t)t * stride + col] = acc;
+}
+
+__global__ void k_cast_f64_to_f32(const double* __restrict__ a, float* __restrict__ b, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+__global__ void k_cast_f32_to_f64(const float* __restrict__ a, double* __restrict__ b, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    b[i] = (double)a[i];
+}
+
+int grid_for(long long n) {
+  return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, (long long)sm_count() * 16));
+}
+
+}  // namespace
+
+// Derivative matrix of order n into this unit's constant memory.
+int k1_set_gmat_rhs(int n, const double* g) {
+  float v[kMaxNK * kMaxNK];
+  for (int a = 0; a < n * n; a++) v[a] = (float)g[a];
+  MJ_CUDA(cudaMemcpyToSymbol(c_gmat32, v, sizeof(float) * n * n, sizeof(float) * kMaxNK * kMaxNK * n));
+  return MJ_OK;
+}
+
+std::vector<RhsVariant> k1_rhs_candidates(int n) {
+  switch (n) {
+    case 2: return {{4, 32}, {8, 16}};
+    case 3: return {{2, 32}, {4, 16}};
+    case 4: return {{1, 32}, {2, 16}};
+    case 5: return {{1, 32}, {1, 16}, {2, 8}};
+    case 6: return {{1, 16}, {1, 8}};
+    case 7: return {{1, 16}, {1, 8}};
+    case 8: return {{1, 8}};
+    case 9: return {{1, 8}};
+  }
+  return {};
+}
+
+}  // namespace mj
+
+using namespace mj;
+
+struct mj_lfb {
+  mj_op* op = nullptr;
+  int S = 0, n_dof = 0;
+  double dt = 0;
+  int E = 1, L = 32, grid = 1, n_tiles = 0;  // tuned element-kernel variant
+  DevBuf R;                                  // element-local results [slot][S]
+  DevBuf ptr, pos, src_val, src_rhs, m, inv_mass64, pulse, ctr;
+  DevBuf ua, ub, stage, rec_idx, rec_w, traces_d;
+  int n_pulse = 0, n_rec = 0, n_rec_w = 0;
+  int step = 0;
+  bool cur_is_a = true, initialised = false;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int graph_steps = 0;
+  std::vector<double> tune_ms;
+  ~mj_lfb() {
+    if (graph) cudaGraphExecDestroy(graph);
+  }
+  float* cur() { return (cur_is_a ? ua : ub).as<float>(); }
+  float* next() { return (cur_is_a ? ub : ua).as<float>(); }
+};
+
+namespace {
+
+void lfb_k1(mj_lfb* b, const float* x, cudaStream_t s) {
+  mj_op* op = b->op;
+  rhs_launch(op->n, b->E, b->L, b->grid, x, op->nodle_e.as<int>(), op->fac_e.as<float>(), b->R.as<float>(),
+             b->n_tiles, b->S, op->err.as<int>(), s);
+  count_launch();
+}
+
+// One leap-frog step of all right-hand sides; q = parity of the pulse counter.
+void lfb_step_launch(mj_lfb* b, float* cur, const float* next, int q, cudaStream_t s) {
+  lfb_k1(b, next, s);
+  const long long total = (long long)b->n_dof * b->S;
+  k_gather_leapfrog_rhs<<<grid_for(total), 256, 0, s>>>(
+      b->R.as<float>(), b->ptr.as<int>(), b->pos.as<int>(), b->src_val.as<float>(), b->src_rhs.as<int>(),
+      b->pulse.as<double>(), b->n_pulse, b->ctr.as<int>(), q, cur, next, b->m.as<float>(), b->n_dof, b->S);
+  count_launch();
+}
+
+int lfb_autotune(mj_lfb* b) {
+  mj_op* op = b->op;
+  const int sms = sm_count();
+  cudaEvent_t e0, e1;
+  MJ_CUDA(cudaEventCreate(&e0));
+  MJ_CUDA(cudaEventCreate(&e1));
+  double best = 1e300;
+  int bi = -1;
+  const std::vector<RhsVariant> cands = k1_rhs_candidates(op->n);
+  for (int c = 0; c < (int)cands.size(); c++) {
+    const RhsVariant v = cands[c];
+    if (b->S % v.L) continue;
+    int ctas = 0;
+    if (rhs_prepare(op->n, v.E, v.L, &ctas) != MJ_OK) continue;
+    b->E = v.E; b->L = v.L; b->n_tiles = op->n_elt_pad / v.E;
+    b->grid = std::max(1, std::min(b->n_tiles, ctas * sms));
+    lfb_k1(b, b->ua.as<float>(), b->stream);
+    MJ_CUDA(cudaEventRecord(e0, b->stream));
+    for (int rep = 0; rep < 2; rep++) lfb_k1(b, b->ua.as<float>(), b->stream);
+    MJ_CUDA(cudaEventRecord(e1, b->stream));
+    MJ_CUDA(cudaEventSynchronize(e1));
+    float f = 0.f;
+    MJ_CUDA(cudaEventElapsedTime(&f, e0, e1));
+    b->tune_ms.push_back(f / 2.0);
+    if (f < best) { best = f; bi = c; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (bi < 0) {
+    set_error("mj_lfb_create: no many-RHS element kernel variant fits (n_rhs must be a multiple of 8)");
+    return MJ_ERR_ARG;
+  }
+  const RhsVariant v = cands[bi];
+  int ctas = 0;
+  int rc = rhs_prepare(op->n, v.E, v.L, &ctas);
+  if (rc) return rc;
+  b->E = v.E; b->L = v.L; b->n_tiles = op->n_elt_pad / v.E;
+  b->grid = std::max(1, std::min(b->n_tiles, ctas * sms));
+  MJ_CUDA(cudaMemset(op->err.ptr, 0, sizeof(int)));
+  return MJ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mj_lfb_create(mj_op* op, const mj_lfb_desc* d, mj_lfb** out) {
+  MJ_CHECK_ARG(op && d && out, "mj_lfb_create: null argument");
+  *out = nullptr;
+  MJ_CHECK_ARG(op->precision == MJ_FP32, "mj_lfb_create: the many-RHS integrator needs an MJ_FP32 operator");
+  MJ_CHECK_ARG(d->n_rhs >= 8 && d->n_rhs % 8 == 0 && d->n_rhs <= 4096, "mj_lfb_create: n_rhs must be a multiple of 8 in [8, 4096]");
+  MJ_CHECK_ARG(d->dt > 0 && std::isfinite(d->dt), "mj_lfb_create: dt must be positive");
+  MJ_CHECK_ARG(d->mass, "mj_lfb_create: mass is required");
+  MJ_CHECK_ARG(d->n_src >= 0 && (d->n_src == 0 || (d->src_idx && d->src_rhs && d->src_val)),
+               "mj_lfb_create: bad source arrays");
+  MJ_CHECK_ARG(d->n_pulse >= 0 && (d->n_pulse == 0 || d->pulse), "mj_lfb_create: bad pulse array");
+  MJ_CHECK_ARG(d->n_rec >= 0 && (d->n_rec == 0 || (d->rec_idx && d->rec_w && d->n_rec_w > 0)),
+               "mj_lfb_create: bad receiver arrays");
+  const int n = op->n_dof, S = d->n_rhs;
+  std::unique_ptr<mj_lfb> b(new mj_lfb());
+  b->op = op; b->S = S; b->n_dof = n; b->dt = d->dt; b->stream = op->stream;
+  std::vector<double> invD(n);
+  std::vector<float> m(n);
+  for (int i = 0; i < n; i++) {
+    MJ_CHECK_ARG(std::isfinite(d->mass[i]) && d->mass[i] > 0, "mj_lfb_create: mass must be positive");
+    invD[i] = d->inv_mass ? d->inv_mass[i] : 1.0 / d->mass[i];
+    m[i] = (float)(d->dt * d->dt * invD[i]);
+  }
+  // CSR of the operator with each dof's source entries appended (sorted by rhs)
+  std::vector<std::vector<int>> src_of(n);
+  for (int t = 0; t < d->n_src; t++) {
+    MJ_CHECK_ARG(d->src_idx[t] >= 0 && d->src_idx[t] < n, "mj_lfb_create: source index out of range");
+    MJ_CHECK_ARG(d->src_rhs[t] >= 0 && d->src_rhs[t] < S, "mj_lfb_create: source right-hand side out of range");
+    src_of[d->src_idx[t]].push_back(t);
+  }
+  std::vector<int> ptr(n + 1, 0), pos;
+  pos.reserve(op->h_pos.size() + d->n_src);
+  for (int i = 0; i < n; i++) {
+    for (int q = op->h_ptr[i]; q < op->h_ptr[i + 1]; q++) pos.push_back(op->h_pos[q]);
+    for (int t : src_of[i]) pos.push_back(-t - 1);
+    ptr[i + 1] = (int)pos.size();
+  }
+  std::vector<float> sv(std::max(1, d->n_src));
+  std::vector<int> sr(std::max(1, d->n_src), -1);
+  for (int t = 0; t < d->n_src; t++) { sv[t] = (float)d->src_val[t]; sr[t] = d->src_rhs[t]; }
+  const size_t rows = (size_t)n * S;
+  MJ_CUDA(b->R.alloc(sizeof(float) * op->r_len * S));
+  MJ_CUDA(b->ptr.alloc(sizeof(int) * (n + 1)));
+  MJ_CUDA(b->pos.alloc(sizeof(int) * pos.size()));
+  MJ_CUDA(b->src_val.alloc(sizeof(float) * sv.size()));
+  MJ_CUDA(b->src_rhs.alloc(sizeof(int) * sr.size()));
+  MJ_CUDA(b->m.alloc(sizeof(float) * n));
+  MJ_CUDA(b->inv_mass64.alloc(sizeof(double) * n));
+  MJ_CUDA(b->pulse.alloc(sizeof(double) * std::max(1, d->n_pulse)));
+  MJ_CUDA(b->ctr.alloc(sizeof(int) * 2));
+  MJ_CUDA(b->ua.alloc(sizeof(float) * rows));
+  MJ_CUDA(b->ub.alloc(sizeof(float) * rows));
+  MJ_CUDA(cudaMemcpy(b->ptr.ptr, ptr.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
+  MJ_CUDA(cudaMemcpy(b->pos.ptr, pos.data(), sizeof(int) * pos.size(), cudaMemcpyHostToDevice));
+  MJ_CUDA(cudaMemcpy(b->src_val.ptr, sv.data(), sizeof(float) * sv.size(), cudaMemcpyHostToDevice));
+  MJ_CUDA(cudaMemcpy(b->src_rhs.ptr, sr.data(), sizeof(int) * sr.size(), cudaMemcpyHostToDevice));
+  MJ_CUDA(cudaMemcpy(b->m.ptr, m.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+  MJ_CUDA(cudaMemcpy(b->inv_mass64.ptr, invD.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+  if (d->n_pulse) MJ_CUDA(cudaMemcpy(b->pulse.ptr, d->pulse, sizeof(double) * d->n_pulse, cudaMemcpyHostToDevice));
+  b->n_pulse = d->n_pulse;
+  MJ_CUDA(cudaMemset(b->ctr.ptr, 0, sizeof(int) * 2));
+  MJ_CUDA(cudaMemset(b->ua.ptr, 0, sizeof(float) * rows));
+  MJ_CUDA(cudaMemset(b->ub.ptr, 0, sizeof(float) * rows));
+  b->n_rec = d->n_rec;
+  b->n_rec_w = d->n_rec_w;
+  if (d->n_rec) {
+    const size_t mrec = (size_t)d->n_rec * d->n_rec_w;
+    for (size_t t = 0; t < mrec; t++)
+      MJ_CHECK_ARG(d->rec_idx[t] >= 0 && d->rec_idx[t] < n, "mj_lfb_create: receiver dof out of range");
+    MJ_CUDA(b->rec_idx.alloc(sizeof(int) * mrec));
+    MJ_CUDA(b->rec_w.alloc(sizeof(double) * mrec));
+    MJ_CUDA(cudaMemcpy(b->rec_idx.ptr, d->rec_idx, sizeof(int) * mrec, cudaMemcpyHostToDevice));
+    MJ_CUDA(cudaMemcpy(b->rec_w.ptr, d->rec_w, sizeof(double) * mrec, cudaMemcpyHostToDevice));
+  }
+  int rc = k1_set_gmat_rhs(op->n, op->gradphi);
+  if (rc) return rc;
+  rc = lfb_autotune(b.get());
+  if (rc) return rc;
+  *out = b.release();
+  return MJ_OK;
+}
+
+int mj_lfb_destroy(mj_lfb* b) {
+  delete b;
+  return MJ_OK;
+}
+
+int mj_lfb_init(mj_lfb* b, const double* u0, const double* du0) {
+  MJ_CHECK_ARG(b, "mj_lfb_init: null integrator");
+  cudaStream_t s = b->stream;
+  const long long rows = (long long)b->n_dof * b->S;
+  if (b->stage.bytes < sizeof(double) * rows) MJ_CUDA(b->stage.alloc(sizeof(double) * rows));
+  // U^0
+  if (u0) {
+    MJ_CUDA(cudaMemcpyAsync(b->stage.ptr, u0, sizeof(double) * rows, cudaMemcpyHostToDevice, s));
+    k_cast_f64_to_f32<<<grid_for(rows), 256, 0, s>>>(b->stage.as<double>(), b->ua.as<float>(), rows);
+    count_launch();
+  } else {
+    MJ_CUDA(cudaMemsetAsync(b->ua.ptr, 0, sizeof(float) * rows, s));
+  }
+  // dU^0 staged in ub, overwritten by U^1 below (each thread reads its own entry first)
+  const float* du = nullptr;
+  if (du0) {
+    MJ_CUDA(cudaMemcpyAsync(b->stage.ptr, du0, sizeof(double) * rows, cudaMemcpyHostToDevice, s));
+    k_cast_f64_to_f32<<<grid_for(rows), 256, 0, s>>>(b->stage.as<double>(), b->ub.as<float>(), rows);
+    count_launch();
+    du = b->ub.as<float>();
+  }
+  lfb_k1(b, b->ua.as<float>(), s);
+  k_gather_init_rhs<<<grid_for(rows), 256, 0, s>>>(b->R.as<float>(), b->ptr.as<int>(), b->pos.as<int>(),
+                                                   b->ua.as<float>(), du, b->inv_mass64.as<double>(), b->dt,
+                                                   b->ub.as<float>(), b->n_dof, b->S);
+  count_launch();
+  MJ_CUDA(cudaMemsetAsync(b->ctr.ptr, 0, sizeof(int) * 2, s));
+  MJ_CUDA(cudaGetLastError());
+  MJ_CUDA(cudaStreamSynchronize(s));
+  b->cur_is_a = true;
+  b->step = 0;
+  b->initialised = true;
+  return MJ_OK;
+}
+
+// Advances nsteps steps of every right-hand side.  With use_graph, chunks of
+// 2*k steps replay one captured CUDA graph (instantiated on first use);
+// traces (if not NULL and receivers were given) are sampled before every
+// step into traces[(k*S + s)*trace_stride + step_in_call] (no graph then).
+int mj_lfb_advance(mj_lfb* b, int nsteps, double* traces, int trace_stride, int use_graph) {
+  MJ_CHECK_ARG(b, "mj_lfb_advance: null integrator");
+  MJ_CHECK_ARG(nsteps >= 0, "mj_lfb_advance: negative step count");
+  if (!b->initialised) {
+    set_error("mj_lfb_advance: mj_lfb_init must be called first");
+    return MJ_ERR_STATE;
+  }
+  cudaStream_t s = b->stream;
+  const bool diag = traces && b->n_rec;
+  if (diag) {
+    MJ_CHECK_ARG(trace_stride >= nsteps, "mj_lfb_advance: trace_stride smaller than nsteps");
+    const size_t bytes = sizeof(double) * (size_t)b->n_rec * b->S * nsteps;
+    if (b->traces_d.bytes < bytes) MJ_CUDA(b->traces_d.alloc(bytes));
+  }
+  int done = 0;
+  const int G = 20;  // steps per captured graph (even: buffers and counters return to their roles)
+  if (use_graph && !diag && nsteps >= G + 1) {
+    if (b->step & 1) {  // realign: graphs start on an even step with ua holding U^n
+      lfb_step_launch(b, b->cur(), b->next(), b->step & 1, s);
+      b->cur_is_a = !b->cur_is_a;
+      b->step++;
+      done++;
+    }
+    if (!b->graph) {
+      cudaStream_t cs;
+      MJ_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+      cudaGraph_t g;
+      const uint64_t launches_before = launch_counter().load();
+      MJ_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+      bool a = true;
+      for (int k = 0; k < G; k++) {
+        float* cur = (a ? b->ua : b->ub).as<float>();
+        float* nxt = (a ? b->ub : b->ua).as<float>();
+        lfb_step_launch(b, cur, nxt, k & 1, cs);
+        a = !a;
+      }
+      MJ_CUDA(cudaStreamEndCapture(cs, &g));
+      launch_counter().store(launches_before);  // captured, not launched
+      MJ_CUDA(cudaGraphInstantiate(&b->graph, g, 0));
+      cudaGraphDestroy(g);
+      cudaStreamDestroy(cs);
+      b->graph_steps = G;
+    }
+    while (nsteps - done >= G) {
+      MJ_CUDA(cudaGraphLaunch(b->graph, s));
+      count_launch(2 * G);
+      done += G;
+      b->step += G;
+    }
+  }
+  for (; done < nsteps; done++) {
+    if (diag) {
+      const int threads = 128, blocks = (b->n_rec * b->S + threads - 1) / threads;
+      k_receivers_rhs<<<blocks, threads, 0, s>>>(b->cur(), b->rec_idx.as<int>(), b->rec_w.as<double>(), b->n_rec,
+                                                 b->n_rec_w, b->S, b->traces_d.as<double>(), nsteps, done);
+      count_launch();
+    }
+    lfb_step_launch(b, b->cur(), b->next(), b->step & 1, s);
+    b->cur_is_a = !b->cur_is_a;
+    b->step++;
+  }
+  MJ_CUDA(cudaGetLastError());
+  if (diag)
+    for (int r = 0; r < b->n_rec * b->S; r++)
+      MJ_CUDA(cudaMemcpyAsync(traces + (size_t)r * trace_stride, b->traces_d.as<double>() + (size_t)r * nsteps,
+                              sizeof(double) * nsteps, cudaMemcpyDeviceToHost, s));
+  int err = 0;
+  MJ_CUDA(cudaMemcpyAsync(&err, b->op->err.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MJ_CUDA(cudaStreamSynchronize(s));
+  if (err) {
+    set_error("mj_lfb_advance: an element kernel wait timed out");
+    return MJ_ERR_CUDA;
+  }
+  return MJ_OK;
+}
+
+int mj_lfb_get_state(mj_lfb* b, double* u_n, double* u_np1) {
+  MJ_CHECK_ARG(b, "mj_lfb_get_state: null integrator");
+  cudaStream_t s = b->stream;
+  const long long rows = (long long)b->n_dof * b->S;
+  if (b->stage.bytes < sizeof(double) * rows) MJ_CUDA(b->stage.alloc(sizeof(double) * rows));
+  const float* src[2] = {b->cur(), b->next()};
+  double* dst[2] = {u_n, u_np1};
+  for (int k = 0; k < 2; k++) {
+    if (!dst[k]) continue;
+    k_cast_f32_to_f64<<<grid_for(rows), 256, 0, s>>>(src[k], b->stage.as<double>(), rows);
+    count_launch();
+    MJ_CUDA(cudaMemcpyAsync(dst[k], b->stage.ptr, sizeof(double) * rows, cudaMemcpyDeviceToHost, s));
+    MJ_CUDA(cudaStreamSynchronize(s));
+  }
+  return MJ_OK;
+}
+
+int mj_lfb_info(const mj_lfb* b, int* n_rhs, int* tile_elems, int* lanes, int* grid, int* step) {
+  MJ_CHECK_ARG(b, "mj_lfb_info: null integrator");
+  if (n_rhs) *n_rhs = b->S;
+  if (tile_elems) *tile_elems = b->E;
+  if (lanes) *lanes = b->L;
+  if (grid) *grid = b->grid;
+  if (step) *step = b->step;
+  return MJ_OK;
+}
+
+}  // extern "C"

@@ -17,6 +17,15 @@ namespace mj {
 constexpr int kMaxOrder = 8;
 constexpr int kMaxN = kMaxOrder + 1;
 
+// Element count padding of the element-major layout: a multiple of every
+// tile size the element kernels use, so any of them covers the mesh with
+// whole tiles of empty (zero) padding elements.
+constexpr int kElemPad = 240;
+
+// Slots per element: n^3 rounded up to 4, so per-element blocks of int32,
+// float and double start on 16-byte boundaries (the bulk-copy rule).
+__host__ __device__ constexpr int elem_slots(int n) { return (n * n * n + 3) / 4 * 4; }
+
 void set_error(const std::string& msg);
 std::atomic<uint64_t>& launch_counter();
 

@@ -1,0 +1,58 @@
+// Internal state of an operator, shared by the translation units of the
+// library (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "mj_common.cuh"
+
+struct mj_op {
+  int order = 0, n = 0, Q = 0, Qp = 0;
+  int n_elt = 0, n_elt_pad = 0, n_dof = 0, precision = MJ_FP64;
+  int E = 1, n_tiles = 0, grid_k1 = 1;  // tile size and grid of the element kernel (autotuned)
+  size_t r_len = 0;                     // slots of R (n_elt_pad * Qp)
+  mj::DevBuf nodle_e, fac_e, R, ptr, pos;
+  mj::DevBuf err;                       // device error flag (bounded-wait timeouts)
+  std::vector<int> h_ptr, h_pos;        // CSR incidences (host copy, for integrators)
+  double gradphi[mj::kMaxN * mj::kMaxN];
+  mj::DevBuf xbuf, ybuf;                // staging for host-vector MltAdd
+  cudaStream_t stream = nullptr;
+  std::vector<double> tune_ms;          // autotuner timings of the candidates (diagnostic)
+  std::vector<int> tune_E;
+  size_t device_bytes() const {
+    return nodle_e.bytes + fac_e.bytes + R.bytes + ptr.bytes + pos.bytes + xbuf.bytes + ybuf.bytes;
+  }
+};
+
+namespace mj {
+
+// Tile sizes E (elements per CTA) instantiated for order n = r + 1, all
+// dividing kElemPad (240).
+std::vector<int> k1_tile_candidates(int n);
+
+// Element-kernel entry points, one set per precision (mj_k1_f64.cu, mj_k1_f32.cu).
+// set_gmat: writes the derivative matrix of order n into that unit's constant memory.
+// prepare: sets the shared-memory attribute of variant (n, E) and returns its
+//   occupancy (CTAs per SM); fails when the variant does not fit.
+// launch: one launch of variant (n, E) on `grid` CTAs.
+int k1_set_gmat_f64(int n, const double* g);
+int k1_set_gmat_f32(int n, const double* g);
+int k1_prepare_f64(int n, int E, int* ctas_per_sm);
+int k1_prepare_f32(int n, int E, int* ctas_per_sm);
+void k1_launch_f64(int n, int E, int grid, const void* x, const int* nodle_e, const void* fac_e, void* R, int n_tiles,
+                   int* err, cudaStream_t s);
+void k1_launch_f32(int n, int E, int grid, const void* x, const int* nodle_e, const void* fac_e, void* R, int n_tiles,
+                   int* err, cudaStream_t s);
+
+// Many right-hand sides (FP32 only, mj_batch.cu).
+struct RhsVariant {
+  int E, L;
+};
+std::vector<RhsVariant> k1_rhs_candidates(int n);
+int k1_set_gmat_rhs(int n, const double* g);
+
+int stream_grid(int n);
+
+}  // namespace mj

@@ -1,0 +1,373 @@
+// Element kernels (K1) of the matrix-free Q_r hexahedral stiffness operator
+// (sm_103a): single right-hand side and many right-hand sides.
+//
+// Data layout in HBM ("element-major").  Every element owns Qp = n^3 rounded
+// up to 4 consecutive slots; point (i,j,k) of element e (i along x) is slot
+// p = (k*n + j)*n + i:
+//   nodle_e[e*Qp + p]            int32 global dof
+//   fac_e  [(e*6 + c)*Qp + p]    the six factors (c = xx,xy,xz,yy,yz,zz)
+//   R      [e*Qp + p]            element-local A*u (single RHS)
+//   R      [(e*Qp + p)*S + s]    element-local A*u (S right-hand sides)
+// The element count is padded to a multiple of 240 with empty elements
+// (Nodle 0, factors 0), so every tile size E that divides 240 covers the mesh
+// with whole tiles and E can be chosen at run time (the autotuner does).
+// A tile of E consecutive elements is one contiguous block per array, so it
+// is brought into shared memory by one 1-D bulk copy per array.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace mj {
+
+using ::uint32_t;
+using ::uint64_t;
+
+constexpr int kMaxNK = 9;  // largest n = r + 1 of the kernels
+
+// Derivative matrices g[a*n + b] = phi_a'(x_b) of every order in constant
+// memory (one slot per n and precision; each translation unit that launches
+// element kernels keeps its own copy, written at operator creation).
+static __constant__ double c_gmat64[kMaxNK + 1][kMaxNK * kMaxNK];
+static __constant__ float c_gmat32[kMaxNK + 1][kMaxNK * kMaxNK];
+
+template <typename Real>
+struct GConst;
+template <>
+struct GConst<double> {
+  __device__ static const double* get(int n) { return c_gmat64[n]; }
+};
+template <>
+struct GConst<float> {
+  __device__ static const float* get(int n) { return c_gmat32[n]; }
+};
+
+// ---------------------------------------------------------------------------
+// Bulk-copy (TMA) and mbarrier helpers.  Every wait is bounded: after
+// kSpinLimit unsuccessful polls the waiter gives up and the kernel reports
+// the timeout through an error flag instead of hanging.
+// ---------------------------------------------------------------------------
+constexpr long kSpinLimit = 1L << 22;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+
+// 1-D bulk copy global -> shared, completion counted on `bar` (16-byte aligned
+// addresses, size a multiple of 16).
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  for (long it = 0; it < kSpinLimit; ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+// Shared-memory plan of one element kernel: two stages of [factors | Nodle]
+// for a tile of E elements, work arrays, two mbarriers.  L = right-hand
+// sides handled per pass (1 for the single-RHS kernel).
+template <typename Real, int N, int E, int L>
+struct K1Plan {
+  static constexpr int NN = N * N;
+  static constexpr int Q = N * NN;
+  static constexpr int Qp = elem_slots(N);
+  static constexpr size_t fac_bytes = sizeof(Real) * 6 * E * Qp;
+  static constexpr size_t nod_bytes = sizeof(int) * E * Qp;
+  static constexpr size_t stage_bytes = fac_bytes + nod_bytes;
+  static constexpr size_t work_bytes = ((sizeof(Real) * 3 * E * Q * L + 15) / 16) * 16;
+  static constexpr size_t total = 2 * stage_bytes + work_bytes + 2 * sizeof(uint64_t);
+  static constexpr int threads = E * NN * L;
+};
+
+// ---------------------------------------------------------------------------
+// K1, single right-hand side: element-local stiffness product, sum-factorised.
+//
+// Per element (MltAdd_ElementH1_Scalar, ProdMatVectScalarH1.cxx:256-668):
+//   u(i,j,k)  = x[Nodle(e, num(i,j,k))]                        gather
+//   gx(l,m,p) = sum_a G[a][l] u(a,m,p)   (gy, gz likewise)      Rh^T
+//   v = B(l,m,p) (gx,gy,gz)                                    geometry
+//   Y(i,j,k)  = sum_a G[i][a] vx(a,j,k) + G[j][a] vy(i,a,k) + G[k][a] vz(i,j,a)   Rh
+//   R = Y                                                      (scatter: K2)
+// E*n*n threads, thread (el, j, i) owning the z-line (i, j, k = 0..n-1) of
+// element el of the tile: z contractions in registers, x and y through shared
+// memory.  A persistent CTA walks tiles blockIdx.x, +gridDim.x, ...; the
+// factors and Nodle of a tile arrive by bulk copy two tiles ahead (double
+// buffer, one mbarrier per stage) and the gather of the next tile's u is in
+// flight during the current tile's divergence.
+// ---------------------------------------------------------------------------
+template <typename Real, int N, int E>
+__global__ void __launch_bounds__(E* N* N)
+    k_local_stiffness(const Real* __restrict__ x, const int* __restrict__ nodle_e,
+                      const Real* __restrict__ fac_e, Real* __restrict__ R, int n_tiles,
+                      int* __restrict__ err) {
+  using P = K1Plan<Real, N, E, 1>;
+  constexpr int NN = P::NN, Qp = P::Qp;
+  const Real* __restrict__ Gm = GConst<Real>::get(N);
+  extern __shared__ __align__(128) unsigned char smem[];
+  auto s_fac = [&](int st) { return reinterpret_cast<Real*>(smem + st * P::stage_bytes); };
+  auto s_nod = [&](int st) { return reinterpret_cast<int*>(smem + st * P::stage_bytes + P::fac_bytes); };
+  Real* s_u = reinterpret_cast<Real*>(smem + 2 * P::stage_bytes);
+  Real* s_vx = s_u + E * N * NN;
+  Real* s_vy = s_vx + E * N * NN;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 2 * P::stage_bytes + P::work_bytes);
+
+  const int t = threadIdx.x;
+  const int el = t / NN;
+  const int ij = t - el * NN;
+  const int j = ij / N;
+  const int i = ij - j * N;
+  Real gci[N], gcj[N], gri[N], grj[N];
+#pragma unroll
+  for (int a = 0; a < N; a++) {
+    gci[a] = Gm[a * N + i];
+    gcj[a] = Gm[a * N + j];
+    gri[a] = Gm[i * N + a];
+    grj[a] = Gm[j * N + a];
+  }
+  const int s_base = el * N * NN;             // element el in the work arrays
+  const int s_line_x = s_base + j * N;        // + k*NN + a   : row (j,k) along x
+  const int s_line_y = s_base + i;            // + k*NN + a*N : row (i,k) along y
+  const int pe = el * Qp + ij;                // slot (k = 0) of this thread in the tile block
+
+  if (t == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  auto issue = [&](int stage, int tile) {
+    if (t == 0 && tile < n_tiles) {
+      mbar_expect_tx(&bar[stage], (uint32_t)P::stage_bytes);
+      bulk_g2s(s_fac(stage), fac_e + (size_t)tile * E * 6 * Qp, (uint32_t)P::fac_bytes, &bar[stage]);
+      bulk_g2s(s_nod(stage), nodle_e + (size_t)tile * E * Qp, (uint32_t)P::nod_bytes, &bar[stage]);
+    }
+  };
+  const int g = gridDim.x;
+  int tile = blockIdx.x;
+  issue(0, tile);
+  issue(1, tile + g);
+  uint32_t ph = 0u;  // bit st: parity of the next completion of stage st
+  Real u[N];
+  if (tile < n_tiles) {
+    const bool ok = mbar_wait_bounded(&bar[0], ph & 1u);
+    if (__syncthreads_or(!ok)) {
+      if (t == 0) atomicExch(err, 1);
+      return;
+    }
+    ph ^= 1u;
+    const int* nd = s_nod(0) + pe;
+#pragma unroll
+    for (int k = 0; k < N; k++) u[k] = __ldg(x + nd[k * NN]);
+  }
+  for (int it = 0; tile < n_tiles; tile += g, ++it) {
+    const int s = it & 1;
+#pragma unroll
+    for (int k = 0; k < N; k++) s_u[s_base + k * NN + ij] = u[k];
+    __syncthreads();
+
+    const Real* f = s_fac(s) + el * 6 * Qp + ij;
+    Real vz[N];
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+      Real gx = 0, gy = 0, gz = 0;
+#pragma unroll
+      for (int a = 0; a < N; a++) {
+        gz += Gm[a * N + k] * u[a];
+        gx += gci[a] * s_u[s_line_x + k * NN + a];
+        gy += gcj[a] * s_u[s_line_y + k * NN + a * N];
+      }
+      const Real* fk = f + k * NN;
+      const Real bxx = fk[0], bxy = fk[Qp], bxz = fk[2 * Qp];
+      const Real byy = fk[3 * Qp], byz = fk[4 * Qp], bzz = fk[5 * Qp];
+      s_vx[s_base + k * NN + ij] = bxx * gx + bxy * gy + bxz * gz;
+      s_vy[s_base + k * NN + ij] = bxy * gx + byy * gy + byz * gz;
+      vz[k] = bxz * gx + byz * gy + bzz * gz;
+    }
+    __syncthreads();
+
+    // gather of the next tile's u, in flight during the divergence below
+    const int nt = tile + g;
+    if (nt < n_tiles) {
+      const int so = s ^ 1;
+      const bool ok = mbar_wait_bounded(&bar[so], (ph >> so) & 1u);
+      if (__syncthreads_or(!ok)) {
+        if (t == 0) atomicExch(err, 1);
+        return;
+      }
+      ph ^= 1u << so;
+      const int* nd = s_nod(so) + pe;
+#pragma unroll
+      for (int k = 0; k < N; k++) u[k] = __ldg(x + nd[k * NN]);
+    }
+
+    Real* Rt = R + ((size_t)tile * E + el) * Qp + ij;
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+      Real y = 0;
+#pragma unroll
+      for (int a = 0; a < N; a++) {
+        y += gri[a] * s_vx[s_line_x + k * NN + a];
+        y += grj[a] * s_vy[s_line_y + k * NN + a * N];
+        y += Gm[k * N + a] * vz[a];
+      }
+      Rt[k * NN] = y;
+    }
+    __syncthreads();  // stage s and the work arrays are free again
+    if (t == 0) fence_proxy_async();
+    issue(s, tile + 2 * g);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// K1, many right-hand sides (FP32 state [dof][S], S a multiple of L):
+// the same element product for S independent right-hand sides sharing the
+// mesh.  L lanes (consecutive threads) carry L right-hand sides of one
+// z-line, so every gather of a dof row and every write of R moves L
+// contiguous values; the factors and Nodle of a tile are staged once and
+// reused for all S/L passes.  E*n*n*L threads.
+// ---------------------------------------------------------------------------
+template <int N, int E, int L>
+__global__ void __launch_bounds__(E* N* N* L)
+    k_local_stiffness_rhs(const float* __restrict__ x, const int* __restrict__ nodle_e,
+                          const float* __restrict__ fac_e, float* __restrict__ R, int n_tiles, int S,
+                          int* __restrict__ err) {
+  using P = K1Plan<float, N, E, L>;
+  constexpr int NN = P::NN, Qp = P::Qp;
+  const float* __restrict__ Gm = GConst<float>::get(N);
+  extern __shared__ __align__(128) unsigned char smem[];
+  auto s_fac = [&](int st) { return reinterpret_cast<float*>(smem + st * P::stage_bytes); };
+  auto s_nod = [&](int st) { return reinterpret_cast<int*>(smem + st * P::stage_bytes + P::fac_bytes); };
+  float* s_u = reinterpret_cast<float*>(smem + 2 * P::stage_bytes);
+  float* s_vx = s_u + E * N * NN * L;
+  float* s_vy = s_vx + E * N * NN * L;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 2 * P::stage_bytes + P::work_bytes);
+
+  const int lane = threadIdx.x % L;
+  const int w = threadIdx.x / L;
+  const int el = w / NN;
+  const int ij = w - el * NN;
+  const int j = ij / N;
+  const int i = ij - j * N;
+  float gci[N], gcj[N], gri[N], grj[N];
+#pragma unroll
+  for (int a = 0; a < N; a++) {
+    gci[a] = Gm[a * N + i];
+    gcj[a] = Gm[a * N + j];
+    gri[a] = Gm[i * N + a];
+    grj[a] = Gm[j * N + a];
+  }
+  // work arrays: value (el, k, j, i) of lane l at ((el*N + k)*NN + j*N + i)*L + l
+  const int s_base = el * N * NN;
+  const int s_line_x = s_base + j * N;
+  const int s_line_y = s_base + i;
+  const int pe = el * Qp + ij;
+
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  auto issue = [&](int stage, int tile) {
+    if (threadIdx.x == 0 && tile < n_tiles) {
+      mbar_expect_tx(&bar[stage], (uint32_t)P::stage_bytes);
+      bulk_g2s(s_fac(stage), fac_e + (size_t)tile * E * 6 * Qp, (uint32_t)P::fac_bytes, &bar[stage]);
+      bulk_g2s(s_nod(stage), nodle_e + (size_t)tile * E * Qp, (uint32_t)P::nod_bytes, &bar[stage]);
+    }
+  };
+  const int g = gridDim.x;
+  int tile = blockIdx.x;
+  issue(0, tile);
+  issue(1, tile + g);
+  uint32_t ph = 0u;
+  const int passes = S / L;
+  for (int it = 0; tile < n_tiles; tile += g, ++it) {
+    const int s = it & 1;
+    const bool ok = mbar_wait_bounded(&bar[s], (ph >> s) & 1u);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicExch(err, 1);
+      return;
+    }
+    ph ^= 1u << s;
+    const int* nd = s_nod(s) + pe;
+    const float* f = s_fac(s) + el * 6 * Qp + ij;
+    int dofs[N];
+#pragma unroll
+    for (int k = 0; k < N; k++) dofs[k] = nd[k * NN];
+    for (int pass = 0; pass < passes; ++pass) {
+      const int col = pass * L + lane;
+      float u[N];
+#pragma unroll
+      for (int k = 0; k < N; k++) {
+        u[k] = __ldg(x + (size_t)dofs[k] * S + col);
+        s_u[(s_base + k * NN + ij) * L + lane] = u[k];
+      }
+      __syncthreads();
+      float vz[N];
+#pragma unroll
+      for (int k = 0; k < N; k++) {
+        float gx = 0, gy = 0, gz = 0;
+#pragma unroll
+        for (int a = 0; a < N; a++) {
+          gz += Gm[a * N + k] * u[a];
+          gx += gci[a] * s_u[(s_line_x + k * NN + a) * L + lane];
+          gy += gcj[a] * s_u[(s_line_y + k * NN + a * N) * L + lane];
+        }
+        const float* fk = f + k * NN;
+        const float bxx = fk[0], bxy = fk[Qp], bxz = fk[2 * Qp];
+        const float byy = fk[3 * Qp], byz = fk[4 * Qp], bzz = fk[5 * Qp];
+        s_vx[(s_base + k * NN + ij) * L + lane] = bxx * gx + bxy * gy + bxz * gz;
+        s_vy[(s_base + k * NN + ij) * L + lane] = bxy * gx + byy * gy + byz * gz;
+        vz[k] = bxz * gx + byz * gy + bzz * gz;
+      }
+      __syncthreads();
+      float* Rt = R + (((size_t)tile * E + el) * Qp + ij) * S + col;
+#pragma unroll
+      for (int k = 0; k < N; k++) {
+        float y = 0;
+#pragma unroll
+        for (int a = 0; a < N; a++) {
+          y += gri[a] * s_vx[(s_line_x + k * NN + a) * L + lane];
+          y += grj[a] * s_vy[(s_line_y + k * NN + a * N) * L + lane];
+          y += Gm[k * N + a] * vz[a];
+        }
+        Rt[(size_t)k * NN * S] = y;
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) fence_proxy_async();
+    issue(s, tile + 2 * g);
+  }
+}
+
+}  // namespace mj

@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "mj_common.cuh"
+#include "mj_internal.cuh"
 #include "mj_kernels.cuh"
 
 namespace mj {
@@ -41,12 +42,6 @@ __global__ void k_norm_final(const double* __restrict__ partial, int nparts, dou
   }
 }
 
-// Elements per tile for each n = r+1 (threads per CTA = E*n*n).
-constexpr int tile_elems_for(int n) {
-  return n == 2 ? 32 : n == 3 ? 14 : n == 4 ? 8 : n == 5 ? 5 : n == 6 ? 4 : n == 7 ? 3 : n == 8 ? 2 : n == 9 ? 2 : 1;
-}
-static int tile_elems(int n) { return tile_elems_for(n); }
-
 template <typename Real>
 __global__ void k_cast_from_f64(const double* __restrict__ a, Real* __restrict__ b, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = Real(a[i]);
@@ -59,23 +54,6 @@ __global__ void k_cast_to_f64(const Real* __restrict__ a, double* __restrict__ b
 }  // namespace mj
 
 using namespace mj;
-
-struct mj_op {
-  int order = 0, n = 0, Q = 0, n_elt = 0, n_dof = 0, precision = MJ_FP64;
-  int E = 1, n_tiles = 0;
-  size_t r_len = 0;  // length of R (tile-layout points)
-  DevBuf nodle_t, fac_t, R, ptr, pos;
-  DevBuf err;                     // device error flag (bounded-wait timeouts)
-  int TS = 0;                     // padded points per tile
-  std::vector<int> h_ptr, h_pos;  // CSR incidences (host copy, for integrators)
-  double gradphi[kMaxN * kMaxN];
-  DevBuf xbuf, ybuf;              // staging for host-vector MltAdd
-  cudaStream_t stream = nullptr;
-  int grid_k1 = 1;
-  size_t device_bytes() const {
-    return nodle_t.bytes + fac_t.bytes + R.bytes + ptr.bytes + pos.bytes + xbuf.bytes + ybuf.bytes;
-  }
-};
 
 struct mj_lf {
   mj_op* op = nullptr;
@@ -112,61 +90,86 @@ struct mj_lf {
 
 namespace {
 
-template <typename Real, int N>
-void launch_k1_n(mj_op* op, const void* x, cudaStream_t s) {
-  constexpr int E = tile_elems_for(N);
-  k_local_stiffness<Real, N, E><<<op->grid_k1, E * N * N, K1Smem<Real, N, E>::total, s>>>(
-      static_cast<const Real*>(x), op->nodle_t.as<int>(), op->fac_t.as<Real>(), op->R.as<Real>(), op->n_tiles,
-      op->err.as<int>());
+// One launch of the element kernel with the operator's tuned variant.
+void launch_k1(mj_op* op, const void* x, cudaStream_t s) {
+  if (op->precision == MJ_FP64)
+    k1_launch_f64(op->n, op->E, op->grid_k1, x, op->nodle_e.as<int>(), op->fac_e.ptr, op->R.ptr, op->n_tiles,
+                  op->err.as<int>(), s);
+  else
+    k1_launch_f32(op->n, op->E, op->grid_k1, x, op->nodle_e.as<int>(), op->fac_e.ptr, op->R.ptr, op->n_tiles,
+                  op->err.as<int>(), s);
   count_launch();
 }
 
 template <typename Real>
 void launch_k1(mj_op* op, const void* x, cudaStream_t s) {
-  switch (op->n) {
-    case 2: launch_k1_n<Real, 2>(op, x, s); break;
-    case 3: launch_k1_n<Real, 3>(op, x, s); break;
-    case 4: launch_k1_n<Real, 4>(op, x, s); break;
-    case 5: launch_k1_n<Real, 5>(op, x, s); break;
-    case 6: launch_k1_n<Real, 6>(op, x, s); break;
-    case 7: launch_k1_n<Real, 7>(op, x, s); break;
-    case 8: launch_k1_n<Real, 8>(op, x, s); break;
-    case 9: launch_k1_n<Real, 9>(op, x, s); break;
+  launch_k1(op, x, s);
+}
+
+// Autotuner: every instantiated tile size E of this order, on a persistent
+// grid of (CTAs per SM x SMs) CTAs, is timed with CUDA events on the
+// operator's own data (3 launches after 1 warm-up); the fastest is kept.
+// Small meshes skip the timing and take the variant with the most resident
+// threads.
+int autotune_k1(mj_op* op) {
+  const std::vector<int> cands = k1_tile_candidates(op->n);
+  const int sms = sm_count();
+  const size_t esz = op->precision == MJ_FP64 ? sizeof(double) : sizeof(float);
+  DevBuf x;
+  MJ_CUDA(x.alloc(esz * op->n_dof));
+  MJ_CUDA(cudaMemset(x.ptr, 0, esz * op->n_dof));
+  cudaEvent_t e0, e1;
+  MJ_CUDA(cudaEventCreate(&e0));
+  MJ_CUDA(cudaEventCreate(&e1));
+  double best = 1e300;
+  int bestE = -1, bestGrid = 1;
+  const bool time_it = (long long)op->n_elt * op->Q >= 2000000;
+  for (int E : cands) {
+    int ctas = 0;
+    const int rc = op->precision == MJ_FP64 ? k1_prepare_f64(op->n, E, &ctas) : k1_prepare_f32(op->n, E, &ctas);
+    if (rc != MJ_OK) continue;
+    const int tiles = op->n_elt_pad / E;
+    const int grid = std::max(1, std::min(tiles, ctas * sms));
+    double ms = 0.0;
+    if (time_it) {
+      op->E = E; op->grid_k1 = grid; op->n_tiles = tiles;
+      launch_k1(op, x.ptr, op->stream);
+      MJ_CUDA(cudaEventRecord(e0, op->stream));
+      for (int rep = 0; rep < 3; rep++) launch_k1(op, x.ptr, op->stream);
+      MJ_CUDA(cudaEventRecord(e1, op->stream));
+      MJ_CUDA(cudaEventSynchronize(e1));
+      float f = 0.f;
+      MJ_CUDA(cudaEventElapsedTime(&f, e0, e1));
+      ms = f / 3.0;
+    } else {
+      ms = -double(ctas) * E * op->n * op->n;  // most resident threads first
+    }
+    op->tune_E.push_back(E);
+    op->tune_ms.push_back(ms);
+    if (ms < best) { best = ms; bestE = E; bestGrid = grid; }
   }
-}
-
-// Occupancy-sized persistent grid for K1.
-template <typename Real, int N>
-int k1_grid_n(int n_tiles) {
-  int per_sm = 1;
-  constexpr int E = tile_elems_for(N);
-  const size_t smem = K1Smem<Real, N, E>::total;
-  cudaFuncSetAttribute(k_local_stiffness<Real, N, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_local_stiffness<Real, N, E>, E * N * N, smem);
-  if (per_sm < 1) per_sm = 1;
-  long g = (long)per_sm * sm_count();
-  return (int)std::max(1L, std::min<long>(g, n_tiles));
-}
-
-template <typename Real>
-int k1_grid(int n, int n_tiles) {
-  switch (n) {
-    case 2: return k1_grid_n<Real, 2>(n_tiles);
-    case 3: return k1_grid_n<Real, 3>(n_tiles);
-    case 4: return k1_grid_n<Real, 4>(n_tiles);
-    case 5: return k1_grid_n<Real, 5>(n_tiles);
-    case 6: return k1_grid_n<Real, 6>(n_tiles);
-    case 7: return k1_grid_n<Real, 7>(n_tiles);
-    case 8: return k1_grid_n<Real, 8>(n_tiles);
-    case 9: return k1_grid_n<Real, 9>(n_tiles);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (bestE < 0) {
+    set_error("mj_op_create: no element kernel variant fits this device");
+    return MJ_ERR_CUDA;
   }
-  return 1;
+  op->E = bestE;
+  op->grid_k1 = bestGrid;
+  op->n_tiles = op->n_elt_pad / bestE;
+  MJ_CUDA(cudaMemset(op->err.ptr, 0, sizeof(int)));
+  MJ_CUDA(cudaGetLastError());
+  return MJ_OK;
 }
 
-int stream_grid(int n) {
+}  // namespace
+
+int mj::stream_grid(int n) {
   long g = (n + 255) / 256;
   return (int)std::max(1L, std::min<long>(g, (long)sm_count() * 16));
 }
+
+namespace {
 
 template <typename Real>
 int mltadd_impl(mj_op* op, double alpha, const void* x, double beta, void* y, cudaStream_t s) {
@@ -236,10 +239,9 @@ int mj_op_create(const mj_mesh_desc* mesh, const mj_geom_desc* geom, int precisi
   std::unique_ptr<mj_op> op(new mj_op());
   op->order = r; op->n = n; op->Q = Q; op->n_elt = mesh->n_elt; op->n_dof = mesh->n_dof;
   op->precision = precision;
-  op->E = tile_elems(n);
-  op->n_tiles = (mesh->n_elt + op->E - 1) / op->E;
-  op->TS = tile_stride(op->E * Q);
-  op->r_len = (size_t)op->n_tiles * op->TS;
+  op->Qp = elem_slots(n);
+  op->n_elt_pad = (mesh->n_elt + kElemPad - 1) / kElemPad * kElemPad;
+  op->r_len = (size_t)op->n_elt_pad * op->Qp;
   MJ_CHECK_ARG(op->r_len < (size_t)INT32_MAX, "mj_op_create: mesh too large for int32 incidences");
 
   // derivative matrix
@@ -254,10 +256,9 @@ int mj_op_create(const mj_mesh_desc* mesh, const mj_geom_desc* geom, int precisi
     MJ_CHECK_ARG(std::isfinite(op->gradphi[a]), "mj_op_create: non-finite derivative matrix");
 
   const std::vector<int> num = hex_local_numbering(r);
-  const int E = op->E;
-  const size_t TS = (size_t)op->TS;
-  // tile-layout connectivity and factors, and CSR incidences
-  std::vector<int> nodle_t(op->r_len, 0);
+  const size_t Qp = (size_t)op->Qp;
+  // element-major connectivity and factors, and CSR incidences
+  std::vector<int> nodle_e(op->r_len, 0);
   std::vector<int> count(op->n_dof + 1, 0);
   for (long long t = 0; t < total_pts; t++) {
     const int d = mesh->nodle[t];
@@ -272,57 +273,55 @@ int mj_op_create(const mj_mesh_desc* mesh, const mj_geom_desc* geom, int precisi
   std::vector<int> fill(op->h_ptr.begin(), op->h_ptr.end() - 1);
 
   const size_t esz = elem_size(precision);
-  std::vector<unsigned char> fac_bytes(op->r_len * 6 * esz, 0);
+  std::vector<unsigned char> fac_bytes((size_t)op->n_elt_pad * 6 * Qp * esz, 0);
   double* fac64 = reinterpret_cast<double*>(fac_bytes.data());
   float* fac32 = reinterpret_cast<float*>(fac_bytes.data());
-  // Iterate R positions in increasing order so each dof's incidences are sorted.
-  for (int tile = 0; tile < op->n_tiles; tile++)
+  // Walk R slots in increasing order so each dof's incidences come out sorted.
+  for (int e = 0; e < mesh->n_elt; e++)
     for (int k = 0; k < n; k++)
-      for (int el = 0; el < E; el++) {
-        const int e = tile * E + el;
-        for (int j = 0; j < n; j++)
-          for (int i = 0; i < n; i++) {
-            const size_t rp = (size_t)tile * TS + ((size_t)k * E + el) * NN + j * n + i;
-            if (e >= mesh->n_elt) continue;  // padding: nodle 0, factors 0, no incidence
-            const int ql = num[(i * n + j) * n + k];
-            const size_t src = (size_t)e * Q + ql;
-            const int d = mesh->nodle[src];
-            nodle_t[rp] = d;
-            op->h_pos[fill[d]++] = (int)rp;
-            for (int c = 0; c < 6; c++) {
-              const double v = geom->factors[src * 6 + c];
-              if (!std::isfinite(v)) {
-                set_error("mj_op_create: non-finite stiffness factor");
-                return MJ_ERR_NONFINITE;
-              }
-              const size_t fp = (size_t)tile * 6 * TS + c * TS + (rp - (size_t)tile * TS);
-              if (precision == MJ_FP64) fac64[fp] = v;
-              else fac32[fp] = (float)v;
+      for (int j = 0; j < n; j++)
+        for (int i = 0; i < n; i++) {
+          const int p = (k * n + j) * n + i;
+          const size_t rp = (size_t)e * Qp + p;
+          const int ql = num[(i * n + j) * n + k];
+          const size_t src = (size_t)e * Q + ql;
+          const int d = mesh->nodle[src];
+          nodle_e[rp] = d;
+          op->h_pos[fill[d]++] = (int)rp;
+          for (int c = 0; c < 6; c++) {
+            const double v = geom->factors[src * 6 + c];
+            if (!std::isfinite(v)) {
+              set_error("mj_op_create: non-finite stiffness factor");
+              return MJ_ERR_NONFINITE;
             }
+            const size_t fp = ((size_t)e * 6 + c) * Qp + p;
+            if (precision == MJ_FP64) fac64[fp] = v;
+            else fac32[fp] = (float)v;
           }
-      }
+        }
 
-  MJ_CUDA(op->nodle_t.alloc(sizeof(int) * op->r_len));
-  MJ_CUDA(op->fac_t.alloc(fac_bytes.size()));
+  MJ_CUDA(op->nodle_e.alloc(sizeof(int) * op->r_len));
+  MJ_CUDA(op->fac_e.alloc(fac_bytes.size()));
   MJ_CUDA(op->R.alloc(esz * op->r_len));
   MJ_CUDA(op->ptr.alloc(sizeof(int) * (op->n_dof + 1)));
   MJ_CUDA(op->pos.alloc(sizeof(int) * op->h_pos.size()));
-  MJ_CUDA(cudaMemcpy(op->nodle_t.ptr, nodle_t.data(), sizeof(int) * op->r_len, cudaMemcpyHostToDevice));
-  MJ_CUDA(cudaMemcpy(op->fac_t.ptr, fac_bytes.data(), fac_bytes.size(), cudaMemcpyHostToDevice));
+  MJ_CUDA(cudaMemcpy(op->nodle_e.ptr, nodle_e.data(), sizeof(int) * op->r_len, cudaMemcpyHostToDevice));
+  MJ_CUDA(cudaMemcpy(op->fac_e.ptr, fac_bytes.data(), fac_bytes.size(), cudaMemcpyHostToDevice));
   MJ_CUDA(cudaMemcpy(op->ptr.ptr, op->h_ptr.data(), sizeof(int) * (op->n_dof + 1), cudaMemcpyHostToDevice));
   MJ_CUDA(cudaMemcpy(op->pos.ptr, op->h_pos.data(), sizeof(int) * op->h_pos.size(), cudaMemcpyHostToDevice));
   MJ_CUDA(cudaMemset(op->R.ptr, 0, esz * op->r_len));
-  {
-    // derivative matrix of this order into the constant-memory slot n
-    std::vector<double> g64(op->gradphi, op->gradphi + NN);
-    std::vector<float> g32(g64.begin(), g64.end());
-    MJ_CUDA(cudaMemcpyToSymbol(c_gmat64, g64.data(), sizeof(double) * NN, sizeof(double) * kMaxNK * kMaxNK * n));
-    MJ_CUDA(cudaMemcpyToSymbol(c_gmat32, g32.data(), sizeof(float) * NN, sizeof(float) * kMaxNK * kMaxNK * n));
-  }
   MJ_CUDA(op->err.alloc(sizeof(int)));
   MJ_CUDA(cudaMemset(op->err.ptr, 0, sizeof(int)));
-  op->grid_k1 = (precision == MJ_FP64) ? k1_grid<double>(n, op->n_tiles) : k1_grid<float>(n, op->n_tiles);
-  MJ_CUDA(cudaGetLastError());
+  {
+    // derivative matrix of this order into the constant-memory slot n of
+    // every unit that launches element kernels
+    int rc = precision == MJ_FP64 ? k1_set_gmat_f64(n, op->gradphi) : k1_set_gmat_f32(n, op->gradphi);
+    if (rc) return rc;
+  }
+  {
+    int rc = autotune_k1(op.get());
+    if (rc) return rc;
+  }
   *out = op.release();
   return MJ_OK;
 }

@@ -123,6 +123,87 @@ class LeapFrogIterator:
             pass
 
 
+class BatchLeapFrog:
+    """S leap-frog runs sharing one mesh and operator (FP32), each with its own
+    sources and state: the reference's order-2 ModifiedEquationIterator run
+    S times, advanced together on the GPU (state n_dof x S, row-major)."""
+
+    def __init__(self, op: FemMatrixFreeOperator, dt: float, n_rhs: int, mass, inv_mass=None, src_idx=None,
+                 src_rhs=None, src_val=None, pulse=None, rec_idx=None, rec_w=None):
+        L = _lib.load()
+        self.op, self.S, self.dt = op, int(n_rhs), float(dt)
+        n = op.n_dof
+        keep = self._keep = []
+
+        def f(a):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            keep.append(a)
+            return a
+
+        def i(a):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=np.int32)
+            keep.append(a)
+            return a
+
+        mass, inv_mass, pulse = f(mass), f(inv_mass), f(pulse)
+        src_idx, src_rhs, src_val = i(src_idx), i(src_rhs), f(src_val)
+        rec_idx, rec_w = i(rec_idx), f(rec_w)
+        if mass.size != n:
+            raise ValueError("mass size differs from the operator size")
+        n_src = 0 if src_idx is None else int(src_idx.size)
+        self.n_rec = 0 if rec_idx is None else int(rec_idx.shape[0])
+        n_rec_w = 0 if rec_idx is None else int(rec_idx.shape[1])
+        desc = _lib.LfbDesc(self.dt, self.S, _lib.dptr(mass), _lib.dptr(inv_mass), n_src, _lib.iptr(src_idx),
+                            _lib.iptr(src_rhs), _lib.dptr(src_val), 0 if pulse is None else int(pulse.size),
+                            _lib.dptr(pulse), self.n_rec, n_rec_w, _lib.iptr(rec_idx), _lib.dptr(rec_w))
+        h = ctypes.c_void_p()
+        _lib.check(L.mj_lfb_create(op.handle, ctypes.byref(desc), ctypes.byref(h)))
+        self._h = h
+
+    def init(self, u0=None, du0=None) -> None:
+        n = self.op.n_dof
+        u0 = None if u0 is None else np.ascontiguousarray(u0, dtype=np.float64).reshape(n, self.S)
+        du0 = None if du0 is None else np.ascontiguousarray(du0, dtype=np.float64).reshape(n, self.S)
+        _lib.check(_lib.load().mj_lfb_init(self._h, _lib.dptr(u0), _lib.dptr(du0)))
+
+    def advance(self, nsteps: int, traces: bool = False, graph: bool = True):
+        """Advances nsteps; with traces, returns the receiver values before each
+        step as an (n_rec, S, nsteps) array."""
+        tr = np.zeros((self.n_rec, self.S, nsteps)) if (traces and self.n_rec) else None
+        _lib.check(_lib.load().mj_lfb_advance(self._h, int(nsteps), _lib.dptr(tr), int(nsteps), int(bool(graph))))
+        return tr
+
+    def state(self):
+        n = self.op.n_dof
+        u, v = np.zeros((n, self.S)), np.zeros((n, self.S))
+        _lib.check(_lib.load().mj_lfb_get_state(self._h, _lib.dptr(u), _lib.dptr(v)))
+        return u, v
+
+    def info(self):
+        vals = [ctypes.c_int() for _ in range(5)]
+        _lib.check(_lib.load().mj_lfb_info(self._h, *[ctypes.byref(v) for v in vals]))
+        return dict(zip(["n_rhs", "tile_elems", "lanes", "grid", "step"], [v.value for v in vals]))
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _lib.load().mj_lfb_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def number_of_iterations(t_begin: float, t_end: float, dt: float) -> int:
     """nb_max_iter = ceil(|t_end - t_begin| / dt) (ModifiedEquation.cxx:23-24)."""
     return int(math.ceil(abs(t_end - t_begin) / dt))
