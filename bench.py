@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the configuration 3 and 4 legs")
+    ap.add_argument("--extra-steps", type=int, default=500)
     return ap.parse_args()
 
 
@@ -133,10 +135,10 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def build_problem(cells, order, nsteps):
+def build_problem(cells, order, nsteps, mesh=None):
     from montjoie_gb300 import mesh as M
     from montjoie_gb300.problem import AcousticProblem, cfl_time_step
-    m = workload_mesh(cells)
+    m = workload_mesh(cells) if mesh is None else mesh
     s = M.AcousticSetup(order=order, dt=1.0, nsteps=nsteps, src_radius=2.0 / cells)
     pb = AcousticProblem(m, s, receivers=receivers(), defer_time=True)
     dt = cfl_time_step(pb, safety=0.5)
@@ -144,20 +146,123 @@ def build_problem(cells, order, nsteps):
     return pb
 
 
-def time_advance(torch, lf, steps, lib):
+def timed_steps(torch, step_fn, steps):
+    """Device time (ms) of step_fn(steps) with CUDA events on the legacy default stream."""
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    start.record()
+    step_fn(steps)
+    end.record()
+    torch.cuda.synchronize()
+    return start.elapsed_time(end)
+
+
+def leg_config3(args, torch, _lib):
+    """BASELINE configuration 3: 32^3 hexahedra, smooth sinusoidal vertex
+    displacement 0.1h, Q8, c = 2 + 0.5 sin sin sin, FP32 state (factors stored
+    FP64, cast to FP32), error stated against the FP64 plain path."""
+    from montjoie_gb300 import mesh as M
+    cells, order, K = 32, 8, args.extra_steps
+    m = M.perturbed_cube(cells, seed=SEED + 30, amplitude=0.1, kind="sin", c_mode="smooth")
+    t0 = time.perf_counter()
+    pb = build_problem(cells, order, K + 20, mesh=m)
+    setup_s = time.perf_counter() - t0
+    zeros = np.zeros(pb.n_dof)
+    op32 = pb.operator("fp32")
+    lf = pb.integrator(op32, diagnostics=False)
+    lf.SetInitialConditionS(zeros)
+    lf.Advance(5)
+    ms32 = timed_steps(torch, lf.Advance, K)
+    lf.close()
+    op64 = pb.operator("fp64")
+    lf = pb.integrator(op64, diagnostics=False)
+    lf.SetInitialConditionS(zeros)
+    lf.Advance(3)
+    K64 = min(K, 100)
+    ms64 = timed_steps(torch, lf.Advance, K64)
+    lf.close()
+    d64 = pb.integrator(op64)
+    u64, n64, _ = d64.Run(zeros, None, K)
+    d32 = pb.integrator(op32)
+    u32, n32, _ = d32.Run(zeros, None, K)
+    d64.close(); d32.close(); op32.close(); op64.close()
+    return {"workload": f"unit cube 32^3 hex Q8, 0.1h sinusoidal vertex displacement, c = 2 + 0.5 sin(2 pi x) sin(2 pi y) "
+                        f"sin(2 pi z) per element, Ricker f0=5, Neumann, dt=0.5 CFL, FP32 state, {K} steps",
+            "n_dof": pb.n_dof, "steps": K, "value": pb.n_dof * K / (ms32 / 1e3), "unit": UNIT,
+            "ms_per_step": ms32 / K, "fp64_value": pb.n_dof * K64 / (ms64 / 1e3), "fp64_ms_per_step": ms64 / K64,
+            "u_rel_l2_vs_fp64": float(np.linalg.norm(u32 - u64) / max(np.linalg.norm(u64), 1e-300)),
+            "norm_history_rel_l2_vs_fp64": float(np.linalg.norm(n32 - n64) / max(np.linalg.norm(n64), 1e-300)),
+            "setup_seconds": setup_s}
+
+
+def leg_config4_sources(args, torch, _lib):
+    """BASELINE configuration 4, first half: 64 independent Ricker sources at
+    seeded random positions on one 32^3 Q4 mesh (c per element in [1,3]),
+    FP32, advanced together, CUDA-graph replay."""
+    from montjoie_gb300 import mesh as M
+    from montjoie_gb300.leapfrog import BatchLeapFrog
+    from montjoie_gb300.problem import gaussian_source
+    cells, order, S, K = 32, 4, 64, args.extra_steps
+    m = M.perturbed_cube(cells, seed=SEED + 40, amplitude=0.05, kind="random", c_mode="element")
+    pb = build_problem(cells, order, K + 40, mesh=m)
+    pos = np.random.default_rng(SEED + 41).uniform(0.1, 0.9, size=(S, 3))
+    idx, rhs, val = [], [], []
+    for s_, c in enumerate(pos):
+        i_, v_ = gaussian_source(pb.nodle, pb.jw, pb.xq, pb.n_dof, c, 2.0 / cells)
+        idx.append(i_); val.append(v_); rhs.append(np.full(i_.size, s_))
+    op = pb.operator("fp32")
+    b = BatchLeapFrog(op, pb.setup.dt, S, pb.mass, None, np.concatenate(idx), np.concatenate(rhs),
+                      np.concatenate(val), pb.pulse)
+    b.init()
+    b.advance(20)
+    l0 = _lib.kernel_launches()
+    ms = timed_steps(torch, b.advance, K)
+    launches = _lib.kernel_launches() - l0
+    u, _ = b.state()
+    info = b.info()
+    b.close()
+    # run 0 against a single-source run of the same FP32 operator
+    lf = LeapFrogIteratorFor(pb, op, idx[0], val[0])
+    lf.SetInitialConditionS(np.zeros(pb.n_dof))
+    lf.Advance(K + 20)
+    u0 = lf.GetIterate()
+    lf.close(); op.close()
+    n_elt, Q = pb.nodle.shape
+    # SURVEY 8d batched bytes per right-hand side and step, divided by the dofs
+    bytes_step = (n_elt * Q * (6 * 4 + 4) / S + pb.n_dof * (3 * 4 + 4 / S)) / pb.n_dof
+    value = pb.n_dof * S * K / (ms / 1e3)
+    peak, _ = measured_peaks()
+    return {"workload": f"64 Ricker sources (Gaussian R=2h, seeded positions in [0.1,0.9]^3) on one 32^3 Q4 mesh, "
+                        f"+-5% h perturbation, c per element in [1,3], FP32, {K} steps, state [dof][64]",
+            "n_dof": pb.n_dof, "n_rhs": S, "steps": K, "value": value, "unit": UNIT, "ms_per_step": ms / K,
+            "variant": info, "gpu_launches": launches,
+            "run0_rel_l2_vs_single_source_run": float(np.linalg.norm(u[:, 0] - u0) / max(np.linalg.norm(u0), 1e-300)),
+            "algorithmic_bytes_per_dof_update": bytes_step,
+            "step_frac_of_hbm": value * bytes_step / 1e9 / peak}
+
+
+def LeapFrogIteratorFor(pb, op, src_idx, src_val):
+    from montjoie_gb300.leapfrog import LeapFrogIterator
+    return LeapFrogIterator(op, pb.setup.dt, pb.mass, None, src_idx, src_val, pb.pulse)
+
+
+def time_advance(torch, lf, steps, lib, prof_steps=100):
     """Times `steps` leap-frog steps (already initialised) with CUDA events on the
-    library's stream (the legacy default stream)."""
+    library's stream (the legacy default stream; CUDA-graph replay), then
+    `prof_steps` more steps launched one by one with events around each kernel
+    for the per-kernel times."""
+    import ctypes
     L = lib.load()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
-    L.mj_lf_profile(lf.handle, 1, None, None, None)
     l0 = lib.kernel_launches()
     start.record()
     lf.Advance(steps)
     end.record()
     torch.cuda.synchronize()
     launches = lib.kernel_launches() - l0
-    import ctypes
+    L.mj_lf_profile(lf.handle, 1, None, None, None)
+    lf.Advance(min(steps, prof_steps))
     e_ms, u_ms, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
     L.mj_lf_profile(lf.handle, 0, ctypes.byref(e_ms), ctypes.byref(u_ms), ctypes.byref(n))
     return start.elapsed_time(end), e_ms.value / max(1, n.value), u_ms.value / max(1, n.value), launches
@@ -257,6 +362,10 @@ def run_ours(args):
                     "update_kernel_ms": k2_64, "fp32_over_fp64": value / world / value64},
            "error_fp32_vs_fp64": err,
            "roofline": roofline, "clocks": clk, "gpu_launches": launches, "e2e": e2e}
+    if not args.no_extras:
+        op32.close(); op64.close()
+        out["config3_q8"] = leg_config3(args, torch, _lib)
+        out["config4_sources"] = leg_config4_sources(args, torch, _lib)
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(args, pb, u_check=None)
     if rank == 0:

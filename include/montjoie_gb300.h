@@ -161,6 +161,12 @@ int mj_lf_device_state(mj_lf* lf, void** u_n, void** u_np1, int* step);
  * reference's phase timers, MONTJOIE/src/Share/Timer.hxx:14-23, play this role). */
 int mj_lf_profile(mj_lf* lf, int enable, double* elem_ms, double* update_ms, int* steps);
 
+/* mj_lf_advance replays a captured CUDA graph of 20 steps (two kernels per
+ * step) when it records no diagnostics and profiling (mj_lf_profile) is off;
+ * enable = 0
+ * launches every kernel from the host instead.  Default: enabled. */
+int mj_lf_set_graph(mj_lf* lf, int enable);
+
 /* Sets the CUDA stream (cudaStream_t) used by the integrator's launches. */
 int mj_lf_set_stream(mj_lf* lf, void* stream);
 

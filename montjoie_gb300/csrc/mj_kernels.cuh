@@ -34,13 +34,20 @@ __global__ void k_gather_mltadd(const Real* __restrict__ R, const int* __restric
 //   FP32:         u_new = 2 u1 - u0 + m Ah,  m = dt^2 / D
 // Source entries are CSR entries with pos < 0 (slot -pos-1 of src_val), placed
 // after the element entries of the dof.  u_new overwrites u0 in place.
+// The pulse of the step is pulse[ctr[q]]; block 0 writes ctr[1-q] = ctr[q]+1
+// for the next step (two counters, so a captured sequence of steps needs no
+// host update of the pulse).
 // ---------------------------------------------------------------------------
 template <typename Real, bool EXACT>
 __global__ void k_gather_leapfrog(const Real* __restrict__ R, const int* __restrict__ ptr,
                                   const int* __restrict__ pos, const Real* __restrict__ src_val,
-                                  Real pulse, Real* __restrict__ u0, const Real* __restrict__ u1,
+                                  const double* __restrict__ pulses, int n_pulse, int* __restrict__ ctr, int qc,
+                                  Real* __restrict__ u0, const Real* __restrict__ u1,
                                   const Real* __restrict__ mass, const Real* __restrict__ minv,
                                   Real dt2, int n_dof) {
+  const int step = ctr[qc];
+  const Real pulse = (step < n_pulse) ? Real(pulses[step]) : Real(0);
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctr[1 - qc] = step + 1;
   for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < n_dof; d += gridDim.x * blockDim.x) {
     Real s = 0;
     const int q1 = __ldg(ptr + d + 1);

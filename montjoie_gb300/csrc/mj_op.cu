@@ -68,7 +68,10 @@ struct mj_lf {
   DevBuf ua, ub;         // state: U^n (cur) and U^{n+1} (next)
   DevBuf du0, tmp;       // staging
   DevBuf partial, norms_d, traces_d, flag;
-  std::vector<double> pulse;
+  DevBuf pulse_d, ctr;   // pulse of every step and the two step counters
+  int n_pulse = 0;
+  cudaGraphExec_t graph = nullptr, graph_prof = nullptr;
+  bool use_graph = true;  // replay captured steps when no diagnostics are asked
   int n_src = 0, n_rec = 0, n_rec_w = 0;
   int step = 0;
   bool initialised = false;
@@ -83,6 +86,8 @@ struct mj_lf {
   int prof_steps = 0;
   ~mj_lf() {
     for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    if (graph) cudaGraphExecDestroy(graph);
+    if (graph_prof) cudaGraphExecDestroy(graph_prof);
   }
   void* cur() { return cur_is_a ? ua.ptr : ub.ptr; }
   void* next() { return cur_is_a ? ub.ptr : ua.ptr; }
@@ -430,7 +435,12 @@ int mj_lf_create(mj_op* op, const mj_lf_desc* desc, mj_lf** out) {
     MJ_CUDA(lf->minv.alloc(sizeof(float) * n));
     MJ_CUDA(cudaMemcpy(lf->minv.ptr, m.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
   }
-  lf->pulse.assign(desc->pulse, desc->pulse + desc->n_pulse);
+  lf->n_pulse = desc->n_pulse;
+  MJ_CUDA(lf->pulse_d.alloc(sizeof(double) * std::max(1, desc->n_pulse)));
+  if (desc->n_pulse)
+    MJ_CUDA(cudaMemcpy(lf->pulse_d.ptr, desc->pulse, sizeof(double) * desc->n_pulse, cudaMemcpyHostToDevice));
+  MJ_CUDA(lf->ctr.alloc(sizeof(int) * 2));
+  MJ_CUDA(cudaMemset(lf->ctr.ptr, 0, sizeof(int) * 2));
   if (desc->norm_weight) {
     MJ_CUDA(lf->norm_w.alloc(sizeof(double) * n));
     MJ_CUDA(cudaMemcpy(lf->norm_w.ptr, desc->norm_weight, sizeof(double) * n, cudaMemcpyHostToDevice));
@@ -496,6 +506,7 @@ int lf_init_impl(mj_lf* lf, const double* u0, const double* du0) {
   lf->step = 0;
   lf->initialised = true;
   MJ_CUDA(cudaMemsetAsync(lf->flag.ptr, 0, sizeof(int), s));
+  MJ_CUDA(cudaMemsetAsync(lf->ctr.ptr, 0, sizeof(int) * 2, s));
   MJ_CUDA(cudaStreamSynchronize(s));
   return MJ_OK;
 }
@@ -520,37 +531,75 @@ int lf_diag(mj_lf* lf, double* norms_d, int norm_col, double* traces_d, int stri
   return MJ_OK;
 }
 
+// Launches of one leap-frog step (capturable): element kernel on U^{n+1},
+// then gather + source + update writing U^{n+2} over U^n.  qc = parity of
+// the pulse counter holding this step's index.
+// Steps per captured CUDA graph (even, so the state buffers and the pulse
+// counters are back in their roles after each replay).
+constexpr int kGraphSteps = 20;
+
 template <typename Real>
-int lf_step(mj_lf* lf) {
+void lf_step_launch(mj_lf* lf, void* cur, const void* next, int qc, cudaStream_t s, bool prof) {
   mj_op* op = lf->op;
-  cudaStream_t s = lf->stream;
   const int n = lf->n_dof;
-  const double p = (lf->step < (int)lf->pulse.size()) ? lf->pulse[lf->step] : 0.0;
-  const bool prof = lf->profile && lf->ev_used + 3 <= (int)lf->ev.size();
-  if (prof) MJ_CUDA(cudaEventRecord(lf->ev[lf->ev_used], s));
-  // U1 = next (u^{n+1}), U0 = cur (u^n); the result u^{n+2} overwrites U0.
-  launch_k1<Real>(op, lf->next(), s);
-  if (prof) MJ_CUDA(cudaEventRecord(lf->ev[lf->ev_used + 1], s));
+  if (prof) cudaEventRecord(lf->ev[lf->ev_used], s);
+  launch_k1<Real>(op, next, s);
+  if (prof) cudaEventRecord(lf->ev[lf->ev_used + 1], s);
   const double dt2 = lf->dt * lf->dt;
   if (op->precision == MJ_FP64) {
     k_gather_leapfrog<Real, true><<<stream_grid(n), 256, 0, s>>>(
-        op->R.as<Real>(), lf->ptr.as<int>(), lf->pos.as<int>(), lf->src_val.as<Real>(), Real(p),
-        static_cast<Real*>(lf->cur()), static_cast<const Real*>(lf->next()), lf->mass.as<Real>(),
-        lf->minv.as<Real>(), Real(dt2), n);
+        op->R.as<Real>(), lf->ptr.as<int>(), lf->pos.as<int>(), lf->src_val.as<Real>(), lf->pulse_d.as<double>(),
+        lf->n_pulse, lf->ctr.as<int>(), qc, static_cast<Real*>(cur), static_cast<const Real*>(next),
+        lf->mass.as<Real>(), lf->minv.as<Real>(), Real(dt2), n);
   } else {
     k_gather_leapfrog<Real, false><<<stream_grid(n), 256, 0, s>>>(
-        op->R.as<Real>(), lf->ptr.as<int>(), lf->pos.as<int>(), lf->src_val.as<Real>(), Real(p),
-        static_cast<Real*>(lf->cur()), static_cast<const Real*>(lf->next()), nullptr,
+        op->R.as<Real>(), lf->ptr.as<int>(), lf->pos.as<int>(), lf->src_val.as<Real>(), lf->pulse_d.as<double>(),
+        lf->n_pulse, lf->ctr.as<int>(), qc, static_cast<Real*>(cur), static_cast<const Real*>(next), nullptr,
         lf->minv.as<Real>(), Real(dt2), n);
   }
   count_launch();
-  MJ_CUDA(cudaGetLastError());
   if (prof) {
-    MJ_CUDA(cudaEventRecord(lf->ev[lf->ev_used + 2], s));
+    cudaEventRecord(lf->ev[lf->ev_used + 2], s);
     lf->ev_used += 3;
   }
+}
+
+template <typename Real>
+int lf_step(mj_lf* lf) {
+  const bool prof = lf->profile && lf->ev_used + 3 <= (int)lf->ev.size() - 3 * kGraphSteps;
+  lf_step_launch<Real>(lf, lf->cur(), lf->next(), lf->step & 1, lf->stream, prof);
+  MJ_CUDA(cudaGetLastError());
   lf->cur_is_a = !lf->cur_is_a;  // new cur = old next; new next = overwritten old cur
   lf->step++;
+  return MJ_OK;
+}
+
+// Captures kGraphSteps steps; with prof, event records around each kernel
+// (events 0..3*kGraphSteps-1 of the pool) are part of the graph, so the last
+// replay's per-kernel times can be read back.
+template <typename Real>
+int lf_capture(mj_lf* lf, bool prof, cudaGraphExec_t* out) {
+  cudaStream_t cs;
+  MJ_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  cudaGraph_t g;
+  const uint64_t before = launch_counter().load();
+  MJ_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+  bool a = true;
+  const int ev_saved = lf->ev_used;
+  const int ev_base = (int)lf->ev.size() - 3 * kGraphSteps;  // the graph's own events, apart from plain steps'
+  lf->ev_used = ev_base;
+  for (int k = 0; k < kGraphSteps; k++) {
+    void* cur = a ? lf->ua.ptr : lf->ub.ptr;
+    void* nxt = a ? lf->ub.ptr : lf->ua.ptr;
+    lf_step_launch<Real>(lf, cur, nxt, k & 1, cs, prof);
+    a = !a;
+  }
+  lf->ev_used = ev_saved;
+  MJ_CUDA(cudaStreamEndCapture(cs, &g));
+  launch_counter().store(before);  // captured, not launched
+  MJ_CUDA(cudaGraphInstantiate(out, g, 0));
+  cudaGraphDestroy(g);
+  cudaStreamDestroy(cs);
   return MJ_OK;
 }
 
@@ -569,7 +618,29 @@ int lf_advance_impl(mj_lf* lf, int nsteps, double* norms, double* traces, int st
     if (lf->traces_d.bytes < b) MJ_CUDA(lf->traces_d.alloc(b));
     td = lf->traces_d.as<double>();
   }
-  for (int s = 0; s < nsteps; s++) {
+  int s0 = 0;
+  bool replayed_prof = false;
+  if (!nd && !td && !lf->profile && lf->use_graph && nsteps >= kGraphSteps + 1) {
+    if (lf->step & 1) {  // realign: replays start on an even step with ua holding U^n
+      lf_step_launch<Real>(lf, lf->cur(), lf->next(), lf->step & 1, lf->stream, false);
+      MJ_CUDA(cudaGetLastError());
+      lf->cur_is_a = !lf->cur_is_a;
+      lf->step++;
+      s0 = 1;
+    }
+    if (!lf->graph) {
+      int rc = lf_capture<Real>(lf, false, &lf->graph);
+      if (rc) return rc;
+    }
+    while (nsteps - s0 >= kGraphSteps) {
+      MJ_CUDA(cudaGraphLaunch(lf->graph, lf->stream));
+      count_launch(2 * kGraphSteps);
+      s0 += kGraphSteps;
+      lf->step += kGraphSteps;
+    }
+    MJ_CUDA(cudaGetLastError());
+  }
+  for (int s = s0; s < nsteps; s++) {
     int rc = lf_diag<Real>(lf, nd, s, td, cols, s);
     if (rc) return rc;
     rc = lf_step<Real>(lf);
@@ -585,9 +656,25 @@ int lf_advance_impl(mj_lf* lf, int nsteps, double* norms, double* traces, int st
     for (int k = 0; k < lf->n_rec; k++)
       MJ_CUDA(cudaMemcpyAsync(traces + (size_t)k * stride, td + (size_t)k * cols, sizeof(double) * cols,
                               cudaMemcpyDeviceToHost, s));
-  int flag = 0;
+  int flag = 0, kerr = 0;
   MJ_CUDA(cudaMemcpyAsync(&flag, lf->flag.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MJ_CUDA(cudaMemcpyAsync(&kerr, lf->op->err.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
   MJ_CUDA(cudaStreamSynchronize(s));
+  if (kerr) {
+    set_error("mj_lf_advance: an element kernel wait timed out");
+    return MJ_ERR_CUDA;
+  }
+  if (replayed_prof) {  // per-kernel times of the last replay
+    const int base = (int)lf->ev.size() - 3 * kGraphSteps;
+    for (int k = 0; k < kGraphSteps; k++) {
+      float a = 0.f, b = 0.f;
+      MJ_CUDA(cudaEventElapsedTime(&a, lf->ev[base + 3 * k], lf->ev[base + 3 * k + 1]));
+      MJ_CUDA(cudaEventElapsedTime(&b, lf->ev[base + 3 * k + 1], lf->ev[base + 3 * k + 2]));
+      lf->prof_elem_ms += a;
+      lf->prof_update_ms += b;
+      lf->prof_steps++;
+    }
+  }
   for (int e = 0; e + 3 <= lf->ev_used; e += 3) {
     float a = 0.f, b = 0.f;
     MJ_CUDA(cudaEventElapsedTime(&a, lf->ev[e], lf->ev[e + 1]));
@@ -648,6 +735,12 @@ int mj_lf_run(mj_lf* lf, const double* u0, const double* du0, int nsteps, double
                                     : lf_advance_impl<float>(lf, nsteps, norms, traces, trace_stride, true);
   if (rc) return rc;
   if (u_final) return mj_lf_get_state(lf, u_final, nullptr);
+  return MJ_OK;
+}
+
+int mj_lf_set_graph(mj_lf* lf, int enable) {
+  MJ_CHECK_ARG(lf, "mj_lf_set_graph: null integrator");
+  lf->use_graph = enable != 0;
   return MJ_OK;
 }
 

@@ -83,6 +83,10 @@ class LeapFrogIterator:
         self.n_time += nsteps
         return norms, traces
 
+    def set_graph(self, enable: bool) -> None:
+        """Replay captured CUDA graphs of 20 steps when no diagnostics are asked (default on)."""
+        _lib.check(_lib.load().mj_lf_set_graph(self._h, int(bool(enable))))
+
     def GetIterate(self) -> np.ndarray:
         u = np.zeros(self.op.n_dof)
         _lib.check(_lib.load().mj_lf_get_state(self._h, _lib.dptr(u), None))

@@ -124,3 +124,20 @@ def test_config1_fp32_error(config1):
     assert rel_l2(norms, g["norms"]) < 1e-4
     assert np.abs(traces - g["traces"]).max() < 1e-4 * np.abs(g["traces"]).max()
     assert rel_l2(_probe_values(pb, g, uf), g["probe_u"]) < 1e-4
+
+
+def test_graph_replay_equals_plain_launches_single_source():
+    g = load_golden("cube4_q4")
+    for precision in ("fp64", "fp32"):
+        op1, lf1 = integrator(g, precision, norms=False)
+        op2, lf2 = integrator(g, precision, norms=False)
+        lf2.set_graph(False)
+        for lf in (lf1, lf2):
+            lf.SetInitialConditionS(np.zeros(g["massD"].size))
+            lf.Advance(1)       # odd start: realignment path
+            lf.Advance(63)
+        u1, v1 = lf1.GetState()
+        u2, v2 = lf2.GetState()
+        assert np.array_equal(u1, u2) and np.array_equal(v1, v2)
+        for o in (lf1, lf2, op1, op2):
+            o.close()
