@@ -217,6 +217,36 @@ int mj_lfb_get_state(mj_lfb* b, double* u_n, double* u_np1);
 /* Tuned variant and progress: runs, elements per CTA, lanes (runs per pass), grid, steps done. */
 int mj_lfb_info(const mj_lfb* b, int* n_rhs, int* tile_elems, int* lanes, int* grid, int* step);
 
+/* ---- media update and adjoint ------------------------------------------ */
+
+/* Scales the stiffness factors of every element: factors(e) = scale[e] *
+ * factors given at creation (e.g. unit-mu factors scaled by mu_e = c_e^2).
+ * Host array of n_elt values >= 0.  The role of changing the media
+ * references (MateriauDielec) and recomputing Glob_matMass_Bh
+ * (MONTJOIE/src/Elliptic/Helmholtz/VarHelmholtz.cxx:54-131). */
+int mj_op_set_element_scale(mj_op* op, const double* scale);
+
+typedef struct mj_adj mj_adj;
+
+/* Discrete adjoint of the many-source leap-frog of `b` over nsteps steps from
+ * zero initial conditions, with the forward states checkpointed every
+ * checkpoint_every steps (0: ceil(sqrt(nsteps))) and replayed segment by
+ * segment in the backward sweep.  No reference counterpart: the reference has
+ * no time-domain adjoint.  `b` must have receivers. */
+int mj_adj_create(mj_lfb* b, int nsteps, int checkpoint_every, mj_adj** out);
+int mj_adj_destroy(mj_adj* a);
+
+/* Forward run storing checkpoints; traces (host, may be NULL) receive the
+ * receiver values of U^0..U^nsteps at traces[(k*S + s)*(nsteps+1) + n]. */
+int mj_adj_forward(mj_adj* a, double* traces);
+
+/* Backward sweep for the loss J = sum g_n(U^n) whose gradient with respect
+ * to the traces is `residual` (same layout as traces, host).  Returns
+ * grad[e] = coef[e] * sum_{n=1}^{nsteps-1} sum_s lambda^{n+1}_s^T A_e U^n_s
+ * (A_e the element's stiffness as currently scaled), host arrays of n_elt.
+ * With A_e = c_e^2 A_e^(1), coef[e] = -2 dt^2 / c_e gives dJ/dc_e. */
+int mj_adj_backward(mj_adj* a, const double* residual, const double* coef, double* grad);
+
 /* ---- setup helpers (geometry, numbering, mass) ------------------------ */
 
 /* Global numbering of a conforming hexahedral mesh of order r: vertices,

@@ -28,6 +28,7 @@ EXPORTED = [
     "mj_lf_get_state", "mj_lf_run", "mj_lf_device_state", "mj_lf_profile", "mj_lf_set_graph", "mj_lf_set_stream", "mj_number_hex_mesh",
     "mj_geometry", "mj_lumped_mass", "mj_stiffness_mltadd_static",
     "mj_lfb_create", "mj_lfb_destroy", "mj_lfb_init", "mj_lfb_advance", "mj_lfb_get_state", "mj_lfb_info",
+    "mj_op_set_element_scale", "mj_adj_create", "mj_adj_destroy", "mj_adj_forward", "mj_adj_backward",
 ]
 
 _D = ctypes.POINTER(ctypes.c_double)
@@ -115,6 +116,11 @@ def load(build_if_missing: bool = True):
     L.mj_lfb_advance.argtypes = [_VP, ctypes.c_int, _D, ctypes.c_int, ctypes.c_int]
     L.mj_lfb_get_state.argtypes = [_VP, _D, _D]
     L.mj_lfb_info.argtypes = [_VP] + [ctypes.POINTER(ctypes.c_int)] * 5
+    L.mj_op_set_element_scale.argtypes = [_VP, _D]
+    L.mj_adj_create.argtypes = [_VP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_VP)]
+    L.mj_adj_destroy.argtypes = [_VP]
+    L.mj_adj_forward.argtypes = [_VP, _D]
+    L.mj_adj_backward.argtypes = [_VP, _D, _D, _D]
     L.mj_stiffness_mltadd_static.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP, ctypes.c_double,
                                              _VP, ctypes.c_double, _VP, _VP]
     _lib = L

@@ -57,6 +57,42 @@ int rhs_prepare(int n, int E, int L, int* ctas) {
   return MJ_ERR_ARG;
 }
 
+template <int N, int E, int L>
+int energy_prepare_one() {
+  using P = K1Plan<float, N, E, L>;
+  MJ_CUDA(cudaFuncSetAttribute(k_local_stiffness_rhs<N, E, L, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)P::total));
+  return MJ_OK;
+}
+
+template <int N, int E, int L>
+void energy_launch_one(int grid, const float* x, const int* nodle_e, const float* fac_e, int n_tiles, int S, int* err,
+                       const float* lam, double* gacc, const double* coef, cudaStream_t s) {
+  using P = K1Plan<float, N, E, L>;
+  k_local_stiffness_rhs<N, E, L, true><<<grid, P::threads, P::total, s>>>(x, nodle_e, fac_e, nullptr, n_tiles, S, err,
+                                                                          lam, gacc, coef);
+}
+
+int energy_prepare(int n, int E, int L) {
+#define MJ_X(NV, EV, LV) \
+  if (n == NV && E == EV && L == LV) return energy_prepare_one<NV, EV, LV>();
+  MJ_RHS_VARIANTS(MJ_X)
+#undef MJ_X
+  set_error("no energy kernel variant for this order");
+  return MJ_ERR_ARG;
+}
+
+void energy_launch(int n, int E, int L, int grid, const float* x, const int* nodle_e, const float* fac_e, int n_tiles,
+                   int S, int* err, const float* lam, double* gacc, const double* coef, cudaStream_t s) {
+#define MJ_X(NV, EV, LV)                                                                              \
+  if (n == NV && E == EV && L == LV) {                                                                \
+    energy_launch_one<NV, EV, LV>(grid, x, nodle_e, fac_e, n_tiles, S, err, lam, gacc, coef, s);      \
+    return;                                                                                           \
+  }
+  MJ_RHS_VARIANTS(MJ_X)
+#undef MJ_X
+}
+
 void rhs_launch(int n, int E, int L, int grid, const float* x, const int* nodle_e, const float* fac_e, float* R,
                 int n_tiles, int S, int* err, cudaStream_t s) {
 #define MJ_X(NV, EV, LV)                                                             \
@@ -76,11 +112,12 @@ void rhs_launch(int n, int E, int L, int grid, const float* x, const int* nodle_
 // src_rhs) applies to right-hand side src_rhs only.  The pulse of the step
 // is pulse[ctr[q]]; block 0 writes ctr[1-q] = ctr[q] + 1 for the next step
 // (two counters, so a captured sequence of steps needs no host update).
+// uout may alias u0 (in-place update: each thread reads its entry first).
 __global__ void k_gather_leapfrog_rhs(const float* __restrict__ R, const int* __restrict__ ptr,
                                       const int* __restrict__ pos, const float* __restrict__ src_val,
                                       const int* __restrict__ src_rhs, const double* __restrict__ pulse, int n_pulse,
-                                      int* __restrict__ ctr, int q, float* __restrict__ u0,
-                                      const float* __restrict__ u1, const float* __restrict__ m, int n_dof, int S) {
+                                      int* __restrict__ ctr, int q, const float* u0, const float* __restrict__ u1,
+                                      float* uout, const float* __restrict__ m, int n_dof, int S) {
   const int step = ctr[q];
   const float p = (step < n_pulse) ? (float)pulse[step] : 0.f;
   if (blockIdx.x == 0 && threadIdx.x == 0) ctr[1 - q] = step + 1;
@@ -96,8 +133,32 @@ __global__ void k_gather_leapfrog_rhs(const float* __restrict__ R, const int* __
       if (ps >= 0) y += __ldg(R + (size_t)ps * S + s);
       else if (__ldg(src_rhs + (-ps - 1)) == s) y += -p * __ldg(src_val + (-ps - 1));
     }
-    u0[t] = 2.f * __ldg(u1 + t) - u0[t] + __ldg(m + d) * (-y);
+    uout[t] = 2.f * __ldg(u1 + t) - u0[t] + __ldg(m + d) * (-y);
   }
+}
+
+// Adjoint source: lam[d][s] += invD[d] * sum_{(k,w) at d} w * res[k][s][col]
+// over the dofs touched by receivers (rdof, CSR rptr/rk/rw).
+__global__ void k_inject_rhs(const int* __restrict__ rdof, const int* __restrict__ rptr, const int* __restrict__ rk,
+                             const double* __restrict__ rw, int n_rd, const double* __restrict__ res, int res_stride,
+                             int col, const double* __restrict__ inv_mass, float* __restrict__ lam, int S) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_rd * S) return;
+  const int i = t / S, s = t - i * S;
+  double acc = 0.0;
+  for (int e = rptr[i]; e < rptr[i + 1]; e++) acc += rw[e] * res[((size_t)rk[e] * S + s) * res_stride + col];
+  const int d = rdof[i];
+  lam[(size_t)d * S + s] += (float)(inv_mass[d] * acc);
+}
+
+// fac = scale[e] * orig for every element (media update of an operator).
+template <typename Real>
+__global__ void k_scale_factors(const Real* __restrict__ orig, const double* __restrict__ scale, Real* __restrict__ fac,
+                                int n_elt, int per_elt) {
+  const long long total = (long long)n_elt * per_elt;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x)
+    fac[t] = Real(double(orig[t]) * scale[t / per_elt]);
 }
 
 // First step U1 = U0 + dt (dU0 + dt/2 D^-1 (-A U0)) for every right-hand side.
@@ -214,7 +275,7 @@ void lfb_step_launch(mj_lfb* b, float* cur, const float* next, int q, cudaStream
   const long long total = (long long)b->n_dof * b->S;
   k_gather_leapfrog_rhs<<<grid_for(total), 256, 0, s>>>(
       b->R.as<float>(), b->ptr.as<int>(), b->pos.as<int>(), b->src_val.as<float>(), b->src_rhs.as<int>(),
-      b->pulse.as<double>(), b->n_pulse, b->ctr.as<int>(), q, cur, next, b->m.as<float>(), b->n_dof, b->S);
+      b->pulse.as<double>(), b->n_pulse, b->ctr.as<int>(), q, cur, next, cur, b->m.as<float>(), b->n_dof, b->S);
   count_launch();
 }
 
@@ -489,6 +550,239 @@ int mj_lfb_info(const mj_lfb* b, int* n_rhs, int* tile_elems, int* lanes, int* g
   if (lanes) *lanes = b->L;
   if (grid) *grid = b->grid;
   if (step) *step = b->step;
+  return MJ_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Discrete adjoint of the many-source leap-frog (no reference counterpart).
+// ---------------------------------------------------------------------------
+
+struct mj_adj {
+  mj_lfb* b = nullptr;
+  int N = 0, K = 0, J = 0;           // steps, checkpoint interval, checkpoints
+  size_t rows = 0;                   // n_dof * S
+  DevBuf ckpt;                       // J x 2 states (U^{jK}, U^{jK+1})
+  DevBuf seg;                        // K states of the segment being replayed
+  DevBuf la, lb;                     // adjoint states
+  DevBuf traces, res;                // n_rec x S x (N+1), FP64
+  DevBuf grad, coef;                 // per element (padded), FP64
+  DevBuf rdof, rptr, rk, rw;         // receiver injection CSR
+  int n_rd = 0;
+  bool have_forward = false;
+};
+
+namespace {
+
+void adj_receivers(mj_adj* a, const float* u, int col, cudaStream_t s) {
+  mj_lfb* b = a->b;
+  const int threads = 128, blocks = (b->n_rec * b->S + threads - 1) / threads;
+  k_receivers_rhs<<<blocks, threads, 0, s>>>(u, b->rec_idx.as<int>(), b->rec_w.as<double>(), b->n_rec, b->n_rec_w,
+                                             b->S, a->traces.as<double>(), a->N + 1, col);
+  count_launch();
+}
+
+// out = 2*u1 - u0 + dt^2 D^-1 (-A u1 + pulse[step] F): the forward update with
+// an explicit step index (pulse counter set on the host first).
+int adj_forward_step(mj_adj* a, const float* u0, const float* u1, float* out, int step, cudaStream_t s) {
+  mj_lfb* b = a->b;
+  MJ_CUDA(cudaMemcpyAsync(b->ctr.as<int>(), &step, sizeof(int), cudaMemcpyHostToDevice, s));
+  lfb_k1(b, u1, s);
+  const long long total = (long long)b->n_dof * b->S;
+  k_gather_leapfrog_rhs<<<grid_for(total), 256, 0, s>>>(
+      b->R.as<float>(), b->ptr.as<int>(), b->pos.as<int>(), b->src_val.as<float>(), b->src_rhs.as<int>(),
+      b->pulse.as<double>(), b->n_pulse, b->ctr.as<int>(), 0, u0, u1, out, b->m.as<float>(), b->n_dof, b->S);
+  count_launch();
+  MJ_CUDA(cudaGetLastError());
+  return MJ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mj_op_set_element_scale(mj_op* op, const double* scale) {
+  MJ_CHECK_ARG(op && scale, "mj_op_set_element_scale: null argument");
+  for (int e = 0; e < op->n_elt; e++)
+    MJ_CHECK_ARG(std::isfinite(scale[e]) && scale[e] >= 0, "mj_op_set_element_scale: scale must be finite and >= 0");
+  const size_t esz = op->precision == MJ_FP64 ? sizeof(double) : sizeof(float);
+  const int per_elt = 6 * op->Qp;
+  if (!op->fac_orig.ptr) {
+    MJ_CUDA(op->fac_orig.alloc(op->fac_e.bytes));
+    MJ_CUDA(cudaMemcpy(op->fac_orig.ptr, op->fac_e.ptr, op->fac_e.bytes, cudaMemcpyDeviceToDevice));
+  }
+  std::vector<double> sc(op->n_elt_pad, 0.0);
+  for (int e = 0; e < op->n_elt; e++) sc[e] = scale[e];
+  DevBuf d;
+  MJ_CUDA(d.alloc(sizeof(double) * sc.size()));
+  MJ_CUDA(cudaMemcpy(d.ptr, sc.data(), sizeof(double) * sc.size(), cudaMemcpyHostToDevice));
+  const long long total = (long long)op->n_elt_pad * per_elt;
+  if (esz == sizeof(double))
+    k_scale_factors<double><<<grid_for(total), 256, 0, op->stream>>>(op->fac_orig.as<double>(), d.as<double>(),
+                                                                     op->fac_e.as<double>(), op->n_elt_pad, per_elt);
+  else
+    k_scale_factors<float><<<grid_for(total), 256, 0, op->stream>>>(op->fac_orig.as<float>(), d.as<double>(),
+                                                                    op->fac_e.as<float>(), op->n_elt_pad, per_elt);
+  count_launch();
+  MJ_CUDA(cudaGetLastError());
+  MJ_CUDA(cudaStreamSynchronize(op->stream));
+  return MJ_OK;
+}
+
+int mj_adj_create(mj_lfb* b, int nsteps, int checkpoint_every, mj_adj** out) {
+  MJ_CHECK_ARG(b && out, "mj_adj_create: null argument");
+  *out = nullptr;
+  MJ_CHECK_ARG(nsteps >= 2, "mj_adj_create: at least 2 steps");
+  MJ_CHECK_ARG(b->n_rec > 0, "mj_adj_create: the integrator needs receivers");
+  std::unique_ptr<mj_adj> a(new mj_adj());
+  a->b = b;
+  a->N = nsteps;
+  a->K = checkpoint_every > 0 ? checkpoint_every : std::max(2, (int)std::ceil(std::sqrt((double)nsteps)));
+  MJ_CHECK_ARG(a->K >= 2, "mj_adj_create: checkpoint interval must be >= 2");
+  a->J = (nsteps + a->K - 1) / a->K;
+  a->rows = (size_t)b->n_dof * b->S;
+  MJ_CUDA(a->ckpt.alloc(sizeof(float) * a->rows * 2 * a->J));
+  MJ_CUDA(a->seg.alloc(sizeof(float) * a->rows * a->K));
+  MJ_CUDA(a->la.alloc(sizeof(float) * a->rows));
+  MJ_CUDA(a->lb.alloc(sizeof(float) * a->rows));
+  const size_t tr = (size_t)b->n_rec * b->S * (nsteps + 1);
+  MJ_CUDA(a->traces.alloc(sizeof(double) * tr));
+  MJ_CUDA(a->res.alloc(sizeof(double) * tr));
+  mj_op* op = b->op;
+  MJ_CUDA(a->grad.alloc(sizeof(double) * op->n_elt_pad));
+  MJ_CUDA(a->coef.alloc(sizeof(double) * op->n_elt_pad));
+  // receiver injection CSR (dofs touched by receivers -> (receiver, weight))
+  std::vector<int> ridx((size_t)b->n_rec * b->n_rec_w);
+  std::vector<double> rwt(ridx.size());
+  MJ_CUDA(cudaMemcpy(ridx.data(), b->rec_idx.ptr, sizeof(int) * ridx.size(), cudaMemcpyDeviceToHost));
+  MJ_CUDA(cudaMemcpy(rwt.data(), b->rec_w.ptr, sizeof(double) * rwt.size(), cudaMemcpyDeviceToHost));
+  std::vector<std::pair<int, int>> ent;  // (dof, t)
+  for (size_t t = 0; t < ridx.size(); t++) ent.push_back({ridx[t], (int)t});
+  std::sort(ent.begin(), ent.end());
+  std::vector<int> rdof, rptr{0}, rk;
+  std::vector<double> rw;
+  for (size_t i = 0; i < ent.size(); i++) {
+    if (i == 0 || ent[i].first != ent[i - 1].first) {
+      if (i) rptr.push_back((int)rk.size());
+      rdof.push_back(ent[i].first);
+    }
+    rk.push_back(ent[i].second / b->n_rec_w);
+    rw.push_back(rwt[ent[i].second]);
+  }
+  rptr.push_back((int)rk.size());
+  a->n_rd = (int)rdof.size();
+  MJ_CUDA(a->rdof.alloc(sizeof(int) * rdof.size()));
+  MJ_CUDA(a->rptr.alloc(sizeof(int) * rptr.size()));
+  MJ_CUDA(a->rk.alloc(sizeof(int) * rk.size()));
+  MJ_CUDA(a->rw.alloc(sizeof(double) * rw.size()));
+  MJ_CUDA(cudaMemcpy(a->rdof.ptr, rdof.data(), sizeof(int) * rdof.size(), cudaMemcpyHostToDevice));
+  MJ_CUDA(cudaMemcpy(a->rptr.ptr, rptr.data(), sizeof(int) * rptr.size(), cudaMemcpyHostToDevice));
+  MJ_CUDA(cudaMemcpy(a->rk.ptr, rk.data(), sizeof(int) * rk.size(), cudaMemcpyHostToDevice));
+  MJ_CUDA(cudaMemcpy(a->rw.ptr, rw.data(), sizeof(double) * rw.size(), cudaMemcpyHostToDevice));
+  int rc = energy_prepare(op->n, b->E, b->L);
+  if (rc) return rc;
+  *out = a.release();
+  return MJ_OK;
+}
+
+int mj_adj_destroy(mj_adj* a) {
+  delete a;
+  return MJ_OK;
+}
+
+int mj_adj_forward(mj_adj* a, double* traces) {
+  MJ_CHECK_ARG(a, "mj_adj_forward: null argument");
+  mj_lfb* b = a->b;
+  cudaStream_t s = b->stream;
+  int rc = mj_lfb_init(b, nullptr, nullptr);  // zero initial conditions
+  if (rc) return rc;
+  const size_t bytes = sizeof(float) * a->rows;
+  float* ck = a->ckpt.as<float>();
+  for (int n = 0; n <= a->N; n++) {
+    adj_receivers(a, b->cur(), n, s);
+    if (n == a->N) break;
+    if (n % a->K == 0) {
+      float* dst = ck + (size_t)(n / a->K) * 2 * a->rows;
+      MJ_CUDA(cudaMemcpyAsync(dst, b->cur(), bytes, cudaMemcpyDeviceToDevice, s));
+      MJ_CUDA(cudaMemcpyAsync(dst + a->rows, b->next(), bytes, cudaMemcpyDeviceToDevice, s));
+    }
+    lfb_step_launch(b, b->cur(), b->next(), b->step & 1, s);
+    b->cur_is_a = !b->cur_is_a;
+    b->step++;
+  }
+  MJ_CUDA(cudaGetLastError());
+  if (traces)
+    MJ_CUDA(cudaMemcpyAsync(traces, a->traces.ptr, sizeof(double) * b->n_rec * b->S * (a->N + 1),
+                            cudaMemcpyDeviceToHost, s));
+  MJ_CUDA(cudaStreamSynchronize(s));
+  a->have_forward = true;
+  return MJ_OK;
+}
+
+int mj_adj_backward(mj_adj* a, const double* residual, const double* coef, double* grad) {
+  MJ_CHECK_ARG(a && residual && coef && grad, "mj_adj_backward: null argument");
+  if (!a->have_forward) {
+    set_error("mj_adj_backward: mj_adj_forward must run first");
+    return MJ_ERR_STATE;
+  }
+  mj_lfb* b = a->b;
+  mj_op* op = b->op;
+  cudaStream_t s = b->stream;
+  const int N = a->N, K = a->K, S = b->S;
+  const size_t rows = a->rows, bytes = sizeof(float) * rows;
+  MJ_CUDA(cudaMemcpyAsync(a->res.ptr, residual, sizeof(double) * b->n_rec * S * (N + 1), cudaMemcpyHostToDevice, s));
+  std::vector<double> cf(op->n_elt_pad, 0.0);
+  for (int e = 0; e < op->n_elt; e++) cf[e] = coef[e];
+  MJ_CUDA(cudaMemcpyAsync(a->coef.ptr, cf.data(), sizeof(double) * cf.size(), cudaMemcpyHostToDevice, s));
+  MJ_CUDA(cudaMemsetAsync(a->grad.ptr, 0, sizeof(double) * op->n_elt_pad, s));
+  MJ_CUDA(cudaMemsetAsync(a->la.ptr, 0, bytes, s));
+  MJ_CUDA(cudaMemsetAsync(a->lb.ptr, 0, bytes, s));
+  float* lam1 = a->la.as<float>();  // lambda^{m+1}
+  float* lam2 = a->lb.as<float>();  // lambda^{m+2}
+  float* seg = a->seg.as<float>();
+  const float* ck = a->ckpt.as<float>();
+  const int inj_blocks = (a->n_rd * S + 127) / 128;
+  for (int j = a->J - 1; j >= 0; j--) {
+    const int n0 = j * K, n1 = std::min(n0 + K, N);
+    // replay U^{n0} .. U^{n1-1} of the segment from its checkpoint
+    MJ_CUDA(cudaMemcpyAsync(seg, ck + (size_t)j * 2 * rows, bytes, cudaMemcpyDeviceToDevice, s));
+    if (n1 - n0 >= 2)
+      MJ_CUDA(cudaMemcpyAsync(seg + rows, ck + (size_t)j * 2 * rows + rows, bytes, cudaMemcpyDeviceToDevice, s));
+    for (int n = n0; n + 2 <= n1 - 1; n++) {
+      int rc = adj_forward_step(a, seg + (size_t)(n - n0) * rows, seg + (size_t)(n + 1 - n0) * rows,
+                                seg + (size_t)(n + 2 - n0) * rows, n, s);
+      if (rc) return rc;
+    }
+    // adjoint steps m = n1 .. max(n0+1, 2), then the gradient term with U^{m-1}
+    for (int m = n1; m >= std::max(n0 + 1, 2); m--) {
+      lfb_k1(b, lam1, s);
+      const long long total = (long long)rows;
+      k_gather_leapfrog_rhs<<<grid_for(total), 256, 0, s>>>(
+          b->R.as<float>(), b->ptr.as<int>(), b->pos.as<int>(), b->src_val.as<float>(), b->src_rhs.as<int>(),
+          b->pulse.as<double>(), 0, b->ctr.as<int>(), 0, lam2, lam1, lam2, b->m.as<float>(), b->n_dof, S);
+      k_inject_rhs<<<inj_blocks, 128, 0, s>>>(a->rdof.as<int>(), a->rptr.as<int>(), a->rk.as<int>(),
+                                              a->rw.as<double>(), a->n_rd, a->res.as<double>(), N + 1, m,
+                                              b->inv_mass64.as<double>(), lam2, S);
+      count_launch(2);
+      std::swap(lam1, lam2);  // lam1 = lambda^m, lam2 = lambda^{m+1}
+      energy_launch(op->n, b->E, b->L, b->grid, seg + (size_t)(m - 1 - n0) * rows, op->nodle_e.as<int>(),
+                    op->fac_e.as<float>(), b->n_tiles, S, op->err.as<int>(), lam1, a->grad.as<double>(),
+                    a->coef.as<double>(), s);
+      count_launch();
+      MJ_CUDA(cudaGetLastError());
+    }
+  }
+  std::vector<double> g(op->n_elt_pad);
+  MJ_CUDA(cudaMemcpyAsync(g.data(), a->grad.ptr, sizeof(double) * g.size(), cudaMemcpyDeviceToHost, s));
+  int err = 0;
+  MJ_CUDA(cudaMemcpyAsync(&err, op->err.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MJ_CUDA(cudaStreamSynchronize(s));
+  if (err) {
+    set_error("mj_adj_backward: an element kernel wait timed out");
+    return MJ_ERR_CUDA;
+  }
+  for (int e = 0; e < op->n_elt; e++) grad[e] = g[e];
   return MJ_OK;
 }
 

@@ -15,6 +15,7 @@ struct mj_op {
   size_t r_len = 0;                     // slots of R (n_elt_pad * Qp)
   mj::DevBuf nodle_e, fac_e, R, ptr, pos;
   mj::DevBuf err;                       // device error flag (bounded-wait timeouts)
+  mj::DevBuf fac_orig;                  // factors before mj_op_set_element_scale (kept on first use)
   std::vector<int> h_ptr, h_pos;        // CSR incidences (host copy, for integrators)
   double gradphi[mj::kMaxN * mj::kMaxN];
   mj::DevBuf xbuf, ybuf;                // staging for host-vector MltAdd
@@ -22,7 +23,7 @@ struct mj_op {
   std::vector<double> tune_ms;          // autotuner timings of the candidates (diagnostic)
   std::vector<int> tune_E;
   size_t device_bytes() const {
-    return nodle_e.bytes + fac_e.bytes + R.bytes + ptr.bytes + pos.bytes + xbuf.bytes + ybuf.bytes;
+    return nodle_e.bytes + fac_e.bytes + fac_orig.bytes + R.bytes + ptr.bytes + pos.bytes + xbuf.bytes + ybuf.bytes;
   }
 };
 

@@ -255,12 +255,17 @@ __global__ void __launch_bounds__(E* N* N)
 // z-line, so every gather of a dof row and every write of R moves L
 // contiguous values; the factors and Nodle of a tile are staged once and
 // reused for all S/L passes.  E*n*n*L threads.
+// ENERGY variant (adjoint gradient): instead of writing R, each element
+// accumulates gacc[e] += coef[e] * sum_s sum_q lam[dof_q][s] (A_e x_s)_q,
+// i.e. lam^T A_e x summed over the right-hand sides, in FP64 (one CTA owns
+// an element per launch, so the update needs no atomics in global memory).
 // ---------------------------------------------------------------------------
-template <int N, int E, int L>
+template <int N, int E, int L, bool ENERGY = false>
 __global__ void __launch_bounds__(E* N* N* L)
     k_local_stiffness_rhs(const float* __restrict__ x, const int* __restrict__ nodle_e,
                           const float* __restrict__ fac_e, float* __restrict__ R, int n_tiles, int S,
-                          int* __restrict__ err) {
+                          int* __restrict__ err, const float* __restrict__ lam = nullptr,
+                          double* __restrict__ gacc = nullptr, const double* __restrict__ coef = nullptr) {
   using P = K1Plan<float, N, E, L>;
   constexpr int NN = P::NN, Qp = P::Qp;
   const float* __restrict__ Gm = GConst<float>::get(N);
@@ -313,6 +318,7 @@ __global__ void __launch_bounds__(E* N* N* L)
   const int passes = S / L;
   for (int it = 0; tile < n_tiles; tile += g, ++it) {
     const int s = it & 1;
+    float energy = 0.f;
     const bool ok = mbar_wait_bounded(&bar[s], (ph >> s) & 1u);
     if (__syncthreads_or(!ok)) {
       if (threadIdx.x == 0) atomicExch(err, 1);
@@ -361,7 +367,27 @@ __global__ void __launch_bounds__(E* N* N* L)
           y += grj[a] * s_vy[(s_line_y + k * NN + a * N) * L + lane];
           y += Gm[k * N + a] * vz[a];
         }
-        Rt[(size_t)k * NN * S] = y;
+        if (ENERGY) energy += y * __ldg(lam + (size_t)dofs[k] * S + col);
+        else Rt[(size_t)k * NN * S] = y;
+      }
+      __syncthreads();
+    }
+    if constexpr (ENERGY) {
+      // Deterministic reduction: thread partials in shared memory, then for
+      // each element one warp sums a fixed strided subset and shuffles.
+      __shared__ double s_thr[E * N * N * L];
+      s_thr[threadIdx.x] = (double)energy;
+      __syncthreads();
+      constexpr int per_elt = N * N * L;
+      const int w = threadIdx.x >> 5, lane32 = threadIdx.x & 31;
+      if (w < E) {
+        double acc = 0.0;
+        for (int t = lane32; t < per_elt; t += 32) acc += s_thr[w * per_elt + t];
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if (lane32 == 0) {
+          const size_t e = (size_t)tile * E + w;
+          gacc[e] += coef[e] * acc;
+        }
       }
       __syncthreads();
     }

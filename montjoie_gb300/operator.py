@@ -68,6 +68,13 @@ class FemMatrixFreeOperator:
         _lib.check(_lib.load().mj_op_mltadd_device(self._h, float(alpha), ctypes.c_void_p(x_ptr), float(beta),
                                                    ctypes.c_void_p(y_ptr), ctypes.c_void_p(stream)))
 
+    def set_element_scale(self, scale: np.ndarray) -> None:
+        """factors(e) <- scale[e] * factors given at creation (media update)."""
+        sc = np.ascontiguousarray(scale, dtype=np.float64)
+        if sc.size != self.n_elt:
+            raise ValueError("one scale per element")
+        _lib.check(_lib.load().mj_op_set_element_scale(self._h, _lib.dptr(sc)))
+
     def device_bytes(self) -> int:
         sz = ctypes.c_size_t()
         _lib.check(_lib.load().mj_op_info(self._h, None, None, None, None, ctypes.byref(sz)))

@@ -240,8 +240,19 @@ void oc_lumped_mass(int ne, int Q, int ndof, const int* nodle, const double* jw,
  * G[i][l], etc.), Vh(q) = B(q) Vh(q) (ProdMatVectScalarH1.cxx:468-481), Uh = Rh Vh
  * (HexahedronLobatto.cxx:220-244), scatter-add alpha*Uh
  * (NumberMap::AddLocalUnknownVector, NumberMap.cxx:745-777). */
+static void element_local(int n, const int* num, const double* G, const int* nodle_e, const double* bh_e,
+                          const double* x, double* Y);
+
 static void element_apply(int n, const int* num, const double* G, const int* nodle_e,
                           const double* bh_e, double alpha, const double* x, double* y) {
+  double Y[OC_MAXE * OC_MAXE * OC_MAXE];
+  element_local(n, num, G, nodle_e, bh_e, x, Y);
+  for (int q = 0; q < n * n * n; q++) y[nodle_e[q]] += alpha * Y[q];
+}
+
+/* Element-local A_e x in local (NumDofs3D) order. */
+static void element_local(int n, const int* num, const double* G, const int* nodle_e, const double* bh_e,
+                          const double* x, double* Y) {
   double U[OC_MAXE * OC_MAXE * OC_MAXE];
   double V[3][OC_MAXE * OC_MAXE * OC_MAXE];
 #define IX(i, j, k) (((i) * n + (j)) * n + (k))
@@ -271,7 +282,7 @@ static void element_apply(int n, const int* num, const double* G, const int* nod
           s += G[j * n + a] * V[1][IX(i, a, k)];
           s += G[k * n + a] * V[2][IX(i, j, a)];
         }
-        y[nodle_e[num[IX(i, j, k)]]] += alpha * s;
+        Y[num[IX(i, j, k)]] = s;
       }
 #undef IX
 }
@@ -480,4 +491,92 @@ int oc_point_weights(int r, const double* verts_e, const int* num, const double*
   for (int a = 0; a < 3; a++)
     if (xi[a] < -tol || xi[a] > 1.0 + tol) return 1;
   return 0;
+}
+
+/* ------------------------------------------------------------ adjoint */
+
+/* Misfit of S leap-frog runs from zero initial conditions and its gradient
+ * with respect to the per-element wave speed c (FP64, all states kept):
+ *   forward  M(U^{n+1} - 2U^n + U^{n-1}) = dt^2 (-A(c) U^n + pulse[n-1] F_s),
+ *            U^0 = U^1 = 0 (ModifiedEquation.cxx:92-124,290-345 from rest);
+ *   traces   r_k^n = W_k . U^n, n = 0..N;  J = 1/2 sum (r - d)^2;
+ *   adjoint  M(l^m - 2l^{m+1} + l^{m+2}) = -dt^2 A l^{m+1} + W^T (r^m - d^m),
+ *            l^{N+1} = l^{N+2} = 0, m = N..2;
+ *   gradient dJ/dc_e = -dt^2 sum_{n=1}^{N-1} (2/c_e) l^{n+1}^T A_e U^n,
+ * where A(c) = sum_e c_e^2 A_e^(1) (rho = 1, mu = c^2).  bh_unit are the
+ * mu = 1 factors.  Source entry t adds pulse * src_val[t] at src_idx[t] of
+ * run src_rhs[t].  Returns J; traces (nrec x S x (N+1)) and grad (ne) are
+ * optional outputs. */
+double oc_adjoint(int r, int ne, int ndof, const int* nodle, const int* num, const double* G,
+                  const double* bh_unit, const double* c, const double* D, const double* invD, int S, int nsrc,
+                  const int* src_idx, const int* src_rhs, const double* src_val, const double* pulse, double dt,
+                  int N, int nrec, const int* rec_idx, const double* rec_w, const double* data, double* traces,
+                  double* grad) {
+  const int n = r + 1, Q = n * n * n;
+  const double dt2 = dt * dt;
+  double* bh = (double*)malloc(sizeof(double) * (size_t)ne * Q * 6);
+  for (int e = 0; e < ne; e++)
+    for (int t = 0; t < Q * 6; t++) bh[(size_t)e * Q * 6 + t] = c[e] * c[e] * bh_unit[(size_t)e * Q * 6 + t];
+  double* U = (double*)malloc(sizeof(double) * (size_t)(N + 1) * ndof);
+  double* ah = (double*)malloc(sizeof(double) * (size_t)ndof);
+  double* l1 = (double*)malloc(sizeof(double) * (size_t)ndof);
+  double* l2 = (double*)malloc(sizeof(double) * (size_t)ndof);
+  double* res = (double*)malloc(sizeof(double) * (size_t)nrec * (N + 1));
+  double Y[OC_MAXE * OC_MAXE * OC_MAXE];
+  double J = 0.0;
+  if (grad) memset(grad, 0, sizeof(double) * (size_t)ne);
+  for (int s = 0; s < S; s++) {
+    memset(U, 0, sizeof(double) * (size_t)2 * ndof);
+    for (int m = 1; m < N; m++) {  /* U^{m+1} from U^m, U^{m-1}; pulse of loop index m-1 */
+      const double* u0 = U + (size_t)(m - 1) * ndof;
+      const double* u1 = U + (size_t)m * ndof;
+      double* u2 = U + (size_t)(m + 1) * ndof;
+      memset(ah, 0, sizeof(double) * (size_t)ndof);
+      for (int e = 0; e < ne; e++) element_apply(n, num, G, nodle + (size_t)e * Q, bh + (size_t)e * Q * 6, -1.0, u1, ah);
+      const double p = pulse ? pulse[m - 1] : 0.0;
+      for (int t = 0; t < nsrc; t++)
+        if (src_rhs[t] == s) ah[src_idx[t]] += p * src_val[t];
+      for (int i = 0; i < ndof; i++) {
+        double a = dt2 * ah[i] - D[i] * u0[i];
+        a += 2.0 * D[i] * u1[i];
+        u2[i] = a * invD[i];
+      }
+    }
+    for (int k = 0; k < nrec; k++)
+      for (int m = 0; m <= N; m++) {
+        double acc = 0.0;
+        for (int t = 0; t < Q; t++) acc += rec_w[(size_t)k * Q + t] * U[(size_t)m * ndof + rec_idx[(size_t)k * Q + t]];
+        const size_t o = ((size_t)k * S + s) * (N + 1) + m;
+        if (traces) traces[o] = acc;
+        res[(size_t)k * (N + 1) + m] = acc - (data ? data[o] : 0.0);
+        J += 0.5 * res[(size_t)k * (N + 1) + m] * res[(size_t)k * (N + 1) + m];
+      }
+    if (!grad) continue;
+    memset(l1, 0, sizeof(double) * (size_t)ndof);  /* lambda^{m+1} */
+    memset(l2, 0, sizeof(double) * (size_t)ndof);  /* lambda^{m+2} */
+    for (int m = N; m >= 2; m--) {
+      memset(ah, 0, sizeof(double) * (size_t)ndof);
+      for (int e = 0; e < ne; e++) element_apply(n, num, G, nodle + (size_t)e * Q, bh + (size_t)e * Q * 6, -1.0, l1, ah);
+      for (int i = 0; i < ndof; i++) {
+        double a = dt2 * ah[i] - D[i] * l2[i] + 2.0 * D[i] * l1[i];
+        l2[i] = a * invD[i];
+      }
+      for (int k = 0; k < nrec; k++)
+        for (int t = 0; t < Q; t++) {
+          const int d = rec_idx[(size_t)k * Q + t];
+          l2[d] += invD[d] * rec_w[(size_t)k * Q + t] * res[(size_t)k * (N + 1) + m];
+        }
+      double* tmp = l1; l1 = l2; l2 = tmp;  /* l1 = lambda^m, l2 = lambda^{m+1} */
+      const double* un = U + (size_t)(m - 1) * ndof;
+      for (int e = 0; e < ne; e++) {
+        const int* nd = nodle + (size_t)e * Q;
+        element_local(n, num, G, nd, bh + (size_t)e * Q * 6, un, Y);
+        double dot = 0.0;
+        for (int q = 0; q < Q; q++) dot += l1[nd[q]] * Y[q];
+        grad[e] += -dt2 * (2.0 / c[e]) * dot;
+      }
+    }
+  }
+  free(bh); free(U); free(ah); free(l1); free(l2); free(res);
+  return J;
 }

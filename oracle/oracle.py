@@ -55,6 +55,10 @@ def lib():
         L.oc_leapfrog.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _I, _D, _D, _D, _D,
                                   ctypes.c_int, _I, _D, _D, ctypes.c_double, ctypes.c_int, _D, _D, _D,
                                   _D, _D, ctypes.c_int, _I, _D, _D, ctypes.c_int, _I, _I]
+        L.oc_adjoint.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _I, _D, _D, _D, _D, _D,
+                                 ctypes.c_int, ctypes.c_int, _I, _I, _D, _D, ctypes.c_double, ctypes.c_int,
+                                 ctypes.c_int, _I, _D, _D, _D, _D]
+        L.oc_adjoint.restype = ctypes.c_double
         L.oc_point_weights.argtypes = [ctypes.c_int, _D, _I, _D, _D, _D]
         L.oc_point_weights.restype = ctypes.c_int
         _lib = L
@@ -288,3 +292,21 @@ def load_dump(outdir: str) -> dict:
         with open(run) as f:
             out["run"] = {l.split()[0]: float(l.split()[1]) for l in f if l.strip()}
     return out
+
+
+def adjoint(r, nodle, bh_unit, c, D, invD, S, src_idx, src_rhs, src_val, pulse, dt, nsteps, rec_idx, rec_w,
+            data=None, want_grad=True):
+    """FP64 misfit J, traces (nrec, S, N+1) and dJ/dc (per element) of S runs from rest."""
+    ne, Q = nodle.shape
+    ndof = D.size
+    G = grad_matrix(r).ravel().copy()
+    num = hex_numbering(r)
+    nrec = rec_idx.shape[0]
+    traces = np.zeros((nrec, S, nsteps + 1))
+    grad = np.zeros(ne) if want_grad else None
+    J = lib().oc_adjoint(r, ne, ndof, _p(i32(nodle), _I), _p(num, _I), _p(G), _p(f64(bh_unit)), _p(f64(c)),
+                         _p(f64(D)), _p(f64(invD)), int(S), int(len(src_idx)), _p(i32(src_idx), _I),
+                         _p(i32(src_rhs), _I), _p(f64(src_val)), _p(f64(pulse)), float(dt), int(nsteps), int(nrec),
+                         _p(i32(rec_idx), _I), _p(f64(rec_w)), _p(None if data is None else f64(data)), _p(traces),
+                         _p(grad))
+    return J, traces, grad
