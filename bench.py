@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the configuration 3 and 4 legs")
     ap.add_argument("--extra-steps", type=int, default=500)
+    ap.add_argument("--adjoint-steps", type=int, default=1000)
     return ap.parse_args()
 
 
@@ -241,6 +242,82 @@ def leg_config4_sources(args, torch, _lib):
             "step_frac_of_hbm": value * bytes_step / 1e9 / peak}
 
 
+def leg_config5_adjoint(args, torch, _lib):
+    """BASELINE configuration 5: 32^3 Q4, per-element c as parameter (start
+    U[1.5,2.5]), 16 sources x 64 receivers, FP32 steps, L2 misfit against
+    traces of a seeded perturbed true c; gradient by the discrete adjoint with
+    sqrt(N) checkpointing.  Timed at full size; the gradient is checked on a
+    small case against central differences (20 elements) and the FP64 CPU adjoint."""
+    from montjoie_gb300 import mesh as M
+    from montjoie_gb300.adjoint import AcousticAdjoint
+    from montjoie_gb300.problem import gaussian_source, geometry, receiver_weights
+    cells, order, S, nrec, N = 32, 4, 16, 64, args.adjoint_steps
+    rng = np.random.default_rng(SEED + 50)
+    m = M.perturbed_cube(cells, seed=SEED + 50, amplitude=0.05, kind="random", c_mode="constant", c_range=(1.0, 1.0))
+    pb = build_problem(cells, order, N + 2, mesh=m)   # unit mu (c = 1) factors
+    c0 = rng.uniform(1.5, 2.5, pb.nodle.shape[0])
+    c_true = c0 * (1.0 + 0.1 * rng.uniform(-1, 1, c0.size))
+    # CFL of the fastest medium: scale the c = 1 step by 1/max c
+    dt = pb.setup.dt / c_true.max()
+    pb.set_time_step(dt, N + 2)
+    idx, rhs, val = [], [], []
+    for s_, c in enumerate(rng.uniform(0.1, 0.9, size=(S, 3))):
+        i_, v_ = gaussian_source(pb.nodle, pb.jw, pb.xq, pb.n_dof, c, 2.0 / cells)
+        idx.append(i_); val.append(v_); rhs.append(np.full(i_.size, s_))
+    rec_idx, rec_w = receiver_weights(order, pb.verts_e, pb.nodle, rng.uniform(0.1, 0.9, size=(nrec, 3)))
+    model = AcousticAdjoint(order, pb.nodle, pb.factors, pb.n_dof, pb.mass, dt, N, S, np.concatenate(idx),
+                            np.concatenate(rhs), np.concatenate(val), pb.pulse, rec_idx, rec_w)
+    data = model.forward(c_true)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    tr = model.forward(c0)
+    t1 = time.perf_counter()
+    res = tr - data
+    grad = model.backward(res)
+    t2 = time.perf_counter()
+    J = 0.5 * float((res * res).sum())
+    model.close()
+    # forward N steps + backward (replay ~N steps, N adjoint steps, N gradient kernels)
+    dof_updates = pb.n_dof * S * N
+    return {"workload": f"32^3 Q4, per-element c (start U[1.5,2.5], true c perturbed by U[-10%,10%]), {S} sources x "
+                        f"{nrec} receivers, {N} FP32 steps, L2 trace misfit, adjoint with sqrt(N) checkpoints",
+            "n_dof": pb.n_dof, "steps": N, "loss": J, "grad_norm": float(np.linalg.norm(grad)),
+            "forward_seconds": t1 - t0, "backward_seconds": t2 - t1,
+            "forward_value": dof_updates / (t1 - t0), "gradient_value": dof_updates / (t2 - t0), "unit": UNIT,
+            "small_case_check": adjoint_small_check()}
+
+
+def adjoint_small_check():
+    """GPU FP32 adjoint vs FP64 CPU adjoint vs central differences on 20 elements (small mesh)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from adjoint_case import build_case, oracle_adjoint
+    from montjoie_gb300.adjoint import AcousticAdjoint
+    case = build_case(S=8, nsteps=80)
+    g = case["g"]
+    model = AcousticAdjoint(case["r"], g["nodle"], case["bh_unit"], g["massD"].size, g["massD"], case["dt"],
+                            case["N"], case["S"], case["src_idx"], case["src_rhs"], case["src_val"], case["pulse"],
+                            case["rec_idx"], case["rec_w"])
+    J, grad = model.loss_and_grad(case["c0"], case["data"])
+    model.close()
+    J64, _, g64 = oracle_adjoint(case, case["c0"], case["data"])
+    rng = np.random.default_rng(7)
+    els = rng.choice(case["c0"].size, size=min(20, case["c0"].size), replace=False)
+    fd = []
+    for e in els:
+        h = 1e-5 * case["c0"][e]
+        cp, cm = case["c0"].copy(), case["c0"].copy()
+        cp[e] += h
+        cm[e] -= h
+        fd.append((oracle_adjoint(case, cp, case["data"], False)[0] - oracle_adjoint(case, cm, case["data"], False)[0])
+                  / (2 * h))
+    fd = np.array(fd)
+    return {"mesh": "3^3 Q4 golden mesh, 8 sources x 4 receivers, 80 steps",
+            "gpu_fp32_vs_fp64_adjoint_rel_l2": float(np.linalg.norm(grad - g64) / np.linalg.norm(g64)),
+            "gpu_fp32_vs_fd_rel_l2_20_elements": float(np.linalg.norm(grad[els] - fd) / np.linalg.norm(fd)),
+            "fp64_adjoint_vs_fd_rel_l2_20_elements": float(np.linalg.norm(g64[els] - fd) / np.linalg.norm(fd)),
+            "loss_rel_diff": abs(J - J64) / J64}
+
+
 def LeapFrogIteratorFor(pb, op, src_idx, src_val):
     from montjoie_gb300.leapfrog import LeapFrogIterator
     return LeapFrogIterator(op, pb.setup.dt, pb.mass, None, src_idx, src_val, pb.pulse)
@@ -366,6 +443,7 @@ def run_ours(args):
         op32.close(); op64.close()
         out["config3_q8"] = leg_config3(args, torch, _lib)
         out["config4_sources"] = leg_config4_sources(args, torch, _lib)
+        out["config5_adjoint"] = leg_config5_adjoint(args, torch, _lib)
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(args, pb, u_check=None)
     if rank == 0:
