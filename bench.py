@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip the configuration 3 and 4 legs")
     ap.add_argument("--extra-steps", type=int, default=500)
     ap.add_argument("--adjoint-steps", type=int, default=1000)
+    ap.add_argument("--leg", default="all", choices=["all", "config3", "config4", "config5"],
+                    help="profiling aid: run one extra leg alone (no JSON line contract)")
     return ap.parse_args()
 
 
@@ -364,6 +366,7 @@ def run_ours(args):
 
     # ---- FP32 chosen form, resident (value)
     op32 = pb.operator("fp32")
+    tuning32 = op32.tuning()
     lf32 = pb.integrator(op32, diagnostics=False)
     lf32.SetInitialConditionS(zeros)
     lf32.Advance(W)
@@ -425,7 +428,7 @@ def run_ours(args):
                 "traffic": None if per_elt is None else per_elt * n_elt,
                 "algorithmic_bytes_per_launch": bytes_k1,
                 "kernel_ms": k1_ms, "update_kernel_ms": k2_ms,
-                "step_frac": (step_bytes / (ms32 / K / 1e3) / 1e9) / peak,
+                "step_frac": (step_bytes / (ms32 / K / 1e3) / 1e9) / peak, "autotuned": tuning32,
                 "step_algorithmic_bytes": step_bytes}
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
@@ -542,6 +545,13 @@ def run_reference(args):
 
 def main():
     args = parse()
+    if args.leg != "all":
+        import torch
+        from montjoie_gb300 import _lib
+        _lib.load(build_if_missing=False)
+        fn = {"config3": leg_config3, "config4": leg_config4_sources, "config5": leg_config5_adjoint}[args.leg]
+        print(json.dumps({args.leg: fn(args, torch, _lib)}))
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -95,6 +95,13 @@ int mj_op_mltadd_device(mj_op* op, double alpha, const void* x, double beta, voi
 int mj_op_info(const mj_op* op, int* order, int* n_elt, int* n_dof, int* precision,
                size_t* device_bytes);
 
+/* Element-kernel variant chosen by the autotuner at creation: elements per
+ * CTA, work layout (1 = vector lines), grid; and the timings (ms per launch,
+ * or a negative occupancy score on meshes too small to time) of the
+ * candidates tried (candidate_ms may be NULL, else room for 64 values). */
+int mj_op_tuning(const mj_op* op, int* tile_elems, int* vector_lines, int* grid, int* n_candidates,
+                 double* candidate_ms);
+
 /* Number of kernels this library launched on the calling process since load. */
 uint64_t mj_kernel_launches(void);
 

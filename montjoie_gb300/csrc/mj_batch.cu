@@ -38,10 +38,10 @@ int rhs_prepare_one(int* ctas) {
 }
 
 template <int N, int E, int L>
-void rhs_launch_one(int grid, const float* x, const int* nodle_e, const float* fac_e, float* R, int n_tiles, int S,
-                    int* err, cudaStream_t s) {
+void rhs_launch_one(int grid, const float* x, const int* nodle_e, const float* fac_e, float* R, const int* slot_e,
+                    int n_tiles, int S, int* err, cudaStream_t s) {
   using P = K1Plan<float, N, E, L>;
-  k_local_stiffness_rhs<N, E, L><<<grid, P::threads, P::total, s>>>(x, nodle_e, fac_e, R, n_tiles, S, err);
+  k_local_stiffness_rhs<N, E, L><<<grid, P::threads, P::total, s>>>(x, nodle_e, fac_e, R, slot_e, n_tiles, S, err);
 }
 
 #define MJ_RHS_VARIANTS(X)                                                                                     \
@@ -69,8 +69,8 @@ template <int N, int E, int L>
 void energy_launch_one(int grid, const float* x, const int* nodle_e, const float* fac_e, int n_tiles, int S, int* err,
                        const float* lam, double* gacc, const double* coef, cudaStream_t s) {
   using P = K1Plan<float, N, E, L>;
-  k_local_stiffness_rhs<N, E, L, true><<<grid, P::threads, P::total, s>>>(x, nodle_e, fac_e, nullptr, n_tiles, S, err,
-                                                                          lam, gacc, coef);
+  k_local_stiffness_rhs<N, E, L, true><<<grid, P::threads, P::total, s>>>(x, nodle_e, fac_e, nullptr, nullptr,
+                                                                          n_tiles, S, err, lam, gacc, coef);
 }
 
 int energy_prepare(int n, int E, int L) {
@@ -94,11 +94,11 @@ void energy_launch(int n, int E, int L, int grid, const float* x, const int* nod
 }
 
 void rhs_launch(int n, int E, int L, int grid, const float* x, const int* nodle_e, const float* fac_e, float* R,
-                int n_tiles, int S, int* err, cudaStream_t s) {
-#define MJ_X(NV, EV, LV)                                                             \
-  if (n == NV && E == EV && L == LV) {                                               \
-    rhs_launch_one<NV, EV, LV>(grid, x, nodle_e, fac_e, R, n_tiles, S, err, s);      \
-    return;                                                                          \
+                const int* slot_e, int n_tiles, int S, int* err, cudaStream_t s) {
+#define MJ_X(NV, EV, LV)                                                                     \
+  if (n == NV && E == EV && L == LV) {                                                       \
+    rhs_launch_one<NV, EV, LV>(grid, x, nodle_e, fac_e, R, slot_e, n_tiles, S, err, s);      \
+    return;                                                                                  \
   }
   MJ_RHS_VARIANTS(MJ_X)
 #undef MJ_X
@@ -106,21 +106,16 @@ void rhs_launch(int n, int E, int L, int grid, const float* x, const int* nodle_
 
 // ---- per-(dof, rhs) kernels ------------------------------------------------
 
-// Gather + sources + leap-frog, thread per (dof d, right-hand side s):
-//   Ah = -(A U1)[d][s] + p * F_s[d];  U[d][s] <- 2 U1 - U0 + (dt^2/D_d) Ah
-// Source entries are CSR entries with pos < 0: slot -pos-1 of (src_val,
-// src_rhs) applies to right-hand side src_rhs only.  The pulse of the step
-// is pulse[ctr[q]]; block 0 writes ctr[1-q] = ctr[q] + 1 for the next step
-// (two counters, so a captured sequence of steps needs no host update).
-// uout may alias u0 (in-place update: each thread reads its entry first).
+// Gather + leap-frog, thread per (dof d, right-hand side s):
+//   U[d][s] <- 2 U1 - U0 + (dt^2/D_d) (-(A U1)[d][s])
+// The contributions to dof d sit in R[ptr[d] .. ptr[d+1]) (rows of S), so a
+// warp streams contiguous memory.  Block 0 advances the step counter
+// ctr[1-q] = ctr[q] + 1 (sources: k_source_rhs).  uout may alias u0
+// (each thread reads its entry first).
 __global__ void k_gather_leapfrog_rhs(const float* __restrict__ R, const int* __restrict__ ptr,
-                                      const int* __restrict__ pos, const float* __restrict__ src_val,
-                                      const int* __restrict__ src_rhs, const double* __restrict__ pulse, int n_pulse,
                                       int* __restrict__ ctr, int q, const float* u0, const float* __restrict__ u1,
                                       float* uout, const float* __restrict__ m, int n_dof, int S) {
-  const int step = ctr[q];
-  const float p = (step < n_pulse) ? (float)pulse[step] : 0.f;
-  if (blockIdx.x == 0 && threadIdx.x == 0) ctr[1 - q] = step + 1;
+  if (ctr && blockIdx.x == 0 && threadIdx.x == 0) ctr[1 - q] = ctr[q] + 1;
   const long long total = (long long)n_dof * S;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x) {
@@ -128,12 +123,22 @@ __global__ void k_gather_leapfrog_rhs(const float* __restrict__ R, const int* __
     const int s = (int)(t - (long long)d * S);
     float y = 0.f;
     const int q1 = __ldg(ptr + d + 1);
-    for (int e = __ldg(ptr + d); e < q1; e++) {
-      const int ps = __ldg(pos + e);
-      if (ps >= 0) y += __ldg(R + (size_t)ps * S + s);
-      else if (__ldg(src_rhs + (-ps - 1)) == s) y += -p * __ldg(src_val + (-ps - 1));
-    }
+    for (int e = __ldg(ptr + d); e < q1; e++) y += __ldg(R + (size_t)e * S + s);
     uout[t] = 2.f * __ldg(u1 + t) - u0[t] + __ldg(m + d) * (-y);
+  }
+}
+
+// Sources of the step just taken: u[idx[t]][rhs[t]] += (dt^2/D) p val[t],
+// p = pulse[ctr[q]] (no pulse past n_pulse).  (dof, rhs) pairs are unique.
+__global__ void k_source_rhs(const int* __restrict__ idx, const int* __restrict__ rhs, const float* __restrict__ val,
+                             int n_src, const double* __restrict__ pulse, int n_pulse, const int* __restrict__ ctr,
+                             int q, const float* __restrict__ m, float* __restrict__ u, int S) {
+  const int step = ctr[q];
+  if (step >= n_pulse) return;
+  const float p = (float)pulse[step];
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n_src; t += gridDim.x * blockDim.x) {
+    const int d = idx[t];
+    u[(size_t)d * S + rhs[t]] += m[d] * p * val[t];
   }
 }
 
@@ -164,7 +169,7 @@ __global__ void k_scale_factors(const Real* __restrict__ orig, const double* __r
 // First step U1 = U0 + dt (dU0 + dt/2 D^-1 (-A U0)) for every right-hand side.
 // du0 and u1 may be the same array (each thread reads its entry before writing it).
 __global__ void k_gather_init_rhs(const float* __restrict__ R, const int* __restrict__ ptr,
-                                  const int* __restrict__ pos, const float* __restrict__ u0, const float* du0,
+                                  const float* __restrict__ u0, const float* du0,
                                   const double* __restrict__ inv_mass, double dt, float* u1, int n_dof, int S) {
   const long long total = (long long)n_dof * S;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
@@ -172,10 +177,7 @@ __global__ void k_gather_init_rhs(const float* __restrict__ R, const int* __rest
     const int d = (int)(t / S);
     const int s = (int)(t - (long long)d * S);
     float y = 0.f;
-    for (int e = ptr[d]; e < ptr[d + 1]; e++) {
-      const int ps = pos[e];
-      if (ps >= 0) y += R[(size_t)ps * S + s];
-    }
+    for (int e = ptr[d]; e < ptr[d + 1]; e++) y += R[(size_t)e * S + s];
     double v = double(-y) * inv_mass[d];
     v *= 0.5 * dt;
     v += du0 ? double(du0[t]) : 0.0;
@@ -244,7 +246,8 @@ struct mj_lfb {
   double dt = 0;
   int E = 1, L = 32, grid = 1, n_tiles = 0;  // tuned element-kernel variant
   DevBuf R;                                  // element-local results [slot][S]
-  DevBuf ptr, pos, src_val, src_rhs, m, inv_mass64, pulse, ctr;
+  DevBuf src_idx, src_val, src_rhs, m, inv_mass64, pulse, ctr;
+  int n_src = 0;
   DevBuf ua, ub, stage, rec_idx, rec_w, traces_d;
   int n_pulse = 0, n_rec = 0, n_rec_w = 0;
   int step = 0;
@@ -265,7 +268,7 @@ namespace {
 void lfb_k1(mj_lfb* b, const float* x, cudaStream_t s) {
   mj_op* op = b->op;
   rhs_launch(op->n, b->E, b->L, b->grid, x, op->nodle_e.as<int>(), op->fac_e.as<float>(), b->R.as<float>(),
-             b->n_tiles, b->S, op->err.as<int>(), s);
+             op->slot_e.as<int>(), b->n_tiles, b->S, op->err.as<int>(), s);
   count_launch();
 }
 
@@ -273,10 +276,15 @@ void lfb_k1(mj_lfb* b, const float* x, cudaStream_t s) {
 void lfb_step_launch(mj_lfb* b, float* cur, const float* next, int q, cudaStream_t s) {
   lfb_k1(b, next, s);
   const long long total = (long long)b->n_dof * b->S;
-  k_gather_leapfrog_rhs<<<grid_for(total), 256, 0, s>>>(
-      b->R.as<float>(), b->ptr.as<int>(), b->pos.as<int>(), b->src_val.as<float>(), b->src_rhs.as<int>(),
-      b->pulse.as<double>(), b->n_pulse, b->ctr.as<int>(), q, cur, next, cur, b->m.as<float>(), b->n_dof, b->S);
+  k_gather_leapfrog_rhs<<<grid_for(total), 256, 0, s>>>(b->R.as<float>(), b->op->ptr.as<int>(), b->ctr.as<int>(), q,
+                                                        cur, next, cur, b->m.as<float>(), b->n_dof, b->S);
   count_launch();
+  if (b->n_src) {
+    k_source_rhs<<<(b->n_src + 255) / 256, 256, 0, s>>>(b->src_idx.as<int>(), b->src_rhs.as<int>(),
+                                                        b->src_val.as<float>(), b->n_src, b->pulse.as<double>(),
+                                                        b->n_pulse, b->ctr.as<int>(), q, b->m.as<float>(), cur, b->S);
+    count_launch();
+  }
 }
 
 int lfb_autotune(mj_lfb* b) {
@@ -347,27 +355,23 @@ int mj_lfb_create(mj_op* op, const mj_lfb_desc* d, mj_lfb** out) {
     invD[i] = d->inv_mass ? d->inv_mass[i] : 1.0 / d->mass[i];
     m[i] = (float)(d->dt * d->dt * invD[i]);
   }
-  // CSR of the operator with each dof's source entries appended (sorted by rhs)
-  std::vector<std::vector<int>> src_of(n);
+  // sparse sources, one entry per (dof, rhs) pair
+  std::vector<std::pair<int, int>> pairs;
   for (int t = 0; t < d->n_src; t++) {
     MJ_CHECK_ARG(d->src_idx[t] >= 0 && d->src_idx[t] < n, "mj_lfb_create: source index out of range");
     MJ_CHECK_ARG(d->src_rhs[t] >= 0 && d->src_rhs[t] < S, "mj_lfb_create: source right-hand side out of range");
-    src_of[d->src_idx[t]].push_back(t);
+    pairs.push_back({d->src_idx[t], d->src_rhs[t]});
   }
-  std::vector<int> ptr(n + 1, 0), pos;
-  pos.reserve(op->h_pos.size() + d->n_src);
-  for (int i = 0; i < n; i++) {
-    for (int q = op->h_ptr[i]; q < op->h_ptr[i + 1]; q++) pos.push_back(op->h_pos[q]);
-    for (int t : src_of[i]) pos.push_back(-t - 1);
-    ptr[i + 1] = (int)pos.size();
-  }
+  std::sort(pairs.begin(), pairs.end());
+  for (size_t t = 1; t < pairs.size(); t++)
+    MJ_CHECK_ARG(pairs[t] != pairs[t - 1], "mj_lfb_create: duplicate (source dof, right-hand side) pair");
   std::vector<float> sv(std::max(1, d->n_src));
-  std::vector<int> sr(std::max(1, d->n_src), -1);
-  for (int t = 0; t < d->n_src; t++) { sv[t] = (float)d->src_val[t]; sr[t] = d->src_rhs[t]; }
+  std::vector<int> sr(std::max(1, d->n_src), 0), si(std::max(1, d->n_src), 0);
+  for (int t = 0; t < d->n_src; t++) { sv[t] = (float)d->src_val[t]; sr[t] = d->src_rhs[t]; si[t] = d->src_idx[t]; }
+  b->n_src = d->n_src;
   const size_t rows = (size_t)n * S;
-  MJ_CUDA(b->R.alloc(sizeof(float) * op->r_len * S));
-  MJ_CUDA(b->ptr.alloc(sizeof(int) * (n + 1)));
-  MJ_CUDA(b->pos.alloc(sizeof(int) * pos.size()));
+  MJ_CUDA(b->R.alloc(sizeof(float) * (op->n_inc + 1) * S));
+  MJ_CUDA(b->src_idx.alloc(sizeof(int) * si.size()));
   MJ_CUDA(b->src_val.alloc(sizeof(float) * sv.size()));
   MJ_CUDA(b->src_rhs.alloc(sizeof(int) * sr.size()));
   MJ_CUDA(b->m.alloc(sizeof(float) * n));
@@ -376,8 +380,7 @@ int mj_lfb_create(mj_op* op, const mj_lfb_desc* d, mj_lfb** out) {
   MJ_CUDA(b->ctr.alloc(sizeof(int) * 2));
   MJ_CUDA(b->ua.alloc(sizeof(float) * rows));
   MJ_CUDA(b->ub.alloc(sizeof(float) * rows));
-  MJ_CUDA(cudaMemcpy(b->ptr.ptr, ptr.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
-  MJ_CUDA(cudaMemcpy(b->pos.ptr, pos.data(), sizeof(int) * pos.size(), cudaMemcpyHostToDevice));
+  MJ_CUDA(cudaMemcpy(b->src_idx.ptr, si.data(), sizeof(int) * si.size(), cudaMemcpyHostToDevice));
   MJ_CUDA(cudaMemcpy(b->src_val.ptr, sv.data(), sizeof(float) * sv.size(), cudaMemcpyHostToDevice));
   MJ_CUDA(cudaMemcpy(b->src_rhs.ptr, sr.data(), sizeof(int) * sr.size(), cudaMemcpyHostToDevice));
   MJ_CUDA(cudaMemcpy(b->m.ptr, m.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
@@ -433,7 +436,7 @@ int mj_lfb_init(mj_lfb* b, const double* u0, const double* du0) {
     du = b->ub.as<float>();
   }
   lfb_k1(b, b->ua.as<float>(), s);
-  k_gather_init_rhs<<<grid_for(rows), 256, 0, s>>>(b->R.as<float>(), b->ptr.as<int>(), b->pos.as<int>(),
+  k_gather_init_rhs<<<grid_for(rows), 256, 0, s>>>(b->R.as<float>(), b->op->ptr.as<int>(),
                                                    b->ua.as<float>(), du, b->inv_mass64.as<double>(), b->dt,
                                                    b->ub.as<float>(), b->n_dof, b->S);
   count_launch();
@@ -495,7 +498,7 @@ int mj_lfb_advance(mj_lfb* b, int nsteps, double* traces, int trace_stride, int 
     }
     while (nsteps - done >= G) {
       MJ_CUDA(cudaGraphLaunch(b->graph, s));
-      count_launch(2 * G);
+      count_launch((uint64_t)G * (2 + (b->n_src > 0)));
       done += G;
       b->step += G;
     }
@@ -590,10 +593,15 @@ int adj_forward_step(mj_adj* a, const float* u0, const float* u1, float* out, in
   MJ_CUDA(cudaMemcpyAsync(b->ctr.as<int>(), &step, sizeof(int), cudaMemcpyHostToDevice, s));
   lfb_k1(b, u1, s);
   const long long total = (long long)b->n_dof * b->S;
-  k_gather_leapfrog_rhs<<<grid_for(total), 256, 0, s>>>(
-      b->R.as<float>(), b->ptr.as<int>(), b->pos.as<int>(), b->src_val.as<float>(), b->src_rhs.as<int>(),
-      b->pulse.as<double>(), b->n_pulse, b->ctr.as<int>(), 0, u0, u1, out, b->m.as<float>(), b->n_dof, b->S);
+  k_gather_leapfrog_rhs<<<grid_for(total), 256, 0, s>>>(b->R.as<float>(), b->op->ptr.as<int>(), b->ctr.as<int>(), 0,
+                                                        u0, u1, out, b->m.as<float>(), b->n_dof, b->S);
   count_launch();
+  if (b->n_src) {
+    k_source_rhs<<<(b->n_src + 255) / 256, 256, 0, s>>>(b->src_idx.as<int>(), b->src_rhs.as<int>(),
+                                                        b->src_val.as<float>(), b->n_src, b->pulse.as<double>(),
+                                                        b->n_pulse, b->ctr.as<int>(), 0, b->m.as<float>(), out, b->S);
+    count_launch();
+  }
   MJ_CUDA(cudaGetLastError());
   return MJ_OK;
 }
@@ -758,9 +766,8 @@ int mj_adj_backward(mj_adj* a, const double* residual, const double* coef, doubl
     for (int m = n1; m >= std::max(n0 + 1, 2); m--) {
       lfb_k1(b, lam1, s);
       const long long total = (long long)rows;
-      k_gather_leapfrog_rhs<<<grid_for(total), 256, 0, s>>>(
-          b->R.as<float>(), b->ptr.as<int>(), b->pos.as<int>(), b->src_val.as<float>(), b->src_rhs.as<int>(),
-          b->pulse.as<double>(), 0, b->ctr.as<int>(), 0, lam2, lam1, lam2, b->m.as<float>(), b->n_dof, S);
+      k_gather_leapfrog_rhs<<<grid_for(total), 256, 0, s>>>(b->R.as<float>(), op->ptr.as<int>(), nullptr, 0, lam2,
+                                                            lam1, lam2, b->m.as<float>(), b->n_dof, S);
       k_inject_rhs<<<inj_blocks, 128, 0, s>>>(a->rdof.as<int>(), a->rptr.as<int>(), a->rk.as<int>(),
                                               a->rw.as<double>(), a->n_rd, a->res.as<double>(), N + 1, m,
                                               b->inv_mass64.as<double>(), lam2, S);

@@ -12,18 +12,21 @@ struct mj_op {
   int order = 0, n = 0, Q = 0, Qp = 0;
   int n_elt = 0, n_elt_pad = 0, n_dof = 0, precision = MJ_FP64;
   int E = 1, n_tiles = 0, grid_k1 = 1;  // tile size and grid of the element kernel (autotuned)
-  size_t r_len = 0;                     // slots of R (n_elt_pad * Qp)
-  mj::DevBuf nodle_e, fac_e, R, ptr, pos;
+  bool vec = false;                     // work layout of the element kernel (autotuned)
+  size_t r_len = 0;                     // element-major slots (n_elt_pad * Qp)
+  size_t n_inc = 0;                     // incidences (n_elt * Q); R has n_inc + 1 entries
+  mj::DevBuf nodle_e, fac_e, slot_e, R, ptr;
   mj::DevBuf err;                       // device error flag (bounded-wait timeouts)
   mj::DevBuf fac_orig;                  // factors before mj_op_set_element_scale (kept on first use)
-  std::vector<int> h_ptr, h_pos;        // CSR incidences (host copy, for integrators)
+  std::vector<int> h_ptr;               // CSR of incidences per dof (host copy)
   double gradphi[mj::kMaxN * mj::kMaxN];
   mj::DevBuf xbuf, ybuf;                // staging for host-vector MltAdd
   cudaStream_t stream = nullptr;
   std::vector<double> tune_ms;          // autotuner timings of the candidates (diagnostic)
-  std::vector<int> tune_E;
+  std::vector<int> tune_E, tune_vec;
   size_t device_bytes() const {
-    return nodle_e.bytes + fac_e.bytes + fac_orig.bytes + R.bytes + ptr.bytes + pos.bytes + xbuf.bytes + ybuf.bytes;
+    return nodle_e.bytes + fac_e.bytes + fac_orig.bytes + slot_e.bytes + R.bytes + ptr.bytes + xbuf.bytes +
+           ybuf.bytes;
   }
 };
 
@@ -40,12 +43,13 @@ std::vector<int> k1_tile_candidates(int n);
 // launch: one launch of variant (n, E) on `grid` CTAs.
 int k1_set_gmat_f64(int n, const double* g);
 int k1_set_gmat_f32(int n, const double* g);
-int k1_prepare_f64(int n, int E, int* ctas_per_sm);
-int k1_prepare_f32(int n, int E, int* ctas_per_sm);
-void k1_launch_f64(int n, int E, int grid, const void* x, const int* nodle_e, const void* fac_e, void* R, int n_tiles,
-                   int* err, cudaStream_t s);
-void k1_launch_f32(int n, int E, int grid, const void* x, const int* nodle_e, const void* fac_e, void* R, int n_tiles,
-                   int* err, cudaStream_t s);
+// vec: the vector-line work layout (FP32 only; FP64 uses the compact one).
+int k1_prepare_f64(int n, int E, bool vec, int* ctas_per_sm);
+int k1_prepare_f32(int n, int E, bool vec, int* ctas_per_sm);
+void k1_launch_f64(int n, int E, bool vec, int grid, const void* x, const int* nodle_e, const void* fac_e, void* R,
+                   const int* slot_e, int n_tiles, int* err, cudaStream_t s);
+void k1_launch_f32(int n, int E, bool vec, int grid, const void* x, const int* nodle_e, const void* fac_e, void* R,
+                   const int* slot_e, int n_tiles, int* err, cudaStream_t s);
 
 // Many right-hand sides (FP32 only, mj_batch.cu).
 struct RhsVariant {

@@ -6,8 +6,12 @@
 // p = (k*n + j)*n + i:
 //   nodle_e[e*Qp + p]            int32 global dof
 //   fac_e  [(e*6 + c)*Qp + p]    the six factors (c = xx,xy,xz,yy,yz,zz)
-//   R      [e*Qp + p]            element-local A*u (single RHS)
-//   R      [(e*Qp + p)*S + s]    element-local A*u (S right-hand sides)
+//   slot_e [e*Qp + p]            where the element kernel writes that point's
+//                                result: its position q in the dof-ordered
+//                                incidence list (CSR), so R[ptr[d] .. ptr[d+1])
+//                                holds the contributions to dof d
+//   R      [q]                   element-local A*u (single RHS)
+//   R      [q*S + s]             element-local A*u (S right-hand sides)
 // The element count is padded to a multiple of 240 with empty elements
 // (Nodle 0, factors 0), so every tile size E that divides 240 covers the mesh
 // with whole tiles and E can be chosen at run time (the autotuner does).
@@ -93,18 +97,40 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
   return false;
 }
 
+// Loads the first RW values of a 16-byte aligned shared-memory line with
+// 16-byte loads.
+template <int RW>
+__device__ __forceinline__ void load_line(const float* p, float (&r)[RW]) {
+#pragma unroll
+  for (int v = 0; v < RW / 4; v++) {
+    const float4 q = reinterpret_cast<const float4*>(p)[v];
+    r[4 * v] = q.x; r[4 * v + 1] = q.y; r[4 * v + 2] = q.z; r[4 * v + 3] = q.w;
+  }
+}
+template <int RW>
+__device__ __forceinline__ void load_line(const double* p, double (&r)[RW]) {
+#pragma unroll
+  for (int v = 0; v < RW / 2; v++) {
+    const double2 q = reinterpret_cast<const double2*>(p)[v];
+    r[2 * v] = q.x; r[2 * v + 1] = q.y;
+  }
+}
+
 // Shared-memory plan of one element kernel: two stages of [factors | Nodle]
 // for a tile of E elements, work arrays, two mbarriers.  L = right-hand
 // sides handled per pass (1 for the single-RHS kernel).
-template <typename Real, int N, int E, int L>
+template <typename Real, int N, int E, int L, bool VEC = false>
 struct K1Plan {
   static constexpr int NN = N * N;
   static constexpr int Q = N * NN;
   static constexpr int Qp = elem_slots(N);
+  // single RHS: lines of n values padded to RW so a line is a few 16-byte loads
+  static constexpr int RW = ((N * (int)sizeof(Real) + 15) / 16) * 16 / (int)sizeof(Real);
   static constexpr size_t fac_bytes = sizeof(Real) * 6 * E * Qp;
   static constexpr size_t nod_bytes = sizeof(int) * E * Qp;
   static constexpr size_t stage_bytes = fac_bytes + nod_bytes;
-  static constexpr size_t work_bytes = ((sizeof(Real) * 3 * E * Q * L + 15) / 16) * 16;
+  static constexpr size_t work_bytes = VEC ? sizeof(Real) * 4 * E * NN * RW
+                                          : ((sizeof(Real) * 3 * E * Q * L + 15) / 16) * 16;
   static constexpr size_t total = 2 * stage_bytes + work_bytes + 2 * sizeof(uint64_t);
   static constexpr int threads = E * NN * L;
 };
@@ -125,20 +151,30 @@ struct K1Plan {
 // buffer, one mbarrier per stage) and the gather of the next tile's u is in
 // flight during the current tile's divergence.
 // ---------------------------------------------------------------------------
-template <typename Real, int N, int E>
+//
+// Two work-array layouts, both timed by the autotuner: VEC = false keeps one
+// compact copy of u, vx, vy ([el][k][j][i]; y lines read with stride n);
+// VEC = true keeps x-lines and y-lines as separate padded copies so every
+// line is read with 16-byte loads (more shared memory, fewer instructions).
+template <typename Real, int N, int E, bool VEC = false>
 __global__ void __launch_bounds__(E* N* N)
     k_local_stiffness(const Real* __restrict__ x, const int* __restrict__ nodle_e,
-                      const Real* __restrict__ fac_e, Real* __restrict__ R, int n_tiles,
-                      int* __restrict__ err) {
-  using P = K1Plan<Real, N, E, 1>;
+                      const Real* __restrict__ fac_e, Real* __restrict__ R, const int* __restrict__ slot_e,
+                      int n_tiles, int* __restrict__ err) {
+  using P = K1Plan<Real, N, E, 1, VEC>;
   constexpr int NN = P::NN, Qp = P::Qp;
   const Real* __restrict__ Gm = GConst<Real>::get(N);
   extern __shared__ __align__(128) unsigned char smem[];
   auto s_fac = [&](int st) { return reinterpret_cast<Real*>(smem + st * P::stage_bytes); };
   auto s_nod = [&](int st) { return reinterpret_cast<int*>(smem + st * P::stage_bytes + P::fac_bytes); };
-  Real* s_u = reinterpret_cast<Real*>(smem + 2 * P::stage_bytes);
-  Real* s_vx = s_u + E * N * NN;
-  Real* s_vy = s_vx + E * N * NN;
+  // VEC: x-lines (el, k, j) hold i = 0..n-1, y-lines (el, k, i) hold j, each
+  // padded to RW; compact: one array per quantity, index (el*n + k)*n*n + j*n + i
+  constexpr int RW = VEC ? P::RW : N;
+  constexpr int YS = VEC ? 1 : N;   // stride along a y-line
+  Real* s_ux = reinterpret_cast<Real*>(smem + 2 * P::stage_bytes);
+  Real* s_uy = VEC ? s_ux + E * NN * RW : s_ux;
+  Real* s_vx = s_uy + E * NN * RW;
+  Real* s_vy = s_vx + E * NN * RW;
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 2 * P::stage_bytes + P::work_bytes);
 
   const int t = threadIdx.x;
@@ -154,10 +190,9 @@ __global__ void __launch_bounds__(E* N* N)
     gri[a] = Gm[i * N + a];
     grj[a] = Gm[j * N + a];
   }
-  const int s_base = el * N * NN;             // element el in the work arrays
-  const int s_line_x = s_base + j * N;        // + k*NN + a   : row (j,k) along x
-  const int s_line_y = s_base + i;            // + k*NN + a*N : row (i,k) along y
-  const int pe = el * Qp + ij;                // slot (k = 0) of this thread in the tile block
+  const int lx = (el * N * N + j) * RW;                        // + k*N*RW: x-line (el,k,j); entry i
+  const int ly = VEC ? (el * N * N + i) * RW : el * N * NN + i;  // + k*N*RW: y-line (el,k,i); entry j*YS
+  const int pe = el * Qp + ij;            // slot (k = 0) of this thread in the tile block
 
   if (t == 0) {
     mbar_init(&bar[0], 1);
@@ -192,25 +227,39 @@ __global__ void __launch_bounds__(E* N* N)
   for (int it = 0; tile < n_tiles; tile += g, ++it) {
     const int s = it & 1;
 #pragma unroll
-    for (int k = 0; k < N; k++) s_u[s_base + k * NN + ij] = u[k];
+    for (int k = 0; k < N; k++) {
+      s_ux[lx + k * N * RW + i] = u[k];
+      if (VEC) s_uy[ly + k * N * RW + j] = u[k];
+    }
     __syncthreads();
 
     const Real* f = s_fac(s) + el * 6 * Qp + ij;
     Real vz[N];
 #pragma unroll
     for (int k = 0; k < N; k++) {
+      Real rx[RW], ry[RW];
+      if constexpr (VEC) {
+        load_line<RW>(s_ux + lx + k * N * RW, rx);
+        load_line<RW>(s_uy + ly + k * N * RW, ry);
+      } else {
+#pragma unroll
+        for (int a = 0; a < N; a++) {
+          rx[a] = s_ux[lx + k * N * RW + a];
+          ry[a] = s_uy[ly + k * N * RW + a * YS];
+        }
+      }
       Real gx = 0, gy = 0, gz = 0;
 #pragma unroll
       for (int a = 0; a < N; a++) {
         gz += Gm[a * N + k] * u[a];
-        gx += gci[a] * s_u[s_line_x + k * NN + a];
-        gy += gcj[a] * s_u[s_line_y + k * NN + a * N];
+        gx += gci[a] * rx[a];
+        gy += gcj[a] * ry[a];
       }
       const Real* fk = f + k * NN;
       const Real bxx = fk[0], bxy = fk[Qp], bxz = fk[2 * Qp];
       const Real byy = fk[3 * Qp], byz = fk[4 * Qp], bzz = fk[5 * Qp];
-      s_vx[s_base + k * NN + ij] = bxx * gx + bxy * gy + bxz * gz;
-      s_vy[s_base + k * NN + ij] = bxy * gx + byy * gy + byz * gz;
+      s_vx[lx + k * N * RW + i] = bxx * gx + bxy * gy + bxz * gz;
+      s_vy[ly + k * N * RW + j * YS] = bxy * gx + byy * gy + byz * gz;
       vz[k] = bxz * gx + byz * gy + bzz * gz;
     }
     __syncthreads();
@@ -230,17 +279,28 @@ __global__ void __launch_bounds__(E* N* N)
       for (int k = 0; k < N; k++) u[k] = __ldg(x + nd[k * NN]);
     }
 
-    Real* Rt = R + ((size_t)tile * E + el) * Qp + ij;
+    const int* st = slot_e + ((size_t)tile * E + el) * Qp + ij;
 #pragma unroll
     for (int k = 0; k < N; k++) {
+      Real rx[RW], ry[RW];
+      if constexpr (VEC) {
+        load_line<RW>(s_vx + lx + k * N * RW, rx);
+        load_line<RW>(s_vy + ly + k * N * RW, ry);
+      } else {
+#pragma unroll
+        for (int a = 0; a < N; a++) {
+          rx[a] = s_vx[lx + k * N * RW + a];
+          ry[a] = s_vy[ly + k * N * RW + a * YS];
+        }
+      }
       Real y = 0;
 #pragma unroll
       for (int a = 0; a < N; a++) {
-        y += gri[a] * s_vx[s_line_x + k * NN + a];
-        y += grj[a] * s_vy[s_line_y + k * NN + a * N];
+        y += gri[a] * rx[a];
+        y += grj[a] * ry[a];
         y += Gm[k * N + a] * vz[a];
       }
-      Rt[k * NN] = y;
+      R[__ldg(st + k * NN)] = y;
     }
     __syncthreads();  // stage s and the work arrays are free again
     if (t == 0) fence_proxy_async();
@@ -263,8 +323,8 @@ __global__ void __launch_bounds__(E* N* N)
 template <int N, int E, int L, bool ENERGY = false>
 __global__ void __launch_bounds__(E* N* N* L)
     k_local_stiffness_rhs(const float* __restrict__ x, const int* __restrict__ nodle_e,
-                          const float* __restrict__ fac_e, float* __restrict__ R, int n_tiles, int S,
-                          int* __restrict__ err, const float* __restrict__ lam = nullptr,
+                          const float* __restrict__ fac_e, float* __restrict__ R, const int* __restrict__ slot_e,
+                          int n_tiles, int S, int* __restrict__ err, const float* __restrict__ lam = nullptr,
                           double* __restrict__ gacc = nullptr, const double* __restrict__ coef = nullptr) {
   using P = K1Plan<float, N, E, L>;
   constexpr int NN = P::NN, Qp = P::Qp;
@@ -357,7 +417,7 @@ __global__ void __launch_bounds__(E* N* N* L)
         vz[k] = bxz * gx + byz * gy + bzz * gz;
       }
       __syncthreads();
-      float* Rt = R + (((size_t)tile * E + el) * Qp + ij) * S + col;
+      const int* st = slot_e + ((size_t)tile * E + el) * Qp + ij;
 #pragma unroll
       for (int k = 0; k < N; k++) {
         float y = 0;
@@ -368,7 +428,7 @@ __global__ void __launch_bounds__(E* N* N* L)
           y += Gm[k * N + a] * vz[a];
         }
         if (ENERGY) energy += y * __ldg(lam + (size_t)dofs[k] * S + col);
-        else Rt[(size_t)k * NN * S] = y;
+        else R[(size_t)__ldg(st + k * NN) * S + col] = y;
       }
       __syncthreads();
     }

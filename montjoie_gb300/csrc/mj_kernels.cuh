@@ -1,7 +1,7 @@
-// Per-dof kernels of the operator and the leap-frog (sm_103a): the gather of
-// the element-local results R written by the element kernels (mj_k1.cuh)
-// through a CSR incidence list (owner computes: deterministic, no atomics),
-// fused with the leap-frog update, plus the norm and receiver diagnostics.
+// Per-dof kernels of the operator and the leap-frog (sm_103a): the sum of
+// the element-local results R, which the element kernels (mj_k1.cuh) wrote
+// in dof order (owner computes: deterministic, no atomics), fused with the
+// leap-frog update; the source term; the norm and receiver diagnostics.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -12,49 +12,40 @@ namespace mj {
 
 
 // ---------------------------------------------------------------------------
-// K2a: y <- beta*y + alpha * sum over the incidences of dof i of R  (MltAdd).
+// K2a: y <- beta*y + alpha * sum R[ptr[d] .. ptr[d+1])  (MltAdd).  The element
+// kernel wrote every contribution to dof d into that contiguous range, so
+// each warp streams one contiguous block of R.
 // ---------------------------------------------------------------------------
 template <typename Real>
-__global__ void k_gather_mltadd(const Real* __restrict__ R, const int* __restrict__ ptr,
-                                const int* __restrict__ pos, Real alpha, Real beta,
+__global__ void k_gather_mltadd(const Real* __restrict__ R, const int* __restrict__ ptr, Real alpha, Real beta,
                                 Real* __restrict__ y, int n_dof) {
   for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < n_dof; d += gridDim.x * blockDim.x) {
     Real s = 0;
     const int q1 = __ldg(ptr + d + 1);
-    for (int q = __ldg(ptr + d); q < q1; q++) s += __ldg(R + __ldg(pos + q));
+    for (int q = __ldg(ptr + d); q < q1; q++) s += __ldg(R + q);
     y[d] = (beta == Real(0)) ? alpha * s : beta * y[d] + alpha * s;
   }
 }
 
 // ---------------------------------------------------------------------------
-// K2b: gather + source + leap-frog update, one dof per thread.
-//   Ah = -(A U1)_i + p F_i        (ApplyOperatorKh + AddScalarTimeSource)
+// K2b: gather + leap-frog update, one dof per thread (sources: K2c).
+//   Ah = -(A U1)_i                (ApplyOperatorKh)
 //   FP64 (EXACT): a = dt2*Ah - D u0;  a += 2 D u1;  u_new = invD a
 //                 (ModifiedEquation.cxx:311-333, operation order kept)
 //   FP32:         u_new = 2 u1 - u0 + m Ah,  m = dt^2 / D
-// Source entries are CSR entries with pos < 0 (slot -pos-1 of src_val), placed
-// after the element entries of the dof.  u_new overwrites u0 in place.
-// The pulse of the step is pulse[ctr[q]]; block 0 writes ctr[1-q] = ctr[q]+1
-// for the next step (two counters, so a captured sequence of steps needs no
-// host update of the pulse).
+// u_new overwrites u0 in place.  Block 0 advances the step counter:
+// ctr[1-qc] = ctr[qc] + 1 (two counters, so a captured sequence of steps
+// needs no host update of the pulse index).
 // ---------------------------------------------------------------------------
 template <typename Real, bool EXACT>
-__global__ void k_gather_leapfrog(const Real* __restrict__ R, const int* __restrict__ ptr,
-                                  const int* __restrict__ pos, const Real* __restrict__ src_val,
-                                  const double* __restrict__ pulses, int n_pulse, int* __restrict__ ctr, int qc,
-                                  Real* __restrict__ u0, const Real* __restrict__ u1,
-                                  const Real* __restrict__ mass, const Real* __restrict__ minv,
-                                  Real dt2, int n_dof) {
-  const int step = ctr[qc];
-  const Real pulse = (step < n_pulse) ? Real(pulses[step]) : Real(0);
-  if (blockIdx.x == 0 && threadIdx.x == 0) ctr[1 - qc] = step + 1;
+__global__ void k_gather_leapfrog(const Real* __restrict__ R, const int* __restrict__ ptr, int* __restrict__ ctr,
+                                  int qc, Real* __restrict__ u0, const Real* __restrict__ u1,
+                                  const Real* __restrict__ mass, const Real* __restrict__ minv, Real dt2, int n_dof) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctr[1 - qc] = ctr[qc] + 1;
   for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < n_dof; d += gridDim.x * blockDim.x) {
     Real s = 0;
     const int q1 = __ldg(ptr + d + 1);
-    for (int q = __ldg(ptr + d); q < q1; q++) {
-      const int p = __ldg(pos + q);
-      s += (p >= 0) ? __ldg(R + p) : -pulse * __ldg(src_val + (-p - 1));
-    }
+    for (int q = __ldg(ptr + d); q < q1; q++) s += __ldg(R + q);
     const Real ah = -s;
     if (EXACT) {
       const Real Dd = __ldg(mass + d);
@@ -67,19 +58,34 @@ __global__ void k_gather_leapfrog(const Real* __restrict__ R, const int* __restr
   }
 }
 
+// ---------------------------------------------------------------------------
+// K2c: source term of the step just taken, added to the new state at the
+// source dofs: u[d] += coef_d * p * F_d with coef = dt^2/D (the source enters
+// Ah as +p F, AddScalarTimeSource, VarInstationary.cxx:2392-2407).  p is
+// pulse[ctr[qc]] (the counter K2b read), no pulse past n_pulse.
+// ---------------------------------------------------------------------------
+template <typename Real>
+__global__ void k_source(const int* __restrict__ idx, const Real* __restrict__ val, int n_src,
+                         const double* __restrict__ pulses, int n_pulse, const int* __restrict__ ctr, int qc,
+                         const double* __restrict__ inv_mass, double dt2, Real* __restrict__ u) {
+  const int step = ctr[qc];
+  if (step >= n_pulse) return;
+  const double p = pulses[step];
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n_src; t += gridDim.x * blockDim.x) {
+    const int d = idx[t];
+    u[d] = Real(double(u[d]) + dt2 * inv_mass[d] * p * double(val[t]));
+  }
+}
+
 // First step U1 = U0 + dt*(du0 + dt/2 * invD*(-A U0))   (SetInitialConditionS)
 template <typename Real>
 __global__ void k_gather_init(const Real* __restrict__ R, const int* __restrict__ ptr,
-                              const int* __restrict__ pos, const Real* __restrict__ u0,
-                              const Real* __restrict__ du0, const double* __restrict__ inv_mass,
-                              double dt, Real* __restrict__ u1, int n_dof) {
+                              const Real* __restrict__ u0, const Real* __restrict__ du0,
+                              const double* __restrict__ inv_mass, double dt, Real* __restrict__ u1, int n_dof) {
   for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < n_dof; d += gridDim.x * blockDim.x) {
     Real s = 0;
     const int q1 = __ldg(ptr + d + 1);
-    for (int q = __ldg(ptr + d); q < q1; q++) {
-      const int p = __ldg(pos + q);
-      if (p >= 0) s += __ldg(R + p);
-    }
+    for (int q = __ldg(ptr + d); q < q1; q++) s += __ldg(R + q);
     double v = double(-s) * inv_mass[d];
     v *= 0.5 * dt;
     v += du0 ? double(du0[d]) : 0.0;

@@ -59,8 +59,7 @@ struct mj_lf {
   mj_op* op = nullptr;
   double dt = 0;
   int n_dof = 0;
-  DevBuf ptr, pos;       // CSR with source entries appended
-  DevBuf src_val;        // op precision
+  DevBuf src_idx, src_val;  // sparse source (value in op precision)
   DevBuf mass, minv;     // op precision (FP64: D and 1/D; FP32: unused / dt^2/D)
   DevBuf inv_mass64;     // FP64 1/D for the initial step
   DevBuf norm_w;         // FP64 weights, or empty
@@ -98,11 +97,11 @@ namespace {
 // One launch of the element kernel with the operator's tuned variant.
 void launch_k1(mj_op* op, const void* x, cudaStream_t s) {
   if (op->precision == MJ_FP64)
-    k1_launch_f64(op->n, op->E, op->grid_k1, x, op->nodle_e.as<int>(), op->fac_e.ptr, op->R.ptr, op->n_tiles,
-                  op->err.as<int>(), s);
+    k1_launch_f64(op->n, op->E, op->vec, op->grid_k1, x, op->nodle_e.as<int>(), op->fac_e.ptr, op->R.ptr,
+                  op->slot_e.as<int>(), op->n_tiles, op->err.as<int>(), s);
   else
-    k1_launch_f32(op->n, op->E, op->grid_k1, x, op->nodle_e.as<int>(), op->fac_e.ptr, op->R.ptr, op->n_tiles,
-                  op->err.as<int>(), s);
+    k1_launch_f32(op->n, op->E, op->vec, op->grid_k1, x, op->nodle_e.as<int>(), op->fac_e.ptr, op->R.ptr,
+                  op->slot_e.as<int>(), op->n_tiles, op->err.as<int>(), s);
   count_launch();
 }
 
@@ -128,31 +127,37 @@ int autotune_k1(mj_op* op) {
   MJ_CUDA(cudaEventCreate(&e1));
   double best = 1e300;
   int bestE = -1, bestGrid = 1;
+  bool bestVec = false;
   const bool time_it = (long long)op->n_elt * op->Q >= 2000000;
-  for (int E : cands) {
-    int ctas = 0;
-    const int rc = op->precision == MJ_FP64 ? k1_prepare_f64(op->n, E, &ctas) : k1_prepare_f32(op->n, E, &ctas);
-    if (rc != MJ_OK) continue;
-    const int tiles = op->n_elt_pad / E;
-    const int grid = std::max(1, std::min(tiles, ctas * sms));
-    double ms = 0.0;
-    if (time_it) {
-      op->E = E; op->grid_k1 = grid; op->n_tiles = tiles;
-      launch_k1(op, x.ptr, op->stream);
-      MJ_CUDA(cudaEventRecord(e0, op->stream));
-      for (int rep = 0; rep < 3; rep++) launch_k1(op, x.ptr, op->stream);
-      MJ_CUDA(cudaEventRecord(e1, op->stream));
-      MJ_CUDA(cudaEventSynchronize(e1));
-      float f = 0.f;
-      MJ_CUDA(cudaEventElapsedTime(&f, e0, e1));
-      ms = f / 3.0;
-    } else {
-      ms = -double(ctas) * E * op->n * op->n;  // most resident threads first
+  const int n_layouts = op->precision == MJ_FP32 ? 2 : 1;
+  for (int lay = 0; lay < n_layouts; lay++)
+    for (int E : cands) {
+      const bool vec = lay == 1;
+      int ctas = 0;
+      const int rc = op->precision == MJ_FP64 ? k1_prepare_f64(op->n, E, vec, &ctas)
+                                              : k1_prepare_f32(op->n, E, vec, &ctas);
+      if (rc != MJ_OK) continue;
+      const int tiles = op->n_elt_pad / E;
+      const int grid = std::max(1, std::min(tiles, ctas * sms));
+      double ms = 0.0;
+      if (time_it) {
+        op->E = E; op->vec = vec; op->grid_k1 = grid; op->n_tiles = tiles;
+        launch_k1(op, x.ptr, op->stream);
+        MJ_CUDA(cudaEventRecord(e0, op->stream));
+        for (int rep = 0; rep < 3; rep++) launch_k1(op, x.ptr, op->stream);
+        MJ_CUDA(cudaEventRecord(e1, op->stream));
+        MJ_CUDA(cudaEventSynchronize(e1));
+        float f = 0.f;
+        MJ_CUDA(cudaEventElapsedTime(&f, e0, e1));
+        ms = f / 3.0;
+      } else {
+        ms = -double(ctas) * E * op->n * op->n + (vec ? 0.5 : 0.0);  // most resident threads first
+      }
+      op->tune_E.push_back(E);
+      op->tune_vec.push_back(vec);
+      op->tune_ms.push_back(ms);
+      if (ms < best) { best = ms; bestE = E; bestGrid = grid; bestVec = vec; }
     }
-    op->tune_E.push_back(E);
-    op->tune_ms.push_back(ms);
-    if (ms < best) { best = ms; bestE = E; bestGrid = grid; }
-  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (bestE < 0) {
@@ -160,7 +165,15 @@ int autotune_k1(mj_op* op) {
     return MJ_ERR_CUDA;
   }
   op->E = bestE;
+  op->vec = bestVec;
   op->grid_k1 = bestGrid;
+  // the chosen variant's shared-memory attribute must be the one set last
+  {
+    int ctas = 0;
+    const int rc = op->precision == MJ_FP64 ? k1_prepare_f64(op->n, bestE, bestVec, &ctas)
+                                            : k1_prepare_f32(op->n, bestE, bestVec, &ctas);
+    if (rc) return rc;
+  }
   op->n_tiles = op->n_elt_pad / bestE;
   MJ_CUDA(cudaMemset(op->err.ptr, 0, sizeof(int)));
   MJ_CUDA(cudaGetLastError());
@@ -179,9 +192,8 @@ namespace {
 template <typename Real>
 int mltadd_impl(mj_op* op, double alpha, const void* x, double beta, void* y, cudaStream_t s) {
   launch_k1<Real>(op, x, s);
-  k_gather_mltadd<Real><<<stream_grid(op->n_dof), 256, 0, s>>>(
-      op->R.as<Real>(), op->ptr.as<int>(), op->pos.as<int>(), Real(alpha), Real(beta),
-      static_cast<Real*>(y), op->n_dof);
+  k_gather_mltadd<Real><<<stream_grid(op->n_dof), 256, 0, s>>>(op->R.as<Real>(), op->ptr.as<int>(), Real(alpha),
+                                                                Real(beta), static_cast<Real*>(y), op->n_dof);
   count_launch();
   MJ_CUDA(cudaGetLastError());
   return MJ_OK;
@@ -247,7 +259,7 @@ int mj_op_create(const mj_mesh_desc* mesh, const mj_geom_desc* geom, int precisi
   op->Qp = elem_slots(n);
   op->n_elt_pad = (mesh->n_elt + kElemPad - 1) / kElemPad * kElemPad;
   op->r_len = (size_t)op->n_elt_pad * op->Qp;
-  MJ_CHECK_ARG(op->r_len < (size_t)INT32_MAX, "mj_op_create: mesh too large for int32 incidences");
+  MJ_CHECK_ARG(op->r_len < (size_t)INT32_MAX - 1, "mj_op_create: mesh too large for int32 incidences");
 
   // derivative matrix
   if (geom->gradphi) {
@@ -274,7 +286,10 @@ int mj_op_create(const mj_mesh_desc* mesh, const mj_geom_desc* geom, int precisi
     MJ_CHECK_ARG(count[d + 1] > 0, "mj_op_create: a dof belongs to no element");
   op->h_ptr.assign(op->n_dof + 1, 0);
   for (int d = 0; d < op->n_dof; d++) op->h_ptr[d + 1] = op->h_ptr[d] + count[d + 1];
-  op->h_pos.assign((size_t)total_pts, 0);
+  op->n_inc = (size_t)total_pts;
+  // slot of every element point: its position in the dof-ordered incidence
+  // list; padding points write to the spare entry R[n_inc]
+  std::vector<int> slot_e(op->r_len, (int)op->n_inc);
   std::vector<int> fill(op->h_ptr.begin(), op->h_ptr.end() - 1);
 
   const size_t esz = elem_size(precision);
@@ -292,7 +307,7 @@ int mj_op_create(const mj_mesh_desc* mesh, const mj_geom_desc* geom, int precisi
           const size_t src = (size_t)e * Q + ql;
           const int d = mesh->nodle[src];
           nodle_e[rp] = d;
-          op->h_pos[fill[d]++] = (int)rp;
+          slot_e[rp] = fill[d]++;
           for (int c = 0; c < 6; c++) {
             const double v = geom->factors[src * 6 + c];
             if (!std::isfinite(v)) {
@@ -306,15 +321,15 @@ int mj_op_create(const mj_mesh_desc* mesh, const mj_geom_desc* geom, int precisi
         }
 
   MJ_CUDA(op->nodle_e.alloc(sizeof(int) * op->r_len));
+  MJ_CUDA(op->slot_e.alloc(sizeof(int) * op->r_len));
   MJ_CUDA(op->fac_e.alloc(fac_bytes.size()));
-  MJ_CUDA(op->R.alloc(esz * op->r_len));
+  MJ_CUDA(op->R.alloc(esz * (op->n_inc + 1)));
   MJ_CUDA(op->ptr.alloc(sizeof(int) * (op->n_dof + 1)));
-  MJ_CUDA(op->pos.alloc(sizeof(int) * op->h_pos.size()));
   MJ_CUDA(cudaMemcpy(op->nodle_e.ptr, nodle_e.data(), sizeof(int) * op->r_len, cudaMemcpyHostToDevice));
+  MJ_CUDA(cudaMemcpy(op->slot_e.ptr, slot_e.data(), sizeof(int) * op->r_len, cudaMemcpyHostToDevice));
   MJ_CUDA(cudaMemcpy(op->fac_e.ptr, fac_bytes.data(), fac_bytes.size(), cudaMemcpyHostToDevice));
   MJ_CUDA(cudaMemcpy(op->ptr.ptr, op->h_ptr.data(), sizeof(int) * (op->n_dof + 1), cudaMemcpyHostToDevice));
-  MJ_CUDA(cudaMemcpy(op->pos.ptr, op->h_pos.data(), sizeof(int) * op->h_pos.size(), cudaMemcpyHostToDevice));
-  MJ_CUDA(cudaMemset(op->R.ptr, 0, esz * op->r_len));
+  MJ_CUDA(cudaMemset(op->R.ptr, 0, esz * (op->n_inc + 1)));
   MJ_CUDA(op->err.alloc(sizeof(int)));
   MJ_CUDA(cudaMemset(op->err.ptr, 0, sizeof(int)));
   {
@@ -343,6 +358,18 @@ int mj_op_info(const mj_op* op, int* order, int* n_elt, int* n_dof, int* precisi
   if (n_dof) *n_dof = op->n_dof;
   if (precision) *precision = op->precision;
   if (device_bytes) *device_bytes = op->device_bytes();
+  return MJ_OK;
+}
+
+int mj_op_tuning(const mj_op* op, int* tile_elems, int* vector_lines, int* grid, int* n_candidates,
+                 double* candidate_ms) {
+  MJ_CHECK_ARG(op, "mj_op_tuning: null operator");
+  if (tile_elems) *tile_elems = op->E;
+  if (vector_lines) *vector_lines = op->vec ? 1 : 0;
+  if (grid) *grid = op->grid_k1;
+  if (n_candidates) *n_candidates = (int)op->tune_ms.size();
+  if (candidate_ms)
+    for (size_t c = 0; c < op->tune_ms.size(); c++) candidate_ms[c] = op->tune_ms[c];
   return MJ_OK;
 }
 
@@ -397,25 +424,17 @@ int mj_lf_create(mj_op* op, const mj_lf_desc* desc, mj_lf** out) {
     MJ_CHECK_ARG(std::isfinite(desc->mass[i]) && desc->mass[i] > 0, "mj_lf_create: mass must be positive");
     invD[i] = desc->inv_mass ? desc->inv_mass[i] : 1.0 / desc->mass[i];
   }
-  // CSR with the source entries appended after each dof's element entries
-  std::vector<int> src_of(n, -1);
+  // sparse source (one entry per dof; applied by k_source after each update)
+  std::vector<char> seen(n, 0);
   for (int s = 0; s < desc->n_src; s++) {
     const int d = desc->src_idx[s];
     MJ_CHECK_ARG(d >= 0 && d < n, "mj_lf_create: source index out of range");
-    MJ_CHECK_ARG(src_of[d] < 0, "mj_lf_create: duplicate source index");
-    src_of[d] = s;
+    MJ_CHECK_ARG(!seen[d], "mj_lf_create: duplicate source index");
+    seen[d] = 1;
   }
-  std::vector<int> ptr(n + 1, 0), pos;
-  pos.reserve(op->h_pos.size() + desc->n_src);
-  for (int d = 0; d < n; d++) {
-    for (int q = op->h_ptr[d]; q < op->h_ptr[d + 1]; q++) pos.push_back(op->h_pos[q]);
-    if (src_of[d] >= 0) pos.push_back(-src_of[d] - 1);
-    ptr[d + 1] = (int)pos.size();
-  }
-  MJ_CUDA(lf->ptr.alloc(sizeof(int) * (n + 1)));
-  MJ_CUDA(lf->pos.alloc(sizeof(int) * pos.size()));
-  MJ_CUDA(cudaMemcpy(lf->ptr.ptr, ptr.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
-  MJ_CUDA(cudaMemcpy(lf->pos.ptr, pos.data(), sizeof(int) * pos.size(), cudaMemcpyHostToDevice));
+  MJ_CUDA(lf->src_idx.alloc(sizeof(int) * std::max(1, desc->n_src)));
+  if (desc->n_src)
+    MJ_CUDA(cudaMemcpy(lf->src_idx.ptr, desc->src_idx, sizeof(int) * desc->n_src, cudaMemcpyHostToDevice));
   lf->n_src = desc->n_src;
   MJ_CUDA(lf->src_val.alloc(esz * std::max(1, desc->n_src)));
   MJ_CUDA(lf->inv_mass64.alloc(sizeof(double) * n));
@@ -497,7 +516,7 @@ int lf_init_impl(mj_lf* lf, const double* u0, const double* du0) {
     du0_d = lf->du0.as<Real>();
   }
   launch_k1<Real>(op, lf->ua.ptr, s);
-  k_gather_init<Real><<<stream_grid(n), 256, 0, s>>>(op->R.as<Real>(), lf->ptr.as<int>(), lf->pos.as<int>(),
+  k_gather_init<Real><<<stream_grid(n), 256, 0, s>>>(op->R.as<Real>(), op->ptr.as<int>(),
                                                       lf->ua.as<Real>(), du0_d, lf->inv_mass64.as<double>(),
                                                       lf->dt, lf->ub.as<Real>(), n);
   count_launch();
@@ -548,14 +567,19 @@ void lf_step_launch(mj_lf* lf, void* cur, const void* next, int qc, cudaStream_t
   const double dt2 = lf->dt * lf->dt;
   if (op->precision == MJ_FP64) {
     k_gather_leapfrog<Real, true><<<stream_grid(n), 256, 0, s>>>(
-        op->R.as<Real>(), lf->ptr.as<int>(), lf->pos.as<int>(), lf->src_val.as<Real>(), lf->pulse_d.as<double>(),
-        lf->n_pulse, lf->ctr.as<int>(), qc, static_cast<Real*>(cur), static_cast<const Real*>(next),
-        lf->mass.as<Real>(), lf->minv.as<Real>(), Real(dt2), n);
+        op->R.as<Real>(), op->ptr.as<int>(), lf->ctr.as<int>(), qc, static_cast<Real*>(cur),
+        static_cast<const Real*>(next), lf->mass.as<Real>(), lf->minv.as<Real>(), Real(dt2), n);
   } else {
     k_gather_leapfrog<Real, false><<<stream_grid(n), 256, 0, s>>>(
-        op->R.as<Real>(), lf->ptr.as<int>(), lf->pos.as<int>(), lf->src_val.as<Real>(), lf->pulse_d.as<double>(),
-        lf->n_pulse, lf->ctr.as<int>(), qc, static_cast<Real*>(cur), static_cast<const Real*>(next), nullptr,
-        lf->minv.as<Real>(), Real(dt2), n);
+        op->R.as<Real>(), op->ptr.as<int>(), lf->ctr.as<int>(), qc, static_cast<Real*>(cur),
+        static_cast<const Real*>(next), nullptr, lf->minv.as<Real>(), Real(dt2), n);
+  }
+  if (lf->n_src) {
+    k_source<Real><<<(lf->n_src + 255) / 256, 256, 0, s>>>(lf->src_idx.as<int>(), lf->src_val.as<Real>(), lf->n_src,
+                                                           lf->pulse_d.as<double>(), lf->n_pulse, lf->ctr.as<int>(),
+                                                           qc, lf->inv_mass64.as<double>(), dt2,
+                                                           static_cast<Real*>(cur));
+    count_launch();
   }
   count_launch();
   if (prof) {
@@ -634,7 +658,7 @@ int lf_advance_impl(mj_lf* lf, int nsteps, double* norms, double* traces, int st
     }
     while (nsteps - s0 >= kGraphSteps) {
       MJ_CUDA(cudaGraphLaunch(lf->graph, lf->stream));
-      count_launch(2 * kGraphSteps);
+      count_launch((uint64_t)kGraphSteps * (2 + (lf->n_src > 0)));
       s0 += kGraphSteps;
       lf->step += kGraphSteps;
     }

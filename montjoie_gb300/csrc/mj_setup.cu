@@ -207,11 +207,16 @@ int mj_number_hex_mesh(int order, int n_elt, int n_vert, const int32_t* hexes, i
   for (long long t = 0; t < 8LL * n_elt; t++)
     MJ_CHECK_ARG(hexes[t] >= 0 && hexes[t] < n_vert, "mj_number_hex_mesh: vertex index out of range");
   std::vector<int> vdof(n_vert, -1);
-  std::unordered_map<EdgeKey, int, EdgeHash> edges;
-  std::unordered_map<FaceKey, int, FaceHash> faces;
+  // edge / face -> ids of its interior nodes in canonical order (-1: not yet numbered)
+  std::unordered_map<EdgeKey, std::vector<int>, EdgeHash> edges;
+  std::unordered_map<FaceKey, std::vector<int>, FaceHash> faces;
   edges.reserve((size_t)n_elt * 3 + 16);
   faces.reserve((size_t)n_elt * 3 + 16);
   long long next = 0;
+  auto fresh = [&](int& id) {
+    if (id < 0) id = (int)next++;
+    return id;
+  };
   for (int e = 0; e < n_elt; e++) {
     const int32_t* hv = hexes + 8LL * e;
     auto gvert = [&](int ci, int cj, int ck) {  // global vertex at corner (ci,cj,ck) in {0,1}^3
@@ -220,95 +225,68 @@ int mj_number_hex_mesh(int order, int n_elt, int n_vert, const int32_t* hexes, i
       return -1;
     };
     int32_t* out = nodle_out + (size_t)e * Q;
-    int interior_base = -1;
-    // Traverse the element's nodes in local-numbering order so dofs are
-    // numbered in first-touch order (vertices, edges, faces, interior).
-    std::vector<int> order_of(Q);
-    for (int i = 0; i < n; i++)
+    // Nodes are visited in tensor order (i fastest, then j, then k) and every
+    // dof gets the next number when first met, so consecutive nodes along x
+    // of an element mostly get consecutive numbers (coalesced gathers).
+    for (int k = 0; k < n; k++)
       for (int j = 0; j < n; j++)
-        for (int k = 0; k < n; k++) order_of[num[(i * n + j) * n + k]] = (i * n + j) * n + k;
-    for (int ql = 0; ql < Q; ql++) {
-      const int lin = order_of[ql];
-      const int i = lin / (n * n), j = (lin / n) % n, k = lin % n;
-      const int c[3] = {i, j, k};
-      int nb = 0;
-      for (int d = 0; d < 3; d++) nb += (c[d] == 0 || c[d] == r);
-      int dof = -1;
-      if (nb == 3) {
-        const int g = gvert(i / r, j / r, k / r);
-        if (vdof[g] < 0) vdof[g] = (int)next++;
-        dof = vdof[g];
-      } else if (nb == 2) {
-        int ax = 0;
-        for (int d = 0; d < 3; d++)
-          if (c[d] != 0 && c[d] != r) ax = d;
-        int lo[3] = {c[0] / r, c[1] / r, c[2] / r}, hi[3] = {c[0] / r, c[1] / r, c[2] / r};
-        lo[ax] = 0;
-        hi[ax] = 1;
-        const int ga = gvert(lo[0], lo[1], lo[2]), gb = gvert(hi[0], hi[1], hi[2]);
-        const int l = c[ax];
-        EdgeKey key{std::min(ga, gb), std::max(ga, gb)};
-        const int lc = (ga < gb) ? l : r - l;
-        auto it = edges.find(key);
-        int base;
-        if (it == edges.end()) {
-          base = (int)next;
-          next += m;
-          edges.emplace(key, base);
-        } else {
-          base = it->second;
+        for (int i = 0; i < n; i++) {
+          const int ql = num[(i * n + j) * n + k];
+          const int c[3] = {i, j, k};
+          int nb = 0;
+          for (int d = 0; d < 3; d++) nb += (c[d] == 0 || c[d] == r);
+          int dof = -1;
+          if (nb == 3) {
+            dof = fresh(vdof[gvert(i / r, j / r, k / r)]);
+          } else if (nb == 2) {
+            int ax = 0;
+            for (int d = 0; d < 3; d++)
+              if (c[d] != 0 && c[d] != r) ax = d;
+            int lo[3] = {c[0] / r, c[1] / r, c[2] / r}, hi[3] = {c[0] / r, c[1] / r, c[2] / r};
+            lo[ax] = 0;
+            hi[ax] = 1;
+            const int ga = gvert(lo[0], lo[1], lo[2]), gb = gvert(hi[0], hi[1], hi[2]);
+            const int l = c[ax];
+            std::vector<int>& ids = edges.try_emplace(EdgeKey{std::min(ga, gb), std::max(ga, gb)}, m, -1).first->second;
+            dof = fresh(ids[((ga < gb) ? l : r - l) - 1]);
+          } else if (nb == 1) {
+            int fx = 0;
+            for (int d = 0; d < 3; d++)
+              if (c[d] == 0 || c[d] == r) fx = d;
+            const int pa = (fx == 0) ? 1 : 0, qa = (fx == 2) ? 1 : 2;  // the two varying axes
+            const int side = c[fx] / r;
+            auto corner = [&](int sp, int sq) {
+              int cc[3];
+              cc[fx] = side;
+              cc[pa] = sp;
+              cc[qa] = sq;
+              return gvert(cc[0], cc[1], cc[2]);
+            };
+            const int g[2][2] = {{corner(0, 0), corner(0, 1)}, {corner(1, 0), corner(1, 1)}};
+            // canonical frame: origin = smallest vertex; first axis towards its
+            // smaller neighbour.
+            int os = 0, oq = 0;
+            for (int a = 0; a < 2; a++)
+              for (int b = 0; b < 2; b++)
+                if (g[a][b] < g[os][oq]) { os = a; oq = b; }
+            const int nP = g[1 - os][oq], nQ = g[os][1 - oq];
+            const bool swap = nQ < nP;  // first canonical axis is q
+            int p = c[pa], q = c[qa];
+            if (os) p = r - p;
+            if (oq) q = r - q;
+            const int u = swap ? q : p, v = swap ? p : q;
+            std::vector<int>& ids =
+                faces.try_emplace(FaceKey{g[os][oq], swap ? nQ : nP, swap ? nP : nQ}, m * m, -1).first->second;
+            dof = fresh(ids[(u - 1) * m + (v - 1)]);
+          } else {
+            dof = (int)next++;
+          }
+          if (next > INT32_MAX) {
+            set_error("mj_number_hex_mesh: too many dofs for int32");
+            return MJ_ERR_ARG;
+          }
+          out[ql] = dof;
         }
-        dof = base + (lc - 1);
-      } else if (nb == 1) {
-        int fx = 0;
-        for (int d = 0; d < 3; d++)
-          if (c[d] == 0 || c[d] == r) fx = d;
-        const int pa = (fx == 0) ? 1 : 0, qa = (fx == 2) ? 1 : 2;  // the two varying axes
-        const int side = c[fx] / r;
-        auto corner = [&](int sp, int sq) {
-          int cc[3];
-          cc[fx] = side;
-          cc[pa] = sp;
-          cc[qa] = sq;
-          return gvert(cc[0], cc[1], cc[2]);
-        };
-        const int g[2][2] = {{corner(0, 0), corner(0, 1)}, {corner(1, 0), corner(1, 1)}};
-        // canonical frame: origin = smallest vertex; first axis towards its
-        // smaller neighbour.
-        int os = 0, oq = 0;
-        for (int a = 0; a < 2; a++)
-          for (int b = 0; b < 2; b++)
-            if (g[a][b] < g[os][oq]) { os = a; oq = b; }
-        const int nP = g[1 - os][oq], nQ = g[os][1 - oq];
-        const bool swap = nQ < nP;  // first canonical axis is q
-        int p = c[pa], q = c[qa];
-        if (os) p = r - p;
-        if (oq) q = r - q;
-        int u = swap ? q : p, v = swap ? p : q;
-        FaceKey key{g[os][oq], swap ? nQ : nP, swap ? nP : nQ};
-        auto it = faces.find(key);
-        int base;
-        if (it == faces.end()) {
-          base = (int)next;
-          next += (long long)m * m;
-          faces.emplace(key, base);
-        } else {
-          base = it->second;
-        }
-        dof = base + (u - 1) * m + (v - 1);
-      } else {
-        if (interior_base < 0) {
-          interior_base = (int)next;
-          next += (long long)m * m * m;
-        }
-        dof = interior_base + ((i - 1) * m + (j - 1)) * m + (k - 1);
-      }
-      if (next > INT32_MAX) {
-        set_error("mj_number_hex_mesh: too many dofs for int32");
-        return MJ_ERR_ARG;
-      }
-      out[ql] = dof;
-    }
   }
   *n_dof = (int)next;
   return MJ_OK;

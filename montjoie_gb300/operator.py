@@ -75,6 +75,14 @@ class FemMatrixFreeOperator:
             raise ValueError("one scale per element")
         _lib.check(_lib.load().mj_op_set_element_scale(self._h, _lib.dptr(sc)))
 
+    def tuning(self) -> dict:
+        """Element-kernel variant picked by the autotuner at creation."""
+        vals = [ctypes.c_int() for _ in range(4)]
+        ms = np.zeros(64)
+        _lib.check(_lib.load().mj_op_tuning(self._h, *[ctypes.byref(v) for v in vals], _lib.dptr(ms)))
+        E, vec, grid, nc = (v.value for v in vals)
+        return {"tile_elems": E, "vector_lines": bool(vec), "grid": grid, "candidate_ms": ms[:nc].tolist()}
+
     def device_bytes(self) -> int:
         sz = ctypes.c_size_t()
         _lib.check(_lib.load().mj_op_info(self._h, None, None, None, None, ctypes.byref(sz)))
