@@ -224,6 +224,39 @@ int mj_lfb_get_state(mj_lfb* b, double* u_n, double* u_np1);
 /* Tuned variant and progress: runs, elements per CTA, lanes (runs per pass), grid, steps done. */
 int mj_lfb_info(const mj_lfb* b, int* n_rhs, int* tile_elems, int* lanes, int* grid, int* step);
 
+/* ---- many meshes of different size and order --------------------------- */
+
+typedef struct mj_mb mj_mb;
+
+/* Groups n_runs leap-frog runs into one batch.  Each run comes from
+ * mj_lf_create on its own MJ_FP32 operator, with its own mesh, order (1..8),
+ * time step, mass, source and pulse.  Every time step of every run is ONE
+ * cooperative persistent kernel: the element products of all meshes, a
+ * grid-wide barrier, then the gather, update and source of all meshes.
+ * Each run keeps its own state.  Between calls it stays usable through
+ * mj_lf_init, mj_lf_advance and mj_lf_get_state.  Runs must not share an
+ * operator.  The reference advances such runs one after the other, each
+ * with its own ModifiedEquationIterator
+ * (MONTJOIE/src/Instationary/ModifiedEquation.cxx:290-345). */
+int mj_mb_create(int n_runs, mj_lf* const* runs, mj_mb** out);
+int mj_mb_destroy(mj_mb* mb);
+
+/* Advances every run by nsteps steps; every run must have been initialised
+ * (mj_lf_init).  use_graph != 0 replays a captured CUDA graph of 20 steps
+ * (one kernel per step). */
+int mj_mb_advance(mj_mb* mb, int nsteps, int use_graph);
+
+/* Launch shape of the batch kernel: CTAs, CTAs per SM, element tiles and dof
+ * chunks per step, and 1 if the last advance replayed a graph. */
+int mj_mb_info(const mj_mb* mb, int* grid, int* ctas_per_sm, int* n_tiles, int* n_chunks, int* graph);
+
+/* Profiling aid: with enable != 0 every step is a plain launch that records
+ * per-CTA time stamps; mj_mb_phase_ms then returns, for the last step, out[0]
+ * = element phase (last CTA), out[1] = element phase (mean CTA), out[2] =
+ * barrier release, out[3] = dof phase, in ms. */
+int mj_mb_profile(mj_mb* mb, int enable);
+int mj_mb_phase_ms(const mj_mb* mb, double* out);
+
 /* ---- media update and adjoint ------------------------------------------ */
 
 /* Scales the stiffness factors of every element: factors(e) = scale[e] *

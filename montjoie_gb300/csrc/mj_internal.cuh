@@ -30,6 +30,44 @@ struct mj_op {
   }
 };
 
+// State of one leap-frog run (mj_lf_*), shared with the mesh-batch unit.
+struct mj_lf {
+  mj_op* op = nullptr;
+  double dt = 0;
+  int n_dof = 0;
+  mj::DevBuf src_idx, src_val;  // sparse source (value in op precision)
+  mj::DevBuf mass, minv;     // op precision (FP64: D and 1/D; FP32: unused / dt^2/D)
+  mj::DevBuf inv_mass64;     // FP64 1/D for the initial step
+  mj::DevBuf norm_w;         // FP64 weights, or empty
+  mj::DevBuf rec_idx, rec_w; // receivers
+  mj::DevBuf ua, ub;         // state: U^n (cur) and U^{n+1} (next)
+  mj::DevBuf du0, tmp;       // staging
+  mj::DevBuf partial, norms_d, traces_d, flag;
+  mj::DevBuf pulse_d, ctr;   // pulse of every step and the two step counters
+  int n_pulse = 0;
+  cudaGraphExec_t graph = nullptr, graph_prof = nullptr;
+  bool use_graph = true;  // replay captured steps when no diagnostics are asked
+  int n_src = 0, n_rec = 0, n_rec_w = 0;
+  int step = 0;
+  bool initialised = false;
+  bool cur_is_a = true;
+  cudaStream_t stream = nullptr;
+  int norm_blocks = 0;
+  // optional per-kernel timing (CUDA events around the two kernels of a step)
+  bool profile = false;
+  std::vector<cudaEvent_t> ev;
+  int ev_used = 0;
+  double prof_elem_ms = 0.0, prof_update_ms = 0.0;
+  int prof_steps = 0;
+  ~mj_lf() {
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    if (graph) cudaGraphExecDestroy(graph);
+    if (graph_prof) cudaGraphExecDestroy(graph_prof);
+  }
+  void* cur() { return cur_is_a ? ua.ptr : ub.ptr; }
+  void* next() { return cur_is_a ? ub.ptr : ua.ptr; }
+};
+
 namespace mj {
 
 // Tile sizes E (elements per CTA) instantiated for order n = r + 1, all

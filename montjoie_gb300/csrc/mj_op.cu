@@ -55,42 +55,6 @@ __global__ void k_cast_to_f64(const Real* __restrict__ a, double* __restrict__ b
 
 using namespace mj;
 
-struct mj_lf {
-  mj_op* op = nullptr;
-  double dt = 0;
-  int n_dof = 0;
-  DevBuf src_idx, src_val;  // sparse source (value in op precision)
-  DevBuf mass, minv;     // op precision (FP64: D and 1/D; FP32: unused / dt^2/D)
-  DevBuf inv_mass64;     // FP64 1/D for the initial step
-  DevBuf norm_w;         // FP64 weights, or empty
-  DevBuf rec_idx, rec_w; // receivers
-  DevBuf ua, ub;         // state: U^n (cur) and U^{n+1} (next)
-  DevBuf du0, tmp;       // staging
-  DevBuf partial, norms_d, traces_d, flag;
-  DevBuf pulse_d, ctr;   // pulse of every step and the two step counters
-  int n_pulse = 0;
-  cudaGraphExec_t graph = nullptr, graph_prof = nullptr;
-  bool use_graph = true;  // replay captured steps when no diagnostics are asked
-  int n_src = 0, n_rec = 0, n_rec_w = 0;
-  int step = 0;
-  bool initialised = false;
-  bool cur_is_a = true;
-  cudaStream_t stream = nullptr;
-  int norm_blocks = 0;
-  // optional per-kernel timing (CUDA events around the two kernels of a step)
-  bool profile = false;
-  std::vector<cudaEvent_t> ev;
-  int ev_used = 0;
-  double prof_elem_ms = 0.0, prof_update_ms = 0.0;
-  int prof_steps = 0;
-  ~mj_lf() {
-    for (cudaEvent_t e : ev) cudaEventDestroy(e);
-    if (graph) cudaGraphExecDestroy(graph);
-    if (graph_prof) cudaGraphExecDestroy(graph_prof);
-  }
-  void* cur() { return cur_is_a ? ua.ptr : ub.ptr; }
-  void* next() { return cur_is_a ? ub.ptr : ua.ptr; }
-};
 
 namespace {
 
@@ -323,13 +287,16 @@ int mj_op_create(const mj_mesh_desc* mesh, const mj_geom_desc* geom, int precisi
   MJ_CUDA(op->nodle_e.alloc(sizeof(int) * op->r_len));
   MJ_CUDA(op->slot_e.alloc(sizeof(int) * op->r_len));
   MJ_CUDA(op->fac_e.alloc(fac_bytes.size()));
-  MJ_CUDA(op->R.alloc(esz * (op->n_inc + 1)));
-  MJ_CUDA(op->ptr.alloc(sizeof(int) * (op->n_dof + 1)));
+  // 3 spare entries past the dummy slot: 16-byte rounded bulk copies of a
+  // dof range of R stay inside the buffer
+  MJ_CUDA(op->R.alloc(esz * (op->n_inc + 4)));
+  MJ_CUDA(op->ptr.alloc(sizeof(int) * (op->n_dof + 8)));  // padded like R
+  MJ_CUDA(cudaMemset(op->ptr.ptr, 0, sizeof(int) * (op->n_dof + 8)));
   MJ_CUDA(cudaMemcpy(op->nodle_e.ptr, nodle_e.data(), sizeof(int) * op->r_len, cudaMemcpyHostToDevice));
   MJ_CUDA(cudaMemcpy(op->slot_e.ptr, slot_e.data(), sizeof(int) * op->r_len, cudaMemcpyHostToDevice));
   MJ_CUDA(cudaMemcpy(op->fac_e.ptr, fac_bytes.data(), fac_bytes.size(), cudaMemcpyHostToDevice));
   MJ_CUDA(cudaMemcpy(op->ptr.ptr, op->h_ptr.data(), sizeof(int) * (op->n_dof + 1), cudaMemcpyHostToDevice));
-  MJ_CUDA(cudaMemset(op->R.ptr, 0, esz * (op->n_inc + 1)));
+  MJ_CUDA(cudaMemset(op->R.ptr, 0, esz * (op->n_inc + 4)));
   MJ_CUDA(op->err.alloc(sizeof(int)));
   MJ_CUDA(cudaMemset(op->err.ptr, 0, sizeof(int)));
   {
@@ -451,7 +418,8 @@ int mj_lf_create(mj_op* op, const mj_lf_desc* desc, mj_lf** out) {
     for (int s = 0; s < desc->n_src; s++) sv[s] = (float)desc->src_val[s];
     for (int i = 0; i < n; i++) m[i] = (float)(desc->dt * desc->dt * invD[i]);
     MJ_CUDA(cudaMemcpy(lf->src_val.ptr, sv.data(), sizeof(float) * sv.size(), cudaMemcpyHostToDevice));
-    MJ_CUDA(lf->minv.alloc(sizeof(float) * n));
+    MJ_CUDA(lf->minv.alloc(sizeof(float) * (n + 4)));
+    MJ_CUDA(cudaMemset(lf->minv.ptr, 0, sizeof(float) * (n + 4)));
     MJ_CUDA(cudaMemcpy(lf->minv.ptr, m.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
   }
   lf->n_pulse = desc->n_pulse;
@@ -475,8 +443,11 @@ int mj_lf_create(mj_op* op, const mj_lf_desc* desc, mj_lf** out) {
     MJ_CUDA(cudaMemcpy(lf->rec_idx.ptr, desc->rec_idx, sizeof(int) * m, cudaMemcpyHostToDevice));
     MJ_CUDA(cudaMemcpy(lf->rec_w.ptr, desc->rec_w, sizeof(double) * m, cudaMemcpyHostToDevice));
   }
-  MJ_CUDA(lf->ua.alloc(esz * n));
-  MJ_CUDA(lf->ub.alloc(esz * n));
+  // state vectors padded by 4 entries (16-byte rounded bulk copies of dof ranges)
+  MJ_CUDA(lf->ua.alloc(esz * (n + 4)));
+  MJ_CUDA(lf->ub.alloc(esz * (n + 4)));
+  MJ_CUDA(cudaMemset(lf->ua.ptr, 0, esz * (n + 4)));
+  MJ_CUDA(cudaMemset(lf->ub.ptr, 0, esz * (n + 4)));
   lf->norm_blocks = std::min(stream_grid(n), 1024);
   MJ_CUDA(lf->partial.alloc(sizeof(double) * lf->norm_blocks));
   MJ_CUDA(lf->flag.alloc(sizeof(int)));

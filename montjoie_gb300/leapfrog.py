@@ -220,3 +220,55 @@ def RunSecondOrderScheme(t_begin: float, t_end: float, dt: float, U0: np.ndarray
     if nsteps < 1:
         return np.array(U0, dtype=np.float64), None, None
     return scheme.Run(U0, dU0_dt, nsteps)
+
+
+class MeshBatch:
+    """Leap-frog runs on meshes of different size and order (each a
+    ``LeapFrogIterator`` on its own FP32 operator) advanced together by one
+    cooperative persistent kernel per time step.  The reference advances such
+    runs one after the other (``ModifiedEquation.cxx:290-345`` per run).
+    Each run stays usable on its own (``SetInitialConditionS``,
+    ``GetIterate``, ``Advance``) between calls."""
+
+    def __init__(self, runs):
+        L = _lib.load()
+        self.runs = list(runs)
+        arr = (ctypes.c_void_p * len(self.runs))(*[r.handle.value for r in self.runs])
+        h = ctypes.c_void_p()
+        _lib.check(L.mj_mb_create(len(self.runs), arr, ctypes.byref(h)))
+        self._h = h
+
+    def advance(self, nsteps: int, graph: bool = True) -> None:
+        _lib.check(_lib.load().mj_mb_advance(self._h, int(nsteps), int(bool(graph))))
+        for r in self.runs:
+            r.n_time += nsteps
+
+    def info(self) -> dict:
+        vals = [ctypes.c_int() for _ in range(5)]
+        _lib.check(_lib.load().mj_mb_info(self._h, *[ctypes.byref(v) for v in vals]))
+        return dict(zip(["grid", "ctas_per_sm", "tiles", "chunks", "graph"], [v.value for v in vals]))
+
+    def n_dof(self) -> int:
+        return sum(r.op.n_dof for r in self.runs)
+
+    def profile(self, enable: bool) -> None:
+        """Plain launches with per-CTA time stamps (no graph) while enabled."""
+        _lib.check(_lib.load().mj_mb_profile(self._h, int(bool(enable))))
+
+    def phase_ms(self) -> dict:
+        """Phase times of the last step (ms): element phase (last and mean CTA),
+        barrier release, dof phase."""
+        out = np.zeros(4)
+        _lib.check(_lib.load().mj_mb_phase_ms(self._h, _lib.dptr(out)))
+        return dict(zip(["element_last", "element_mean", "barrier", "dof"], out.tolist()))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _lib.load().mj_mb_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

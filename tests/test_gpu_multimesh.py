@@ -1,0 +1,116 @@
+"""Heterogeneous batch of meshes (orders 1..8, one cooperative kernel per
+step) against the reference's trajectories and against the same runs
+advanced one by one.
+
+- Reference: the golden snapshots of u at 30 and 40 steps, within the FP32
+  chosen-form tolerance (relative L2 <= 1e-4, as for single FP32 runs).
+- Single runs: every batched run equals the same run advanced alone through
+  mj_lf_advance (same FP32 arithmetic; relative L2 <= 1e-6).
+- The batch keeps each run's state, step counter and pulse index consistent
+  across graph replays, odd step counts and a run advanced on its own.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+CASES = ["cube2_q1", "cube2_q2", "cube2_q3", "regular2_q4", "cube3_q4", "cube2_q6", "cube2_q8", "cube4_q4"]
+FP32_TOL = 1e-4
+SAME_TOL = 1e-6
+
+
+def run_fp32(g):
+    from montjoie_gb300.leapfrog import LeapFrogIterator
+    from montjoie_gb300.operator import FemMatrixFreeOperator
+    op = FemMatrixFreeOperator(int(g["order"]), g["nodle"], g["bh"], g["massD"].size, "fp32", gradphi=g["gradphi"])
+    lf = LeapFrogIterator(op, float(g["dt"]), g["massD"], g["invD"], g["src_idx"], g["src_val"], g["pulse"])
+    lf.SetInitialConditionS(np.zeros(g["massD"].size))
+    return op, lf
+
+
+def snapshot(g, step):
+    steps = g["snap_steps"].tolist()
+    return g["snaps"][steps.index(step)] if step in steps else None
+
+
+def test_batch_matches_reference_and_single_runs():
+    from montjoie_gb300.leapfrog import MeshBatch
+    gs = [load_golden(c) for c in CASES]
+    batch_runs = [run_fp32(g) for g in gs]
+    single_runs = [run_fp32(g) for g in gs]
+    mb = MeshBatch([lf for _, lf in batch_runs])
+    info = mb.info()
+    assert info["tiles"] > 0 and info["chunks"] >= len(CASES) and info["grid"] >= 1
+    mb.advance(30)  # one 20-step graph + 10 launches
+    assert mb.info()["graph"] == 1
+    for g, (_, lf), (_, ls) in zip(gs, batch_runs, single_runs):
+        ls.Advance(30)
+        u = lf.GetIterate()
+        assert rel_l2(u, ls.GetIterate()) < SAME_TOL
+        ref = snapshot(g, 30)
+        if ref is not None:
+            assert rel_l2(u, ref) < FP32_TOL
+    mb.advance(10, graph=False)
+    for g, (_, lf), (_, ls) in zip(gs, batch_runs, single_runs):
+        ls.Advance(10)
+        u = lf.GetIterate()
+        assert rel_l2(u, ls.GetIterate()) < SAME_TOL
+        ref = snapshot(g, 40)
+        if ref is not None:
+            assert rel_l2(u, ref) < FP32_TOL
+    # odd counts: the graph starting at an odd offset, then a run advanced alone
+    mb.advance(21)
+    mb.advance(25)
+    batch_runs[3][1].Advance(3)
+    mb.advance(22)
+    for k, ((_, lf), (_, ls)) in enumerate(zip(batch_runs, single_runs)):
+        ls.Advance(68 + (3 if k == 3 else 0))
+        u0, u1 = lf.GetState()
+        v0, v1 = ls.GetState()
+        assert rel_l2(u0, v0) < SAME_TOL and rel_l2(u1, v1) < SAME_TOL
+        assert lf.n_time == ls.n_time
+    mb.close()
+    for op, lf in batch_runs + single_runs:
+        lf.close()
+        op.close()
+
+
+def test_batch_long_run_matches_reference():
+    """cube4_q4 (200 steps) and cube3_q4 (120 steps) batched with a Q8 mesh:
+    final iterates against the reference's."""
+    from montjoie_gb300.leapfrog import MeshBatch
+    gs = [load_golden("cube4_q4"), load_golden("cube3_q4"), load_golden("cube2_q8")]
+    runs = [run_fp32(g) for g in gs]
+    mb = MeshBatch([lf for _, lf in runs])
+    mb.advance(120)
+    assert rel_l2(runs[1][1].GetIterate(), gs[1]["u_final"]) < FP32_TOL
+    mb.advance(80)
+    assert rel_l2(runs[0][1].GetIterate(), gs[0]["u_final"]) < FP32_TOL
+    mb.close()
+    for op, lf in runs:
+        lf.close()
+        op.close()
+
+
+def test_batch_rejects_bad_runs():
+    from montjoie_gb300 import _lib
+    from montjoie_gb300.leapfrog import LeapFrogIterator, MeshBatch
+    from montjoie_gb300.operator import FemMatrixFreeOperator
+    g = load_golden("cube2_q2")
+    op64 = FemMatrixFreeOperator(2, g["nodle"], g["bh"], g["massD"].size, "fp64")
+    lf64 = LeapFrogIterator(op64, float(g["dt"]), g["massD"])
+    with pytest.raises(_lib.MontjoieError):
+        MeshBatch([lf64])
+    op, lf = run_fp32(g)
+    lf2 = LeapFrogIterator(op, float(g["dt"]), g["massD"])
+    with pytest.raises(_lib.MontjoieError):
+        MeshBatch([lf, lf2])  # shared operator
+    lf3 = LeapFrogIterator(op, float(g["dt"]), g["massD"])
+    mb = MeshBatch([lf3])
+    with pytest.raises(_lib.MontjoieError):
+        mb.advance(1)  # not initialised
+    mb.close()
+    for x in (lf64, lf, lf2, lf3, op64, op):
+        x.close()
