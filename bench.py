@@ -275,6 +275,7 @@ def leg_config4_meshes(args, torch, _lib):
     ms = timed_steps(torch, mb.advance, K)
     launches = _lib.kernel_launches() - l0
     info = mb.info()
+    info["tuning"] = mb.tuning()
     u_batch = [x[4].GetIterate() for x in runs]
     mb.profile(True)  # phase times of one extra step (per-CTA time stamps)
     mb.advance(1)

@@ -257,6 +257,17 @@ int mj_mb_info(const mj_mb* mb, int* grid, int* ctas_per_sm, int* n_tiles, int* 
 int mj_mb_profile(mj_mb* mb, int enable);
 int mj_mb_phase_ms(const mj_mb* mb, double* out);
 
+/* Launch configuration chosen by timing both candidates on the batch at its
+ * first advance (run states are restored afterwards): threads per CTA (256:
+ * large tiles, 128: small tiles, more CTAs per SM; 0 before the first
+ * advance) and the two candidates' ms per step (candidate_ms: room for 2,
+ * may be NULL).  At most 48 runs per batch. */
+int mj_mb_tuning(const mj_mb* mb, int* threads, double* candidate_ms);
+
+/* Forces the launch configuration (threads = 128 or 256), or 0 to time both
+ * again at the next advance. */
+int mj_mb_set_config(mj_mb* mb, int threads);
+
 /* ---- media update and adjoint ------------------------------------------ */
 
 /* Scales the stiffness factors of every element: factors(e) = scale[e] *

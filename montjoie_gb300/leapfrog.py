@@ -251,6 +251,18 @@ class MeshBatch:
     def n_dof(self) -> int:
         return sum(r.op.n_dof for r in self.runs)
 
+    def tuning(self) -> dict:
+        """Launch configuration picked at the first advance and the timings of both."""
+        th = ctypes.c_int()
+        ms = np.zeros(2)
+        _lib.check(_lib.load().mj_mb_tuning(self._h, ctypes.byref(th), _lib.dptr(ms)))
+        return {"threads": th.value, "candidate_ms": {"256": ms[0], "128": ms[1]}}
+
+    def set_config(self, threads: int) -> None:
+        """Forces the launch configuration (128 or 256 threads per CTA), or 0
+        to time both again at the next advance."""
+        _lib.check(_lib.load().mj_mb_set_config(self._h, int(threads)))
+
     def profile(self, enable: bool) -> None:
         """Plain launches with per-CTA time stamps (no graph) while enabled."""
         _lib.check(_lib.load().mj_mb_profile(self._h, int(bool(enable))))

@@ -35,16 +35,21 @@ def snapshot(g, step):
     return g["snaps"][steps.index(step)] if step in steps else None
 
 
-def test_batch_matches_reference_and_single_runs():
+@pytest.mark.parametrize("threads", [0, 128, 256])
+def test_batch_matches_reference_and_single_runs(threads):
+    """threads = 0: the autotuned launch configuration; 128 / 256: forced."""
     from montjoie_gb300.leapfrog import MeshBatch
     gs = [load_golden(c) for c in CASES]
     batch_runs = [run_fp32(g) for g in gs]
     single_runs = [run_fp32(g) for g in gs]
     mb = MeshBatch([lf for _, lf in batch_runs])
+    if threads:
+        mb.set_config(threads)
     info = mb.info()
     assert info["tiles"] > 0 and info["chunks"] >= len(CASES) and info["grid"] >= 1
     mb.advance(30)  # one 20-step graph + 10 launches
     assert mb.info()["graph"] == 1
+    assert mb.tuning()["threads"] == (threads or mb.tuning()["threads"]) and mb.tuning()["threads"] in (128, 256)
     for g, (_, lf), (_, ls) in zip(gs, batch_runs, single_runs):
         ls.Advance(30)
         u = lf.GetIterate()
