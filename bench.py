@@ -225,6 +225,13 @@ def leg_config4_sources(args, torch, _lib):
     launches = _lib.kernel_launches() - l0
     u, _ = b.state()
     info = b.info()
+    info["one_kernel_step"] = b.step_info()
+    # the same runs with two kernels per step (element kernel, then gather + update)
+    b.set_fused(False)
+    b.init()
+    b.advance(20)
+    ms_two = timed_steps(torch, b.advance, K)
+    u_two, _ = b.state()
     b.close()
     # run 0 against a single-source run of the same FP32 operator
     lf = LeapFrogIteratorFor(pb, op, idx[0], val[0])
@@ -238,9 +245,12 @@ def leg_config4_sources(args, torch, _lib):
     value = pb.n_dof * S * K / (ms / 1e3)
     peak, _ = measured_peaks()
     return {"workload": f"64 Ricker sources (Gaussian R=2h, seeded positions in [0.1,0.9]^3) on one 32^3 Q4 mesh, "
-                        f"+-5% h perturbation, c per element in [1,3], FP32, {K} steps, state [dof][64]",
+                        f"+-5% h perturbation, c per element in [1,3], FP32, {K} steps, state [dof][64], "
+                        f"one cooperative kernel per step",
             "n_dof": pb.n_dof, "n_rhs": S, "steps": K, "value": value, "unit": UNIT, "ms_per_step": ms / K,
             "variant": info, "gpu_launches": launches,
+            "two_kernel_ms_per_step": ms_two / K,
+            "one_vs_two_kernel_rel_l2": float(np.linalg.norm(u - u_two) / max(np.linalg.norm(u_two), 1e-300)),
             "run0_rel_l2_vs_single_source_run": float(np.linalg.norm(u[:, 0] - u0) / max(np.linalg.norm(u0), 1e-300)),
             "algorithmic_bytes_per_dof_update": bytes_step,
             "step_frac_of_hbm": value * bytes_step / 1e9 / peak}

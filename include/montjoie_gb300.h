@@ -224,6 +224,19 @@ int mj_lfb_get_state(mj_lfb* b, double* u_n, double* u_np1);
 /* Tuned variant and progress: runs, elements per CTA, lanes (runs per pass), grid, steps done. */
 int mj_lfb_info(const mj_lfb* b, int* n_rhs, int* tile_elems, int* lanes, int* grid, int* step);
 
+/* mj_lfb_advance runs every step as ONE cooperative persistent kernel
+ * (element products of all runs, grid barrier, gather + update + sources),
+ * its variant chosen at creation by timing the candidates of the order; with
+ * enable = 0 it uses two kernels per step (element kernel, then gather and
+ * update) instead.  Default: one kernel when a variant fits (MJ_ERR_STATE
+ * otherwise). */
+int mj_lfb_set_fused(mj_lfb* b, int enable);
+
+/* One-kernel step: whether it is in use, threads per CTA and grid of the
+ * chosen variant, and the timings (ms per step) of the candidates tried
+ * (candidate_ms: room for 16, may be NULL). */
+int mj_lfb_step_info(const mj_lfb* b, int* fused, int* threads, int* grid, int* n_candidates, double* candidate_ms);
+
 /* ---- many meshes of different size and order --------------------------- */
 
 typedef struct mj_mb mj_mb;

@@ -45,7 +45,8 @@ void rhs_launch_one(int grid, const float* x, const int* nodle_e, const float* f
 }
 
 #define MJ_RHS_VARIANTS(X)                                                                                     \
-  X(2, 4, 32) X(2, 8, 16) X(3, 2, 32) X(3, 4, 16) X(4, 1, 32) X(4, 2, 16) X(5, 1, 32) X(5, 1, 16) X(5, 2, 8) \
+  X(2, 4, 32) X(2, 8, 16) X(2, 8, 8) X(3, 2, 32) X(3, 4, 16) X(3, 4, 8) X(4, 1, 32) X(4, 2, 16) X(4, 2, 8)    \
+  X(5, 1, 32) X(5, 1, 16) X(5, 2, 8)                                                                           \
   X(6, 1, 16) X(6, 1, 8) X(7, 1, 16) X(7, 1, 8) X(8, 1, 8) X(9, 1, 8)
 
 int rhs_prepare(int n, int E, int L, int* ctas) {
@@ -214,6 +215,15 @@ int grid_for(long long n) {
 
 }  // namespace
 
+// Receiver values of every run before a step: out column `col` of
+// b->traces_d (stride = steps of the call).
+void lfb_receivers(mj_lfb* b, const float* u, int stride, int col, cudaStream_t s) {
+  const int threads = 128, blocks = (b->n_rec * b->S + threads - 1) / threads;
+  k_receivers_rhs<<<blocks, threads, 0, s>>>(u, b->rec_idx.as<int>(), b->rec_w.as<double>(), b->n_rec, b->n_rec_w,
+                                             b->S, b->traces_d.as<double>(), stride, col);
+  count_launch();
+}
+
 // Derivative matrix of order n into this unit's constant memory.
 int k1_set_gmat_rhs(int n, const double* g) {
   float v[kMaxNK * kMaxNK];
@@ -224,9 +234,9 @@ int k1_set_gmat_rhs(int n, const double* g) {
 
 std::vector<RhsVariant> k1_rhs_candidates(int n) {
   switch (n) {
-    case 2: return {{4, 32}, {8, 16}};
-    case 3: return {{2, 32}, {4, 16}};
-    case 4: return {{1, 32}, {2, 16}};
+    case 2: return {{4, 32}, {8, 16}, {8, 8}};
+    case 3: return {{2, 32}, {4, 16}, {4, 8}};
+    case 4: return {{1, 32}, {2, 16}, {2, 8}};
     case 5: return {{1, 32}, {1, 16}, {2, 8}};
     case 6: return {{1, 16}, {1, 8}};
     case 7: return {{1, 16}, {1, 8}};
@@ -240,28 +250,6 @@ std::vector<RhsVariant> k1_rhs_candidates(int n) {
 
 using namespace mj;
 
-struct mj_lfb {
-  mj_op* op = nullptr;
-  int S = 0, n_dof = 0;
-  double dt = 0;
-  int E = 1, L = 32, grid = 1, n_tiles = 0;  // tuned element-kernel variant
-  DevBuf R;                                  // element-local results [slot][S]
-  DevBuf src_idx, src_val, src_rhs, m, inv_mass64, pulse, ctr;
-  int n_src = 0;
-  DevBuf ua, ub, stage, rec_idx, rec_w, traces_d;
-  int n_pulse = 0, n_rec = 0, n_rec_w = 0;
-  int step = 0;
-  bool cur_is_a = true, initialised = false;
-  cudaStream_t stream = nullptr;
-  cudaGraphExec_t graph = nullptr;
-  int graph_steps = 0;
-  std::vector<double> tune_ms;
-  ~mj_lfb() {
-    if (graph) cudaGraphExecDestroy(graph);
-  }
-  float* cur() { return (cur_is_a ? ua : ub).as<float>(); }
-  float* next() { return (cur_is_a ? ub : ua).as<float>(); }
-};
 
 namespace {
 
@@ -374,7 +362,8 @@ int mj_lfb_create(mj_op* op, const mj_lfb_desc* d, mj_lfb** out) {
   MJ_CUDA(b->src_idx.alloc(sizeof(int) * si.size()));
   MJ_CUDA(b->src_val.alloc(sizeof(float) * sv.size()));
   MJ_CUDA(b->src_rhs.alloc(sizeof(int) * sr.size()));
-  MJ_CUDA(b->m.alloc(sizeof(float) * n));
+  MJ_CUDA(b->m.alloc(sizeof(float) * (n + 8)));  // padded: 16-byte rounded bulk copies of dof ranges
+  MJ_CUDA(cudaMemset(b->m.ptr, 0, sizeof(float) * (n + 8)));
   MJ_CUDA(b->inv_mass64.alloc(sizeof(double) * n));
   MJ_CUDA(b->pulse.alloc(sizeof(double) * std::max(1, d->n_pulse)));
   MJ_CUDA(b->ctr.alloc(sizeof(int) * 2));
@@ -404,6 +393,8 @@ int mj_lfb_create(mj_op* op, const mj_lfb_desc* d, mj_lfb** out) {
   int rc = k1_set_gmat_rhs(op->n, op->gradphi);
   if (rc) return rc;
   rc = lfb_autotune(b.get());
+  if (rc) return rc;
+  rc = lfb_fused_setup(b.get());
   if (rc) return rc;
   *out = b.release();
   return MJ_OK;
@@ -467,6 +458,7 @@ int mj_lfb_advance(mj_lfb* b, int nsteps, double* traces, int trace_stride, int 
     const size_t bytes = sizeof(double) * (size_t)b->n_rec * b->S * nsteps;
     if (b->traces_d.bytes < bytes) MJ_CUDA(b->traces_d.alloc(bytes));
   }
+  if (b->fused) return lfb_fused_advance(b, nsteps, traces, trace_stride, use_graph != 0);
   int done = 0;
   const int G = 20;  // steps per captured graph (even: buffers and counters return to their roles)
   if (use_graph && !diag && nsteps >= G + 1) {
@@ -543,6 +535,27 @@ int mj_lfb_get_state(mj_lfb* b, double* u_n, double* u_np1) {
     MJ_CUDA(cudaMemcpyAsync(dst[k], b->stage.ptr, sizeof(double) * rows, cudaMemcpyDeviceToHost, s));
     MJ_CUDA(cudaStreamSynchronize(s));
   }
+  return MJ_OK;
+}
+
+int mj_lfb_set_fused(mj_lfb* b, int enable) {
+  MJ_CHECK_ARG(b, "mj_lfb_set_fused: null integrator");
+  if (enable && b->rs_variant < 0) {
+    set_error("mj_lfb_set_fused: no one-kernel step variant fits this integrator");
+    return MJ_ERR_STATE;
+  }
+  b->fused = enable != 0;
+  return MJ_OK;
+}
+
+int mj_lfb_step_info(const mj_lfb* b, int* fused, int* threads, int* grid, int* n_candidates, double* candidate_ms) {
+  MJ_CHECK_ARG(b, "mj_lfb_step_info: null integrator");
+  if (fused) *fused = b->fused ? 1 : 0;
+  if (threads) *threads = b->rs_threads;
+  if (grid) *grid = b->rs_grid;
+  if (n_candidates) *n_candidates = (int)b->rs_tune_ms.size();
+  if (candidate_ms)
+    for (size_t c = 0; c < b->rs_tune_ms.size(); c++) candidate_ms[c] = b->rs_tune_ms[c];
   return MJ_OK;
 }
 

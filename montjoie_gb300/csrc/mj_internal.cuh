@@ -68,6 +68,42 @@ struct mj_lf {
   void* next() { return cur_is_a ? ub.ptr : ua.ptr; }
 };
 
+// State of S leap-frog runs sharing one mesh (mj_lfb_*), shared by the
+// many-source units.
+struct mj_lfb {
+  mj_op* op = nullptr;
+  int S = 0, n_dof = 0;
+  double dt = 0;
+  int E = 1, L = 32, grid = 1, n_tiles = 0;  // tuned element-kernel variant
+  mj::DevBuf R;                                  // element-local results [slot][S]
+  mj::DevBuf src_idx, src_val, src_rhs, m, inv_mass64, pulse, ctr;
+  int n_src = 0;
+  mj::DevBuf ua, ub, stage, rec_idx, rec_w, traces_d;
+  int n_pulse = 0, n_rec = 0, n_rec_w = 0;
+  int step = 0;
+  bool cur_is_a = true, initialised = false;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int graph_steps = 0;
+  std::vector<double> tune_ms;
+  // one cooperative kernel per step (mj_rhs_step.cu): chosen variant, launch
+  // shape, dof chunks, sources grouped by dof, barrier state, graphs by parity
+  bool fused = true;
+  int rs_variant = -1, rs_grid = 0, rs_threads = 0, rs_n_chunks = 0;
+  mj::DevBuf rs_chunks, rs_src_dof, rs_src_ptr, rs_src_rhs, rs_src_val, rs_sync, rs_err;
+  int rs_n_src_dof = 0;
+  cudaGraphExec_t rs_graph[2] = {nullptr, nullptr};
+  std::vector<double> rs_tune_ms;
+  std::vector<int> rs_tune_variant;
+  ~mj_lfb() {
+    if (graph) cudaGraphExecDestroy(graph);
+    for (auto& g : rs_graph)
+      if (g) cudaGraphExecDestroy(g);
+  }
+  float* cur() { return (cur_is_a ? ua : ub).as<float>(); }
+  float* next() { return (cur_is_a ? ub : ua).as<float>(); }
+};
+
 namespace mj {
 
 // Tile sizes E (elements per CTA) instantiated for order n = r + 1, all
@@ -97,5 +133,11 @@ std::vector<RhsVariant> k1_rhs_candidates(int n);
 int k1_set_gmat_rhs(int n, const double* g);
 
 int stream_grid(int n);
+
+// One cooperative kernel per step for S right-hand sides (mj_rhs_step.cu):
+// variant choice at creation, and the advance used by mj_lfb_advance.
+int lfb_fused_setup(mj_lfb* b);
+int lfb_fused_advance(mj_lfb* b, int nsteps, double* traces, int trace_stride, bool use_graph);
+void lfb_receivers(mj_lfb* b, const float* u, int stride, int col, cudaStream_t s);
 
 }  // namespace mj

@@ -66,6 +66,13 @@ __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier
 
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
+// Orders this thread's generic-proxy global accesses with async-proxy (bulk
+// copy) accesses: global data written by plain stores and read back by bulk
+// copies in the same kernel (after a grid barrier) needs it on both sides.
+__device__ __forceinline__ void fence_proxy_async_global() {
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
                : "memory");

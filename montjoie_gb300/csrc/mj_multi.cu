@@ -39,6 +39,7 @@
 
 #include "mj_internal.cuh"
 #include "mj_k1.cuh"
+#include "mj_sync.cuh"
 
 namespace mj {
 namespace {
@@ -135,56 +136,6 @@ struct Work {
 struct Chunk {
   int mesh, d0, d1, q0, q1, has_src, pad0, pad1;
 };
-
-struct SyncState {
-  unsigned count;  // arrivals at the barrier
-  unsigned gen;    // barrier generation
-};
-
-__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
-  unsigned v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-
-__device__ __forceinline__ unsigned long long global_ns() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-// Grid-wide barrier of a cooperative launch.  Thread 0 of each CTA arrives on
-// a counter; the last arrival resets it and bumps the generation the others
-// wait on.  The wait gives up after 2 s (or 2^26 polls): the CTA then sets
-// *err = 2 and the barrier reports failure.
-__device__ bool grid_barrier(SyncState* s, int* err) {
-  __shared__ int s_ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int ok = 1;
-    const unsigned g0 = ld_acquire(&s->gen);
-    __threadfence();
-    if (atomicAdd(&s->count, 1u) == gridDim.x - 1) {
-      atomicExch(&s->count, 0u);
-      __threadfence();
-      atomicAdd(&s->gen, 1u);
-    } else {
-      const unsigned long long t0 = global_ns();
-      for (long it = 0; ld_acquire(&s->gen) == g0; ++it) {
-        if (it > (1L << 26) || global_ns() - t0 > 2000000000ull) {
-          ok = 0;
-          atomicExch(err, 2);
-          break;
-        }
-        __nanosleep(100);
-      }
-    }
-    __threadfence();
-    s_ok = ok;
-  }
-  __syncthreads();
-  return s_ok != 0;
-}
 
 __device__ __forceinline__ const float* next_state(const MeshDev& m, int k) {
   return ((k + m.cur_par) & 1) == 0 ? m.ub : m.ua;  // U^{n+1}
@@ -465,6 +416,7 @@ __global__ void __launch_bounds__(T, MbCfg<T>::min_ctas)
   }
 
   if (stamps && t == 0) stamps[4 * blockIdx.x + 1] = global_ns();
+  fence_proxy_async_global();  // this thread's R stores before the bulk copies of phase 2
   if (!grid_barrier(sync, err)) return;
   if (stamps && t == 0) stamps[4 * blockIdx.x + 2] = global_ns();
 
@@ -476,7 +428,8 @@ __global__ void __launch_bounds__(T, MbCfg<T>::min_ctas)
   Chunk ccur = load_chunk(chunks, n_chunks, c);
   Chunk cnxt = load_chunk(chunks, n_chunks, c + G);
   if (t == 0) {
-    fence_proxy_async();  // phase-1 use of this shared memory is over
+    fence_proxy_async();         // phase-1 use of this shared memory is over
+    fence_proxy_async_global();  // every CTA's R stores (ordered by the barrier) before the copies
     if (ccur.mesh >= 0) issue_chunk<T>(tab.m[ccur.mesh], ccur, k, smem, &bar[2]);
     if (cnxt.mesh >= 0) issue_chunk<T>(tab.m[cnxt.mesh], cnxt, k, smem + P::kP2Buf, &bar[3]);
   }

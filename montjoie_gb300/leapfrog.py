@@ -192,6 +192,17 @@ class BatchLeapFrog:
         _lib.check(_lib.load().mj_lfb_info(self._h, *[ctypes.byref(v) for v in vals]))
         return dict(zip(["n_rhs", "tile_elems", "lanes", "grid", "step"], [v.value for v in vals]))
 
+    def set_fused(self, enable: bool) -> None:
+        """One cooperative kernel per step (default) or two kernels per step."""
+        _lib.check(_lib.load().mj_lfb_set_fused(self._h, int(bool(enable))))
+
+    def step_info(self) -> dict:
+        vals = [ctypes.c_int() for _ in range(4)]
+        ms = np.zeros(16)
+        _lib.check(_lib.load().mj_lfb_step_info(self._h, *[ctypes.byref(v) for v in vals], _lib.dptr(ms)))
+        fused, threads, grid, nc = (v.value for v in vals)
+        return {"one_kernel": bool(fused), "threads": threads, "grid": grid, "candidate_ms": ms[:nc].tolist()}
+
     @property
     def handle(self):
         return self._h

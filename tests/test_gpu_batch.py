@@ -82,3 +82,45 @@ def test_batched_initial_conditions_and_traces():
         assert rel_l2(u[:, s], uo) < 1e-4
         assert np.abs(tr[:, s, :] - to[:, :n]).max() < 1e-4 * np.abs(to).max()
     b.close(); op.close()
+
+
+@pytest.mark.parametrize("case,S", [("cube3_q4", 64), ("cube2_q2", 16), ("cube2_q8", 8), ("cube2_q1", 24),
+                                    ("cube2_q6", 32), ("cube4_q4", 40)])
+def test_one_kernel_step_equals_two_kernel_step(case, S):
+    """The default step (one cooperative kernel: element products, grid
+    barrier, gather + update + sources) against the two-kernel step on the same
+    integrator set-up: same FP32 arithmetic per (dof, source), relative L2
+    <= 1e-6 (measured: bitwise equal), including odd step counts and the graph."""
+    g = load_golden(case)
+    op1, b1 = _batch(g, S)
+    op2, b2 = _batch(g, S)
+    info = b1.step_info()
+    assert info["one_kernel"] and info["threads"] > 0 and info["grid"] > 0 and len(info["candidate_ms"]) >= 1
+    b2.set_fused(False)
+    assert not b2.step_info()["one_kernel"]
+    b1.init(); b2.init()
+    for k, gr in ((3, False), (45, True), (20, True), (7, False)):
+        b1.advance(k, graph=gr)
+        b2.advance(k, graph=gr)
+    u1, v1 = b1.state()
+    u2, v2 = b2.state()
+    assert rel_l2(u1, u2) < 1e-6 and rel_l2(v1, v2) < 1e-6
+    assert b1.info()["step"] == b2.info()["step"] == 75
+    b1.close(); b2.close(); op1.close(); op2.close()
+
+
+def test_one_kernel_step_traces_match_two_kernel_step():
+    from montjoie_gb300.problem import receiver_weights
+    g = load_golden("cube3_q4")
+    S = 16
+    rng = np.random.default_rng(5)
+    rec = receiver_weights(int(g["order"]), g["verts_e"], g["nodle"], rng.uniform(0.1, 0.9, size=(4, 3)))
+    op1, b1 = _batch(g, S, receivers=rec)
+    op2, b2 = _batch(g, S, receivers=rec)
+    b2.set_fused(False)
+    u0 = rng.uniform(-1, 1, (g["massD"].size, S))
+    b1.init(u0); b2.init(u0)
+    t1 = b1.advance(30, traces=True)
+    t2 = b2.advance(30, traces=True)
+    assert np.abs(t1 - t2).max() <= 1e-6 * np.abs(t2).max()
+    b1.close(); b2.close(); op1.close(); op2.close()
