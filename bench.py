@@ -226,6 +226,10 @@ def leg_config4_sources(args, torch, _lib):
     u, _ = b.state()
     info = b.info()
     info["one_kernel_step"] = b.step_info()
+    b.profile(True)  # phase times of one extra step (per-CTA time stamps)
+    b.advance(1)
+    info["phase_ms_one_step"] = b.phase_ms()
+    b.profile(False)
     # the same runs with two kernels per step (element kernel, then gather + update)
     b.set_fused(False)
     b.init()

@@ -237,6 +237,13 @@ int mj_lfb_set_fused(mj_lfb* b, int enable);
  * (candidate_ms: room for 16, may be NULL). */
 int mj_lfb_step_info(const mj_lfb* b, int* fused, int* threads, int* grid, int* n_candidates, double* candidate_ms);
 
+/* Profiling aid for the one-kernel step: with enable != 0 every step is a
+ * plain launch recording per-CTA time stamps; mj_lfb_phase_ms then returns,
+ * for the last step, out[0] = element phase (last CTA), out[1] = element phase
+ * (mean CTA), out[2] = barrier release, out[3] = dof phase, in ms. */
+int mj_lfb_profile(mj_lfb* b, int enable);
+int mj_lfb_phase_ms(const mj_lfb* b, double* out);
+
 /* ---- many meshes of different size and order --------------------------- */
 
 typedef struct mj_mb mj_mb;

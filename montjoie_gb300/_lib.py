@@ -29,7 +29,7 @@ EXPORTED = [
     "mj_geometry", "mj_lumped_mass", "mj_stiffness_mltadd_static",
     "mj_lfb_create", "mj_lfb_destroy", "mj_lfb_init", "mj_lfb_advance", "mj_lfb_get_state", "mj_lfb_info",
     "mj_op_set_element_scale", "mj_adj_create", "mj_adj_destroy", "mj_adj_forward", "mj_adj_backward",
-    "mj_lfb_set_fused", "mj_lfb_step_info", "mj_mb_create", "mj_mb_destroy", "mj_mb_advance", "mj_mb_info", "mj_mb_profile", "mj_mb_phase_ms", "mj_mb_tuning", "mj_mb_set_config",
+    "mj_lfb_set_fused", "mj_lfb_step_info", "mj_lfb_profile", "mj_lfb_phase_ms", "mj_mb_create", "mj_mb_destroy", "mj_mb_advance", "mj_mb_info", "mj_mb_profile", "mj_mb_phase_ms", "mj_mb_tuning", "mj_mb_set_config",
 ]
 
 _D = ctypes.POINTER(ctypes.c_double)
@@ -124,6 +124,8 @@ def load(build_if_missing: bool = True):
     L.mj_adj_forward.argtypes = [_VP, _D]
     L.mj_adj_backward.argtypes = [_VP, _D, _D, _D]
     L.mj_lfb_set_fused.argtypes = [_VP, ctypes.c_int]
+    L.mj_lfb_profile.argtypes = [_VP, ctypes.c_int]
+    L.mj_lfb_phase_ms.argtypes = [_VP, _D]
     L.mj_lfb_step_info.argtypes = [_VP] + [ctypes.POINTER(ctypes.c_int)] * 4 + [_D]
     L.mj_mb_create.argtypes = [ctypes.c_int, ctypes.POINTER(_VP), ctypes.POINTER(_VP)]
     L.mj_mb_destroy.argtypes = [_VP]

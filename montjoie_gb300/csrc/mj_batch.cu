@@ -548,6 +548,17 @@ int mj_lfb_set_fused(mj_lfb* b, int enable) {
   return MJ_OK;
 }
 
+int mj_lfb_profile(mj_lfb* b, int enable) {
+  MJ_CHECK_ARG(b, "mj_lfb_profile: null integrator");
+  b->rs_profile = enable != 0;
+  return MJ_OK;
+}
+
+int mj_lfb_phase_ms(const mj_lfb* b, double* out) {
+  MJ_CHECK_ARG(b && out, "mj_lfb_phase_ms: null argument");
+  return lfb_phase_ms(b, out);
+}
+
 int mj_lfb_step_info(const mj_lfb* b, int* fused, int* threads, int* grid, int* n_candidates, double* candidate_ms) {
   MJ_CHECK_ARG(b, "mj_lfb_step_info: null integrator");
   if (fused) *fused = b->fused ? 1 : 0;

@@ -95,6 +95,8 @@ struct mj_lfb {
   cudaGraphExec_t rs_graph[2] = {nullptr, nullptr};
   std::vector<double> rs_tune_ms;
   std::vector<int> rs_tune_variant;
+  bool rs_profile = false;  // plain launches with per-CTA phase time stamps
+  mj::DevBuf rs_stamps;
   ~mj_lfb() {
     if (graph) cudaGraphExecDestroy(graph);
     for (auto& g : rs_graph)
@@ -139,5 +141,6 @@ int stream_grid(int n);
 int lfb_fused_setup(mj_lfb* b);
 int lfb_fused_advance(mj_lfb* b, int nsteps, double* traces, int trace_stride, bool use_graph);
 void lfb_receivers(mj_lfb* b, const float* u, int stride, int col, cudaStream_t s);
+int lfb_phase_ms(const mj_lfb* b, double* out);
 
 }  // namespace mj

@@ -126,7 +126,7 @@ __host__ __device__ __forceinline__ RsBuf rs_buf(int d0, int d1, int q0, int q1,
 template <int N, int E, int LB, int V>
 __global__ void __launch_bounds__(RsPlan<N, E, LB, V>::T)
     k_rhs_step(const RsParams p, const RsChunk* __restrict__ chunks, int n_chunks, SyncState* sync, int par,
-               int* err) {
+               int* err, unsigned long long* __restrict__ stamps) {
   using P = RsPlan<N, E, LB, V>;
   constexpr int NN = P::NN, Q = P::Q, Qp = P::Qp, W = P::W;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -145,6 +145,8 @@ __global__ void __launch_bounds__(RsPlan<N, E, LB, V>::T)
   const float* __restrict__ nxt = par == 0 ? p.ub : p.ua;  // U^{n+1}
   // step counters: ctr[1-par] = ctr[par] + 1 (phase 2 reads ctr[par] only)
   if (blockIdx.x == 0 && t == 0) p.ctr[1 - par] = p.ctr[par] + 1;
+  // optional phase time stamps of this CTA: start, phase 1 done, barrier passed, end
+  if (stamps && t == 0) stamps[4 * blockIdx.x] = global_ns();
 
   const float* __restrict__ Gm = c_gmat32[N];
   float gci[N], gcj[N], gri[N], grj[N];
@@ -260,7 +262,9 @@ __global__ void __launch_bounds__(RsPlan<N, E, LB, V>::T)
   }
 
   fence_proxy_async_global();  // this thread's R stores before the bulk copies of phase 2
+  if (stamps && t == 0) stamps[4 * blockIdx.x + 1] = global_ns();
   if (!grid_barrier(sync, err)) return;
+  if (stamps && t == 0) stamps[4 * blockIdx.x + 2] = global_ns();
 
   // ---- phase 2
   const int step = p.ctr[par];
@@ -343,6 +347,10 @@ __global__ void __launch_bounds__(RsPlan<N, E, LB, V>::T)
       issue_chunk(c + 2 * G, b);
     }
   }
+  if (stamps) {
+    __syncthreads();
+    if (t == 0) stamps[4 * blockIdx.x + 3] = global_ns();
+  }
 }
 
 // ---- variants: (n, E, LB, V) per order -------------------------------------
@@ -386,7 +394,7 @@ int rs_prepare(const RsVariant& v, int* ctas) {
 }
 
 int rs_launch(const RsVariant& v, int grid, const RsParams& prm, const RsChunk* chunks, int n_chunks,
-              SyncState* sync, int par, int* err, cudaStream_t s) {
+              SyncState* sync, int par, int* err, cudaStream_t s, unsigned long long* stamps = nullptr) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(v.threads);
@@ -399,7 +407,8 @@ int rs_launch(const RsVariant& v, int grid, const RsParams& prm, const RsChunk* 
   cfg.numAttrs = 1;
 #define MJ_X(N_, E_, LB_, V_)                                                                                \
   if (v.n == N_ && v.E == E_ && v.LB == LB_ && v.V == V_) {                                                  \
-    MJ_CUDA(cudaLaunchKernelEx(&cfg, k_rhs_step<N_, E_, LB_, V_>, prm, chunks, n_chunks, sync, par, err)); \
+    MJ_CUDA(cudaLaunchKernelEx(&cfg, k_rhs_step<N_, E_, LB_, V_>, prm, chunks, n_chunks, sync, par, err,  \
+                               stamps));                                                                     \
     count_launch();                                                                                          \
     return MJ_OK;                                                                                            \
   }
@@ -589,12 +598,16 @@ int lfb_fused_advance(mj_lfb* b, int nsteps, double* traces, int trace_stride, b
   const RsParams prm = rs_params(b, v);
   cudaStream_t s = b->stream;
   const bool diag = traces && b->n_rec;
+  const bool prof = b->rs_profile;
+  if (prof && b->rs_stamps.bytes < sizeof(unsigned long long) * 4 * b->rs_grid)
+    MJ_CUDA(b->rs_stamps.alloc(sizeof(unsigned long long) * 4 * b->rs_grid));
   auto launch = [&](int par, cudaStream_t st) {
     return rs_launch(v, b->rs_grid, prm, b->rs_chunks.as<RsChunk>(), b->rs_n_chunks, b->rs_sync.as<SyncState>(),
-                     par, b->rs_err.as<int>(), st);
+                     par, b->rs_err.as<int>(), st,
+                     prof ? b->rs_stamps.as<unsigned long long>() : (unsigned long long*)nullptr);
   };
   int done = 0;
-  if (use_graph && !diag && nsteps >= kGraphStepsRs) {
+  if (use_graph && !diag && !prof && nsteps >= kGraphStepsRs) {
     const int p0 = b->step & 1;
     if (!b->rs_graph[p0]) {
       cudaStream_t cs;
@@ -635,6 +648,32 @@ int lfb_fused_advance(mj_lfb* b, int nsteps, double* traces, int trace_stride, b
       MJ_CUDA(cudaMemcpyAsync(traces + (size_t)r * trace_stride, b->traces_d.as<double>() + (size_t)r * nsteps,
                               sizeof(double) * nsteps, cudaMemcpyDeviceToHost, s));
   return rs_check_err(b, s);
+}
+
+// Phase times (ms) of the last profiled step: element phase (last CTA,
+// mean CTA), barrier release, dof phase.
+int lfb_phase_ms(const mj_lfb* b, double* out) {
+  if (!b->rs_stamps.ptr) {
+    set_error("mj_lfb_phase_ms: no profiled step has run (mj_lfb_profile)");
+    return MJ_ERR_STATE;
+  }
+  const int grid = b->rs_grid;
+  std::vector<unsigned long long> st(4 * (size_t)grid);
+  MJ_CUDA(cudaMemcpy(st.data(), b->rs_stamps.ptr, sizeof(unsigned long long) * st.size(), cudaMemcpyDeviceToHost));
+  unsigned long long t0 = ~0ull, p1max = 0, p2 = 0, end = 0;
+  double p1sum = 0;
+  for (int c = 0; c < grid; c++) t0 = std::min(t0, st[4 * c]);
+  for (int c = 0; c < grid; c++) {
+    p1max = std::max(p1max, st[4 * c + 1]);
+    p1sum += double(st[4 * c + 1] - t0);
+    p2 = std::max(p2, st[4 * c + 2]);
+    end = std::max(end, st[4 * c + 3]);
+  }
+  out[0] = double(p1max - t0) * 1e-6;
+  out[1] = p1sum / grid * 1e-6;
+  out[2] = double(p2 - p1max) * 1e-6;
+  out[3] = double(end - p2) * 1e-6;
+  return MJ_OK;
 }
 
 }  // namespace mj

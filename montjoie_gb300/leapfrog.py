@@ -196,6 +196,15 @@ class BatchLeapFrog:
         """One cooperative kernel per step (default) or two kernels per step."""
         _lib.check(_lib.load().mj_lfb_set_fused(self._h, int(bool(enable))))
 
+    def profile(self, enable: bool) -> None:
+        """Plain launches with per-CTA phase time stamps (no graph) while enabled."""
+        _lib.check(_lib.load().mj_lfb_profile(self._h, int(bool(enable))))
+
+    def phase_ms(self) -> dict:
+        out = np.zeros(4)
+        _lib.check(_lib.load().mj_lfb_phase_ms(self._h, _lib.dptr(out)))
+        return dict(zip(["element_last", "element_mean", "barrier", "dof"], out.tolist()))
+
     def step_info(self) -> dict:
         vals = [ctypes.c_int() for _ in range(4)]
         ms = np.zeros(16)
