@@ -174,6 +174,17 @@ int mj_lf_profile(mj_lf* lf, int enable, double* elem_ms, double* update_ms, int
  * launches every kernel from the host instead.  Default: enabled. */
 int mj_lf_set_graph(mj_lf* lf, int enable);
 
+/* Time scheme of the integrator: order 2 (the leap-frog, default) or order 4,
+ * the modified-equation leap-frog of ModifiedEquationIterator with order 4
+ * (MONTJOIE/src/Instationary/ModifiedEquation.cxx:125-175 start, :346-408
+ * step; no damping term).  Order 4 takes two stiffness products per step and
+ * allows a CFL constant of 2 sqrt(3) instead of 2 (:217-225).  pulse_d2: the
+ * second time derivative of the pulse at t_n + dt for n = 0..n_pulse_d2-1
+ * (derivative order 3 of the source primitive, TimeSource.cxx:826-880), host.
+ * Call before mj_lf_init; the iterate handed out and returned is u(t_n) as
+ * for order 2. */
+int mj_lf_set_scheme(mj_lf* lf, int order, int n_pulse_d2, const double* pulse_d2);
+
 /* Sets the CUDA stream (cudaStream_t) used by the integrator's launches. */
 int mj_lf_set_stream(mj_lf* lf, void* stream);
 

@@ -59,6 +59,14 @@ struct mj_lf {
   int ev_used = 0;
   double prof_elem_ms = 0.0, prof_update_ms = 0.0;
   int prof_steps = 0;
+  // order-4 modified-equation scheme (mj_lf_set_scheme): second derivative
+  // of the pulse, scratch vectors, sources looked up per dof
+  int time_order = 2;
+  mj::DevBuf pulse3_d;
+  int n_pulse3 = 0;
+  mj::DevBuf w4, z4, d3_4;
+  mj::DevBuf src_mask, src_sidx, src_sval;
+  int n_src_sorted = 0;
   ~mj_lf() {
     for (cudaEvent_t e : ev) cudaEventDestroy(e);
     if (graph) cudaGraphExecDestroy(graph);

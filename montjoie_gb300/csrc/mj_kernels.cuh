@@ -95,6 +95,135 @@ __global__ void k_gather_init(const Real* __restrict__ R, const int* __restrict_
 }
 
 // ---------------------------------------------------------------------------
+// Order-4 modified-equation leap-frog (ModifiedEquationIterator with order 4,
+// MONTJOIE/src/Instationary/ModifiedEquation.cxx:346-408), without damping:
+// two element products per step, on U^{n+1} and on Z.  Sources are looked up
+// per dof (bit mask + sorted list) inside the gathers.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int sorted_position(const int* __restrict__ idx, int n, int d) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(idx + mid) < d) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+template <typename Real>
+__device__ __forceinline__ double source_at(const unsigned* __restrict__ mask, const int* __restrict__ sidx,
+                                            const Real* __restrict__ sval, int nsrc, int d) {
+  if (nsrc == 0 || !((__ldg(mask + (d >> 5)) >> (d & 31)) & 1u)) return 0.0;
+  return double(sval[sorted_position(sidx, nsrc, d)]);
+}
+
+// First gather of a step, pulse p = pulse[ctr[qc]]:
+//   EXACT (FP64): P = (-(A U^{n+1}) + p F) dt^2,  Z = invD P     (w <- P, z <- Z)
+//   FP32:         w = -(A U^{n+1}) + p F,         z = (dt^2/D) w
+template <typename Real, bool EXACT>
+__global__ void k_gather_o4a(const Real* __restrict__ R, const int* __restrict__ ptr, const int* __restrict__ ctr,
+                             int qc, const double* __restrict__ pulse, int n_pulse,
+                             const unsigned* __restrict__ mask, const int* __restrict__ sidx,
+                             const Real* __restrict__ sval, int nsrc, const Real* __restrict__ minv, Real dt2,
+                             Real* __restrict__ w, Real* __restrict__ z, int n_dof) {
+  const int step = ctr[qc];
+  const double p = step < n_pulse ? pulse[step] : 0.0;
+  for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < n_dof; d += gridDim.x * blockDim.x) {
+    Real s = 0;
+    const int q1 = __ldg(ptr + d + 1);
+    for (int q = __ldg(ptr + d); q < q1; q++) s += __ldg(R + q);
+    Real a = -s;
+    if (p != 0.0) {
+      const double f = source_at(mask, sidx, sval, nsrc, d);
+      if (f != 0.0) a = EXACT ? a + Real(p) * Real(f) : Real(double(a) + p * f);
+    }
+    if (EXACT) {
+      a *= dt2;
+      w[d] = a;
+      z[d] = a * __ldg(minv + d);
+    } else {
+      w[d] = a;
+      z[d] = __ldg(minv + d) * a;
+    }
+  }
+}
+
+// Second gather and the update written over u0 = U^n, pulse'' p3 = pulse3[ctr[qc]]:
+//   Y = -(A Z) + dt^2 p3 F
+//   EXACT: a = P + (dt^2/12) Y + 2 D U^{n+1} - D U^n,  U^{n+2} = invD a
+//   FP32:  U^{n+2} = 2 U^{n+1} - U^n + (dt^2/D)(w + Y/12)
+// Block 0 advances the step counter: ctr[1-qc] = ctr[qc] + 1.
+template <typename Real, bool EXACT>
+__global__ void k_gather_o4b(const Real* __restrict__ R, const int* __restrict__ ptr, int* __restrict__ ctr, int qc,
+                             const double* __restrict__ pulse3, int n_pulse3, const unsigned* __restrict__ mask,
+                             const int* __restrict__ sidx, const Real* __restrict__ sval, int nsrc,
+                             const Real* __restrict__ w, Real* __restrict__ u0, const Real* __restrict__ u1,
+                             const Real* __restrict__ mass, const Real* __restrict__ minv, Real dt2, int n_dof) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctr[1 - qc] = ctr[qc] + 1;
+  const int step = ctr[qc];
+  const double p3 = step < n_pulse3 ? pulse3[step] : 0.0;
+  for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < n_dof; d += gridDim.x * blockDim.x) {
+    Real s = 0;
+    const int q1 = __ldg(ptr + d + 1);
+    for (int q = __ldg(ptr + d); q < q1; q++) s += __ldg(R + q);
+    Real y = -s;
+    if (p3 != 0.0) {
+      const double f = source_at(mask, sidx, sval, nsrc, d);
+      if (f != 0.0) y = EXACT ? y + Real(double(dt2) * p3) * Real(f) : Real(double(y) + double(dt2) * p3 * f);
+    }
+    if (EXACT) {
+      const Real Dd = __ldg(mass + d);
+      Real a = __ldg(w + d);
+      a += (dt2 / Real(12)) * y;
+      a += Real(2) * Dd * __ldg(u1 + d);
+      a += -Dd * u0[d];
+      u0[d] = a * __ldg(minv + d);
+    } else {
+      u0[d] = Real(2) * __ldg(u1 + d) - u0[d] + __ldg(minv + d) * (__ldg(w + d) + y * Real(1.0 / 12));
+    }
+  }
+}
+
+// out = invD * (-(A x)): the second and third time derivatives of the
+// order-4 start (SetInitialConditionS, ModifiedEquation.cxx:142-157).
+template <typename Real>
+__global__ void k_gather_scaled(const Real* __restrict__ R, const int* __restrict__ ptr,
+                                const double* __restrict__ inv_mass, Real* __restrict__ out, int n_dof) {
+  for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < n_dof; d += gridDim.x * blockDim.x) {
+    Real s = 0;
+    const int q1 = __ldg(ptr + d + 1);
+    for (int q = __ldg(ptr + d); q < q1; q++) s += __ldg(R + q);
+    out[d] = Real(double(-s) * inv_mass[d]);
+  }
+}
+
+// U^1 of the order-4 start in the reference's Horner form
+// (ModifiedEquation.cxx:159-163): d4 = invD(-(A d2)),
+// U^1 = U^0 + dt(du0 + dt(d2/2 + dt(d3/6 + dt d4/24))).
+template <typename Real>
+__global__ void k_gather_o4_init(const Real* __restrict__ R, const int* __restrict__ ptr,
+                                 const double* __restrict__ inv_mass, const Real* __restrict__ u0,
+                                 const Real* __restrict__ du0, const Real* __restrict__ d2,
+                                 const Real* __restrict__ d3, double dt, Real* __restrict__ u1, int n_dof) {
+  for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < n_dof; d += gridDim.x * blockDim.x) {
+    Real s = 0;
+    const int q1 = __ldg(ptr + d + 1);
+    for (int q = __ldg(ptr + d); q < q1; q++) s += __ldg(R + q);
+    const double d4 = double(-s) * inv_mass[d];
+    double v = d4 * (1.0 / 24);
+    v *= dt;
+    v += (d3 ? double(d3[d]) : 0.0) * (1.0 / 6);
+    v *= dt;
+    v += double(d2[d]) * (1.0 / 2);
+    v *= dt;
+    v += du0 ? double(du0[d]) : 0.0;
+    v *= dt;
+    v += double(u0[d]);
+    u1[d] = Real(v);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // K3: weighted norm sum_i M_i u_i^2 in FP64 (GetNormeSolution,
 // VarInstationary.cxx:2696-2745, with M_i the J*w summed over the points on
 // dof i).  Two passes, fixed summation order (deterministic).

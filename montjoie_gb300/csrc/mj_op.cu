@@ -486,11 +486,33 @@ int lf_init_impl(mj_lf* lf, const double* u0, const double* du0) {
     if (rc) return rc;
     du0_d = lf->du0.as<Real>();
   }
-  launch_k1<Real>(op, lf->ua.ptr, s);
-  k_gather_init<Real><<<stream_grid(n), 256, 0, s>>>(op->R.as<Real>(), op->ptr.as<int>(),
-                                                      lf->ua.as<Real>(), du0_d, lf->inv_mass64.as<double>(),
-                                                      lf->dt, lf->ub.as<Real>(), n);
-  count_launch();
+  if (lf->time_order == 4) {
+    // order-4 start (SetInitialConditionS, ModifiedEquation.cxx:125-175):
+    // d2 = invD(-A u0), d3 = invD(-A du0), then U^1 by the Taylor step with
+    // d4 = invD(-A d2)
+    launch_k1<Real>(op, lf->ua.ptr, s);
+    k_gather_scaled<Real><<<stream_grid(n), 256, 0, s>>>(op->R.as<Real>(), op->ptr.as<int>(),
+                                                          lf->inv_mass64.as<double>(), lf->z4.as<Real>(), n);
+    const Real* d3 = nullptr;
+    if (du0_d) {
+      launch_k1<Real>(op, du0_d, s);
+      k_gather_scaled<Real><<<stream_grid(n), 256, 0, s>>>(op->R.as<Real>(), op->ptr.as<int>(),
+                                                            lf->inv_mass64.as<double>(), lf->d3_4.as<Real>(), n);
+      d3 = lf->d3_4.as<Real>();
+      count_launch();
+    }
+    launch_k1<Real>(op, lf->z4.ptr, s);
+    k_gather_o4_init<Real><<<stream_grid(n), 256, 0, s>>>(op->R.as<Real>(), op->ptr.as<int>(),
+                                                           lf->inv_mass64.as<double>(), lf->ua.as<Real>(), du0_d,
+                                                           lf->z4.as<Real>(), d3, lf->dt, lf->ub.as<Real>(), n);
+    count_launch(2);
+  } else {
+    launch_k1<Real>(op, lf->ua.ptr, s);
+    k_gather_init<Real><<<stream_grid(n), 256, 0, s>>>(op->R.as<Real>(), op->ptr.as<int>(),
+                                                        lf->ua.as<Real>(), du0_d, lf->inv_mass64.as<double>(),
+                                                        lf->dt, lf->ub.as<Real>(), n);
+    count_launch();
+  }
   MJ_CUDA(cudaGetLastError());
   lf->cur_is_a = true;
   lf->step = 0;
@@ -528,8 +550,43 @@ int lf_diag(mj_lf* lf, double* norms_d, int norm_col, double* traces_d, int stri
 // counters are back in their roles after each replay).
 constexpr int kGraphSteps = 20;
 
+// Kernels one step launches (launch accounting of graph replays).
+int lf_kernels_per_step(const mj_lf* lf) { return lf->time_order == 4 ? 4 : 2 + (lf->n_src > 0); }
+
+// One order-4 step: element product of U^{n+1}, first gather (P, Z),
+// element product of Z, second gather + update over U^n.
+template <typename Real>
+void lf_step4_launch(mj_lf* lf, void* cur, const void* next, int qc, cudaStream_t s, bool prof) {
+  mj_op* op = lf->op;
+  const int n = lf->n_dof;
+  const Real dt2 = Real(lf->dt * lf->dt);
+  constexpr bool EXACT = sizeof(Real) == 8;
+  if (prof) cudaEventRecord(lf->ev[lf->ev_used], s);
+  launch_k1<Real>(op, next, s);
+  if (prof) cudaEventRecord(lf->ev[lf->ev_used + 1], s);
+  k_gather_o4a<Real, EXACT><<<stream_grid(n), 256, 0, s>>>(
+      op->R.as<Real>(), op->ptr.as<int>(), lf->ctr.as<int>(), qc, lf->pulse_d.as<double>(), lf->n_pulse,
+      lf->src_mask.as<unsigned>(), lf->src_sidx.as<int>(), lf->src_sval.as<Real>(), lf->n_src_sorted,
+      lf->minv.as<Real>(), dt2, lf->w4.as<Real>(), lf->z4.as<Real>(), n);
+  launch_k1<Real>(op, lf->z4.ptr, s);
+  k_gather_o4b<Real, EXACT><<<stream_grid(n), 256, 0, s>>>(
+      op->R.as<Real>(), op->ptr.as<int>(), lf->ctr.as<int>(), qc, lf->pulse3_d.as<double>(), lf->n_pulse3,
+      lf->src_mask.as<unsigned>(), lf->src_sidx.as<int>(), lf->src_sval.as<Real>(), lf->n_src_sorted,
+      lf->w4.as<Real>(), static_cast<Real*>(cur), static_cast<const Real*>(next),
+      EXACT ? lf->mass.as<Real>() : nullptr, lf->minv.as<Real>(), dt2, n);
+  count_launch(2);
+  if (prof) {
+    cudaEventRecord(lf->ev[lf->ev_used + 2], s);
+    lf->ev_used += 3;
+  }
+}
+
 template <typename Real>
 void lf_step_launch(mj_lf* lf, void* cur, const void* next, int qc, cudaStream_t s, bool prof) {
+  if (lf->time_order == 4) {
+    lf_step4_launch<Real>(lf, cur, next, qc, s, prof);
+    return;
+  }
   mj_op* op = lf->op;
   const int n = lf->n_dof;
   if (prof) cudaEventRecord(lf->ev[lf->ev_used], s);
@@ -629,7 +686,7 @@ int lf_advance_impl(mj_lf* lf, int nsteps, double* norms, double* traces, int st
     }
     while (nsteps - s0 >= kGraphSteps) {
       MJ_CUDA(cudaGraphLaunch(lf->graph, lf->stream));
-      count_launch((uint64_t)kGraphSteps * (2 + (lf->n_src > 0)));
+      count_launch((uint64_t)kGraphSteps * lf_kernels_per_step(lf));
       s0 += kGraphSteps;
       lf->step += kGraphSteps;
     }
@@ -730,6 +787,57 @@ int mj_lf_run(mj_lf* lf, const double* u0, const double* du0, int nsteps, double
                                     : lf_advance_impl<float>(lf, nsteps, norms, traces, trace_stride, true);
   if (rc) return rc;
   if (u_final) return mj_lf_get_state(lf, u_final, nullptr);
+  return MJ_OK;
+}
+
+int mj_lf_set_scheme(mj_lf* lf, int order, int n_pulse_d2, const double* pulse_d2) {
+  MJ_CHECK_ARG(lf, "mj_lf_set_scheme: null integrator");
+  MJ_CHECK_ARG(order == 2 || order == 4, "mj_lf_set_scheme: order must be 2 or 4");
+  MJ_CHECK_ARG(order == 2 || n_pulse_d2 == 0 || pulse_d2, "mj_lf_set_scheme: null pulse_d2");
+  MJ_CHECK_ARG(n_pulse_d2 >= 0, "mj_lf_set_scheme: negative n_pulse_d2");
+  for (cudaGraphExec_t* g : {&lf->graph, &lf->graph_prof})
+    if (*g) {
+      cudaGraphExecDestroy(*g);
+      *g = nullptr;
+    }
+  lf->initialised = false;
+  lf->time_order = order;
+  if (order == 2) return MJ_OK;
+  const int n = lf->n_dof;
+  const size_t esz = elem_size(lf->op->precision);
+  MJ_CUDA(lf->w4.alloc(esz * n));
+  MJ_CUDA(lf->z4.alloc(esz * n));
+  MJ_CUDA(lf->d3_4.alloc(esz * n));
+  lf->n_pulse3 = n_pulse_d2;
+  MJ_CUDA(lf->pulse3_d.alloc(sizeof(double) * std::max(1, n_pulse_d2)));
+  if (n_pulse_d2)
+    MJ_CUDA(cudaMemcpy(lf->pulse3_d.ptr, pulse_d2, sizeof(double) * n_pulse_d2, cudaMemcpyHostToDevice));
+  // sources sorted by dof with a per-dof bit mask (looked up inside the gathers)
+  const int ns = lf->n_src, words = (n + 31) / 32;
+  std::vector<int> idx(std::max(1, ns));
+  std::vector<unsigned char> val(esz * std::max(1, ns));
+  if (ns) {
+    MJ_CUDA(cudaMemcpy(idx.data(), lf->src_idx.ptr, sizeof(int) * ns, cudaMemcpyDeviceToHost));
+    MJ_CUDA(cudaMemcpy(val.data(), lf->src_val.ptr, esz * ns, cudaMemcpyDeviceToHost));
+  }
+  std::vector<int> order_(ns);
+  for (int t = 0; t < ns; t++) order_[t] = t;
+  std::sort(order_.begin(), order_.end(), [&](int a, int b) { return idx[a] < idx[b]; });
+  std::vector<int> si(std::max(1, ns), 0);
+  std::vector<unsigned char> sv(esz * std::max(1, ns), 0);
+  std::vector<unsigned> mask(std::max(1, words), 0u);
+  for (int t = 0; t < ns; t++) {
+    si[t] = idx[order_[t]];
+    std::memcpy(&sv[esz * t], &val[esz * order_[t]], esz);
+    mask[si[t] >> 5] |= 1u << (si[t] & 31);
+  }
+  MJ_CUDA(lf->src_sidx.alloc(sizeof(int) * si.size()));
+  MJ_CUDA(lf->src_sval.alloc(sv.size()));
+  MJ_CUDA(lf->src_mask.alloc(sizeof(unsigned) * mask.size()));
+  MJ_CUDA(cudaMemcpy(lf->src_sidx.ptr, si.data(), sizeof(int) * si.size(), cudaMemcpyHostToDevice));
+  MJ_CUDA(cudaMemcpy(lf->src_sval.ptr, sv.data(), sv.size(), cudaMemcpyHostToDevice));
+  MJ_CUDA(cudaMemcpy(lf->src_mask.ptr, mask.data(), sizeof(unsigned) * mask.size(), cudaMemcpyHostToDevice));
+  lf->n_src_sorted = ns;
   return MJ_OK;
 }
 

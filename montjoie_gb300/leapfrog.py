@@ -22,7 +22,11 @@ from .operator import FemMatrixFreeOperator
 
 class LeapFrogIterator:
     def __init__(self, op: FemMatrixFreeOperator, dt: float, mass: np.ndarray, inv_mass: np.ndarray | None = None,
-                 src_idx=None, src_val=None, pulse=None, norm_weight=None, rec_idx=None, rec_w=None):
+                 src_idx=None, src_val=None, pulse=None, norm_weight=None, rec_idx=None, rec_w=None,
+                 time_order: int = 2, pulse_d2=None):
+        """time_order = 4 selects the modified-equation leap-frog of order 4
+        (ModifiedEquation.cxx:125-175, 346-408); pulse_d2 is then the second
+        time derivative of the pulse at t_n + dt."""
         L = _lib.load()
         self.op = op
         self.dt = float(dt)
@@ -63,6 +67,10 @@ class LeapFrogIterator:
         _lib.check(L.mj_lf_create(op.handle, ctypes.byref(desc), ctypes.byref(handle)))
         self._h = handle
         self.n_time = 0
+        self.time_order = int(time_order)
+        if self.time_order != 2:
+            p2 = f(pulse_d2)
+            _lib.check(L.mj_lf_set_scheme(self._h, self.time_order, 0 if p2 is None else int(p2.size), _lib.dptr(p2)))
 
     @property
     def handle(self):

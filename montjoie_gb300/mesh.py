@@ -164,6 +164,7 @@ class AcousticSetup:
     t0: float = 0.0
     nsteps: int = 200
     print_level: int = 0
+    time_order: int = 2   # 2: leap-frog; 4: modified-equation leap-frog (OrderTimeScheme = 4 LEAP_FROG)
 
     @property
     def tf(self) -> float:
@@ -199,7 +200,7 @@ def write_deck(path: str, mesh_file: str, mesh: HexMesh, setup: AcousticSetup) -
         "ElectricOrMagnetic = 0",
         f"TimeStep = {setup.dt:.17g}",
         f"TimeInterval = {setup.t0:.17g} {setup.tf:.17g}",
-        "OrderTimeScheme = 2 LEAP_FROG",
+        f"OrderTimeScheme = {setup.time_order} LEAP_FROG",
         f"PrintLevel = {setup.print_level}",
     ]
     with open(path, "w") as f:

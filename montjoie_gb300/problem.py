@@ -124,10 +124,13 @@ def ricker_primitive(f0: float, t: np.ndarray) -> np.ndarray:
     return np.where((t <= -0.9 / f0) | (t >= 2.9 / f0), 0.0, v)
 
 
-def ricker_pulse(f0: float, t_init: float, dt: float, nsteps: int, eps_time: float, tlimit: float | None = None):
-    """p(t_n + dt) for n = 0..nsteps-1: spectral derivative of the degree-24
-    Gauss-Lobatto interpolant of the Ricker primitive on windows of length
-    0.5/f0 (TimeSourceHyperbolic, TimeSource.cxx:798-880); zero from
+def ricker_pulse(f0: float, t_init: float, dt: float, nsteps: int, eps_time: float, tlimit: float | None = None,
+                 nb_deriv: int = 1):
+    """Derivative nb_deriv of the source primitive at t_n + dt for
+    n = 0..nsteps-1 (1: the pulse p; 3: its second derivative p''): spectral
+    derivative of the degree-24 Gauss-Lobatto interpolant of the Ricker
+    primitive on windows of length 0.5/f0, the derivative matrix applied
+    nb_deriv times (TimeSourceHyperbolic, TimeSource.cxx:826-880); zero from
     tlimit = 2.5/f0 on (VarInstationary.cxx:2392-2396)."""
     if tlimit is None:
         tlimit = 2.5 / f0
@@ -143,8 +146,9 @@ def ricker_pulse(f0: float, t_init: float, dt: float, nsteps: int, eps_time: flo
                 t0, t1 = t1, t1 + (t1 - t0)
             der = None
         if der is None:
-            val = ricker_primitive(f0, (1.0 - pts) * t0 + pts * t1)
-            der = (G.T @ val) * (1.0 / (t1 - t0))
+            der = ricker_primitive(f0, (1.0 - pts) * t0 + pts * t1)
+            for _ in range(nb_deriv):
+                der = (G.T @ der) * (1.0 / (t1 - t0))
         p = float(lagrange_values(pts, (t - t0) / (t1 - t0)) @ der)
         out[s] = 0.0 if t >= tlimit else p
     return out
@@ -281,6 +285,10 @@ class AcousticProblem:
         self.setup.dt, self.setup.nsteps = float(dt), int(nsteps)
         eps_time = (self.setup.tf - self.setup.t0) * 1e-15
         self.pulse = ricker_pulse(self.setup.f0, self.setup.t0, self.setup.dt, self.setup.nsteps, eps_time)
+        self.pulse_d2 = None
+        if self.setup.time_order == 4:
+            self.pulse_d2 = ricker_pulse(self.setup.f0, self.setup.t0, self.setup.dt, self.setup.nsteps, eps_time,
+                                         nb_deriv=3)
 
     def operator(self, precision: str = "fp64") -> FemMatrixFreeOperator:
         return FemMatrixFreeOperator(self.order, self.nodle, self.factors, self.n_dof, precision)
@@ -288,13 +296,15 @@ class AcousticProblem:
     def integrator(self, op: FemMatrixFreeOperator, diagnostics: bool = True) -> LeapFrogIterator:
         return LeapFrogIterator(op, self.setup.dt, self.mass, None, self.src_idx, self.src_val, self.pulse,
                                 self.norm_weight if diagnostics else None,
-                                self.rec_idx if diagnostics else None, self.rec_w if diagnostics else None)
+                                self.rec_idx if diagnostics else None, self.rec_w if diagnostics else None,
+                                time_order=self.setup.time_order, pulse_d2=self.pulse_d2)
 
 
 def cfl_time_step(pb: AcousticProblem, safety: float = 0.5, iters: int = 40, seed: int = 0) -> float:
-    """dt = safety * 2 / sqrt(lambda_max(D^-1 A)): leap-frog CFL constant 2
-    (ModifiedEquation.cxx:217-225); lambda_max by power iteration with the GPU
-    operator (the reference needs ARPACK/SLEPc for TimeStep = AUTO)."""
+    """dt = safety * C / sqrt(lambda_max(D^-1 A)) with the scheme's CFL
+    constant C = 2 (order 2) or 2 sqrt(3) (order 4) (ModifiedEquation.cxx:217-225);
+    lambda_max by power iteration with the GPU operator (the reference needs
+    ARPACK/SLEPc for TimeStep = AUTO)."""
     op = pb.operator("fp32")
     rng = np.random.default_rng(seed)
     x = rng.uniform(-1.0, 1.0, pb.n_dof)
@@ -308,4 +318,5 @@ def cfl_time_step(pb: AcousticProblem, safety: float = 0.5, iters: int = 40, see
         lam = nrm / np.linalg.norm(x)
         x = y / nrm
     op.close()
-    return safety * 2.0 / math.sqrt(lam * 1.05)
+    c = 2.0 if pb.setup.time_order == 2 else 2.0 * math.sqrt(3.0)
+    return safety * c / math.sqrt(lam * 1.05)

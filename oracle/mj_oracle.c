@@ -331,8 +331,16 @@ static double ricker_primitive(double f0, double t) {
  * differentiated with the GL derivative matrix, and the derivative is
  * interpolated; the window jumps forward when t > t1 + eps_time.  No pulse
  * at or after tlimit = 2.5/f0 (AddScalarSourceAtTime, VarInstationary.cxx:2392-2396). */
-void oc_ricker_pulse(double f0, double t_init, double dt, int nsteps, double eps_time,
-                     double tlimit, double* pulse) {
+/* Derivative number nb_deriv of the Ricker primitive at t_n + dt, n = 0..nsteps-1
+ * (TimeSourceHyperbolic::GenerateValues / EvaluateDerivative,
+ * MONTJOIE/src/Source/TimeSource.cxx:826-880): degree-24 Gauss-Lobatto
+ * interpolant of the primitive on windows [t0, t0 + 0.5/f0], derivative values
+ * at the nodes obtained by applying the derivative matrix nb_deriv times
+ * (each level scaled by 1/(t1-t0)), the window moved on when t > t1 + eps;
+ * zero from tlimit on (VarInstationary.cxx:2392-2396).  nb_deriv = 1 is the
+ * pulse p, 3 its second derivative. */
+void oc_ricker_pulse_deriv(double f0, double t_init, double dt, int nsteps, double eps_time, double tlimit,
+                           int nb_deriv, double* pulse) {
   enum { R = 24, N = 25 };
   double pts[N], wts[N], G[N * N], val[N], der[N], phi[N];
   oc_gauss_lobatto(R, pts, wts);
@@ -350,18 +358,26 @@ void oc_ricker_pulse(double f0, double t_init, double dt, int nsteps, double eps
     }
     if (!have) {
       for (int i = 0; i < N; i++) val[i] = ricker_primitive(f0, (1.0 - pts[i]) * t0 + pts[i] * t1);
-      for (int j = 0; j < N; j++) {
-        double acc = 0.0;
-        for (int k = 0; k < N; k++) acc += G[k * N + j] * val[k];
-        der[j] = acc * (1.0 / (t1 - t0));
+      for (int m = 0; m < nb_deriv; m++) {
+        for (int j = 0; j < N; j++) {
+          double acc = 0.0;
+          for (int k = 0; k < N; k++) acc += G[k * N + j] * val[k];
+          der[j] = acc * (1.0 / (t1 - t0));
+        }
+        memcpy(val, der, sizeof(val));
       }
       have = 1;
     }
     lagrange_values(N, pts, (t - t0) / (t1 - t0), phi);
     double p = 0.0;
-    for (int i = 0; i < N; i++) p += phi[i] * der[i];
+    for (int i = 0; i < N; i++) p += phi[i] * val[i];
     pulse[s] = (t >= tlimit) ? 0.0 : p;
   }
+}
+
+void oc_ricker_pulse(double f0, double t_init, double dt, int nsteps, double eps_time,
+                     double tlimit, double* pulse) {
+  oc_ricker_pulse_deriv(f0, t_init, dt, nsteps, eps_time, tlimit, 1, pulse);
 }
 
 /* Gaussian amplitude g(x) = beta exp(-alpha r^2) for r < R, alpha = -ln(1e-6)/R^2,
@@ -439,6 +455,87 @@ void oc_leapfrog(int r, int ne, int ndof, const int* nodle, const int* num, cons
     }
   }
   free(ah);
+}
+
+/* Order-4 modified-equation leap-frog (ModifiedEquationIterator with
+ * order 4, MONTJOIE/src/Instationary/ModifiedEquation.cxx), without damping
+ * (Sh = 0: Neumann boundaries, no absorbing layer), in the reference's
+ * operation order.
+ * Start (SetInitialConditionS :125-175): U1 = u0 and the Taylor step
+ *   d2 = invD(-A u0), d3 = invD(-A du0), d4 = invD(-A d2),
+ *   U2 = U1 + dt(du0 + dt(d2/2 + dt(d3/6 + dt d4/24)))   (Horner, as there).
+ * Step n (Advance :346-408; the dU/dt and d^3U/dt^3 terms only enter
+ * through Sh and vanish):
+ *   P = -A U2;  P += p_n F;  P *= dt^2;   Z = invD P;
+ *   Y = -A Z;   Y += dt^2 p''_n F;        P += dt^2/12 Y;
+ *   P += 2 D U2;  P += -D U1;   U1 <- U2;  U2 <- invD P.
+ * The iterate handed out at loop index n is U1 (GetIterate).  On return
+ * u0 = U1 = U^{nsteps} and u1 = U2 = U^{nsteps+1}; norms / traces as in
+ * oc_leapfrog. */
+void oc_leapfrog4(int r, int ne, int ndof, const int* nodle, const int* num, const double* G,
+                  const double* bh, const double* D, const double* invD, int nsrc,
+                  const int* src_idx, const double* src_val, const double* pulse, const double* pulse3,
+                  double dt, int nsteps, double* u0, const double* du0, double* u1, const double* jw,
+                  double* norms, int nrec, const int* rec_idx, const double* rec_w, double* traces,
+                  int ncolors, const int* color_ptr, const int* color_elems) {
+  int n = r + 1, Q = n * n * n;
+  (void)n;
+  double dt2 = dt * dt;
+  size_t bytes = sizeof(double) * (size_t)ndof;
+  double* U1 = (double*)malloc(bytes);
+  double* U2 = (double*)malloc(bytes);
+  double* P = (double*)malloc(bytes);
+  double* Z = (double*)malloc(bytes);
+  double* d3 = (double*)calloc((size_t)ndof, sizeof(double));
+  memcpy(U1, u0, bytes);
+  /* d2 = invD(-A U0) */
+  oc_stiffness_mltadd(r, ne, ndof, nodle, num, G, bh, -1.0, u0, 0.0, Z, ncolors, color_ptr, color_elems);
+  for (int i = 0; i < ndof; i++) Z[i] *= invD[i];
+  /* d3 = invD(-A du0) */
+  if (du0) {
+    oc_stiffness_mltadd(r, ne, ndof, nodle, num, G, bh, -1.0, du0, 0.0, d3, ncolors, color_ptr, color_elems);
+    for (int i = 0; i < ndof; i++) d3[i] *= invD[i];
+  }
+  /* d4 = invD(-A d2) */
+  oc_stiffness_mltadd(r, ne, ndof, nodle, num, G, bh, -1.0, Z, 0.0, P, ncolors, color_ptr, color_elems);
+  for (int i = 0; i < ndof; i++) P[i] *= invD[i];
+  for (int i = 0; i < ndof; i++) {
+    double d4 = P[i] * (1.0 / 24), e3 = d3[i] * (1.0 / 6), e2 = Z[i] * (1.0 / 2);
+    double v = d4;
+    v *= dt; v += e3; v *= dt; v += e2; v *= dt; v += du0 ? du0[i] : 0.0; v *= dt; v += U1[i];
+    U2[i] = v;
+  }
+  for (int s = 0; s <= nsteps; s++) {
+    if (norms) norms[s] = oc_norm(ne, Q, nodle, jw, U1);
+    if (traces)
+      for (int k = 0; k < nrec; k++) {
+        double acc = 0.0;
+        for (int t = 0; t < Q; t++) acc += rec_w[(size_t)k * Q + t] * U1[rec_idx[(size_t)k * Q + t]];
+        traces[(size_t)k * (nsteps + 1) + s] = acc;
+      }
+    if (s == nsteps) break;
+    oc_stiffness_mltadd(r, ne, ndof, nodle, num, G, bh, -1.0, U2, 0.0, P, ncolors, color_ptr, color_elems);
+    double p = pulse ? pulse[s] : 0.0;
+    if (p != 0.0)
+      for (int t = 0; t < nsrc; t++) P[src_idx[t]] += p * src_val[t];
+    for (int i = 0; i < ndof; i++) P[i] *= dt2;
+    for (int i = 0; i < ndof; i++) Z[i] = P[i] * invD[i];
+    oc_stiffness_mltadd(r, ne, ndof, nodle, num, G, bh, -1.0, Z, 0.0, d3, ncolors, color_ptr, color_elems);
+    double p3 = pulse3 ? dt2 * pulse3[s] : 0.0;
+    if (p3 != 0.0)
+      for (int t = 0; t < nsrc; t++) d3[src_idx[t]] += p3 * src_val[t];
+    for (int i = 0; i < ndof; i++) {
+      double a = P[i];
+      a += (dt2 / 12) * d3[i];
+      a += 2.0 * D[i] * U2[i];
+      a += -D[i] * U1[i];
+      U1[i] = U2[i];
+      U2[i] = a * invD[i];
+    }
+  }
+  memcpy(u0, U1, bytes);
+  memcpy(u1, U2, bytes);
+  free(U1); free(U2); free(P); free(Z); free(d3);
 }
 
 /* ------------------------------------------------------------ receivers */

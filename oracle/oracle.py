@@ -48,6 +48,11 @@ def lib():
                                           ctypes.c_double, _D, ctypes.c_double, _D, ctypes.c_int, _I, _I]
         L.oc_ricker_pulse.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                       ctypes.c_double, ctypes.c_double, _D]
+        L.oc_ricker_pulse_deriv.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                            ctypes.c_double, ctypes.c_double, ctypes.c_int, _D]
+        L.oc_leapfrog4.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _I, _D, _D, _D, _D,
+                                   ctypes.c_int, _I, _D, _D, _D, ctypes.c_double, ctypes.c_int, _D, _D, _D,
+                                   _D, _D, ctypes.c_int, _I, _D, _D, ctypes.c_int, _I, _I]
         L.oc_gaussian_source.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _D, _D, _D,
                                          ctypes.c_double, _D]
         L.oc_norm.argtypes = [ctypes.c_int, ctypes.c_int, _I, _D, _D]
@@ -164,11 +169,13 @@ def stiffness_mltadd(r, nodle, bh, alpha, x, beta, y, colors=None):
     return y
 
 
-def ricker_pulse(f0, t_init, dt, nsteps, eps_time, tlimit=None):
+def ricker_pulse(f0, t_init, dt, nsteps, eps_time, tlimit=None, nb_deriv=1):
+    """Derivative nb_deriv of the interpolated Ricker primitive at t_n + dt (1: the pulse)."""
     if tlimit is None:
         tlimit = 2.5 / f0
     out = np.zeros(nsteps)
-    lib().oc_ricker_pulse(float(f0), float(t_init), float(dt), int(nsteps), float(eps_time), float(tlimit), _p(out))
+    lib().oc_ricker_pulse_deriv(float(f0), float(t_init), float(dt), int(nsteps), float(eps_time), float(tlimit),
+                                int(nb_deriv), _p(out))
     return out
 
 
@@ -214,6 +221,32 @@ def leapfrog(r, nodle, bh, D, invD, src_idx, src_val, pulse, dt, nsteps, u0, u1=
                       _p(None if rec_idx is None else i32(rec_idx), _I), _p(None if rec_w is None else f64(rec_w)),
                       _p(traces), nc, _p(None if ptr is None else i32(ptr), _I),
                       _p(None if elems is None else i32(elems), _I))
+    return u0, u1, norms, traces
+
+
+def leapfrog4(r, nodle, bh, D, invD, src_idx, src_val, pulse, pulse3, dt, nsteps, u0, du0=None, jw=None,
+              rec_idx=None, rec_w=None, colors=None):
+    """Run the reference's order-4 modified-equation leap-frog on the CPU.
+    Returns (u_N, u_{N+1}, norms, traces)."""
+    ne, Q = nodle.shape
+    ndof = D.size
+    G = grad_matrix(r).ravel().copy()
+    num = hex_numbering(r)
+    u0 = f64(u0).copy()
+    u1 = np.zeros(ndof)
+    norms = np.zeros(nsteps + 1) if jw is not None else None
+    nrec = 0 if rec_idx is None else rec_idx.shape[0]
+    traces = np.zeros((nrec, nsteps + 1)) if nrec else None
+    ptr, elems = (None, None) if colors is None else colors
+    nc = 0 if colors is None else len(ptr) - 1
+    lib().oc_leapfrog4(r, ne, ndof, _p(i32(nodle), _I), _p(num, _I), _p(G), _p(f64(bh)), _p(f64(D)), _p(f64(invD)),
+                       int(len(src_idx)), _p(i32(src_idx), _I), _p(f64(src_val)),
+                       _p(None if pulse is None else f64(pulse)), _p(None if pulse3 is None else f64(pulse3)),
+                       float(dt), int(nsteps), _p(u0), _p(None if du0 is None else f64(du0)), _p(u1),
+                       _p(None if jw is None else f64(jw)), _p(norms), nrec,
+                       _p(None if rec_idx is None else i32(rec_idx), _I), _p(None if rec_w is None else f64(rec_w)),
+                       _p(traces), nc, _p(None if ptr is None else i32(ptr), _I),
+                       _p(None if elems is None else i32(elems), _I))
     return u0, u1, norms, traces
 
 
@@ -267,7 +300,7 @@ def load_dump(outdir: str) -> dict:
     shapes = {
         "nodle.i32": (ne, Q), "verts.f64": (ne, 8, 3), "elem_ref.i32": (ne,), "affine.i32": (ne,),
         "variable.i32": (ne,), "bh.f64": (ne, Q, 6), "jw.f64": (ne, Q), "massD.f64": (ndof,),
-        "invD.f64": (ndof,), "src_idx.i32": (-1,), "src_val.f64": (-1,), "pulse.f64": (-1,),
+        "invD.f64": (ndof,), "src_idx.i32": (-1,), "src_val.f64": (-1,), "pulse.f64": (-1,), "pulse3.f64": (-1,),
         "points1d.f64": (r + 1,), "weights1d.f64": (r + 1,), "gradphi.f64": (r + 1, r + 1),
         "numdofs3d.i32": ((r + 1) ** 3,), "kh_y.f64": (ndof,), "kh_ax.f64": (ndof,),
         "norms.f64": (-1,), "times.f64": (-1,), "u_final.f64": (ndof,),

@@ -13,7 +13,8 @@
 //   - Glob_jacobian (J*w per point, VarGeometryProblem.cxx:706-709),
 //   - the lumped mass D and its inverse (TimeAcoustic.cxx:889-1000),
 //   - the sparse source vector F (VarInstationary.cxx:620-676),
-//   - the pulse p(t+dt) of every step (TimeSource.cxx:778-880),
+//   - the pulse p(t+dt) of every step and its second derivative
+//     (TimeSource.cxx:778-880),
 //   - y = beta*y0 + alpha*Kh*x for a caller-given x (FemMatrixFreeClass.cxx:953),
 //   - the "Norme solution" of every iterate (VarInstationary.cxx:2696-2745),
 //   - selected iterates u^n.
@@ -185,6 +186,22 @@ class DumpingProblem : public HyperbolicProblem<AcousticEquation<Dimension3> > {
         pulse[n] = (t >= this->tlimit_source) ? 0.0 : p;
       }
       write_raw(outdir + "/pulse.f64", pulse.data(), pulse.size());
+    }
+    {
+      // d^2 p / dt^2 at the same times (derivative order 3 of the primitive),
+      // which the order-4 modified-equation step adds as dt^2 p'' F
+      // (ModifiedEquation.cxx:381-385)
+      TimeSourceHyperbolic ts;
+      VirtualTimeSource<Real_wp>* fsrc = this->GetNewTimeSource();
+      ts.Init(fsrc, pb.GetFrequency(), this->epsilon_time, t0);
+      std::vector<double> pulse3(nsteps);
+      for (int n = 0; n < nsteps; n++) {
+        double t = t0 + n * dt + dt;
+        Real_wp p = 0;
+        ts.EvaluateDerivative(t, 3, p);
+        pulse3[n] = (t >= this->tlimit_source) ? 0.0 : p;
+      }
+      write_raw(outdir + "/pulse3.f64", pulse3.data(), pulse3.size());
     }
 
     // Operator product y = beta*y0 + alpha*Kh*x through the reference's

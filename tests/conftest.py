@@ -11,6 +11,8 @@ if ROOT not in sys.path:
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 SMALL_CASES = ["regular2_q4", "cube2_q1", "cube2_q2", "cube2_q3", "cube3_q4", "cube2_q6", "cube2_q8", "cube4_q4"]
+# the same kind of runs with the order-4 modified-equation leap-frog
+ORDER4_CASES = ["cube2_q2_o4", "cube3_q4_o4", "cube2_q8_o4"]
 
 
 def pytest_configure(config):
@@ -24,6 +26,11 @@ def load_golden(name):
 
 @pytest.fixture(params=SMALL_CASES)
 def golden_case(request):
+    return request.param, load_golden(request.param)
+
+
+@pytest.fixture(params=ORDER4_CASES)
+def golden_case4(request):
     return request.param, load_golden(request.param)
 
 

@@ -25,7 +25,7 @@ from oracle import oracle as oc  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
 
-# name: (cells per axis, order, perturbation kind, amplitude, c_mode, steps, source radius, snaps)
+# name: (cells per axis, order, perturbation kind, amplitude, c_mode, steps, source radius, snaps[, time order])
 CASES = {
     "regular2_q4": (2, 4, "none", 0.0, "constant", 30, 0.35, (0, 30)),
     "cube2_q1": (2, 1, "random", 0.1, "element", 40, 0.45, (0, 40)),
@@ -35,20 +35,25 @@ CASES = {
     "cube2_q6": (2, 6, "random", 0.1, "element", 40, 0.3, (0, 40)),
     "cube2_q8": (2, 8, "sin", 0.1, "smooth", 30, 0.3, (0, 30)),
     "cube4_q4": (4, 4, "random", 0.05, "element", 200, 0.25, (0, 100, 200)),
+    # order-4 modified-equation leap-frog (OrderTimeScheme = 4 LEAP_FROG)
+    "cube3_q4_o4": (3, 4, "random", 0.1, "element", 120, 0.3, (0, 60, 120), 4),
+    "cube2_q2_o4": (2, 2, "random", 0.1, "element", 60, 0.35, (0, 30, 60), 4),
+    "cube2_q8_o4": (2, 8, "sin", 0.1, "smooth", 30, 0.3, (0, 30), 4),
 }
 
 SEED = 20251203
 
 
-def cfl_dt(r, ref, factor=0.5):
-    """dt = factor * 2 / sqrt(lambda_max(D^-1 A)) (leap-frog CFL constant 2,
-    ModifiedEquation.cxx:217-225), lambda_max by power iteration on the
-    reference's own arrays."""
+def cfl_dt(r, ref, factor=0.5, time_order=2):
+    """dt = factor * C / sqrt(lambda_max(D^-1 A)) with the scheme's CFL constant
+    C = 2 (order 2) or 2 sqrt(3) (order 4) (ModifiedEquation.cxx:217-225),
+    lambda_max by power iteration on the reference's own arrays."""
     lam = oc.power_iteration_lambda_max(r, ref["nodle"], ref["bh"], ref["invD"], iters=300)
-    return factor * 2.0 / np.sqrt(lam * 1.02)
+    c = 2.0 if time_order == 2 else 2.0 * np.sqrt(3.0)
+    return factor * c / np.sqrt(lam * 1.02)
 
 
-def run_case(name, n, r, kind, amp, c_mode, steps, radius, snaps, work):
+def run_case(name, n, r, kind, amp, c_mode, steps, radius, snaps, time_order=2, work=None):
     m = M.perturbed_cube(n, seed=SEED + n * 10 + r, amplitude=amp, kind=kind, c_mode=c_mode)
     mesh_file = os.path.join(work, f"{name}.mesh")
     M.write_medit(mesh_file, m)
@@ -57,8 +62,8 @@ def run_case(name, n, r, kind, amp, c_mode, steps, radius, snaps, work):
     deck = os.path.join(work, f"{name}.ini")
     M.write_deck(deck, mesh_file, m, s)
     probe = oc.run_reference(deck, os.path.join(work, name + "_probe"))
-    dt = cfl_dt(r, probe)
-    s = M.AcousticSetup(order=r, dt=dt, nsteps=steps, src_radius=radius)
+    dt = cfl_dt(r, probe, time_order=time_order)
+    s = M.AcousticSetup(order=r, dt=dt, nsteps=steps, src_radius=radius, time_order=time_order)
     M.write_deck(deck, mesh_file, m, s)
     rng = np.random.default_rng(SEED + 7)
     ndof = probe["meta"]["n_dof"]
@@ -79,6 +84,7 @@ def run_case(name, n, r, kind, amp, c_mode, steps, radius, snaps, work):
         x=x, y0=y0, alpha=alpha, beta=beta, kh_y=ref["kh_y"], kh_ax=ref["kh_ax"],
         norms=ref["norms"], times=ref["times"], u_final=ref["u_final"],
         snap_steps=np.array(sorted(ref["snaps"])), snaps=np.stack([ref["snaps"][k] for k in sorted(ref["snaps"])]),
+        time_order=time_order, pulse3=ref["pulse3"],
     )
     np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
     print(f"{name}: ndof={ndof} dt={dt:.3e} steps={steps} norm_final={ref['norms'][-1]:.6e}")

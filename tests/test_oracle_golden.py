@@ -81,3 +81,47 @@ def test_config1_pulse_and_norm_history():
     assert rel_l2(p, g["pulse"]) < 1e-12
     assert g["norms"].size == int(g["nsteps"]) + 1
     assert np.all(np.isfinite(g["norms"])) and g["norms"][-1] > 0
+
+
+# ---- order-4 modified-equation leap-frog (ModifiedEquation.cxx:125-175, 346-408)
+
+def test_order4_pulse_derivatives(golden_case4):
+    """p and p'' (derivative orders 1 and 3 of the interpolated primitive)
+    against the reference's own TimeSourceHyperbolic: <= 1e-12 / 1e-9 relative
+    (p'' amplifies rounding of the 25-point interpolant)."""
+    from montjoie_gb300.problem import ricker_pulse
+    name, g = golden_case4
+    n = int(g["nsteps"])
+    eps = (float(g["tf"]) - float(g["t0"])) * 1e-15
+    for fn in (oc.ricker_pulse, ricker_pulse):
+        p1 = fn(float(g["f0"]), float(g["t0"]), float(g["dt"]), n, eps, float(g["tlimit"]))
+        p3 = fn(float(g["f0"]), float(g["t0"]), float(g["dt"]), n, eps, float(g["tlimit"]), nb_deriv=3)
+        assert np.abs(p1 - g["pulse"]).max() <= 1e-12 * np.abs(g["pulse"]).max()
+        assert np.abs(p3 - g["pulse3"]).max() <= 1e-9 * np.abs(g["pulse3"]).max()
+
+
+def test_order4_trajectory(golden_case4):
+    """The C restatement of the order-4 scheme against the reference's run:
+    final iterate, snapshots and norm history <= 1e-11 relative."""
+    name, g = golden_case4
+    n = int(g["nsteps"])
+    args = (int(g["order"]), g["nodle"], g["bh"], g["massD"], g["invD"], g["src_idx"], g["src_val"], g["pulse"],
+            g["pulse3"], float(g["dt"]))
+    uf, _, norms, _ = oc.leapfrog4(*args, n, np.zeros(g["massD"].size), jw=g["jw"])
+    assert rel_l2(uf, g["u_final"]) < 1e-11
+    assert rel_l2(norms, g["norms"]) < 1e-11
+    for k, snap in zip(g["snap_steps"].tolist(), g["snaps"]):
+        if k:
+            uk, _, _, _ = oc.leapfrog4(*args, k, np.zeros(g["massD"].size))
+            assert rel_l2(uk, snap) < 1e-11
+
+
+def test_order4_differs_from_order2():
+    """The order-4 and order-2 schemes give different iterates on the same
+    inputs (the d^4u/dt^4 correction is active)."""
+    g = load_golden("cube3_q4_o4")
+    n = 40
+    args = (int(g["order"]), g["nodle"], g["bh"], g["massD"], g["invD"], g["src_idx"], g["src_val"], g["pulse"])
+    u4, _, _, _ = oc.leapfrog4(*args, g["pulse3"], float(g["dt"]), n, np.zeros(g["massD"].size))
+    u2, _, _, _ = oc.leapfrog(*args, float(g["dt"]), n, np.zeros(g["massD"].size))
+    assert rel_l2(u2, u4) > 1e-6
