@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--adjoint-steps", type=int, default=1000)
     ap.add_argument("--mb-max-cells", type=int, default=40,
                     help="largest mesh of the heterogeneous batch (40 = the configuration; smaller for profiling)")
-    ap.add_argument("--leg", default="all", choices=["all", "config3", "config4", "config4m", "config5"],
+    ap.add_argument("--leg", default="all", choices=["all", "config3", "config4", "config4m", "config5", "order4"],
                     help="profiling aid: run one extra leg alone (no JSON line contract)")
     return ap.parse_args()
 
@@ -140,11 +140,11 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def build_problem(cells, order, nsteps, mesh=None):
+def build_problem(cells, order, nsteps, mesh=None, time_order=2):
     from montjoie_gb300 import mesh as M
     from montjoie_gb300.problem import AcousticProblem, cfl_time_step
     m = workload_mesh(cells) if mesh is None else mesh
-    s = M.AcousticSetup(order=order, dt=1.0, nsteps=nsteps, src_radius=2.0 / cells)
+    s = M.AcousticSetup(order=order, dt=1.0, nsteps=nsteps, src_radius=2.0 / cells, time_order=time_order)
     pb = AcousticProblem(m, s, receivers=receivers(), defer_time=True)
     dt = cfl_time_step(pb, safety=0.5)
     pb.set_time_step(dt, nsteps)
@@ -327,6 +327,47 @@ def leg_config4_meshes(args, torch, _lib):
             "algorithmic_bytes_per_step": step_bytes,
             "step_frac_of_hbm": step_bytes / (ms / K / 1e3) / 1e9 / peak,
             "setup_seconds": setup_s}
+
+
+def leg_order4(args, torch, _lib):
+    """The order-4 modified-equation leap-frog (two stiffness products per
+    step, CFL constant 2 sqrt(3)) on the configuration-2 mesh, 64^3 Q4, at
+    dt = 0.5 CFL of that scheme: FP32 and FP64 step rates, FP32 error against
+    FP64, and simulated time per second against the order-2 leap-frog."""
+    cells, order, K = args.cells, args.order, args.extra_steps
+    pb = build_problem(cells, order, K + 40, time_order=4)
+    zeros = np.zeros(pb.n_dof)
+    op32 = pb.operator("fp32")
+    lf = pb.integrator(op32, diagnostics=False)
+    lf.SetInitialConditionS(zeros)
+    lf.Advance(20)
+    l0 = _lib.kernel_launches()
+    ms32 = timed_steps(torch, lf.Advance, K)
+    launches = _lib.kernel_launches() - l0
+    lf.close()
+    op64 = pb.operator("fp64")
+    lf = pb.integrator(op64, diagnostics=False)
+    lf.SetInitialConditionS(zeros)
+    lf.Advance(3)
+    K64 = min(K, 100)
+    ms64 = timed_steps(torch, lf.Advance, K64)
+    lf.close()
+    KE = min(K, 200)
+    d64 = pb.integrator(op64)
+    u64, n64, _ = d64.Run(zeros, None, KE)
+    d32 = pb.integrator(op32)
+    u32, n32, _ = d32.Run(zeros, None, KE)
+    d64.close(); d32.close(); op32.close(); op64.close()
+    return {"workload": workload_name(cells, order).replace("leap-frog dt=0.5 CFL",
+                                                           "order-4 modified-equation leap-frog dt=0.5 CFL(2 sqrt 3)")
+            + f", FP32 state, {K} steps",
+            "n_dof": pb.n_dof, "dt": pb.setup.dt, "steps": K, "value": pb.n_dof * K / (ms32 / 1e3), "unit": UNIT,
+            "ms_per_step": ms32 / K, "gpu_launches": launches,
+            "fp64_value": pb.n_dof * K64 / (ms64 / 1e3), "fp64_ms_per_step": ms64 / K64,
+            "simulated_time_per_second_fp32": pb.setup.dt * K / (ms32 / 1e3),
+            "error_steps": KE,
+            "u_rel_l2_vs_fp64": float(np.linalg.norm(u32 - u64) / max(np.linalg.norm(u64), 1e-300)),
+            "norm_history_rel_l2_vs_fp64": float(np.linalg.norm(n32 - n64) / max(np.linalg.norm(n64), 1e-300))}
 
 
 def leg_config5_adjoint(args, torch, _lib):
@@ -533,6 +574,9 @@ def run_ours(args):
         out["config4_sources"] = leg_config4_sources(args, torch, _lib)
         out["config4_meshes"] = leg_config4_meshes(args, torch, _lib)
         out["config5_adjoint"] = leg_config5_adjoint(args, torch, _lib)
+        o4 = leg_order4(args, torch, _lib)
+        o4["simulated_time_per_second_order2_fp32"] = pb.setup.dt * K / (ms32 / 1e3)
+        out["order4_scheme"] = o4
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(args, pb, u_check=None)
     if rank == 0:
@@ -636,7 +680,7 @@ def main():
         from montjoie_gb300 import _lib
         _lib.load(build_if_missing=False)
         fn = {"config3": leg_config3, "config4": leg_config4_sources, "config4m": leg_config4_meshes,
-              "config5": leg_config5_adjoint}[args.leg]
+              "config5": leg_config5_adjoint, "order4": leg_order4}[args.leg]
         print(json.dumps({args.leg: fn(args, torch, _lib)}))
         return
     if args.impl == "reference":
