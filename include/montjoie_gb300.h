@@ -185,6 +185,13 @@ int mj_lf_set_graph(mj_lf* lf, int enable);
  * for order 2. */
 int mj_lf_set_scheme(mj_lf* lf, int order, int n_pulse_d2, const double* pulse_d2);
 
+/* FP32 order-2 step: with enable != 0 (the default for MJ_FP32) the gather,
+ * update and source run as one streaming kernel that stages each chunk of
+ * dofs (states, dt^2/D, CSR offsets, contributions) in shared memory by bulk
+ * copy; enable = 0 uses a gather kernel and a separate source kernel.  Both
+ * give the same states bit for bit. */
+int mj_lf_set_stream_gather(mj_lf* lf, int enable);
+
 /* Sets the CUDA stream (cudaStream_t) used by the integrator's launches. */
 int mj_lf_set_stream(mj_lf* lf, void* stream);
 

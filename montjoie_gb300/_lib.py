@@ -25,7 +25,7 @@ MJ_FP32 = 1
 EXPORTED = [
     "mj_last_error", "mj_version", "mj_op_create", "mj_op_destroy", "mj_op_mltadd", "mj_op_mltadd_device",
     "mj_op_info", "mj_op_tuning", "mj_kernel_launches", "mj_lf_create", "mj_lf_destroy", "mj_lf_init", "mj_lf_advance",
-    "mj_lf_get_state", "mj_lf_run", "mj_lf_device_state", "mj_lf_profile", "mj_lf_set_graph", "mj_lf_set_scheme", "mj_lf_set_stream", "mj_number_hex_mesh",
+    "mj_lf_get_state", "mj_lf_run", "mj_lf_device_state", "mj_lf_profile", "mj_lf_set_graph", "mj_lf_set_scheme", "mj_lf_set_stream_gather", "mj_lf_set_stream", "mj_number_hex_mesh",
     "mj_geometry", "mj_lumped_mass", "mj_stiffness_mltadd_static",
     "mj_lfb_create", "mj_lfb_destroy", "mj_lfb_init", "mj_lfb_advance", "mj_lfb_get_state", "mj_lfb_info",
     "mj_op_set_element_scale", "mj_adj_create", "mj_adj_destroy", "mj_adj_forward", "mj_adj_backward",
@@ -109,6 +109,7 @@ def load(build_if_missing: bool = True):
     L.mj_lf_set_stream.argtypes = [_VP, _VP]
     L.mj_lf_set_graph.argtypes = [_VP, ctypes.c_int]
     L.mj_lf_set_scheme.argtypes = [_VP, ctypes.c_int, ctypes.c_int, _D]
+    L.mj_lf_set_stream_gather.argtypes = [_VP, ctypes.c_int]
     L.mj_lf_profile.argtypes = [_VP, ctypes.c_int, _D, _D, ctypes.POINTER(ctypes.c_int)]
     L.mj_number_hex_mesh.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _I, ctypes.POINTER(ctypes.c_int)]
     L.mj_geometry.argtypes = [ctypes.c_int, ctypes.c_int, _D, _D, _D, _D, _D]

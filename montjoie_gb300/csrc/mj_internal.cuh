@@ -67,6 +67,10 @@ struct mj_lf {
   mj::DevBuf w4, z4, d3_4;
   mj::DevBuf src_mask, src_sidx, src_sval;
   int n_src_sorted = 0;
+  // FP32 order-2 step: streaming gather (k_gather_leapfrog_stream) over dof chunks
+  bool stream_gather = false;
+  mj::DevBuf stream_chunks;
+  int n_stream_chunks = 0, stream_grid_ = 0;
   ~mj_lf() {
     for (cudaEvent_t e : ev) cudaEventDestroy(e);
     if (graph) cudaGraphExecDestroy(graph);

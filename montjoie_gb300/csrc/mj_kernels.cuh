@@ -8,6 +8,8 @@
 
 #include <cstdint>
 
+#include "mj_k1.cuh"
+
 namespace mj {
 
 
@@ -220,6 +222,109 @@ __global__ void k_gather_o4_init(const Real* __restrict__ R, const int* __restri
     v *= dt;
     v += double(u0[d]);
     u1[d] = Real(v);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// K2s: the FP32 gather + leap-frog update + source as a streaming kernel.
+// Persistent CTAs walk chunks of at most kStreamDofs dofs (starting on a
+// multiple of 4).  A chunk's u^{n+1}, u^n, dt^2/D, CSR offsets and its
+// contiguous range of contributions R[ptr[d0] .. ptr[d1]) arrive by 1-D bulk
+// copies (16-byte rounded; every buffer carries spare entries past its end)
+// into one of two shared-memory buffers, the next chunk's while this one is
+// summed.  Same arithmetic as k_gather_leapfrog<float, false> followed by
+// k_source (the source in FP64 after the update), so the states agree bit
+// for bit.  Every mbarrier wait is bounded (error flag on timeout).
+// ---------------------------------------------------------------------------
+constexpr int kStreamThreads = 256;
+constexpr int kStreamDofs = 1024;
+constexpr int kStreamBuf = 32768;                         // bytes per chunk buffer
+constexpr int kStreamM = 2 * kStreamDofs * 4;             // offsets inside a buffer
+constexpr int kStreamP = kStreamM + (kStreamDofs + 4) * 4;
+constexpr int kStreamR = kStreamP + (kStreamDofs + 8) * 4;
+constexpr int kStreamRCap = (kStreamBuf - kStreamR) / 4;  // R entries one chunk may stage
+constexpr int kStreamSmem = 2 * kStreamBuf + 16;
+static_assert(kStreamM % 16 == 0 && kStreamP % 16 == 0 && kStreamR % 16 == 0, "aligned buffer segments");
+
+struct StreamChunk {
+  int d0, d1, q0, q1;  // dofs [d0, d1); R range [q0, q1) rounded to multiples of 4
+  int has_src, pad0, pad1, pad2;
+};
+
+__global__ void __launch_bounds__(kStreamThreads)
+    k_gather_leapfrog_stream(const float* __restrict__ R, const int* __restrict__ ptr, int* __restrict__ ctr, int qc,
+                             float* __restrict__ u0, const float* __restrict__ u1, const float* __restrict__ m,
+                             const StreamChunk* __restrict__ chunks, int n_chunks,
+                             const unsigned* __restrict__ mask, const int* __restrict__ sidx,
+                             const float* __restrict__ sval, int nsrc, const double* __restrict__ pulse, int n_pulse,
+                             const double* __restrict__ inv_mass, double dt2, int* __restrict__ err) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 2 * kStreamBuf);
+  const int t = threadIdx.x, G = gridDim.x;
+  if (blockIdx.x == 0 && t == 0) ctr[1 - qc] = ctr[qc] + 1;
+  const int step = ctr[qc];
+  const bool src_on = nsrc > 0 && step < n_pulse;
+  const double p = src_on ? pulse[step] : 0.0;
+  auto issue = [&](int c, int b) {
+    if (c >= n_chunks) return;
+    const StreamChunk ch = chunks[c];
+    unsigned char* dst = smem + b * kStreamBuf;
+    const uint32_t sb = (uint32_t)(((ch.d1 - ch.d0 + 3) & ~3) * 4);
+    const uint32_t pb = (uint32_t)(((ch.d1 - ch.d0 + 1 + 3) & ~3) * 4);
+    const uint32_t rb = (uint32_t)((ch.q1 - ch.q0) * 4);
+    mbar_expect_tx(&bar[b], 3u * sb + pb + rb);
+    bulk_g2s(dst, u1 + ch.d0, sb, &bar[b]);
+    bulk_g2s(dst + kStreamDofs * 4, u0 + ch.d0, sb, &bar[b]);
+    bulk_g2s(dst + kStreamM, m + ch.d0, sb, &bar[b]);
+    bulk_g2s(dst + kStreamP, ptr + ch.d0, pb, &bar[b]);
+    bulk_g2s(dst + kStreamR, R + ch.q0, rb, &bar[b]);
+  };
+  if (t == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+    issue(blockIdx.x, 0);
+    issue(blockIdx.x + G, 1);
+  }
+  __syncthreads();
+  uint32_t ph = 0u;
+  for (int c = blockIdx.x, it = 0; c < n_chunks; c += G, ++it) {
+    const int b = it & 1;
+    const StreamChunk ch = chunks[c];
+    const bool ok = mbar_wait_bounded(&bar[b], (ph >> b) & 1u);
+    if (__syncthreads_or(!ok)) {
+      if (t == 0) atomicExch(err, 1);
+      return;
+    }
+    ph ^= 1u << b;
+    const unsigned char* buf = smem + b * kStreamBuf;
+    const float* su1 = reinterpret_cast<const float*>(buf);
+    const float* su0 = su1 + kStreamDofs;
+    const float* sm = reinterpret_cast<const float*>(buf + kStreamM);
+    const int* sp = reinterpret_cast<const int*>(buf + kStreamP);
+    const float* sR = reinterpret_cast<const float*>(buf + kStreamR);
+#pragma unroll
+    for (int v = 0; v < kStreamDofs / kStreamThreads; v++) {
+      const int dl = v * kStreamThreads + t;
+      const int d = ch.d0 + dl;
+      if (d < ch.d1) {
+        float s = 0.f;
+        const int qb = sp[dl + 1] - ch.q0;
+        for (int q = sp[dl] - ch.q0; q < qb; q++) s += sR[q];
+        const float ah = -s;
+        float un = 2.f * su1[dl] - su0[dl] + sm[dl] * ah;
+        if (src_on && ch.has_src) {
+          const double f = source_at(mask, sidx, sval, nsrc, d);
+          if (f != 0.0) un = float(double(un) + dt2 * inv_mass[d] * p * f);
+        }
+        u0[d] = un;
+      }
+    }
+    __syncthreads();  // buffer b is free
+    if (t == 0) {
+      fence_proxy_async();
+      issue(c + 2 * G, b);
+    }
   }
 }
 

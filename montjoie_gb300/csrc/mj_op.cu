@@ -369,6 +369,87 @@ int mj_op_mltadd(mj_op* op, double alpha, const double* x, double beta, double* 
   return MJ_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Sources sorted by dof with a per-dof bit mask, looked up inside the
+// order-4 and streaming gathers.
+int lf_sorted_sources(mj_lf* lf) {
+  const int n = lf->n_dof;
+  const size_t esz = elem_size(lf->op->precision);
+  // sources sorted by dof with a per-dof bit mask (looked up inside the gathers)
+  const int ns = lf->n_src, words = (n + 31) / 32;
+  std::vector<int> idx(std::max(1, ns));
+  std::vector<unsigned char> val(esz * std::max(1, ns));
+  if (ns) {
+    MJ_CUDA(cudaMemcpy(idx.data(), lf->src_idx.ptr, sizeof(int) * ns, cudaMemcpyDeviceToHost));
+    MJ_CUDA(cudaMemcpy(val.data(), lf->src_val.ptr, esz * ns, cudaMemcpyDeviceToHost));
+  }
+  std::vector<int> order_(ns);
+  for (int t = 0; t < ns; t++) order_[t] = t;
+  std::sort(order_.begin(), order_.end(), [&](int a, int b) { return idx[a] < idx[b]; });
+  std::vector<int> si(std::max(1, ns), 0);
+  std::vector<unsigned char> sv(esz * std::max(1, ns), 0);
+  std::vector<unsigned> mask(std::max(1, words), 0u);
+  for (int t = 0; t < ns; t++) {
+    si[t] = idx[order_[t]];
+    std::memcpy(&sv[esz * t], &val[esz * order_[t]], esz);
+    mask[si[t] >> 5] |= 1u << (si[t] & 31);
+  }
+  MJ_CUDA(lf->src_sidx.alloc(sizeof(int) * si.size()));
+  MJ_CUDA(lf->src_sval.alloc(sv.size()));
+  MJ_CUDA(lf->src_mask.alloc(sizeof(unsigned) * mask.size()));
+  MJ_CUDA(cudaMemcpy(lf->src_sidx.ptr, si.data(), sizeof(int) * si.size(), cudaMemcpyHostToDevice));
+  MJ_CUDA(cudaMemcpy(lf->src_sval.ptr, sv.data(), sv.size(), cudaMemcpyHostToDevice));
+  MJ_CUDA(cudaMemcpy(lf->src_mask.ptr, mask.data(), sizeof(unsigned) * mask.size(), cudaMemcpyHostToDevice));
+  lf->n_src_sorted = ns;
+  return MJ_OK;
+}
+
+// Dof chunks of the streaming gather: start on a multiple of 4, at most
+// kStreamDofs dofs, the 16-byte rounded range of their contributions within
+// kStreamRCap; then the launch shape.
+int lf_stream_setup(mj_lf* lf) {
+  const mj_op* op = lf->op;
+  const std::vector<int>& ptr = op->h_ptr;
+  std::vector<char> is_src(op->n_dof, 0);
+  {
+    std::vector<int> idx(std::max(1, lf->n_src));
+    if (lf->n_src)
+      MJ_CUDA(cudaMemcpy(idx.data(), lf->src_idx.ptr, sizeof(int) * lf->n_src, cudaMemcpyDeviceToHost));
+    for (int t = 0; t < lf->n_src; t++) is_src[idx[t]] = 1;
+  }
+  std::vector<StreamChunk> chunks;
+  for (int d = 0; d < op->n_dof;) {
+    int e = std::min(op->n_dof, d + kStreamDofs);
+    auto range = [&](int e2) { return ((ptr[e2] + 3) & ~3) - (ptr[d] & ~3); };
+    while (range(e) > kStreamRCap) e = d + std::max(4, ((e - d) / 2) & ~3);
+    if (range(e) > kStreamRCap) {
+      set_error("streaming gather: a dof has too many contributions for one chunk buffer");
+      return MJ_ERR_ARG;
+    }
+    StreamChunk ch = {d, e, ptr[d] & ~3, (ptr[e] + 3) & ~3, 0, 0, 0, 0};
+    for (int x = d; x < e; x++) ch.has_src |= is_src[x];
+    chunks.push_back(ch);
+    d = e;
+  }
+  MJ_CUDA(lf->stream_chunks.alloc(sizeof(StreamChunk) * chunks.size()));
+  MJ_CUDA(cudaMemcpy(lf->stream_chunks.ptr, chunks.data(), sizeof(StreamChunk) * chunks.size(),
+                     cudaMemcpyHostToDevice));
+  lf->n_stream_chunks = (int)chunks.size();
+  MJ_CUDA(cudaFuncSetAttribute(k_gather_leapfrog_stream, cudaFuncAttributeMaxDynamicSharedMemorySize, kStreamSmem));
+  int ctas = 0;
+  MJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctas, k_gather_leapfrog_stream, kStreamThreads, kStreamSmem));
+  MJ_CHECK_ARG(ctas >= 1, "streaming gather cannot be resident");
+  lf->stream_grid_ = std::max(1, std::min(lf->n_stream_chunks, ctas * sm_count()));
+  return MJ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 // ------------------------------------------------------------------ leap-frog
 
 int mj_lf_create(mj_op* op, const mj_lf_desc* desc, mj_lf** out) {
@@ -452,6 +533,12 @@ int mj_lf_create(mj_op* op, const mj_lf_desc* desc, mj_lf** out) {
   MJ_CUDA(lf->partial.alloc(sizeof(double) * lf->norm_blocks));
   MJ_CUDA(lf->flag.alloc(sizeof(int)));
   MJ_CUDA(cudaMemset(lf->flag.ptr, 0, sizeof(int)));
+  if (op->precision == MJ_FP32) {
+    int rc = lf_sorted_sources(lf.get());
+    if (!rc) rc = lf_stream_setup(lf.get());
+    if (rc) return rc;
+    lf->stream_gather = true;
+  }
   *out = lf.release();
   return MJ_OK;
 }
@@ -551,7 +638,11 @@ int lf_diag(mj_lf* lf, double* norms_d, int norm_col, double* traces_d, int stri
 constexpr int kGraphSteps = 20;
 
 // Kernels one step launches (launch accounting of graph replays).
-int lf_kernels_per_step(const mj_lf* lf) { return lf->time_order == 4 ? 4 : 2 + (lf->n_src > 0); }
+int lf_kernels_per_step(const mj_lf* lf) {
+  if (lf->time_order == 4) return 4;
+  if (lf->stream_gather && lf->op->precision == MJ_FP32) return 2;
+  return 2 + (lf->n_src > 0);
+}
 
 // One order-4 step: element product of U^{n+1}, first gather (P, Z),
 // element product of Z, second gather + update over U^n.
@@ -593,6 +684,20 @@ void lf_step_launch(mj_lf* lf, void* cur, const void* next, int qc, cudaStream_t
   launch_k1<Real>(op, next, s);
   if (prof) cudaEventRecord(lf->ev[lf->ev_used + 1], s);
   const double dt2 = lf->dt * lf->dt;
+  if (lf->stream_gather && op->precision == MJ_FP32) {
+    k_gather_leapfrog_stream<<<lf->stream_grid_, kStreamThreads, kStreamSmem, s>>>(
+        op->R.as<float>(), op->ptr.as<int>(), lf->ctr.as<int>(), qc, static_cast<float*>(cur),
+        static_cast<const float*>(next), lf->minv.as<float>(), lf->stream_chunks.as<StreamChunk>(),
+        lf->n_stream_chunks, lf->src_mask.as<unsigned>(), lf->src_sidx.as<int>(), lf->src_sval.as<float>(),
+        lf->n_src_sorted, lf->pulse_d.as<double>(), lf->n_pulse, lf->inv_mass64.as<double>(), dt2,
+        op->err.as<int>());
+    count_launch();
+    if (prof) {
+      cudaEventRecord(lf->ev[lf->ev_used + 2], s);
+      lf->ev_used += 3;
+    }
+    return;
+  }
   if (op->precision == MJ_FP64) {
     k_gather_leapfrog<Real, true><<<stream_grid(n), 256, 0, s>>>(
         op->R.as<Real>(), op->ptr.as<int>(), lf->ctr.as<int>(), qc, static_cast<Real*>(cur),
@@ -812,32 +917,22 @@ int mj_lf_set_scheme(mj_lf* lf, int order, int n_pulse_d2, const double* pulse_d
   MJ_CUDA(lf->pulse3_d.alloc(sizeof(double) * std::max(1, n_pulse_d2)));
   if (n_pulse_d2)
     MJ_CUDA(cudaMemcpy(lf->pulse3_d.ptr, pulse_d2, sizeof(double) * n_pulse_d2, cudaMemcpyHostToDevice));
-  // sources sorted by dof with a per-dof bit mask (looked up inside the gathers)
-  const int ns = lf->n_src, words = (n + 31) / 32;
-  std::vector<int> idx(std::max(1, ns));
-  std::vector<unsigned char> val(esz * std::max(1, ns));
-  if (ns) {
-    MJ_CUDA(cudaMemcpy(idx.data(), lf->src_idx.ptr, sizeof(int) * ns, cudaMemcpyDeviceToHost));
-    MJ_CUDA(cudaMemcpy(val.data(), lf->src_val.ptr, esz * ns, cudaMemcpyDeviceToHost));
+  {
+    const int rc = lf_sorted_sources(lf);
+    if (rc) return rc;
   }
-  std::vector<int> order_(ns);
-  for (int t = 0; t < ns; t++) order_[t] = t;
-  std::sort(order_.begin(), order_.end(), [&](int a, int b) { return idx[a] < idx[b]; });
-  std::vector<int> si(std::max(1, ns), 0);
-  std::vector<unsigned char> sv(esz * std::max(1, ns), 0);
-  std::vector<unsigned> mask(std::max(1, words), 0u);
-  for (int t = 0; t < ns; t++) {
-    si[t] = idx[order_[t]];
-    std::memcpy(&sv[esz * t], &val[esz * order_[t]], esz);
-    mask[si[t] >> 5] |= 1u << (si[t] & 31);
-  }
-  MJ_CUDA(lf->src_sidx.alloc(sizeof(int) * si.size()));
-  MJ_CUDA(lf->src_sval.alloc(sv.size()));
-  MJ_CUDA(lf->src_mask.alloc(sizeof(unsigned) * mask.size()));
-  MJ_CUDA(cudaMemcpy(lf->src_sidx.ptr, si.data(), sizeof(int) * si.size(), cudaMemcpyHostToDevice));
-  MJ_CUDA(cudaMemcpy(lf->src_sval.ptr, sv.data(), sv.size(), cudaMemcpyHostToDevice));
-  MJ_CUDA(cudaMemcpy(lf->src_mask.ptr, mask.data(), sizeof(unsigned) * mask.size(), cudaMemcpyHostToDevice));
-  lf->n_src_sorted = ns;
+  return MJ_OK;
+}
+
+int mj_lf_set_stream_gather(mj_lf* lf, int enable) {
+  MJ_CHECK_ARG(lf, "mj_lf_set_stream_gather: null integrator");
+  MJ_CHECK_ARG(!enable || lf->op->precision == MJ_FP32, "mj_lf_set_stream_gather: FP32 integrators only");
+  for (cudaGraphExec_t* g : {&lf->graph, &lf->graph_prof})
+    if (*g) {
+      cudaGraphExecDestroy(*g);
+      *g = nullptr;
+    }
+  lf->stream_gather = enable != 0;
   return MJ_OK;
 }
 

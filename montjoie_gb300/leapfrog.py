@@ -91,6 +91,11 @@ class LeapFrogIterator:
         self.n_time += nsteps
         return norms, traces
 
+    def set_stream_gather(self, enable: bool) -> None:
+        """FP32: streaming gather + update + source kernel (default) or the
+        gather kernel followed by the source kernel (bitwise the same states)."""
+        _lib.check(_lib.load().mj_lf_set_stream_gather(self._h, int(bool(enable))))
+
     def set_graph(self, enable: bool) -> None:
         """Replay captured CUDA graphs of 20 steps when no diagnostics are asked (default on)."""
         _lib.check(_lib.load().mj_lf_set_graph(self._h, int(bool(enable))))
