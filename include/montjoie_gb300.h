@@ -102,6 +102,12 @@ int mj_op_info(const mj_op* op, int* order, int* n_elt, int* n_dof, int* precisi
 int mj_op_tuning(const mj_op* op, int* tile_elems, int* vector_lines, int* grid, int* n_candidates,
                  double* candidate_ms);
 
+/* Forces the element-kernel variant (tile_elems elements per CTA, vector-line
+ * work layout or compact) instead of the autotuner's choice; MJ_ERR_ARG when
+ * no such variant exists for the order.  Integrators bound to the operator
+ * keep captured CUDA graphs of the old variant until re-created. */
+int mj_op_set_variant(mj_op* op, int tile_elems, int vector_lines);
+
 /* Number of kernels this library launched on the calling process since load. */
 uint64_t mj_kernel_launches(void);
 

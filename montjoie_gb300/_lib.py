@@ -24,7 +24,7 @@ MJ_FP32 = 1
 
 EXPORTED = [
     "mj_last_error", "mj_version", "mj_op_create", "mj_op_destroy", "mj_op_mltadd", "mj_op_mltadd_device",
-    "mj_op_info", "mj_op_tuning", "mj_kernel_launches", "mj_lf_create", "mj_lf_destroy", "mj_lf_init", "mj_lf_advance",
+    "mj_op_info", "mj_op_tuning", "mj_op_set_variant", "mj_kernel_launches", "mj_lf_create", "mj_lf_destroy", "mj_lf_init", "mj_lf_advance",
     "mj_lf_get_state", "mj_lf_run", "mj_lf_device_state", "mj_lf_profile", "mj_lf_set_graph", "mj_lf_set_scheme", "mj_lf_set_stream_gather", "mj_lf_set_stream", "mj_number_hex_mesh",
     "mj_geometry", "mj_lumped_mass", "mj_stiffness_mltadd_static",
     "mj_lfb_create", "mj_lfb_destroy", "mj_lfb_init", "mj_lfb_advance", "mj_lfb_get_state", "mj_lfb_info",
@@ -99,6 +99,7 @@ def load(build_if_missing: bool = True):
                              ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                              ctypes.POINTER(ctypes.c_size_t)]
     L.mj_op_tuning.argtypes = [_VP] + [ctypes.POINTER(ctypes.c_int)] * 4 + [_D]
+    L.mj_op_set_variant.argtypes = [_VP, ctypes.c_int, ctypes.c_int]
     L.mj_lf_create.argtypes = [_VP, ctypes.POINTER(LfDesc), ctypes.POINTER(_VP)]
     L.mj_lf_destroy.argtypes = [_VP]
     L.mj_lf_init.argtypes = [_VP, _D, _D]

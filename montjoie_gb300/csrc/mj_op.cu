@@ -340,6 +340,23 @@ int mj_op_tuning(const mj_op* op, int* tile_elems, int* vector_lines, int* grid,
   return MJ_OK;
 }
 
+int mj_op_set_variant(mj_op* op, int tile_elems, int vector_lines) {
+  MJ_CHECK_ARG(op, "mj_op_set_variant: null operator");
+  const std::vector<int> cands = k1_tile_candidates(op->n);
+  MJ_CHECK_ARG(std::find(cands.begin(), cands.end(), tile_elems) != cands.end(),
+               "mj_op_set_variant: no element kernel with this tile size for this order");
+  MJ_CHECK_ARG(!vector_lines || op->precision == MJ_FP32, "mj_op_set_variant: vector lines are FP32 only");
+  int ctas = 0;
+  const int rc = op->precision == MJ_FP64 ? k1_prepare_f64(op->n, tile_elems, vector_lines != 0, &ctas)
+                                          : k1_prepare_f32(op->n, tile_elems, vector_lines != 0, &ctas);
+  if (rc) return rc;
+  op->E = tile_elems;
+  op->vec = vector_lines != 0;
+  op->n_tiles = op->n_elt_pad / tile_elems;
+  op->grid_k1 = std::max(1, std::min(op->n_tiles, ctas * sm_count()));
+  return MJ_OK;
+}
+
 int mj_op_mltadd_device(mj_op* op, double alpha, const void* x, double beta, void* y, void* stream) {
   MJ_CHECK_ARG(op && x && y, "mj_op_mltadd_device: null argument");
   cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -83,6 +83,10 @@ class FemMatrixFreeOperator:
         E, vec, grid, nc = (v.value for v in vals)
         return {"tile_elems": E, "vector_lines": bool(vec), "grid": grid, "candidate_ms": ms[:nc].tolist()}
 
+    def set_variant(self, tile_elems: int, vector_lines: bool) -> None:
+        """Forces the element-kernel variant (otherwise chosen by the autotuner)."""
+        _lib.check(_lib.load().mj_op_set_variant(self._h, int(tile_elems), int(bool(vector_lines))))
+
     def device_bytes(self) -> int:
         sz = ctypes.c_size_t()
         _lib.check(_lib.load().mj_op_info(self._h, None, None, None, None, ctypes.byref(sz)))

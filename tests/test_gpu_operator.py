@@ -106,3 +106,35 @@ def test_kernel_launch_counter_moves(lib):
     y = np.zeros_like(g["x"])
     op.MltVector(g["x"], y)
     assert lib.kernel_launches() >= before + 2
+
+
+K1_TILES = {1: (30, 60), 2: (12, 24), 3: (8, 16), 4: (4, 5, 8, 10), 5: (3, 4, 6), 6: (2, 3, 4, 5), 7: (2, 3, 4),
+            8: (1, 2, 3)}
+
+
+@pytest.mark.parametrize("case", ["cube2_q1", "cube2_q2", "cube2_q3", "cube3_q4", "cube2_q6", "cube2_q8"])
+def test_every_element_kernel_variant(case):
+    """Every instantiated element-kernel variant (tile size x work layout),
+    forced in turn, against the reference's MltAdd: FP64 (compact) <= 1e-12,
+    FP32 (compact and vector lines) <= 2e-5 relative L2."""
+    from montjoie_gb300.operator import FemMatrixFreeOperator
+    g = load_golden(case)
+    r = int(g["order"])
+    n_dof = g["massD"].size
+    from montjoie_gb300._lib import MontjoieError
+    for precision, layouts, tol in (("fp64", (False,), 1e-12), ("fp32", (False, True), 2e-5)):
+        op = FemMatrixFreeOperator(r, g["nodle"], g["bh"], n_dof, precision, gradphi=g["gradphi"])
+        tried = set()
+        for E in K1_TILES[r]:
+            for vec in layouts:
+                try:
+                    op.set_variant(E, vec)
+                except MontjoieError as e:  # the largest tiles of high orders exceed shared memory
+                    assert "does not fit" in str(e)
+                    continue
+                tried.add(vec)
+                y = g["y0"].copy()
+                op.MltAddVector(float(g["alpha"]), g["x"], float(g["beta"]), y)
+                assert rel_l2(y, g["kh_y"]) < tol, (precision, E, vec)
+        assert tried == set(layouts)
+        op.close()
