@@ -96,15 +96,16 @@ int mj_op_info(const mj_op* op, int* order, int* n_elt, int* n_dof, int* precisi
                size_t* device_bytes);
 
 /* Element-kernel variant chosen by the autotuner at creation: elements per
- * CTA, work layout (1 = vector lines), grid; and the timings (ms per launch,
+ * CTA, work layout (0 compact, 1 vector lines, 2 one element per warp), grid; and the timings (ms per launch,
  * or a negative occupancy score on meshes too small to time) of the
  * candidates tried (candidate_ms may be NULL, else room for 64 values). */
 int mj_op_tuning(const mj_op* op, int* tile_elems, int* vector_lines, int* grid, int* n_candidates,
                  double* candidate_ms);
 
-/* Forces the element-kernel variant (tile_elems elements per CTA, vector-line
- * work layout or compact) instead of the autotuner's choice; MJ_ERR_ARG when
- * no such variant exists for the order.  Integrators bound to the operator
+/* Forces the element-kernel variant instead of the autotuner's choice:
+ * tile_elems elements per CTA and the work layout (vector_lines: 0 compact,
+ * 1 vector lines, 2 one element per warp; 1 and 2 are FP32 only, 2 exists
+ * for order 4); MJ_ERR_ARG when no such variant exists for the order.  Integrators bound to the operator
  * keep captured CUDA graphs of the old variant until re-created. */
 int mj_op_set_variant(mj_op* op, int tile_elems, int vector_lines);
 

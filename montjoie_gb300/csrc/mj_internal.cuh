@@ -13,6 +13,7 @@ struct mj_op {
   int n_elt = 0, n_elt_pad = 0, n_dof = 0, precision = MJ_FP64;
   int E = 1, n_tiles = 0, grid_k1 = 1;  // tile size and grid of the element kernel (autotuned)
   bool vec = false;                     // work layout of the element kernel (autotuned)
+  bool warp = false;                    // warp-per-element layout (FP32, order 4; autotuned)
   size_t r_len = 0;                     // element-major slots (n_elt_pad * Qp)
   size_t n_inc = 0;                     // incidences (n_elt * Q); R has n_inc + 1 entries
   mj::DevBuf nodle_e, fac_e, slot_e, R, ptr;
@@ -138,6 +139,11 @@ void k1_launch_f64(int n, int E, bool vec, int grid, const void* x, const int* n
                    const int* slot_e, int n_tiles, int* err, cudaStream_t s);
 void k1_launch_f32(int n, int E, bool vec, int grid, const void* x, const int* nodle_e, const void* fac_e, void* R,
                    const int* slot_e, int n_tiles, int* err, cudaStream_t s);
+// Warp-per-element layout (FP32; orders with (r+1)^2 <= 32 that are instantiated).
+std::vector<int> k1_warp_tile_candidates(int n);
+int k1_prepare_w_f32(int n, int E, int* ctas_per_sm);
+void k1_launch_w_f32(int n, int E, int grid, const void* x, const int* nodle_e, const void* fac_e, void* R,
+                     const int* slot_e, int n_tiles, int* err, cudaStream_t s);
 
 // Many right-hand sides (FP32 only, mj_batch.cu).
 struct RhsVariant {

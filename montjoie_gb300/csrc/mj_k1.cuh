@@ -316,6 +316,155 @@ __global__ void __launch_bounds__(E* N* N)
 }
 
 // ---------------------------------------------------------------------------
+// K1, warp-per-element layout (n*n <= 32, i.e. orders up to 4): element el
+// of the tile belongs to warp el, lane (j, i) owning the z-line (i, j, .);
+// lanes >= n*n idle.  The compact work arrays of an element are touched by
+// its own warp only, so the exchanges of u and of the fluxes need warp
+// barriers, not block barriers: one block barrier per tile remains (stage
+// release, which also carries the timeout vote of the warps' bounded stage
+// waits).  Same operation order as k_local_stiffness.
+// ---------------------------------------------------------------------------
+template <typename Real, int N, int E>
+__global__ void __launch_bounds__(E * 32)
+    k_local_stiffness_w(const Real* __restrict__ x, const int* __restrict__ nodle_e,
+                        const Real* __restrict__ fac_e, Real* __restrict__ R, const int* __restrict__ slot_e,
+                        int n_tiles, int* __restrict__ err) {
+  static_assert(N * N <= 32, "one element per warp");
+  using P = K1Plan<Real, N, E, 1, false>;
+  constexpr int NN = P::NN, Q = P::Q, Qp = P::Qp;
+  const Real* __restrict__ Gm = GConst<Real>::get(N);
+  extern __shared__ __align__(128) unsigned char smem[];
+  auto s_fac = [&](int st) { return reinterpret_cast<Real*>(smem + st * P::stage_bytes); };
+  auto s_nod = [&](int st) { return reinterpret_cast<int*>(smem + st * P::stage_bytes + P::fac_bytes); };
+  Real* s_u = reinterpret_cast<Real*>(smem + 2 * P::stage_bytes);
+  Real* s_vx = s_u + E * Q;
+  Real* s_vy = s_vx + E * Q;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 2 * P::stage_bytes + P::work_bytes);
+
+  const int t = threadIdx.x;
+  const int el = t >> 5;
+  const int lane = t & 31;
+  const bool act = lane < NN;
+  const int ij = act ? lane : 0;
+  const int j = ij / N;
+  const int i = ij - j * N;
+  Real gci[N], gcj[N], gri[N], grj[N];
+#pragma unroll
+  for (int a = 0; a < N; a++) {
+    gci[a] = Gm[a * N + i];
+    gcj[a] = Gm[a * N + j];
+    gri[a] = Gm[i * N + a];
+    grj[a] = Gm[j * N + a];
+  }
+  const int lx = el * Q + j * N;  // + k*NN + a: x-line (el, k, j)
+  const int ly = el * Q + i;      // + k*NN + a*N: y-line (el, k, i)
+  const int pe = el * Qp + ij;
+
+  if (t == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  auto issue = [&](int stage, int tile) {
+    if (t == 0 && tile < n_tiles) {
+      mbar_expect_tx(&bar[stage], (uint32_t)P::stage_bytes);
+      bulk_g2s(s_fac(stage), fac_e + (size_t)tile * E * 6 * Qp, (uint32_t)P::fac_bytes, &bar[stage]);
+      bulk_g2s(s_nod(stage), nodle_e + (size_t)tile * E * Qp, (uint32_t)P::nod_bytes, &bar[stage]);
+    }
+  };
+  const int g = gridDim.x;
+  int tile = blockIdx.x;
+  issue(0, tile);
+  issue(1, tile + g);
+  uint32_t ph = 0u;
+  Real u[N];
+  if (tile < n_tiles) {
+    const bool ok = mbar_wait_bounded(&bar[0], ph & 1u);
+    if (__syncthreads_or(!ok)) {
+      if (t == 0) atomicExch(err, 1);
+      return;
+    }
+    ph ^= 1u;
+    const int* nd = s_nod(0) + pe;
+    if (act) {
+#pragma unroll
+      for (int k = 0; k < N; k++) u[k] = __ldg(x + nd[k * NN]);
+    }
+  }
+  for (int it = 0; tile < n_tiles; tile += g, ++it) {
+    const int s = it & 1;
+    if (act) {
+#pragma unroll
+      for (int k = 0; k < N; k++) s_u[lx + k * NN + i] = u[k];
+    }
+    __syncwarp();
+    const Real* f = s_fac(s) + el * 6 * Qp + ij;
+    Real vz[N];
+    if (act) {
+#pragma unroll
+      for (int k = 0; k < N; k++) {
+        Real rx[N], ry[N];
+#pragma unroll
+        for (int a = 0; a < N; a++) {
+          rx[a] = s_u[lx + k * NN + a];
+          ry[a] = s_u[ly + k * NN + a * N];
+        }
+        Real gx = 0, gy = 0, gz = 0;
+#pragma unroll
+        for (int a = 0; a < N; a++) {
+          gz += Gm[a * N + k] * u[a];
+          gx += gci[a] * rx[a];
+          gy += gcj[a] * ry[a];
+        }
+        const Real* fk = f + k * NN;
+        const Real bxx = fk[0], bxy = fk[Qp], bxz = fk[2 * Qp];
+        const Real byy = fk[3 * Qp], byz = fk[4 * Qp], bzz = fk[5 * Qp];
+        s_vx[lx + k * NN + i] = bxx * gx + bxy * gy + bxz * gz;
+        s_vy[ly + k * NN + j * N] = bxy * gx + byy * gy + byz * gz;
+        vz[k] = bxz * gx + byz * gy + bzz * gz;
+      }
+    }
+    __syncwarp();
+    // next tile's stage (every warp waits for it itself) and u gather, in
+    // flight during the divergence
+    const int nt = tile + g;
+    bool bad = false;
+    if (nt < n_tiles) {
+      const int so = s ^ 1;
+      const bool ok = mbar_wait_bounded(&bar[so], (ph >> so) & 1u);
+      bad = __any_sync(0xffffffffu, !ok);
+      ph ^= 1u << so;
+      if (!bad && act) {
+        const int* nd = s_nod(so) + pe;
+#pragma unroll
+        for (int k = 0; k < N; k++) u[k] = __ldg(x + nd[k * NN]);
+      }
+    }
+    if (act) {
+      const int* st = slot_e + ((size_t)tile * E + el) * Qp + ij;
+#pragma unroll
+      for (int k = 0; k < N; k++) {
+        Real y = 0;
+#pragma unroll
+        for (int a = 0; a < N; a++) {
+          y += gri[a] * s_vx[lx + k * NN + a];
+          y += grj[a] * s_vy[ly + k * NN + a * N];
+          y += Gm[k * N + a] * vz[a];
+        }
+        R[__ldg(st + k * NN)] = y;
+      }
+    }
+    if (__syncthreads_or(bad)) {  // stage s and the work arrays are free; any wait timed out?
+      if (t == 0) atomicExch(err, 1);
+      return;
+    }
+    if (t == 0) fence_proxy_async();
+    issue(s, tile + 2 * g);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // K1, many right-hand sides (FP32 state [dof][S], S a multiple of L):
 // the same element product for S independent right-hand sides sharing the
 // mesh.  L lanes (consecutive threads) carry L right-hand sides of one

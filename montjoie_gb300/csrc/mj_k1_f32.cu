@@ -11,6 +11,47 @@ void k1_launch_f32(int n, int E, bool vec, int grid, const void* x, const int* n
   launch_any(n, E, vec, grid, x, nodle_e, fac_e, R, slot_e, n_tiles, err, s);
 }
 
+// warp-per-element layout, order 4 (n = 5): E warps per CTA
+namespace {
+template <int E>
+int prepare_w_one(int* ctas) {
+  using P = K1Plan<float, 5, E, 1, false>;
+  MJ_CUDA(cudaFuncSetAttribute(k_local_stiffness_w<float, 5, E>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)P::total));
+  MJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas, k_local_stiffness_w<float, 5, E>, E * 32, P::total));
+  if (*ctas < 1) {
+    set_error("element kernel variant cannot be resident");
+    return MJ_ERR_ARG;
+  }
+  return MJ_OK;
+}
+template <int E>
+void launch_w_one(int grid, const void* x, const int* nodle_e, const void* fac_e, void* R, const int* slot_e,
+                  int n_tiles, int* err, cudaStream_t s) {
+  using P = K1Plan<float, 5, E, 1, false>;
+  k_local_stiffness_w<float, 5, E><<<grid, E * 32, P::total, s>>>(static_cast<const float*>(x), nodle_e,
+                                                                   static_cast<const float*>(fac_e),
+                                                                   static_cast<float*>(R), slot_e, n_tiles, err);
+}
+}  // namespace
+
+std::vector<int> k1_warp_tile_candidates(int n) { return n == 5 ? std::vector<int>{4, 5, 8} : std::vector<int>{}; }
+
+int k1_prepare_w_f32(int n, int E, int* ctas) {
+  if (n == 5 && E == 4) return prepare_w_one<4>(ctas);
+  if (n == 5 && E == 5) return prepare_w_one<5>(ctas);
+  if (n == 5 && E == 8) return prepare_w_one<8>(ctas);
+  set_error("no warp-per-element kernel variant for this order and tile size");
+  return MJ_ERR_ARG;
+}
+
+void k1_launch_w_f32(int n, int E, int grid, const void* x, const int* nodle_e, const void* fac_e, void* R,
+                     const int* slot_e, int n_tiles, int* err, cudaStream_t s) {
+  if (n == 5 && E == 4) launch_w_one<4>(grid, x, nodle_e, fac_e, R, slot_e, n_tiles, err, s);
+  if (n == 5 && E == 5) launch_w_one<5>(grid, x, nodle_e, fac_e, R, slot_e, n_tiles, err, s);
+  if (n == 5 && E == 8) launch_w_one<8>(grid, x, nodle_e, fac_e, R, slot_e, n_tiles, err, s);
+}
+
 std::vector<int> k1_tile_candidates(int n) {
   switch (n) {
     case 2: return {30, 60};

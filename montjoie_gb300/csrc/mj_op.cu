@@ -60,6 +60,12 @@ namespace {
 
 // One launch of the element kernel with the operator's tuned variant.
 void launch_k1(mj_op* op, const void* x, cudaStream_t s) {
+  if (op->warp) {
+    k1_launch_w_f32(op->n, op->E, op->grid_k1, x, op->nodle_e.as<int>(), op->fac_e.ptr, op->R.ptr,
+                    op->slot_e.as<int>(), op->n_tiles, op->err.as<int>(), s);
+    count_launch();
+    return;
+  }
   if (op->precision == MJ_FP64)
     k1_launch_f64(op->n, op->E, op->vec, op->grid_k1, x, op->nodle_e.as<int>(), op->fac_e.ptr, op->R.ptr,
                   op->slot_e.as<int>(), op->n_tiles, op->err.as<int>(), s);
@@ -91,21 +97,22 @@ int autotune_k1(mj_op* op) {
   MJ_CUDA(cudaEventCreate(&e1));
   double best = 1e300;
   int bestE = -1, bestGrid = 1;
-  bool bestVec = false;
+  bool bestVec = false, bestWarp = false;
   const bool time_it = (long long)op->n_elt * op->Q >= 2000000;
-  const int n_layouts = op->precision == MJ_FP32 ? 2 : 1;
+  const int n_layouts = op->precision == MJ_FP32 ? 3 : 1;
   for (int lay = 0; lay < n_layouts; lay++)
-    for (int E : cands) {
-      const bool vec = lay == 1;
+    for (int E : (lay == 2 ? k1_warp_tile_candidates(op->n) : cands)) {
+      const bool vec = lay == 1, warp = lay == 2;
       int ctas = 0;
-      const int rc = op->precision == MJ_FP64 ? k1_prepare_f64(op->n, E, vec, &ctas)
-                                              : k1_prepare_f32(op->n, E, vec, &ctas);
+      const int rc = warp ? k1_prepare_w_f32(op->n, E, &ctas)
+                          : op->precision == MJ_FP64 ? k1_prepare_f64(op->n, E, vec, &ctas)
+                                                     : k1_prepare_f32(op->n, E, vec, &ctas);
       if (rc != MJ_OK) continue;
       const int tiles = op->n_elt_pad / E;
       const int grid = std::max(1, std::min(tiles, ctas * sms));
       double ms = 0.0;
       if (time_it) {
-        op->E = E; op->vec = vec; op->grid_k1 = grid; op->n_tiles = tiles;
+        op->E = E; op->vec = vec; op->warp = warp; op->grid_k1 = grid; op->n_tiles = tiles;
         launch_k1(op, x.ptr, op->stream);
         MJ_CUDA(cudaEventRecord(e0, op->stream));
         for (int rep = 0; rep < 3; rep++) launch_k1(op, x.ptr, op->stream);
@@ -115,12 +122,12 @@ int autotune_k1(mj_op* op) {
         MJ_CUDA(cudaEventElapsedTime(&f, e0, e1));
         ms = f / 3.0;
       } else {
-        ms = -double(ctas) * E * op->n * op->n + (vec ? 0.5 : 0.0);  // most resident threads first
+        ms = -double(ctas) * E * op->n * op->n + (vec ? 0.5 : 0.0) + (warp ? 0.75 : 0.0);  // most resident threads first
       }
       op->tune_E.push_back(E);
-      op->tune_vec.push_back(vec);
+      op->tune_vec.push_back(lay);
       op->tune_ms.push_back(ms);
-      if (ms < best) { best = ms; bestE = E; bestGrid = grid; bestVec = vec; }
+      if (ms < best) { best = ms; bestE = E; bestGrid = grid; bestVec = vec; bestWarp = warp; }
     }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -130,6 +137,7 @@ int autotune_k1(mj_op* op) {
   }
   op->E = bestE;
   op->vec = bestVec;
+  op->warp = bestWarp;
   op->grid_k1 = bestGrid;
   // the chosen variant's shared-memory attribute must be the one set last
   {
@@ -332,7 +340,7 @@ int mj_op_tuning(const mj_op* op, int* tile_elems, int* vector_lines, int* grid,
                  double* candidate_ms) {
   MJ_CHECK_ARG(op, "mj_op_tuning: null operator");
   if (tile_elems) *tile_elems = op->E;
-  if (vector_lines) *vector_lines = op->vec ? 1 : 0;
+  if (vector_lines) *vector_lines = op->warp ? 2 : op->vec ? 1 : 0;
   if (grid) *grid = op->grid_k1;
   if (n_candidates) *n_candidates = (int)op->tune_ms.size();
   if (candidate_ms)
@@ -342,16 +350,21 @@ int mj_op_tuning(const mj_op* op, int* tile_elems, int* vector_lines, int* grid,
 
 int mj_op_set_variant(mj_op* op, int tile_elems, int vector_lines) {
   MJ_CHECK_ARG(op, "mj_op_set_variant: null operator");
-  const std::vector<int> cands = k1_tile_candidates(op->n);
+  MJ_CHECK_ARG(vector_lines >= 0 && vector_lines <= 2, "mj_op_set_variant: layout must be 0, 1 or 2");
+  const bool warp = vector_lines == 2, vec = vector_lines == 1;
+  const std::vector<int> cands = warp ? k1_warp_tile_candidates(op->n) : k1_tile_candidates(op->n);
   MJ_CHECK_ARG(std::find(cands.begin(), cands.end(), tile_elems) != cands.end(),
-               "mj_op_set_variant: no element kernel with this tile size for this order");
-  MJ_CHECK_ARG(!vector_lines || op->precision == MJ_FP32, "mj_op_set_variant: vector lines are FP32 only");
+               "mj_op_set_variant: no element kernel with this tile size and layout for this order");
+  MJ_CHECK_ARG(vector_lines == 0 || op->precision == MJ_FP32,
+               "mj_op_set_variant: vector-line and warp layouts are FP32 only");
   int ctas = 0;
-  const int rc = op->precision == MJ_FP64 ? k1_prepare_f64(op->n, tile_elems, vector_lines != 0, &ctas)
-                                          : k1_prepare_f32(op->n, tile_elems, vector_lines != 0, &ctas);
+  const int rc = warp ? k1_prepare_w_f32(op->n, tile_elems, &ctas)
+                      : op->precision == MJ_FP64 ? k1_prepare_f64(op->n, tile_elems, false, &ctas)
+                                                 : k1_prepare_f32(op->n, tile_elems, vec, &ctas);
   if (rc) return rc;
   op->E = tile_elems;
-  op->vec = vector_lines != 0;
+  op->vec = vec;
+  op->warp = warp;
   op->n_tiles = op->n_elt_pad / tile_elems;
   op->grid_k1 = std::max(1, std::min(op->n_tiles, ctas * sm_count()));
   return MJ_OK;

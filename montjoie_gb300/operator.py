@@ -80,12 +80,14 @@ class FemMatrixFreeOperator:
         vals = [ctypes.c_int() for _ in range(4)]
         ms = np.zeros(64)
         _lib.check(_lib.load().mj_op_tuning(self._h, *[ctypes.byref(v) for v in vals], _lib.dptr(ms)))
-        E, vec, grid, nc = (v.value for v in vals)
-        return {"tile_elems": E, "vector_lines": bool(vec), "grid": grid, "candidate_ms": ms[:nc].tolist()}
+        E, lay, grid, nc = (v.value for v in vals)
+        return {"tile_elems": E, "layout": ["compact", "vector_lines", "warp_per_element"][lay], "grid": grid,
+                "candidate_ms": ms[:nc].tolist()}
 
-    def set_variant(self, tile_elems: int, vector_lines: bool) -> None:
-        """Forces the element-kernel variant (otherwise chosen by the autotuner)."""
-        _lib.check(_lib.load().mj_op_set_variant(self._h, int(tile_elems), int(bool(vector_lines))))
+    def set_variant(self, tile_elems: int, layout) -> None:
+        """Forces the element-kernel variant (otherwise chosen by the autotuner):
+        layout 0 / False compact, 1 / True vector lines, 2 one element per warp."""
+        _lib.check(_lib.load().mj_op_set_variant(self._h, int(tile_elems), int(layout)))
 
     def device_bytes(self) -> int:
         sz = ctypes.c_size_t()

@@ -122,19 +122,21 @@ def test_every_element_kernel_variant(case):
     r = int(g["order"])
     n_dof = g["massD"].size
     from montjoie_gb300._lib import MontjoieError
-    for precision, layouts, tol in (("fp64", (False,), 1e-12), ("fp32", (False, True), 2e-5)):
+    for precision, layouts, tol in (("fp64", (0,), 1e-12), ("fp32", (0, 1, 2), 2e-5)):
         op = FemMatrixFreeOperator(r, g["nodle"], g["bh"], n_dof, precision, gradphi=g["gradphi"])
         tried = set()
-        for E in K1_TILES[r]:
+        for E in sorted(set(K1_TILES[r]) | ({4, 5, 8} if r == 4 else set())):
             for vec in layouts:
+                if vec == 2 and (r != 4 or E not in (4, 5, 8)):
+                    continue
                 try:
                     op.set_variant(E, vec)
                 except MontjoieError as e:  # the largest tiles of high orders exceed shared memory
-                    assert "does not fit" in str(e)
+                    assert "does not fit" in str(e) or "no element kernel" in str(e)
                     continue
                 tried.add(vec)
                 y = g["y0"].copy()
                 op.MltAddVector(float(g["alpha"]), g["x"], float(g["beta"]), y)
                 assert rel_l2(y, g["kh_y"]) < tol, (precision, E, vec)
-        assert tried == set(layouts)
+        assert tried == (set(layouts) if r == 4 else set(layouts) - {2})
         op.close()
