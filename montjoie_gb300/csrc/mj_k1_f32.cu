@@ -35,21 +35,33 @@ void launch_w_one(int grid, const void* x, const int* nodle_e, const void* fac_e
 }
 }  // namespace
 
-std::vector<int> k1_warp_tile_candidates(int n) { return n == 5 ? std::vector<int>{4, 5, 8} : std::vector<int>{}; }
+std::vector<int> k1_warp_tile_candidates(int n) {
+  return n == 5 ? std::vector<int>{1, 2, 3, 4, 5, 6, 8, 10} : std::vector<int>{};
+}
 
 int k1_prepare_w_f32(int n, int E, int* ctas) {
+  if (n == 5 && E == 1) return prepare_w_one<1>(ctas);
+  if (n == 5 && E == 2) return prepare_w_one<2>(ctas);
+  if (n == 5 && E == 3) return prepare_w_one<3>(ctas);
   if (n == 5 && E == 4) return prepare_w_one<4>(ctas);
   if (n == 5 && E == 5) return prepare_w_one<5>(ctas);
+  if (n == 5 && E == 6) return prepare_w_one<6>(ctas);
   if (n == 5 && E == 8) return prepare_w_one<8>(ctas);
+  if (n == 5 && E == 10) return prepare_w_one<10>(ctas);
   set_error("no warp-per-element kernel variant for this order and tile size");
   return MJ_ERR_ARG;
 }
 
 void k1_launch_w_f32(int n, int E, int grid, const void* x, const int* nodle_e, const void* fac_e, void* R,
                      const int* slot_e, int n_tiles, int* err, cudaStream_t s) {
+  if (n == 5 && E == 1) launch_w_one<1>(grid, x, nodle_e, fac_e, R, slot_e, n_tiles, err, s);
+  if (n == 5 && E == 2) launch_w_one<2>(grid, x, nodle_e, fac_e, R, slot_e, n_tiles, err, s);
+  if (n == 5 && E == 3) launch_w_one<3>(grid, x, nodle_e, fac_e, R, slot_e, n_tiles, err, s);
   if (n == 5 && E == 4) launch_w_one<4>(grid, x, nodle_e, fac_e, R, slot_e, n_tiles, err, s);
   if (n == 5 && E == 5) launch_w_one<5>(grid, x, nodle_e, fac_e, R, slot_e, n_tiles, err, s);
+  if (n == 5 && E == 6) launch_w_one<6>(grid, x, nodle_e, fac_e, R, slot_e, n_tiles, err, s);
   if (n == 5 && E == 8) launch_w_one<8>(grid, x, nodle_e, fac_e, R, slot_e, n_tiles, err, s);
+  if (n == 5 && E == 10) launch_w_one<10>(grid, x, nodle_e, fac_e, R, slot_e, n_tiles, err, s);
 }
 
 std::vector<int> k1_tile_candidates(int n) {

@@ -142,8 +142,9 @@ int autotune_k1(mj_op* op) {
   // the chosen variant's shared-memory attribute must be the one set last
   {
     int ctas = 0;
-    const int rc = op->precision == MJ_FP64 ? k1_prepare_f64(op->n, bestE, bestVec, &ctas)
-                                            : k1_prepare_f32(op->n, bestE, bestVec, &ctas);
+    const int rc = bestWarp ? k1_prepare_w_f32(op->n, bestE, &ctas)
+                            : op->precision == MJ_FP64 ? k1_prepare_f64(op->n, bestE, bestVec, &ctas)
+                                                       : k1_prepare_f32(op->n, bestE, bestVec, &ctas);
     if (rc) return rc;
   }
   op->n_tiles = op->n_elt_pad / bestE;

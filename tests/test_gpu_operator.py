@@ -125,9 +125,9 @@ def test_every_element_kernel_variant(case):
     for precision, layouts, tol in (("fp64", (0,), 1e-12), ("fp32", (0, 1, 2), 2e-5)):
         op = FemMatrixFreeOperator(r, g["nodle"], g["bh"], n_dof, precision, gradphi=g["gradphi"])
         tried = set()
-        for E in sorted(set(K1_TILES[r]) | ({4, 5, 8} if r == 4 else set())):
+        for E in sorted(set(K1_TILES[r]) | ({1, 2, 3, 4, 5, 6, 8, 10} if r == 4 else set())):
             for vec in layouts:
-                if vec == 2 and (r != 4 or E not in (4, 5, 8)):
+                if vec == 2 and (r != 4 or E not in (1, 2, 3, 4, 5, 6, 8, 10)):
                     continue
                 try:
                     op.set_variant(E, vec)
