@@ -548,7 +548,11 @@ def run_ours(args):
     achieved = bytes_k1 / (k1_ms / 1e3) / 1e9
     per_elt = ncu_traffic_per_element(f"k_local_stiffness_fp32_q{args.order}.md")
     step_bytes = n_elt * Q * (6 * 4 + 4) + n_dof * (3 * 4 + 4)
-    roofline = {"bound": "hbm", "kernel": "k_local_stiffness<float,5,5> (element kernel)",
+    kname = ("k_local_stiffness_w<float,%d,%d>" % (args.order + 1, tuning32["tile_elems"])
+             if tuning32["layout"] == "warp_per_element" else
+             "k_local_stiffness<float,%d,%d,%s>" % (args.order + 1, tuning32["tile_elems"],
+                                                   "vec" if tuning32["layout"] == "vector_lines" else "compact"))
+    roofline = {"bound": "hbm", "kernel": kname + " (element kernel, autotuned)",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s",
                 "traffic": None if per_elt is None else per_elt * n_elt,

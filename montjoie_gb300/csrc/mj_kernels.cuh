@@ -329,18 +329,48 @@ __global__ void __launch_bounds__(kStreamThreads)
 }
 
 // ---------------------------------------------------------------------------
-// K3: weighted norm sum_i M_i u_i^2 in FP64 (GetNormeSolution,
+// K3: weighted norm sum_i M_i u_i^2 accumulated in FP64 (GetNormeSolution,
 // VarInstationary.cxx:2696-2745, with M_i the J*w summed over the points on
 // dof i).  Two passes, fixed summation order (deterministic).
 // ---------------------------------------------------------------------------
+// Four terms w_i u_i^2 of one thread, summed for the FP64 accumulator:
+// FP64 state: every term in FP64 (the plain form's norm history is pinned to
+// the reference at 1e-10); FP32 state: the four products and their sum in
+// FP32 (relative error ~1e-7, the state's own precision), one FP64 add.
+template <typename Real>
+__device__ __forceinline__ double norm_group(const double (&w)[4], const Real (&u)[4]);
+template <>
+__device__ __forceinline__ double norm_group<double>(const double (&w)[4], const double (&u)[4]) {
+  return (w[0] * u[0] * u[0] + w[1] * u[1] * u[1]) + (w[2] * u[2] * u[2] + w[3] * u[3] * u[3]);
+}
+template <>
+__device__ __forceinline__ double norm_group<float>(const double (&w)[4], const float (&u)[4]) {
+  return double((float(w[0]) * u[0] * u[0] + float(w[1]) * u[1] * u[1]) +
+                (float(w[2]) * u[2] * u[2] + float(w[3]) * u[3] * u[3]));
+}
+
 template <typename Real>
 __global__ void k_norm_partial(const Real* __restrict__ u, const double* __restrict__ w, int n,
                                double* __restrict__ partial) {
   __shared__ double sh[32];
+  // each thread: groups of four strided terms into one FP64 accumulator,
+  // then a fixed warp and block tree: deterministic for a given grid
   double acc = 0.0;
-  for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < n; d += gridDim.x * blockDim.x) {
-    const double v = double(u[d]);
-    acc += w[d] * v * v;
+  const int stride = gridDim.x * blockDim.x;
+  int d = blockIdx.x * blockDim.x + threadIdx.x;
+  for (; d + 3 * stride < n; d += 4 * stride) {
+    double wv[4];
+    Real uv[4];
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      wv[v] = __ldg(w + d + v * stride);
+      uv[v] = __ldg(u + d + v * stride);
+    }
+    acc += norm_group<Real>(wv, uv);
+  }
+  for (; d < n; d += stride) {
+    const double x = double(__ldg(u + d));
+    acc += __ldg(w + d) * x * x;
   }
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;

@@ -32,11 +32,15 @@ int sm_count() {
   return n > 0 ? n : 1;
 }
 
+// Sum of the per-block partial norms by one warp in a fixed order (lane l
+// sums partials l, l+32, ..., then a fixed shuffle tree): deterministic.
 __global__ void k_norm_final(const double* __restrict__ partial, int nparts, double* __restrict__ out,
                              int* __restrict__ nonfinite_flag) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    double s = 0.0;
-    for (int b = 0; b < nparts; b++) s += partial[b];
+  if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+  double s = 0.0;
+  for (int b = threadIdx.x; b < nparts; b += 32) s += partial[b];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (threadIdx.x == 0) {
     *out = s;
     if (!isfinite(s)) *nonfinite_flag = 1;
   }
