@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip the configuration 3 and 4 legs")
     ap.add_argument("--extra-steps", type=int, default=500)
     ap.add_argument("--adjoint-steps", type=int, default=1000)
+    ap.add_argument("--mb-orders", default="2,3,4,6,8",
+                    help="orders cycled over the heterogeneous batch (2,3,4,6,8 = the configuration)")
     ap.add_argument("--mb-max-cells", type=int, default=40,
                     help="largest mesh of the heterogeneous batch (40 = the configuration; smaller for profiling)")
     ap.add_argument("--leg", default="all", choices=["all", "config3", "config4", "config4m", "config5", "order4"],
@@ -271,11 +273,11 @@ def leg_config4_meshes(args, torch, _lib):
     from montjoie_gb300 import mesh as M
     from montjoie_gb300.leapfrog import MeshBatch
     K = args.extra_steps
-    orders = [2, 3, 4, 6, 8]
+    orders = [int(o) for o in args.mb_orders.split(",")]
     t0 = time.perf_counter()
     runs = []
     for i in range(24):
-        cells, r = 8 + round((args.mb_max_cells - 8) * i / 23), orders[i % 5]
+        cells, r = 8 + round((args.mb_max_cells - 8) * i / 23), orders[i % len(orders)]
         m = M.perturbed_cube(cells, seed=SEED + 60 + i, amplitude=0.05, kind="random", c_mode="element")
         pb = build_problem(cells, r, K + 40, mesh=m)
         op = pb.operator("fp32")
@@ -316,7 +318,7 @@ def leg_config4_meshes(args, torch, _lib):
         x[4].close(); x[3].close()
     value = n_dof * K / (ms / 1e3)
     peak, _ = measured_peaks()
-    return {"workload": f"24 meshes 8^3..{args.mb_max_cells}^3 hex, orders 2,3,4,6,8 cycling, +-5% h perturbation, c per element in "
+    return {"workload": f"24 meshes 8^3..{args.mb_max_cells}^3 hex, orders {args.mb_orders} cycling, +-5% h perturbation, c per element in "
                         f"[1,3], own Ricker source and dt each, FP32, {K} steps, one cooperative kernel per step",
             "meshes": [[x[0], x[1], x[2].n_dof] for x in runs], "n_dof": n_dof, "steps": K,
             "value": value, "unit": UNIT, "ms_per_step": ms / K, "gpu_launches": launches, "launch": info,
