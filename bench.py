@@ -239,12 +239,19 @@ def leg_config4_sources(args, torch, _lib):
     ms_two = timed_steps(torch, b.advance, K)
     u_two, _ = b.state()
     b.close()
-    # run 0 against a single-source run of the same FP32 operator
+    # run 0 against a single-source run of the same FP32 operator and
+    # against the FP64 plain form of that run
     lf = LeapFrogIteratorFor(pb, op, idx[0], val[0])
     lf.SetInitialConditionS(np.zeros(pb.n_dof))
     lf.Advance(K + 20)
     u0 = lf.GetIterate()
     lf.close(); op.close()
+    op64 = pb.operator("fp64")
+    lf = LeapFrogIteratorFor(pb, op64, idx[0], val[0])
+    lf.SetInitialConditionS(np.zeros(pb.n_dof))
+    lf.Advance(K + 20)
+    u0_64 = lf.GetIterate()
+    lf.close(); op64.close()
     n_elt, Q = pb.nodle.shape
     # SURVEY 8d batched bytes per right-hand side and step, divided by the dofs
     bytes_step = (n_elt * Q * (6 * 4 + 4) / S + pb.n_dof * (3 * 4 + 4 / S)) / pb.n_dof
@@ -258,6 +265,8 @@ def leg_config4_sources(args, torch, _lib):
             "two_kernel_ms_per_step": ms_two / K,
             "one_vs_two_kernel_rel_l2": float(np.linalg.norm(u - u_two) / max(np.linalg.norm(u_two), 1e-300)),
             "run0_rel_l2_vs_single_source_run": float(np.linalg.norm(u[:, 0] - u0) / max(np.linalg.norm(u0), 1e-300)),
+            "run0_rel_l2_vs_fp64_plain_form": float(np.linalg.norm(u[:, 0] - u0_64) / max(np.linalg.norm(u0_64), 1e-300)),
+            "error_steps": K + 20,
             "algorithmic_bytes_per_dof_update": bytes_step,
             "step_frac_of_hbm": value * bytes_step / 1e9 / peak}
 
@@ -531,7 +540,16 @@ def run_ours(args):
     u32, n32, tr32 = lf32d.Run(zeros, None, args.error_steps)
     e2e_s = time.perf_counter() - t0
     lf32d.close()
-    err = {"steps": args.error_steps,
+    # the same comparison every 100 steps (Advance in chunks; states read back)
+    series = []
+    a64, a32 = pb.integrator(op64, diagnostics=False), pb.integrator(op32, diagnostics=False)
+    a64.SetInitialConditionS(zeros); a32.SetInitialConditionS(zeros)
+    for k in range(0, args.error_steps, 100):
+        a64.Advance(min(100, args.error_steps - k)); a32.Advance(min(100, args.error_steps - k))
+        v64, v32 = a64.GetIterate(), a32.GetIterate()
+        series.append([a64.n_time, float(np.linalg.norm(v32 - v64) / max(np.linalg.norm(v64), 1e-300))])
+    a64.close(); a32.close()
+    err = {"steps": args.error_steps, "u_rel_l2_every_100_steps": series,
            "u_rel_l2": float(np.linalg.norm(u32 - u64) / max(np.linalg.norm(u64), 1e-300)),
            "norm_history_rel_l2": float(np.linalg.norm(n32 - n64) / max(np.linalg.norm(n64), 1e-300)),
            "traces_rel_max": float(np.abs(tr32 - tr64).max() / max(np.abs(tr64).max(), 1e-300)),

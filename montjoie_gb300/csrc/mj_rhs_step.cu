@@ -123,8 +123,11 @@ __host__ __device__ __forceinline__ RsBuf rs_buf(int d0, int d1, int q0, int q1,
   return b;
 }
 
+// CTAs per SM the register allocation aims at (smaller CTAs: more of them)
+__host__ __device__ constexpr int rs_min_ctas(int T) { return T <= 128 ? 4 : T <= 216 ? 3 : 1; }
+
 template <int N, int E, int LB, int V>
-__global__ void __launch_bounds__(RsPlan<N, E, LB, V>::T)
+__global__ void __launch_bounds__(RsPlan<N, E, LB, V>::T, rs_min_ctas(RsPlan<N, E, LB, V>::T))
     k_rhs_step(const RsParams p, const RsChunk* __restrict__ chunks, int n_chunks, SyncState* sync, int par,
                int* err, unsigned long long* __restrict__ stamps) {
   using P = RsPlan<N, E, LB, V>;
