@@ -615,6 +615,8 @@ void adj_receivers(mj_adj* a, const float* u, int col, cudaStream_t s) {
 int adj_forward_step(mj_adj* a, const float* u0, const float* u1, float* out, int step, cudaStream_t s) {
   mj_lfb* b = a->b;
   MJ_CUDA(cudaMemcpyAsync(b->ctr.as<int>(), &step, sizeof(int), cudaMemcpyHostToDevice, s));
+  if (b->fused)  // the one-kernel step (bitwise the same arithmetic)
+    return lfb_fused_step_on(b, const_cast<float*>(u0), const_cast<float*>(u1), out, true, s);
   lfb_k1(b, u1, s);
   const long long total = (long long)b->n_dof * b->S;
   k_gather_leapfrog_rhs<<<grid_for(total), 256, 0, s>>>(b->R.as<float>(), b->op->ptr.as<int>(), b->ctr.as<int>(), 0,
@@ -739,11 +741,20 @@ int mj_adj_forward(mj_adj* a, double* traces) {
       MJ_CUDA(cudaMemcpyAsync(dst, b->cur(), bytes, cudaMemcpyDeviceToDevice, s));
       MJ_CUDA(cudaMemcpyAsync(dst + a->rows, b->next(), bytes, cudaMemcpyDeviceToDevice, s));
     }
-    lfb_step_launch(b, b->cur(), b->next(), b->step & 1, s);
+    if (b->fused) {
+      const int rc = lfb_fused_step(b, s);
+      if (rc) return rc;
+    } else {
+      lfb_step_launch(b, b->cur(), b->next(), b->step & 1, s);
+    }
     b->cur_is_a = !b->cur_is_a;
     b->step++;
   }
   MJ_CUDA(cudaGetLastError());
+  if (b->fused) {
+    const int rc = lfb_fused_check(b, s);
+    if (rc) return rc;
+  }
   if (traces)
     MJ_CUDA(cudaMemcpyAsync(traces, a->traces.ptr, sizeof(double) * b->n_rec * b->S * (a->N + 1),
                             cudaMemcpyDeviceToHost, s));
@@ -788,14 +799,20 @@ int mj_adj_backward(mj_adj* a, const double* residual, const double* coef, doubl
     }
     // adjoint steps m = n1 .. max(n0+1, 2), then the gradient term with U^{m-1}
     for (int m = n1; m >= std::max(n0 + 1, 2); m--) {
-      lfb_k1(b, lam1, s);
-      const long long total = (long long)rows;
-      k_gather_leapfrog_rhs<<<grid_for(total), 256, 0, s>>>(b->R.as<float>(), op->ptr.as<int>(), nullptr, 0, lam2,
-                                                            lam1, lam2, b->m.as<float>(), b->n_dof, S);
+      if (b->fused) {  // lambda^m = 2 lambda^{m+1} - lambda^{m+2} + m (-A lambda^{m+1}), one kernel
+        const int rc = lfb_fused_step_on(b, lam2, lam1, lam2, false, s);
+        if (rc) return rc;
+      } else {
+        lfb_k1(b, lam1, s);
+        const long long total = (long long)rows;
+        k_gather_leapfrog_rhs<<<grid_for(total), 256, 0, s>>>(b->R.as<float>(), op->ptr.as<int>(), nullptr, 0,
+                                                              lam2, lam1, lam2, b->m.as<float>(), b->n_dof, S);
+        count_launch();
+      }
       k_inject_rhs<<<inj_blocks, 128, 0, s>>>(a->rdof.as<int>(), a->rptr.as<int>(), a->rk.as<int>(),
                                               a->rw.as<double>(), a->n_rd, a->res.as<double>(), N + 1, m,
                                               b->inv_mass64.as<double>(), lam2, S);
-      count_launch(2);
+      count_launch();
       std::swap(lam1, lam2);  // lam1 = lambda^m, lam2 = lambda^{m+1}
       energy_launch(op->n, b->E, b->L, b->grid, seg + (size_t)(m - 1 - n0) * rows, op->nodle_e.as<int>(),
                     op->fac_e.as<float>(), b->n_tiles, S, op->err.as<int>(), lam1, a->grad.as<double>(),
@@ -803,6 +820,10 @@ int mj_adj_backward(mj_adj* a, const double* residual, const double* coef, doubl
       count_launch();
       MJ_CUDA(cudaGetLastError());
     }
+  }
+  if (b->fused) {
+    const int rc = lfb_fused_check(b, s);
+    if (rc) return rc;
   }
   std::vector<double> g(op->n_elt_pad);
   MJ_CUDA(cudaMemcpyAsync(g.data(), a->grad.ptr, sizeof(double) * g.size(), cudaMemcpyDeviceToHost, s));

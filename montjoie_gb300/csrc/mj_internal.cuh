@@ -160,5 +160,8 @@ int lfb_fused_setup(mj_lfb* b);
 int lfb_fused_advance(mj_lfb* b, int nsteps, double* traces, int trace_stride, bool use_graph);
 void lfb_receivers(mj_lfb* b, const float* u, int stride, int col, cudaStream_t s);
 int lfb_phase_ms(const mj_lfb* b, double* out);
+int lfb_fused_step_on(mj_lfb* b, float* u0, float* u1, float* out, bool sources, cudaStream_t s);
+int lfb_fused_step(mj_lfb* b, cudaStream_t s);
+int lfb_fused_check(mj_lfb* b, cudaStream_t s);
 
 }  // namespace mj

@@ -98,6 +98,7 @@ struct RsParams {
   const int* src_ptr;  // their entries [src_ptr[i], src_ptr[i+1]) in
   const int* src_rhs;  //   (right-hand side, value) pairs
   const float* src_val;
+  float* uout;         // where U^{n+2} goes (nullptr: over U^n)
   int n_src_dof, n_pulse, S, n_tiles;
 };
 
@@ -270,6 +271,7 @@ __global__ void __launch_bounds__(RsPlan<N, E, LB, V>::T, rs_min_ctas(RsPlan<N, 
   if (stamps && t == 0) stamps[4 * blockIdx.x + 2] = global_ns();
 
   // ---- phase 2
+  float* __restrict__ dst = p.uout ? p.uout : cur;
   const int step = p.ctr[par];
   const bool pulse_on = step < p.n_pulse;
   const float pf = pulse_on ? (float)p.pulse[step] : 0.f;
@@ -342,7 +344,7 @@ __global__ void __launch_bounds__(RsPlan<N, E, LB, V>::T, rs_min_ctas(RsPlan<N, 
             if ((r >> 2) == c4) un[r & 3] += md * pf * __ldg(p.src_val + e);
           }
       }
-      *reinterpret_cast<float4*>(cur + (size_t)d * S + 4 * c4) = make_float4(un[0], un[1], un[2], un[3]);
+      *reinterpret_cast<float4*>(dst + (size_t)d * S + 4 * c4) = make_float4(un[0], un[1], un[2], un[3]);
     }
     __syncthreads();  // buffer b is free
     if (t == 0) {
@@ -438,6 +440,7 @@ RsParams rs_params(mj_lfb* b, const RsVariant& v) {
   p.src_ptr = b->rs_src_ptr.as<int>();
   p.src_rhs = b->rs_src_rhs.as<int>();
   p.src_val = b->rs_src_val.as<float>();
+  p.uout = nullptr;
   p.n_src_dof = b->rs_n_src_dof;
   p.n_pulse = b->n_pulse;
   p.S = b->S;
@@ -651,6 +654,36 @@ int lfb_fused_advance(mj_lfb* b, int nsteps, double* traces, int trace_stride, b
       MJ_CUDA(cudaMemcpyAsync(traces + (size_t)r * trace_stride, b->traces_d.as<double>() + (size_t)r * nsteps,
                               sizeof(double) * nsteps, cudaMemcpyDeviceToHost, s));
   return rs_check_err(b, s);
+}
+
+// One step of the one-kernel form on caller-given states: U^n = u0,
+// U^{n+1} = u1, U^{n+2} written to out (out may be u0); the pulse index is
+// ctr[0] (set by the caller), sources only when `sources`.  Used by the
+// adjoint's checkpoint replays and its adjoint steps.
+int lfb_fused_step_on(mj_lfb* b, float* u0, float* u1, float* out, bool sources, cudaStream_t s) {
+  const RsVariant& v = rs_variants()[b->rs_variant];
+  RsParams prm = rs_params(b, v);
+  prm.ua = u0;
+  prm.ub = u1;
+  prm.uout = out;
+  if (!sources) {
+    prm.n_src_dof = 0;
+    prm.n_pulse = 0;
+  }
+  return rs_launch(v, b->rs_grid, prm, b->rs_chunks.as<RsChunk>(), b->rs_n_chunks, b->rs_sync.as<SyncState>(), 0,
+                   b->rs_err.as<int>(), s);
+}
+
+// Error flag of the one-kernel step (bounded waits), reset when set.
+int lfb_fused_check(mj_lfb* b, cudaStream_t s) { return rs_check_err(b, s); }
+
+// One ordinary step of the one-kernel form (the integrator's own states and
+// step counter).
+int lfb_fused_step(mj_lfb* b, cudaStream_t s) {
+  const RsVariant& v = rs_variants()[b->rs_variant];
+  const RsParams prm = rs_params(b, v);
+  return rs_launch(v, b->rs_grid, prm, b->rs_chunks.as<RsChunk>(), b->rs_n_chunks, b->rs_sync.as<SyncState>(),
+                   b->step & 1, b->rs_err.as<int>(), s);
 }
 
 // Phase times (ms) of the last profiled step: element phase (last CTA,

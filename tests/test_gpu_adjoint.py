@@ -59,3 +59,18 @@ def test_torch_autograd_function(case):
     J.backward()
     assert rel_l2(c.grad.numpy(), g_ref) < 1e-3
     model.close()
+
+
+def test_one_kernel_and_two_kernel_steps_give_the_same_gradient(case):
+    """Forward, checkpoint replays and adjoint steps run on the one-kernel
+    step by default; the two-kernel form gives the same traces and gradient
+    (same FP32 arithmetic: bitwise, asserted at 1e-12)."""
+    m1 = make_model(case, checkpoint_every=5)
+    m2 = make_model(case, checkpoint_every=5)
+    assert m1.batch.step_info()["one_kernel"]
+    m2.batch.set_fused(False)
+    J1, g1 = m1.loss_and_grad(case["c0"], case["data"])
+    J2, g2 = m2.loss_and_grad(case["c0"], case["data"])
+    assert abs(J1 - J2) <= 1e-12 * abs(J2)
+    assert rel_l2(g1, g2) <= 1e-12
+    m1.close(); m2.close()
