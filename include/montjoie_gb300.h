@@ -292,13 +292,18 @@ int mj_mb_destroy(mj_mb* mb);
 int mj_mb_advance(mj_mb* mb, int nsteps, int use_graph);
 
 /* Launch shape of the batch kernel: CTAs, CTAs per SM, element tiles and dof
- * chunks per step, and 1 if the last advance replayed a graph. */
-int mj_mb_info(const mj_mb* mb, int* grid, int* ctas_per_sm, int* n_tiles, int* n_chunks, int* graph);
+ * chunks per step, 1 if the last advance replayed a graph, and the order
+ * index n = r+1 when every mesh has that order (the batch then runs the
+ * kernel instance of that order alone), else 0.  Any output may be NULL. */
+int mj_mb_info(const mj_mb* mb, int* grid, int* ctas_per_sm, int* n_tiles, int* n_chunks, int* graph,
+               int* single_order);
 
 /* Profiling aid: with enable != 0 every step is a plain launch that records
- * per-CTA time stamps; mj_mb_phase_ms then returns, for the last step, out[0]
- * = element phase (last CTA), out[1] = element phase (mean CTA), out[2] =
- * barrier release, out[3] = dof phase, in ms. */
+ * per-CTA time stamps; mj_mb_phase_ms then returns, for the last step (out:
+ * room for 6), out[0] = element phase (last CTA), out[1] = element phase
+ * (mean CTA), out[2] = barrier release, out[3] = dof phase, out[4] = time a
+ * CTA spent waiting for its element tiles' bulk copies, out[5] = the same for
+ * its dof chunks (means over the CTAs), in ms. */
 int mj_mb_profile(mj_mb* mb, int enable);
 int mj_mb_phase_ms(const mj_mb* mb, double* out);
 

@@ -133,7 +133,7 @@ def load(build_if_missing: bool = True):
     L.mj_mb_create.argtypes = [ctypes.c_int, ctypes.POINTER(_VP), ctypes.POINTER(_VP)]
     L.mj_mb_destroy.argtypes = [_VP]
     L.mj_mb_advance.argtypes = [_VP, ctypes.c_int, ctypes.c_int]
-    L.mj_mb_info.argtypes = [_VP] + [ctypes.POINTER(ctypes.c_int)] * 5
+    L.mj_mb_info.argtypes = [_VP] + [ctypes.POINTER(ctypes.c_int)] * 6
     L.mj_mb_profile.argtypes = [_VP, ctypes.c_int]
     L.mj_mb_phase_ms.argtypes = [_VP, _D]
     L.mj_mb_tuning.argtypes = [_VP, ctypes.POINTER(ctypes.c_int), _D]

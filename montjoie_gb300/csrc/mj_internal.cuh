@@ -164,4 +164,10 @@ int lfb_fused_step_on(mj_lfb* b, float* u0, float* u1, float* out, bool sources,
 int lfb_fused_step(mj_lfb* b, cudaStream_t s);
 int lfb_fused_check(mj_lfb* b, cudaStream_t s);
 
+// Single-order instances of the many-mesh batch kernel (mj_multi_one.cu):
+// the kernel for `threads` per CTA and order n (2..9), and the FP32
+// derivative matrix of order n in that translation unit's constant bank.
+const void* mb_one_order_kernel(int threads, int n);
+int mb_one_order_set_gmat(int n, const float* v);
+
 }  // namespace mj

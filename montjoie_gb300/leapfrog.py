@@ -277,9 +277,11 @@ class MeshBatch:
             r.n_time += nsteps
 
     def info(self) -> dict:
-        vals = [ctypes.c_int() for _ in range(5)]
+        """Launch shape; single_order = n when every mesh has order n-1 (the
+        batch runs that order's kernel instance), else 0."""
+        vals = [ctypes.c_int() for _ in range(6)]
         _lib.check(_lib.load().mj_mb_info(self._h, *[ctypes.byref(v) for v in vals]))
-        return dict(zip(["grid", "ctas_per_sm", "tiles", "chunks", "graph"], [v.value for v in vals]))
+        return dict(zip(["grid", "ctas_per_sm", "tiles", "chunks", "graph", "single_order"], [v.value for v in vals]))
 
     def n_dof(self) -> int:
         return sum(r.op.n_dof for r in self.runs)
@@ -302,10 +304,12 @@ class MeshBatch:
 
     def phase_ms(self) -> dict:
         """Phase times of the last step (ms): element phase (last and mean CTA),
-        barrier release, dof phase."""
-        out = np.zeros(4)
+        barrier release, dof phase, and the mean time a CTA waited for the bulk
+        copies of its element tiles and of its dof chunks."""
+        out = np.zeros(6)
         _lib.check(_lib.load().mj_mb_phase_ms(self._h, _lib.dptr(out)))
-        return dict(zip(["element_last", "element_mean", "barrier", "dof"], out.tolist()))
+        return dict(zip(["element_last", "element_mean", "barrier", "dof", "element_copy_wait", "dof_copy_wait"],
+                        out.tolist()))
 
     def close(self) -> None:
         if getattr(self, "_h", None):

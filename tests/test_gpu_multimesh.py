@@ -47,6 +47,7 @@ def test_batch_matches_reference_and_single_runs(threads):
         mb.set_config(threads)
     info = mb.info()
     assert info["tiles"] > 0 and info["chunks"] >= len(CASES) and info["grid"] >= 1
+    assert info["single_order"] == 0  # several orders: the all-orders kernel
     mb.advance(30)  # one 20-step graph + 10 launches
     assert mb.info()["graph"] == 1
     assert mb.tuning()["threads"] == (threads or mb.tuning()["threads"]) and mb.tuning()["threads"] in (128, 256)
@@ -76,6 +77,33 @@ def test_batch_matches_reference_and_single_runs(threads):
         v0, v1 = ls.GetState()
         assert rel_l2(u0, v0) < SAME_TOL and rel_l2(u1, v1) < SAME_TOL
         assert lf.n_time == ls.n_time
+    mb.close()
+    for op, lf in batch_runs + single_runs:
+        lf.close()
+        op.close()
+
+
+@pytest.mark.parametrize("threads", [128, 256])
+@pytest.mark.parametrize("cases,n", [(["regular2_q4", "cube3_q4", "cube4_q4"], 5), (["cube2_q8", "cube2_q8"], 9)])
+def test_single_order_batch(cases, n, threads):
+    """Meshes of one order run that order's kernel instance: the same states
+    as the runs advanced one by one, and the reference's snapshots."""
+    from montjoie_gb300.leapfrog import MeshBatch
+    gs = [load_golden(c) for c in cases]
+    batch_runs = [run_fp32(g) for g in gs]
+    single_runs = [run_fp32(g) for g in gs]
+    mb = MeshBatch([lf for _, lf in batch_runs])
+    mb.set_config(threads)
+    assert mb.info()["single_order"] == n
+    for steps, kw in ((30, {}), (9, {"graph": False}), (1, {})):
+        mb.advance(steps, **kw)
+        for g, (_, lf), (_, ls) in zip(gs, batch_runs, single_runs):
+            ls.Advance(steps)
+            u = lf.GetIterate()
+            assert rel_l2(u, ls.GetIterate()) < SAME_TOL
+            ref = snapshot(g, lf.n_time)
+            if ref is not None:
+                assert rel_l2(u, ref) < FP32_TOL
     mb.close()
     for op, lf in batch_runs + single_runs:
         lf.close()
