@@ -231,20 +231,27 @@ __global__ void k_gather_o4_init(const Real* __restrict__ R, const int* __restri
 // multiple of 4).  A chunk's u^{n+1}, u^n, dt^2/D, CSR offsets and its
 // contiguous range of contributions R[ptr[d0] .. ptr[d1]) arrive by 1-D bulk
 // copies (16-byte rounded; every buffer carries spare entries past its end)
-// into one of two shared-memory buffers, the next chunk's while this one is
-// summed.  Same arithmetic as k_gather_leapfrog<float, false> followed by
+// into a ring of kStreamNB shared-memory buffers: the next kStreamNB - 1
+// chunks' copies are in flight while one chunk is summed.  Same arithmetic as k_gather_leapfrog<float, false> followed by
 // k_source (the source in FP64 after the update), so the states agree bit
 // for bit.  Every mbarrier wait is bounded (error flag on timeout).
 // ---------------------------------------------------------------------------
+// Shape measured at 64^3 Q4 (K2 alone, CUDA events): 256 threads, 2 buffers
+// of 12 KB and chunks of up to 512 dofs (8 CTAs per SM) take 0.077 ms against
+// 0.094 ms for 2 x 32 KB / 1024 dofs (3 CTAs per SM); deeper rings at fewer
+// CTAs per SM were slower still: the summing, not the copies, sets the pace.
 constexpr int kStreamThreads = 256;
-constexpr int kStreamDofs = 1024;
-constexpr int kStreamBuf = 32768;                         // bytes per chunk buffer
+constexpr int kStreamNB = 2;                              // buffers per CTA
+constexpr int kStreamDofs = 512;
+constexpr int kStreamBuf = 12288;                         // bytes per chunk buffer
 constexpr int kStreamM = 2 * kStreamDofs * 4;             // offsets inside a buffer
 constexpr int kStreamP = kStreamM + (kStreamDofs + 4) * 4;
 constexpr int kStreamR = kStreamP + (kStreamDofs + 8) * 4;
 constexpr int kStreamRCap = (kStreamBuf - kStreamR) / 4;  // R entries one chunk may stage
-constexpr int kStreamSmem = 2 * kStreamBuf + 16;
-static_assert(kStreamM % 16 == 0 && kStreamP % 16 == 0 && kStreamR % 16 == 0, "aligned buffer segments");
+constexpr int kStreamSmem = kStreamNB * kStreamBuf + 8 * kStreamNB;
+static_assert(kStreamM % 16 == 0 && kStreamP % 16 == 0 && kStreamR % 16 == 0 && kStreamBuf % 16 == 0,
+              "aligned buffer segments");
+static_assert(kStreamDofs % kStreamThreads == 0 && kStreamNB >= 2 && kStreamNB <= 8, "chunk shape");
 
 struct StreamChunk {
   int d0, d1, q0, q1;  // dofs [d0, d1); R range [q0, q1) rounded to multiples of 4
@@ -259,7 +266,7 @@ __global__ void __launch_bounds__(kStreamThreads)
                              const float* __restrict__ sval, int nsrc, const double* __restrict__ pulse, int n_pulse,
                              const double* __restrict__ inv_mass, double dt2, int* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char smem[];
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 2 * kStreamBuf);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + kStreamNB * kStreamBuf);
   const int t = threadIdx.x, G = gridDim.x;
   if (blockIdx.x == 0 && t == 0) ctr[1 - qc] = ctr[qc] + 1;
   const int step = ctr[qc];
@@ -280,16 +287,14 @@ __global__ void __launch_bounds__(kStreamThreads)
     bulk_g2s(dst + kStreamR, R + ch.q0, rb, &bar[b]);
   };
   if (t == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
+    for (int b = 0; b < kStreamNB; b++) mbar_init(&bar[b], 1);
     fence_mbar_init();
-    issue(blockIdx.x, 0);
-    issue(blockIdx.x + G, 1);
+    for (int b = 0; b < kStreamNB; b++) issue(blockIdx.x + b * G, b);
   }
   __syncthreads();
-  uint32_t ph = 0u;
-  for (int c = blockIdx.x, it = 0; c < n_chunks; c += G, ++it) {
-    const int b = it & 1;
+  uint32_t ph = 0u;  // bit b: parity of buffer b's next completion
+  int b = 0;
+  for (int c = blockIdx.x; c < n_chunks; c += G, b = (b + 1 == kStreamNB ? 0 : b + 1)) {
     const StreamChunk ch = chunks[c];
     const bool ok = mbar_wait_bounded(&bar[b], (ph >> b) & 1u);
     if (__syncthreads_or(!ok)) {
@@ -323,7 +328,7 @@ __global__ void __launch_bounds__(kStreamThreads)
     __syncthreads();  // buffer b is free
     if (t == 0) {
       fence_proxy_async();
-      issue(c + 2 * G, b);
+      issue(c + kStreamNB * G, b);
     }
   }
 }
