@@ -104,6 +104,31 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
   return false;
 }
 
+// Sums of the staged contributions of V dofs of one thread (dof-ordered
+// CSR: dof dl[v] owns sR[sp[dl] - q0 .. sp[dl + 1] - q0)).  Each sum is
+// 0 + R[qa] + R[qa + 1] + ... in CSR order, the order of the plain gather;
+// the first terms of all V dofs are loaded together before the rest, so
+// their latencies overlap.
+template <int V>
+__device__ __forceinline__ void contrib_sums(const int* sp, const float* sR, int q0, const int (&dl)[V],
+                                             const bool (&on)[V], float (&s)[V]) {
+  int qa[V], qb[V];
+  float first[V];
+#pragma unroll
+  for (int v = 0; v < V; v++) {
+    qa[v] = on[v] ? sp[dl[v]] - q0 : 0;
+    qb[v] = on[v] ? sp[dl[v] + 1] - q0 : 0;
+  }
+#pragma unroll
+  for (int v = 0; v < V; v++) first[v] = qa[v] < qb[v] ? sR[qa[v]] : 0.f;
+#pragma unroll
+  for (int v = 0; v < V; v++) {
+    s[v] = 0.f;
+    if (qa[v] < qb[v]) s[v] += first[v];
+    for (int q = qa[v] + 1; q < qb[v]; q++) s[v] += sR[q];
+  }
+}
+
 // Loads the first RW values of a 16-byte aligned shared-memory line with
 // 16-byte loads.
 template <int RW>

@@ -308,15 +308,22 @@ __global__ void __launch_bounds__(kStreamThreads)
     const float* sm = reinterpret_cast<const float*>(buf + kStreamM);
     const int* sp = reinterpret_cast<const int*>(buf + kStreamP);
     const float* sR = reinterpret_cast<const float*>(buf + kStreamR);
+    constexpr int V = kStreamDofs / kStreamThreads;
+    int dls[V];
+    bool on[V];
+    float sums[V];
 #pragma unroll
-    for (int v = 0; v < kStreamDofs / kStreamThreads; v++) {
-      const int dl = v * kStreamThreads + t;
+    for (int v = 0; v < V; v++) {
+      dls[v] = v * kStreamThreads + t;
+      on[v] = ch.d0 + dls[v] < ch.d1;
+    }
+    contrib_sums<V>(sp, sR, ch.q0, dls, on, sums);
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+      const int dl = dls[v];
       const int d = ch.d0 + dl;
-      if (d < ch.d1) {
-        float s = 0.f;
-        const int qb = sp[dl + 1] - ch.q0;
-        for (int q = sp[dl] - ch.q0; q < qb; q++) s += sR[q];
-        const float ah = -s;
+      if (on[v]) {
+        const float ah = -sums[v];
         float un = 2.f * su1[dl] - su0[dl] + sm[dl] * ah;
         if (src_on && ch.has_src) {
           const double f = source_at(mask, sidx, sval, nsrc, d);

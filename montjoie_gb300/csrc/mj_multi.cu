@@ -106,8 +106,8 @@ int mb_launch(mj_mb* mb, int which, int k, cudaStream_t s) {
 }
 
 // Tile and chunk lists of configuration T: tiles sorted by decreasing cost
-// (dealt round-robin to the CTAs), chunks of at most kChunkDofs dofs whose
-// 16-byte rounded range of contributions fits kRCap.
+// (dealt round-robin to the CTAs), chunks of at most kChunkDofs dofs (one
+// warp's) whose 16-byte rounded range of contributions fits kRCap.
 template <int T>
 int mb_build_lists(mj_mb* mb, const std::vector<std::vector<int>>& src_dofs, MbLists& L) {
   using P = MbPlan<T>;

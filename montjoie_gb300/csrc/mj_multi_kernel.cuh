@@ -55,19 +55,24 @@ struct MbPlan {
                                      cmax(cmax(work_of(6), work_of(7)), cmax(work_of(8), work_of(9)))) +
                                 3) / 4 * 4;
   static constexpr int kArea = 2 * kStage + 3 * kWork * 4;  // stages + work arrays (u, vx, vy)
-  static constexpr int kSmem = kArea + 32;                  // + 4 mbarriers
   static constexpr int kMaxG = (kWork + T - 1) / T;         // gathered values per thread
-  // phase 2: two chunk buffers [u^{n+1} | u^n | dt^2/D | offsets | R range]
-  static constexpr int kDofsPerThread = 4;
-  static constexpr int kChunkDofs = T * kDofsPerThread;
-  static constexpr int kP2Buf = kArea / 2 / 16 * 16;
+  // phase 2: every warp streams its own dof chunks through two buffers
+  // [u^{n+1} | u^n | dt^2/D | offsets | R range] carved from the same area
+  static constexpr int kWarps = T / 32;
+  static constexpr int kDofsPerLane = 8;
+  static constexpr int kChunkDofs = 32 * kDofsPerLane;
+  static constexpr int kP2Buf = kArea / (2 * kWarps) / 16 * 16;
   static constexpr int kP2Ptr = 3 * kChunkDofs * 4;
   static constexpr int kP2R = kP2Ptr + (kChunkDofs + 4) * 4;
   static constexpr int kRCap = (kP2Buf - kP2R) / 4;
+  // mbarriers after the area: 2 tile stages, then 2 chunk buffers per warp
+  static constexpr int kBars = 2 + 2 * kWarps;
+  static constexpr int kSmem = kArea + 8 * kBars;
   static_assert(kStage % 128 == 0 && kArea % 16 == 0, "stages, work arrays and mbarriers are aligned");
-  static_assert(2 * kP2Buf <= kArea, "chunk buffers end before the mbarriers");
-  static_assert(kP2R % 16 == 0, "bulk-copy destinations are 16-byte aligned");
-  static_assert(kRCap >= 8 * kChunkDofs + 3, "a chunk of Q1 dofs (8 contributions each) must fit");
+  static_assert(2 * kWarps * kP2Buf <= kArea, "chunk buffers end before the mbarriers");
+  static_assert(kP2R % 16 == 0 && kP2Buf % 16 == 0, "bulk-copy destinations are 16-byte aligned");
+  // the chunk builder halves a chunk whose contributions do not fit, down to 4 dofs
+  static_assert(kRCap >= 8 * 4 + 3, "4 dofs of Q1 (8 contributions each) must fit");
   static_assert(C::min_ctas * (kSmem + 1024) <= 228 * 1024, "CTAs per SM");
 };
 
@@ -346,7 +351,7 @@ __global__ void __launch_bounds__(T, MbCfg<T>::min_ctas)
   Work cur = load_work(work, n_work, w);
   Work nxt = load_work(work, n_work, w + G);
   if (t == 0) {
-    for (int b = 0; b < 4; b++) mbar_init(&bar[b], 1);  // 0,1: tile stages; 2,3: chunk buffers
+    for (int b = 0; b < P::kBars; b++) mbar_init(&bar[b], 1);  // 0,1: tile stages; then 2 per warp
     fence_mbar_init();
     if (cur.mesh >= 0) issue_tile<T>(tab.m[cur.mesh], cur.tile, smem, &bar[0]);
     if (nxt.mesh >= 0) issue_tile<T>(tab.m[nxt.mesh], nxt.tile, smem + P::kStage, &bar[1]);
@@ -428,66 +433,84 @@ __global__ void __launch_bounds__(T, MbCfg<T>::min_ctas)
   if (!grid_barrier(sync, err)) return;
   if (prof && t == 0) stamps[kStamps * blockIdx.x + 2] = global_ns();
 
-  // ---- phase 2: dof chunks b, b+G, ..., two buffers per CTA.  A chunk's
-  // u^{n+1}, u^n, dt^2/D, CSR offsets and contributions R[ptr[d0] ..
+  // ---- phase 2: each warp walks its own dof chunks (global warp index,
+  // stride the grid's warp count) through two buffers of its own.  A
+  // chunk's u^{n+1}, u^n, dt^2/D, CSR offsets and contributions R[ptr[d0] ..
   // ptr[d1]) (contiguous: R is in dof order) arrive by bulk copy, the next
-  // chunk's while this one is summed, updated and written back.
-  int c = blockIdx.x;
-  Chunk ccur = load_chunk(chunks, n_chunks, c);
-  Chunk cnxt = load_chunk(chunks, n_chunks, c + G);
-  if (t == 0) {
-    fence_proxy_async();         // phase-1 use of this shared memory is over
-    fence_proxy_async_global();  // every CTA's R stores (ordered by the barrier) before the copies
-    if (ccur.mesh >= 0) issue_chunk<T>(tab.m[ccur.mesh], ccur, k, smem, &bar[2]);
-    if (cnxt.mesh >= 0) issue_chunk<T>(tab.m[cnxt.mesh], cnxt, k, smem + P::kP2Buf, &bar[3]);
-  }
-  uint32_t ph2 = 0u;
-  for (int it = 0; ccur.mesh >= 0; ++it) {
-    const Chunk cn2 = load_chunk(chunks, n_chunks, c + 2 * G);
-    const int b = it & 1;
-    unsigned char* buf = smem + b * P::kP2Buf;
-    const MeshDev& m = tab.m[ccur.mesh];
-    const unsigned long long w0 = prof ? global_ns() : 0ull;
-    const bool ok = mbar_wait_bounded(&bar[2 + b], (ph2 >> b) & 1u);
-    if (prof) wns2 += global_ns() - w0;
-    if (__syncthreads_or(!ok)) {
-      if (t == 0) atomicExch(err, 1);
-      return;
+  // chunk's while this one is summed, updated and written back; warps sync
+  // among their own lanes only.
+  {
+    const int lane = t & 31, wid = t >> 5;
+    const int GW = G * P::kWarps;
+    uint64_t* wbar = bar + 2 + 2 * wid;
+    unsigned char* wbuf = smem + 2 * wid * P::kP2Buf;
+    int c = blockIdx.x * P::kWarps + wid;
+    Chunk ccur = load_chunk(chunks, n_chunks, c);
+    Chunk cnxt = load_chunk(chunks, n_chunks, c + GW);
+    if (lane == 0) {
+      fence_proxy_async();         // phase-1 use of this shared memory is over
+      fence_proxy_async_global();  // every CTA's R stores (ordered by the barrier) before the copies
+      if (ccur.mesh >= 0) issue_chunk<T>(tab.m[ccur.mesh], ccur, k, wbuf, &wbar[0]);
+      if (cnxt.mesh >= 0) issue_chunk<T>(tab.m[cnxt.mesh], cnxt, k, wbuf + P::kP2Buf, &wbar[1]);
     }
-    ph2 ^= 1u << b;
-    const float* su1 = reinterpret_cast<const float*>(buf);
-    const float* su0 = su1 + P::kChunkDofs;
-    const float* smv = su0 + P::kChunkDofs;
-    const int* sptr = reinterpret_cast<const int*>(buf + P::kP2Ptr);
-    const float* sR = reinterpret_cast<const float*>(buf + P::kP2R);
-    float* __restrict__ u0 = ((k + m.cur_par) & 1) == 0 ? m.ua : m.ub;  // U^n, overwritten by U^{n+2}
-    const int step = ccur.has_src ? m.ctr[(k + m.qc_par) & 1] : 0;
-#pragma unroll
-    for (int v = 0; v < P::kDofsPerThread; v++) {
-      const int dl = v * T + t;
-      const int d = ccur.d0 + dl;
-      if (d < ccur.d1) {
-        float sum = 0;
-        const int qb = sptr[dl + 1] - ccur.q0;
-        for (int q = sptr[dl] - ccur.q0; q < qb; q++) sum += sR[q];
-        const float ah = -sum;
-        float un = float(2) * su1[dl] - su0[dl] + smv[dl] * ah;
-        if (ccur.has_src && ((__ldg(m.src_mask + (d >> 5)) >> (d & 31)) & 1u) && step < m.n_pulse) {
-          const int ts = find_source(m.src_idx, m.n_src, d);
-          un = float(double(un) + m.dt2 * __ldg(m.inv_mass + d) * __ldg(m.pulse + step) *
-                                      double(__ldg(m.src_val + ts)));
-        }
-        u0[d] = un;
+    uint32_t ph2 = 0u;
+    for (int it = 0; ccur.mesh >= 0; ++it) {
+      const Chunk cn2 = load_chunk(chunks, n_chunks, c + 2 * GW);
+      const int b = it & 1;
+      unsigned char* buf = wbuf + b * P::kP2Buf;
+      const MeshDev& m = tab.m[ccur.mesh];
+      const unsigned long long w0 = prof ? global_ns() : 0ull;
+      const bool ok = mbar_wait_bounded(&wbar[b], (ph2 >> b) & 1u);
+      if (prof) wns2 += global_ns() - w0;
+      if (__any_sync(0xffffffffu, !ok)) {
+        // report, then wait (bounded) for this warp's copies still in flight
+        if (lane == 0) atomicExch(err, 1);
+        mbar_wait_bounded(&wbar[b], (ph2 >> b) & 1u);
+        if (cnxt.mesh >= 0) mbar_wait_bounded(&wbar[b ^ 1], (ph2 >> (b ^ 1)) & 1u);
+        break;
       }
+      ph2 ^= 1u << b;
+      const float* su1 = reinterpret_cast<const float*>(buf);
+      const float* su0 = su1 + P::kChunkDofs;
+      const float* smv = su0 + P::kChunkDofs;
+      const int* sptr = reinterpret_cast<const int*>(buf + P::kP2Ptr);
+      const float* sR = reinterpret_cast<const float*>(buf + P::kP2R);
+      float* __restrict__ u0 = ((k + m.cur_par) & 1) == 0 ? m.ua : m.ub;  // U^n, overwritten by U^{n+2}
+      const int step = ccur.has_src ? m.ctr[(k + m.qc_par) & 1] : 0;
+      constexpr int V = P::kDofsPerLane;
+      int dls[V];
+      bool on[V];
+      float sums[V];
+#pragma unroll
+      for (int v = 0; v < V; v++) {
+        dls[v] = v * 32 + lane;
+        on[v] = ccur.d0 + dls[v] < ccur.d1;
+      }
+      contrib_sums<V>(sptr, sR, ccur.q0, dls, on, sums);
+#pragma unroll
+      for (int v = 0; v < V; v++) {
+        const int dl = dls[v];
+        const int d = ccur.d0 + dl;
+        if (on[v]) {
+          const float ah = -sums[v];
+          float un = float(2) * su1[dl] - su0[dl] + smv[dl] * ah;
+          if (ccur.has_src && ((__ldg(m.src_mask + (d >> 5)) >> (d & 31)) & 1u) && step < m.n_pulse) {
+            const int ts = find_source(m.src_idx, m.n_src, d);
+            un = float(double(un) + m.dt2 * __ldg(m.inv_mass + d) * __ldg(m.pulse + step) *
+                                        double(__ldg(m.src_val + ts)));
+          }
+          u0[d] = un;
+        }
+      }
+      __syncwarp();  // buffer b is free
+      if (lane == 0 && cn2.mesh >= 0) {
+        fence_proxy_async();
+        issue_chunk<T>(tab.m[cn2.mesh], cn2, k, buf, &wbar[b]);
+      }
+      c += GW;
+      ccur = cnxt;
+      cnxt = cn2;
     }
-    __syncthreads();  // buffer b is free
-    if (t == 0 && cn2.mesh >= 0) {
-      fence_proxy_async();
-      issue_chunk<T>(tab.m[cn2.mesh], cn2, k, buf, &bar[2 + b]);
-    }
-    c += G;
-    ccur = cnxt;
-    cnxt = cn2;
   }
   if (prof) {
     __syncthreads();
