@@ -40,6 +40,7 @@ struct mj_lf {
   mj::DevBuf mass, minv;     // op precision (FP64: D and 1/D; FP32: unused / dt^2/D)
   mj::DevBuf inv_mass64;     // FP64 1/D for the initial step
   mj::DevBuf norm_w;         // FP64 weights, or empty
+  mj::DevBuf norm_w32;       // the same rounded to FP32 (FP32 integrators), or empty
   mj::DevBuf rec_idx, rec_w; // receivers
   mj::DevBuf ua, ub;         // state: U^n (cur) and U^{n+1} (next)
   mj::DevBuf du0, tmp;       // staging

@@ -361,9 +361,11 @@ __device__ __forceinline__ double norm_group<float>(const double (&w)[4], const 
                 (float(w[2]) * u[2] * u[2] + float(w[3]) * u[3] * u[3]));
 }
 
+// w32: for FP32 state, the weights rounded to FP32 once (norm_group<float>
+// rounds them so), read in the grouped loop instead of the FP64 ones.
 template <typename Real>
-__global__ void k_norm_partial(const Real* __restrict__ u, const double* __restrict__ w, int n,
-                               double* __restrict__ partial) {
+__global__ void k_norm_partial(const Real* __restrict__ u, const double* __restrict__ w,
+                               const float* __restrict__ w32, int n, double* __restrict__ partial) {
   __shared__ double sh[32];
   // each thread: groups of four strided terms into one FP64 accumulator,
   // then a fixed warp and block tree: deterministic for a given grid
@@ -375,7 +377,7 @@ __global__ void k_norm_partial(const Real* __restrict__ u, const double* __restr
     Real uv[4];
 #pragma unroll
     for (int v = 0; v < 4; v++) {
-      wv[v] = __ldg(w + d + v * stride);
+      wv[v] = w32 ? double(__ldg(w32 + d + v * stride)) : __ldg(w + d + v * stride);
       uv[v] = __ldg(u + d + v * stride);
     }
     acc += norm_group<Real>(wv, uv);

@@ -547,6 +547,11 @@ int mj_lf_create(mj_op* op, const mj_lf_desc* desc, mj_lf** out) {
   if (desc->norm_weight) {
     MJ_CUDA(lf->norm_w.alloc(sizeof(double) * n));
     MJ_CUDA(cudaMemcpy(lf->norm_w.ptr, desc->norm_weight, sizeof(double) * n, cudaMemcpyHostToDevice));
+    if (op->precision == MJ_FP32) {  // the FP32 norm rounds the weights to FP32: read them so (8 B per dof less)
+      std::vector<float> w32(desc->norm_weight, desc->norm_weight + n);
+      MJ_CUDA(lf->norm_w32.alloc(sizeof(float) * n));
+      MJ_CUDA(cudaMemcpy(lf->norm_w32.ptr, w32.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+    }
   }
   lf->n_rec = desc->n_rec;
   lf->n_rec_w = desc->n_rec_w;
@@ -651,7 +656,8 @@ int lf_diag(mj_lf* lf, double* norms_d, int norm_col, double* traces_d, int stri
   const int n = lf->n_dof;
   const Real* u = static_cast<const Real*>(lf->cur());
   if (norms_d && lf->norm_w.ptr) {
-    k_norm_partial<Real><<<lf->norm_blocks, 256, 0, s>>>(u, lf->norm_w.as<double>(), n, lf->partial.as<double>());
+    k_norm_partial<Real><<<lf->norm_blocks, 256, 0, s>>>(u, lf->norm_w.as<double>(), lf->norm_w32.as<float>(), n,
+                                                         lf->partial.as<double>());
     k_norm_final<<<1, 32, 0, s>>>(lf->partial.as<double>(), lf->norm_blocks, norms_d + norm_col, lf->flag.as<int>());
     count_launch(2);
   }

@@ -110,12 +110,15 @@ class LeapFrogIterator:
         _lib.check(_lib.load().mj_lf_get_state(self._h, _lib.dptr(u), _lib.dptr(v)))
         return u, v
 
-    def Run(self, u0, du0, nsteps: int):
+    def Run(self, u0, du0, nsteps: int, out=None):
         """Whole RunSecondOrderScheme in one C-ABI call: returns (u_final, norms, traces)
-        with nsteps+1 diagnostic columns (iterates 0..nsteps)."""
+        with nsteps+1 diagnostic columns (iterates 0..nsteps).  out: an optional
+        float64 array of n_dof (e.g. in pinned host memory) that receives u_final."""
         u0 = np.ascontiguousarray(u0, dtype=np.float64)
         du0 = None if du0 is None else np.ascontiguousarray(du0, dtype=np.float64)
-        uf = np.zeros(self.op.n_dof)
+        if out is not None and (out.dtype != np.float64 or out.size != self.op.n_dof or not out.flags.c_contiguous):
+            raise ValueError("Run: out must be a contiguous float64 array of n_dof values")
+        uf = np.zeros(self.op.n_dof) if out is None else out
         norms = np.zeros(nsteps + 1) if self.has_norm else None
         traces = np.zeros((self.n_rec, nsteps + 1)) if self.n_rec else None
         _lib.check(_lib.load().mj_lf_run(self._h, _lib.dptr(u0), _lib.dptr(du0), int(nsteps), _lib.dptr(uf),
