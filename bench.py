@@ -62,6 +62,20 @@ def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def max_over_ranks(x, dist, device):
+    """Largest x over the ranks of the default process group (the slowest
+    replica's time)."""
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, world, ms_max):
+    """Units all replicas processed per second, timed by the slowest one."""
+    return units_per_rank * world / (ms_max / 1e3)
+
+
 def workload_mesh(cells):
     from montjoie_gb300 import mesh as M
     return M.perturbed_cube(cells, seed=SEED, amplitude=0.05, kind="random", c_mode="blocks", c_blocks=8)
@@ -462,20 +476,25 @@ def LeapFrogIteratorFor(pb, op, src_idx, src_val):
     return LeapFrogIterator(op, pb.setup.dt, pb.mass, None, src_idx, src_val, pb.pulse)
 
 
-def time_advance(torch, lf, steps, lib, prof_steps=100):
+def time_advance(torch, lf, steps, lib, prof_steps=100, barrier=None):
     """Times `steps` leap-frog steps (already initialised) with CUDA events on the
-    library's stream (the legacy default stream; CUDA-graph replay), then
-    `prof_steps` more steps launched one by one with events around each kernel
-    for the per-kernel times."""
+    library's stream (the legacy default stream; CUDA-graph replay), bracketed
+    by `barrier` (the replicas' barrier, if any) and a device synchronisation
+    on both sides; then `prof_steps` more steps launched one by one with events
+    around each kernel for the per-kernel times."""
     import ctypes
     L = lib.load()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
+    if barrier:
+        barrier()
     l0 = lib.kernel_launches()
     start.record()
     lf.Advance(steps)
     end.record()
     torch.cuda.synchronize()
+    if barrier:
+        barrier()
     launches = lib.kernel_launches() - l0
     L.mj_lf_profile(lf.handle, 1, None, None, None)
     lf.Advance(min(steps, prof_steps))
@@ -509,10 +528,7 @@ def run_ours(args):
     lf32.Advance(W)
     clocks = ClockSampler(local)
     clocks.start()
-    if world > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
-    ms32, k1_ms, k2_ms, launches = time_advance(torch, lf32, K, _lib)
+    ms32, k1_ms, k2_ms, launches = time_advance(torch, lf32, K, _lib, barrier=dist.barrier if world > 1 else None)
     # ---- FP64 plain form, resident
     op64 = pb.operator("fp64")
     lf64 = pb.integrator(op64, diagnostics=False)
@@ -522,10 +538,8 @@ def run_ours(args):
     ms64, k1_64, k2_64, _ = time_advance(torch, lf64, K64, _lib)
     clk = clocks.stop()
     if world > 1:
-        t = torch.tensor([ms32], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms32 = float(t.item())
-    value = n_dof * K * world / (ms32 / 1e3)
+        ms32 = max_over_ranks(ms32, dist, "cuda")
+    value = whole_job_rate(n_dof * K, world, ms32)
     value64 = n_dof * K64 / (ms64 / 1e3)
     lf32.close(); lf64.close()
 
