@@ -43,6 +43,7 @@ struct MbCfg<128> {
 template <int T>
 struct MbPlan {
   using C = MbCfg<T>;
+  static_assert(C::threads == T, "configuration keyed by its thread count");
   static constexpr int stage_of(int n) { return C::tile(n) * elem_slots(n) * 28; }  // factors + Nodle
   static constexpr int work_of(int n) { return C::tile(n) * n * n * n; }
   static constexpr int stage_max =
