@@ -45,9 +45,11 @@ struct mj_lf {
   mj::DevBuf ua, ub;         // state: U^n (cur) and U^{n+1} (next)
   mj::DevBuf du0, tmp;       // staging
   mj::DevBuf partial, norms_d, traces_d, flag;
+  mj::DevBuf diag_done, diag_where;  // fused diagnostics: finished-block counter, DiagDev of graph replays
   mj::DevBuf pulse_d, ctr;   // pulse of every step and the two step counters
   int n_pulse = 0;
   cudaGraphExec_t graph = nullptr, graph_prof = nullptr;
+  cudaGraphExec_t graph_diag = nullptr;  // steps with norm and receivers, columns read from diag_where
   bool use_graph = true;  // replay captured steps when no diagnostics are asked
   int n_src = 0, n_rec = 0, n_rec_w = 0;
   int step = 0;
@@ -77,6 +79,7 @@ struct mj_lf {
     for (cudaEvent_t e : ev) cudaEventDestroy(e);
     if (graph) cudaGraphExecDestroy(graph);
     if (graph_prof) cudaGraphExecDestroy(graph_prof);
+    if (graph_diag) cudaGraphExecDestroy(graph_diag);
   }
   void* cur() { return cur_is_a ? ua.ptr : ub.ptr; }
   void* next() { return cur_is_a ? ub.ptr : ua.ptr; }

@@ -361,17 +361,19 @@ __device__ __forceinline__ double norm_group<float>(const double (&w)[4], const 
                 (float(w[2]) * u[2] * u[2] + float(w[3]) * u[3] * u[3]));
 }
 
-// w32: for FP32 state, the weights rounded to FP32 once (norm_group<float>
-// rounds them so), read in the grouped loop instead of the FP64 ones.
+// Block `blk` of `nb` (blockDim.x threads) of the norm's first pass: each
+// thread groups four strided terms into one FP64 accumulator, then a fixed
+// warp and block tree; returns the block's sum in thread 0.  Deterministic
+// for a given nb.  w32: for FP32 state, the weights rounded to FP32 once
+// (norm_group<float> rounds them so), read in the grouped loop instead of
+// the FP64 ones.
 template <typename Real>
-__global__ void k_norm_partial(const Real* __restrict__ u, const double* __restrict__ w,
-                               const float* __restrict__ w32, int n, double* __restrict__ partial) {
+__device__ __forceinline__ double norm_block_sum(const Real* __restrict__ u, const double* __restrict__ w,
+                                                 const float* __restrict__ w32, int n, int blk, int nb) {
   __shared__ double sh[32];
-  // each thread: groups of four strided terms into one FP64 accumulator,
-  // then a fixed warp and block tree: deterministic for a given grid
   double acc = 0.0;
-  const int stride = gridDim.x * blockDim.x;
-  int d = blockIdx.x * blockDim.x + threadIdx.x;
+  const int stride = nb * blockDim.x;
+  int d = blk * blockDim.x + threadIdx.x;
   for (; d + 3 * stride < n; d += 4 * stride) {
     double wv[4];
     Real uv[4];
@@ -392,27 +394,69 @@ __global__ void k_norm_partial(const Real* __restrict__ u, const double* __restr
   if (threadIdx.x < 32) {
     acc = (threadIdx.x < (blockDim.x >> 5)) ? sh[threadIdx.x] : 0.0;
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if (threadIdx.x == 0) partial[blockIdx.x] = acc;
+  }
+  return acc;
+}
+
+// Where a diagnostic launch writes: the column of the iterate in the norm
+// array and in each receiver's row of the trace array.  Graph replays read
+// it from device memory (the column advances by one graph's steps per
+// replay); plain launches pass it by value.
+struct DiagDev {
+  double* norms;
+  double* traces;
+  int stride, col;
+};
+
+// K3 + K6 in one launch (GetNormeSolution, VarInstationary.cxx:2696-2745,
+// and the receiver traces): blocks [0, nb) sum M_i u_i^2, and the last of
+// them to finish adds the nb block sums in a fixed order (one warp, lane l
+// takes blocks l, l+32, ..., then a shuffle tree), so the value does not
+// depend on which block finishes last; blocks [nb, ...) take one receiver
+// per warp, r_k = sum_t W[k][t] u[idx[k][t]].  `done` is zero between
+// launches.  A non-finite norm sets *flag.
+template <typename Real>
+__global__ void __launch_bounds__(256)
+    k_diag(const Real* __restrict__ u, const double* __restrict__ w, const float* __restrict__ w32, int n, int nb,
+           double* __restrict__ partial, unsigned* __restrict__ done, int* __restrict__ flag,
+           const int* __restrict__ rec_idx, const double* __restrict__ rec_w, int n_rec, int n_w,
+           const DiagDev* __restrict__ dd, DiagDev direct, int k) {
+  const DiagDev where = dd ? *dd : direct;
+  const int col = where.col + k;
+  if ((int)blockIdx.x >= nb) {
+    const int warp = (((int)blockIdx.x - nb) * (int)blockDim.x + (int)threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= n_rec) return;
+    double acc = 0.0;
+    for (int t = lane; t < n_w; t += 32)
+      acc += rec_w[(size_t)warp * n_w + t] * double(u[rec_idx[(size_t)warp * n_w + t]]);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0 && where.traces) where.traces[(size_t)warp * where.stride + col] = acc;
+    return;
+  }
+  __shared__ bool last;
+  const double b = norm_block_sum<Real>(u, w, w32, n, blockIdx.x, nb);
+  if (threadIdx.x == 0) {
+    partial[blockIdx.x] = b;
+    __threadfence();
+    last = atomicAdd(done, 1u) == (unsigned)nb - 1u;
+  }
+  __syncthreads();
+  if (last && threadIdx.x < 32) {
+    __threadfence();
+    double s = 0.0;
+    for (int q = threadIdx.x; q < nb; q += 32) s += __ldcg(partial + q);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) {
+      if (where.norms) where.norms[col] = s;
+      if (!isfinite(s)) *flag = 1;
+      *done = 0u;
+    }
   }
 }
 
-__global__ void k_norm_final(const double* __restrict__ partial, int nparts, double* __restrict__ out,
-                             int* __restrict__ nonfinite_flag);
-
-// ---------------------------------------------------------------------------
-// K6: receiver traces r_k = sum_t W[k][t] u[idx[k][t]], one warp per receiver.
-// ---------------------------------------------------------------------------
-template <typename Real>
-__global__ void k_receivers(const Real* __restrict__ u, const int* __restrict__ idx,
-                            const double* __restrict__ w, int n_rec, int n_w,
-                            double* __restrict__ out, int stride, int col) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (warp >= n_rec) return;
-  double acc = 0.0;
-  for (int t = lane; t < n_w; t += 32) acc += w[(size_t)warp * n_w + t] * double(u[idx[(size_t)warp * n_w + t]]);
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-  if (lane == 0) out[(size_t)warp * stride + col] = acc;
-}
+// A graph replay of diagnosed steps ends by moving the column on.
+__global__ void k_diag_advance(DiagDev* dd, int steps) { dd->col += steps; }
+__global__ void k_diag_set(DiagDev* dd, DiagDev v) { *dd = v; }
 
 }  // namespace mj

@@ -34,18 +34,6 @@ int sm_count() {
 
 // Sum of the per-block partial norms by one warp in a fixed order (lane l
 // sums partials l, l+32, ..., then a fixed shuffle tree): deterministic.
-__global__ void k_norm_final(const double* __restrict__ partial, int nparts, double* __restrict__ out,
-                             int* __restrict__ nonfinite_flag) {
-  if (blockIdx.x != 0 || threadIdx.x >= 32) return;
-  double s = 0.0;
-  for (int b = threadIdx.x; b < nparts; b += 32) s += partial[b];
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-  if (threadIdx.x == 0) {
-    *out = s;
-    if (!isfinite(s)) *nonfinite_flag = 1;
-  }
-}
-
 template <typename Real>
 __global__ void k_cast_from_f64(const double* __restrict__ a, Real* __restrict__ b, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = Real(a[i]);
@@ -572,6 +560,9 @@ int mj_lf_create(mj_op* op, const mj_lf_desc* desc, mj_lf** out) {
   lf->norm_blocks = std::min(stream_grid(n), 1024);
   MJ_CUDA(lf->partial.alloc(sizeof(double) * lf->norm_blocks));
   MJ_CUDA(lf->flag.alloc(sizeof(int)));
+  MJ_CUDA(lf->diag_done.alloc(sizeof(unsigned)));
+  MJ_CUDA(cudaMemset(lf->diag_done.ptr, 0, sizeof(unsigned)));
+  MJ_CUDA(lf->diag_where.alloc(sizeof(DiagDev)));
   MJ_CUDA(cudaMemset(lf->flag.ptr, 0, sizeof(int)));
   if (op->precision == MJ_FP32) {
     int rc = lf_sorted_sources(lf.get());
@@ -650,23 +641,28 @@ int lf_init_impl(mj_lf* lf, const double* u0, const double* du0) {
   return MJ_OK;
 }
 
+// Norm and receiver traces of the current iterate in one launch: plain
+// launches write column `col` of norms_d / traces_d (row stride `stride`);
+// with `where` (graph capture) the kernel reads the arrays and the column
+// base from device memory and adds `col`.
+template <typename Real>
+void lf_diag_launch(mj_lf* lf, const void* u, double* norms_d, double* traces_d, int stride, int col,
+                    const DiagDev* where, cudaStream_t s) {
+  const int nb = (norms_d || where) && lf->norm_w.ptr ? lf->norm_blocks : 0;
+  const int rb = (traces_d || where) && lf->n_rec ? (lf->n_rec * 32 + 255) / 256 : 0;
+  if (nb + rb == 0) return;
+  const DiagDev direct = {norms_d, traces_d, stride, 0};
+  k_diag<Real><<<nb + rb, 256, 0, s>>>(static_cast<const Real*>(u), lf->norm_w.as<double>(), lf->norm_w32.as<float>(),
+                                      lf->n_dof, nb, lf->partial.as<double>(), lf->diag_done.as<unsigned>(),
+                                      lf->flag.as<int>(), lf->rec_idx.as<int>(), lf->rec_w.as<double>(),
+                                      rb ? lf->n_rec : 0, lf->n_rec_w, where, direct, col);
+  count_launch();
+}
+
 template <typename Real>
 int lf_diag(mj_lf* lf, double* norms_d, int norm_col, double* traces_d, int stride, int col) {
-  cudaStream_t s = lf->stream;
-  const int n = lf->n_dof;
-  const Real* u = static_cast<const Real*>(lf->cur());
-  if (norms_d && lf->norm_w.ptr) {
-    k_norm_partial<Real><<<lf->norm_blocks, 256, 0, s>>>(u, lf->norm_w.as<double>(), lf->norm_w32.as<float>(), n,
-                                                         lf->partial.as<double>());
-    k_norm_final<<<1, 32, 0, s>>>(lf->partial.as<double>(), lf->norm_blocks, norms_d + norm_col, lf->flag.as<int>());
-    count_launch(2);
-  }
-  if (traces_d && lf->n_rec) {
-    const int threads = 128, blocks = (lf->n_rec * 32 + threads - 1) / threads;
-    k_receivers<Real><<<blocks, threads, 0, s>>>(u, lf->rec_idx.as<int>(), lf->rec_w.as<double>(), lf->n_rec,
-                                                 lf->n_rec_w, traces_d, stride, col);
-    count_launch();
-  }
+  (void)norm_col;  // the norm and the traces share the column
+  lf_diag_launch<Real>(lf, lf->cur(), norms_d, traces_d, stride, col, nullptr, lf->stream);
   MJ_CUDA(cudaGetLastError());
   return MJ_OK;
 }
@@ -775,8 +771,11 @@ int lf_step(mj_lf* lf) {
 // Captures kGraphSteps steps; with prof, event records around each kernel
 // (events 0..3*kGraphSteps-1 of the pool) are part of the graph, so the last
 // replay's per-kernel times can be read back.
+// diag: each step starts with the fused norm/receiver launch of its iterate
+// (arrays and column base read from lf->diag_where, the column advanced by
+// kGraphSteps at the end of the graph).
 template <typename Real>
-int lf_capture(mj_lf* lf, bool prof, cudaGraphExec_t* out) {
+int lf_capture(mj_lf* lf, bool prof, cudaGraphExec_t* out, bool diag = false) {
   cudaStream_t cs;
   MJ_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
   cudaGraph_t g;
@@ -789,8 +788,13 @@ int lf_capture(mj_lf* lf, bool prof, cudaGraphExec_t* out) {
   for (int k = 0; k < kGraphSteps; k++) {
     void* cur = a ? lf->ua.ptr : lf->ub.ptr;
     void* nxt = a ? lf->ub.ptr : lf->ua.ptr;
+    if (diag) lf_diag_launch<Real>(lf, cur, nullptr, nullptr, 0, k, lf->diag_where.as<DiagDev>(), cs);
     lf_step_launch<Real>(lf, cur, nxt, k & 1, cs, prof);
     a = !a;
+  }
+  if (diag) {
+    k_diag_advance<<<1, 1, 0, cs>>>(lf->diag_where.as<DiagDev>(), kGraphSteps);
+    count_launch();
   }
   lf->ev_used = ev_saved;
   MJ_CUDA(cudaStreamEndCapture(cs, &g));
@@ -833,6 +837,31 @@ int lf_advance_impl(mj_lf* lf, int nsteps, double* norms, double* traces, int st
     while (nsteps - s0 >= kGraphSteps) {
       MJ_CUDA(cudaGraphLaunch(lf->graph, lf->stream));
       count_launch((uint64_t)kGraphSteps * lf_kernels_per_step(lf));
+      s0 += kGraphSteps;
+      lf->step += kGraphSteps;
+    }
+    MJ_CUDA(cudaGetLastError());
+  }
+  if ((nd || td) && !lf->profile && lf->use_graph && nsteps >= kGraphSteps + 1) {
+    // diagnosed steps: graph replays whose kernels read the arrays and the
+    // column from diag_where
+    if (lf->step & 1) {  // realign on an even step
+      int rc = lf_diag<Real>(lf, nd, 0, td, cols, 0);
+      if (rc) return rc;
+      rc = lf_step<Real>(lf);
+      if (rc) return rc;
+      s0 = 1;
+    }
+    if (!lf->graph_diag) {
+      int rc = lf_capture<Real>(lf, false, &lf->graph_diag, true);
+      if (rc) return rc;
+    }
+    const DiagDev where = {nd, td, cols, s0};
+    k_diag_set<<<1, 1, 0, lf->stream>>>(lf->diag_where.as<DiagDev>(), where);
+    count_launch();
+    while (nsteps - s0 >= kGraphSteps) {
+      MJ_CUDA(cudaGraphLaunch(lf->graph_diag, lf->stream));
+      count_launch((uint64_t)kGraphSteps * (lf_kernels_per_step(lf) + 1) + 1);
       s0 += kGraphSteps;
       lf->step += kGraphSteps;
     }
@@ -941,7 +970,7 @@ int mj_lf_set_scheme(mj_lf* lf, int order, int n_pulse_d2, const double* pulse_d
   MJ_CHECK_ARG(order == 2 || order == 4, "mj_lf_set_scheme: order must be 2 or 4");
   MJ_CHECK_ARG(order == 2 || n_pulse_d2 == 0 || pulse_d2, "mj_lf_set_scheme: null pulse_d2");
   MJ_CHECK_ARG(n_pulse_d2 >= 0, "mj_lf_set_scheme: negative n_pulse_d2");
-  for (cudaGraphExec_t* g : {&lf->graph, &lf->graph_prof})
+  for (cudaGraphExec_t* g : {&lf->graph, &lf->graph_prof, &lf->graph_diag})
     if (*g) {
       cudaGraphExecDestroy(*g);
       *g = nullptr;
@@ -968,7 +997,7 @@ int mj_lf_set_scheme(mj_lf* lf, int order, int n_pulse_d2, const double* pulse_d
 int mj_lf_set_stream_gather(mj_lf* lf, int enable) {
   MJ_CHECK_ARG(lf, "mj_lf_set_stream_gather: null integrator");
   MJ_CHECK_ARG(!enable || lf->op->precision == MJ_FP32, "mj_lf_set_stream_gather: FP32 integrators only");
-  for (cudaGraphExec_t* g : {&lf->graph, &lf->graph_prof})
+  for (cudaGraphExec_t* g : {&lf->graph, &lf->graph_prof, &lf->graph_diag})
     if (*g) {
       cudaGraphExecDestroy(*g);
       *g = nullptr;

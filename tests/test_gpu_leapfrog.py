@@ -126,6 +126,26 @@ def test_config1_fp32_error(config1):
     assert rel_l2(_probe_values(pb, g, uf), g["probe_u"]) < 1e-4
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_diagnosed_graph_replay_equals_plain_launches(config1, precision):
+    """Steps with the norm and the receivers every step: graph replays (from
+    an odd step too) give the same norms, traces and states, bit for bit, as
+    steps launched one by one (chunks too short for a graph)."""
+    g, pb = config1
+    runs = []
+    for chunks in ((3, 45, 25), (7,) * 10 + (3,)):
+        op = pb.operator(precision)
+        lf = pb.integrator(op)
+        lf.SetInitialConditionS(np.zeros(pb.n_dof))
+        out = [lf.Advance(k) for k in chunks]
+        runs.append((np.concatenate([o[0] for o in out]), np.concatenate([o[1] for o in out], axis=1),
+                     lf.GetIterate()))
+        lf.close(); op.close()
+    (n1, t1, u1), (n2, t2, u2) = runs
+    assert n1.shape == (73,) and t1.shape == (8, 73)
+    assert np.array_equal(n1, n2) and np.array_equal(t1, t2) and np.array_equal(u1, u2)
+
+
 def test_graph_replay_equals_plain_launches_single_source():
     g = load_golden("cube4_q4")
     for precision in ("fp64", "fp32"):
