@@ -46,6 +46,7 @@ struct mj_lf {
   mj::DevBuf du0, tmp;       // staging
   mj::DevBuf partial, norms_d, traces_d, flag;
   mj::DevBuf diag_done, diag_where;  // fused diagnostics: finished-block counter, DiagDev of graph replays
+  mj::DevBuf stream_partial;         // per-CTA norm partials of the streaming gather's diagnostics
   mj::DevBuf pulse_d, ctr;   // pulse of every step and the two step counters
   int n_pulse = 0;
   cudaGraphExec_t graph = nullptr, graph_prof = nullptr;

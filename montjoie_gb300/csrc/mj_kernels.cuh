@@ -253,18 +253,106 @@ static_assert(kStreamM % 16 == 0 && kStreamP % 16 == 0 && kStreamR % 16 == 0 && 
               "aligned buffer segments");
 static_assert(kStreamDofs % kStreamThreads == 0 && kStreamNB >= 2 && kStreamNB <= 8, "chunk shape");
 
+// Where a diagnostic launch writes: the column of the iterate in the norm
+// array and in each receiver's row of the trace array (row stride `stride`);
+// nothing is written at columns >= ncols.  Graph replays read it from device
+// memory (the column advances by one graph's steps per replay); plain
+// launches pass it by value.
+struct DiagDev {
+  double* norms;
+  double* traces;
+  int stride, col, ncols;
+};
+
+// Norm and receivers of the new iterate, fused into the streaming gather
+// (FP32): weights rounded to FP32, one partial per CTA, the finished-CTA
+// counter (zero between launches), the non-finite flag, the receivers, and
+// where to write: (dd ? *dd : direct), column where.col + col.
+struct StreamDiag {
+  const float* w32;
+  double* partial;
+  unsigned* done;
+  int* flag;
+  const int* rec_idx;
+  const double* rec_w;
+  int n_rec, n_w;
+  const DiagDev* dd;
+  DiagDev direct;
+  int col;
+};
+
 struct StreamChunk {
   int d0, d1, q0, q1;  // dofs [d0, d1); R range [q0, q1) rounded to multiples of 4
   int has_src, pad0, pad1, pad2;
 };
 
-__global__ void __launch_bounds__(kStreamThreads)
+// One dof's term of the fused norm, rounded the same way wherever it is
+// computed: FP32 w*u, then one FP32 fused multiply-add.
+__device__ __forceinline__ float stream_norm_term(float w, float u, float acc) {
+  return __fmaf_rn(__fmul_rn(w, u), u, acc);
+}
+
+// End of a fused-diagnostics launch over the streaming chunks (grid G):
+// block tree of the threads' sums, one partial per CTA; the last CTA to
+// finish adds the partials in a fixed order and samples the receivers from
+// the finished state u.
+__device__ __forceinline__ void stream_diag_finish(double nacc, const StreamDiag& dg, const float* u, int G) {
+  __shared__ double sh[kStreamThreads / 32];
+  __shared__ bool last;
+  const int t = threadIdx.x;
+  for (int o = 16; o > 0; o >>= 1) nacc += __shfl_down_sync(0xffffffffu, nacc, o);
+  if ((t & 31) == 0) sh[t >> 5] = nacc;
+  __syncthreads();  // also: every thread's state writes are done
+  if (t < 32) {
+    double a = t < kStreamThreads / 32 ? sh[t] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    if (t == 0) {
+      dg.partial[blockIdx.x] = a;
+      __threadfence();
+      last = atomicAdd(dg.done, 1u) == (unsigned)G - 1u;
+    }
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const DiagDev where = dg.dd ? *dg.dd : dg.direct;
+  const int col = where.col + dg.col;
+  const int warp = t >> 5, lane = t & 31;
+  if (col < where.ncols) {
+    if (warp == 0) {
+      double s = 0.0;
+      for (int q = lane; q < G; q += 32) s += __ldcg(dg.partial + q);
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+      if (lane == 0) {
+        if (where.norms) where.norms[col] = s;
+        if (!isfinite(s)) *dg.flag = 1;
+      }
+    }
+    if (where.traces)
+      for (int r = warp; r < dg.n_rec; r += kStreamThreads / 32) {
+        double acc = 0.0;
+        for (int q = lane; q < dg.n_w; q += 32)
+          acc += dg.rec_w[(size_t)r * dg.n_w + q] * double(__ldcg(u + dg.rec_idx[(size_t)r * dg.n_w + q]));
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if (lane == 0) where.traces[(size_t)r * where.stride + col] = acc;
+      }
+  }
+  if (t == 0) *dg.done = 0u;
+}
+
+// DIAG: the norm and the receiver traces of U^{n+2} as well (StreamDiag):
+// each thread sums w*u^2 of its dofs in FP32 per chunk and accumulates in
+// FP64, then a block tree gives one partial per CTA; the last CTA to finish
+// adds the partials in a fixed order (deterministic for a given grid) and
+// samples the receivers from the finished state.
+template <bool DIAG>
+__global__ void __launch_bounds__(kStreamThreads, 8)  // 8 CTAs per SM: 32 registers at most
     k_gather_leapfrog_stream(const float* __restrict__ R, const int* __restrict__ ptr, int* __restrict__ ctr, int qc,
                              float* __restrict__ u0, const float* __restrict__ u1, const float* __restrict__ m,
                              const StreamChunk* __restrict__ chunks, int n_chunks,
                              const unsigned* __restrict__ mask, const int* __restrict__ sidx,
                              const float* __restrict__ sval, int nsrc, const double* __restrict__ pulse, int n_pulse,
-                             const double* __restrict__ inv_mass, double dt2, int* __restrict__ err) {
+                             const double* __restrict__ inv_mass, double dt2, int* __restrict__ err, StreamDiag dg) {
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + kStreamNB * kStreamBuf);
   const int t = threadIdx.x, G = gridDim.x;
@@ -294,12 +382,17 @@ __global__ void __launch_bounds__(kStreamThreads)
   __syncthreads();
   uint32_t ph = 0u;  // bit b: parity of buffer b's next completion
   int b = 0;
+  double nacc = 0.0;  // DIAG: this thread's sum of w u^2
   for (int c = blockIdx.x; c < n_chunks; c += G, b = (b + 1 == kStreamNB ? 0 : b + 1)) {
     const StreamChunk ch = chunks[c];
     const bool ok = mbar_wait_bounded(&bar[b], (ph >> b) & 1u);
     if (__syncthreads_or(!ok)) {
+      // report, wait (bounded) for this CTA's copies still in flight, and
+      // still take part in the diagnostics' finished-CTA count
       if (t == 0) atomicExch(err, 1);
-      return;
+      for (int i = 0, cb = b; i < kStreamNB; i++, cb = (cb + 1 == kStreamNB ? 0 : cb + 1))
+        if (c + i * G < n_chunks) mbar_wait_bounded(&bar[cb], (ph >> cb) & 1u);
+      break;
     }
     ph ^= 1u << b;
     const unsigned char* buf = smem + b * kStreamBuf;
@@ -318,6 +411,7 @@ __global__ void __launch_bounds__(kStreamThreads)
       on[v] = ch.d0 + dls[v] < ch.d1;
     }
     contrib_sums<V>(sp, sR, ch.q0, dls, on, sums);
+    float wsum = 0.f;
 #pragma unroll
     for (int v = 0; v < V; v++) {
       const int dl = dls[v];
@@ -330,14 +424,39 @@ __global__ void __launch_bounds__(kStreamThreads)
           if (f != 0.0) un = float(double(un) + dt2 * inv_mass[d] * p * f);
         }
         u0[d] = un;
+        if (DIAG && dg.w32) wsum = stream_norm_term(__ldg(dg.w32 + d), un, wsum);
       }
     }
+    if (DIAG) nacc += double(wsum);
     __syncthreads();  // buffer b is free
     if (t == 0) {
       fence_proxy_async();
       issue(c + kStreamNB * G, b);
     }
   }
+  if constexpr (DIAG) stream_diag_finish(nacc, dg, u0, G);
+}
+
+// The fused diagnostics of a state u on their own (the iterates a call
+// starts from): the same chunks, grid, grouping and reduction as the
+// streaming gather's DIAG form, so every column has the same arithmetic.
+__global__ void __launch_bounds__(kStreamThreads)
+    k_stream_diag(const float* __restrict__ u, const StreamChunk* __restrict__ chunks, int n_chunks, StreamDiag dg) {
+  const int t = threadIdx.x, G = gridDim.x;
+  constexpr int V = kStreamDofs / kStreamThreads;
+  double nacc = 0.0;
+  if (dg.w32)
+    for (int c = blockIdx.x; c < n_chunks; c += G) {
+      const StreamChunk ch = chunks[c];
+      float wsum = 0.f;
+#pragma unroll
+      for (int v = 0; v < V; v++) {
+        const int d = ch.d0 + v * kStreamThreads + t;
+        if (d < ch.d1) wsum = stream_norm_term(__ldg(dg.w32 + d), __ldg(u + d), wsum);
+      }
+      nacc += double(wsum);
+    }
+  stream_diag_finish(nacc, dg, u, G);
 }
 
 // ---------------------------------------------------------------------------
@@ -398,16 +517,6 @@ __device__ __forceinline__ double norm_block_sum(const Real* __restrict__ u, con
   return acc;
 }
 
-// Where a diagnostic launch writes: the column of the iterate in the norm
-// array and in each receiver's row of the trace array.  Graph replays read
-// it from device memory (the column advances by one graph's steps per
-// replay); plain launches pass it by value.
-struct DiagDev {
-  double* norms;
-  double* traces;
-  int stride, col;
-};
-
 // K3 + K6 in one launch (GetNormeSolution, VarInstationary.cxx:2696-2745,
 // and the receiver traces): blocks [0, nb) sum M_i u_i^2, and the last of
 // them to finish adds the nb block sums in a fixed order (one warp, lane l
@@ -423,6 +532,7 @@ __global__ void __launch_bounds__(256)
            const DiagDev* __restrict__ dd, DiagDev direct, int k) {
   const DiagDev where = dd ? *dd : direct;
   const int col = where.col + k;
+  const bool put = col < where.ncols;
   if ((int)blockIdx.x >= nb) {
     const int warp = (((int)blockIdx.x - nb) * (int)blockDim.x + (int)threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -431,7 +541,7 @@ __global__ void __launch_bounds__(256)
     for (int t = lane; t < n_w; t += 32)
       acc += rec_w[(size_t)warp * n_w + t] * double(u[rec_idx[(size_t)warp * n_w + t]]);
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if (lane == 0 && where.traces) where.traces[(size_t)warp * where.stride + col] = acc;
+    if (lane == 0 && where.traces && put) where.traces[(size_t)warp * where.stride + col] = acc;
     return;
   }
   __shared__ bool last;
@@ -448,7 +558,7 @@ __global__ void __launch_bounds__(256)
     for (int q = threadIdx.x; q < nb; q += 32) s += __ldcg(partial + q);
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
     if (threadIdx.x == 0) {
-      if (where.norms) where.norms[col] = s;
+      if (where.norms && put) where.norms[col] = s;
       if (!isfinite(s)) *flag = 1;
       *done = 0u;
     }

@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -461,11 +462,16 @@ int lf_stream_setup(mj_lf* lf) {
   MJ_CUDA(cudaMemcpy(lf->stream_chunks.ptr, chunks.data(), sizeof(StreamChunk) * chunks.size(),
                      cudaMemcpyHostToDevice));
   lf->n_stream_chunks = (int)chunks.size();
-  MJ_CUDA(cudaFuncSetAttribute(k_gather_leapfrog_stream, cudaFuncAttributeMaxDynamicSharedMemorySize, kStreamSmem));
+  MJ_CUDA(cudaFuncSetAttribute(k_gather_leapfrog_stream<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               kStreamSmem));
+  MJ_CUDA(cudaFuncSetAttribute(k_gather_leapfrog_stream<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               kStreamSmem));
   int ctas = 0;
-  MJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctas, k_gather_leapfrog_stream, kStreamThreads, kStreamSmem));
+  MJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctas, k_gather_leapfrog_stream<false>, kStreamThreads,
+                                                        kStreamSmem));
   MJ_CHECK_ARG(ctas >= 1, "streaming gather cannot be resident");
   lf->stream_grid_ = std::max(1, std::min(lf->n_stream_chunks, ctas * sm_count()));
+  MJ_CUDA(lf->stream_partial.alloc(sizeof(double) * lf->stream_grid_));
   return MJ_OK;
 }
 
@@ -651,7 +657,7 @@ void lf_diag_launch(mj_lf* lf, const void* u, double* norms_d, double* traces_d,
   const int nb = (norms_d || where) && lf->norm_w.ptr ? lf->norm_blocks : 0;
   const int rb = (traces_d || where) && lf->n_rec ? (lf->n_rec * 32 + 255) / 256 : 0;
   if (nb + rb == 0) return;
-  const DiagDev direct = {norms_d, traces_d, stride, 0};
+  const DiagDev direct = {norms_d, traces_d, stride, 0, INT_MAX};
   k_diag<Real><<<nb + rb, 256, 0, s>>>(static_cast<const Real*>(u), lf->norm_w.as<double>(), lf->norm_w32.as<float>(),
                                       lf->n_dof, nb, lf->partial.as<double>(), lf->diag_done.as<unsigned>(),
                                       lf->flag.as<int>(), lf->rec_idx.as<int>(), lf->rec_w.as<double>(),
@@ -709,8 +715,16 @@ void lf_step4_launch(mj_lf* lf, void* cur, const void* next, int qc, cudaStream_
   }
 }
 
+// Diagnostics fused into the step: the FP32 order-2 step with the streaming
+// gather computes the norm and the receivers of the iterate it produces.
+bool lf_fused_diag(const mj_lf* lf) {
+  return lf->stream_gather && lf->op->precision == MJ_FP32 && lf->time_order == 2;
+}
+
+// dg: the step's fused diagnostics (streaming gather only), or nullptr.
 template <typename Real>
-void lf_step_launch(mj_lf* lf, void* cur, const void* next, int qc, cudaStream_t s, bool prof) {
+void lf_step_launch(mj_lf* lf, void* cur, const void* next, int qc, cudaStream_t s, bool prof,
+                    const StreamDiag* dg = nullptr) {
   if (lf->time_order == 4) {
     lf_step4_launch<Real>(lf, cur, next, qc, s, prof);
     return;
@@ -722,12 +736,13 @@ void lf_step_launch(mj_lf* lf, void* cur, const void* next, int qc, cudaStream_t
   if (prof) cudaEventRecord(lf->ev[lf->ev_used + 1], s);
   const double dt2 = lf->dt * lf->dt;
   if (lf->stream_gather && op->precision == MJ_FP32) {
-    k_gather_leapfrog_stream<<<lf->stream_grid_, kStreamThreads, kStreamSmem, s>>>(
+    auto k2 = dg ? k_gather_leapfrog_stream<true> : k_gather_leapfrog_stream<false>;
+    k2<<<lf->stream_grid_, kStreamThreads, kStreamSmem, s>>>(
         op->R.as<float>(), op->ptr.as<int>(), lf->ctr.as<int>(), qc, static_cast<float*>(cur),
         static_cast<const float*>(next), lf->minv.as<float>(), lf->stream_chunks.as<StreamChunk>(),
         lf->n_stream_chunks, lf->src_mask.as<unsigned>(), lf->src_sidx.as<int>(), lf->src_sval.as<float>(),
         lf->n_src_sorted, lf->pulse_d.as<double>(), lf->n_pulse, lf->inv_mass64.as<double>(), dt2,
-        op->err.as<int>());
+        op->err.as<int>(), dg ? *dg : StreamDiag{});
     count_launch();
     if (prof) {
       cudaEventRecord(lf->ev[lf->ev_used + 2], s);
@@ -758,10 +773,27 @@ void lf_step_launch(mj_lf* lf, void* cur, const void* next, int qc, cudaStream_t
   }
 }
 
+// The StreamDiag of a step whose new iterate goes to column where.col + col.
+StreamDiag lf_stream_diag(mj_lf* lf, const DiagDev* dd, DiagDev direct, int col) {
+  StreamDiag g = {};
+  g.w32 = lf->norm_w32.as<float>();
+  g.partial = lf->stream_partial.as<double>();
+  g.done = lf->diag_done.as<unsigned>();
+  g.flag = lf->flag.as<int>();
+  g.rec_idx = lf->rec_idx.as<int>();
+  g.rec_w = lf->rec_w.as<double>();
+  g.n_rec = lf->n_rec;
+  g.n_w = lf->n_rec_w;
+  g.dd = dd;
+  g.direct = direct;
+  g.col = col;
+  return g;
+}
+
 template <typename Real>
-int lf_step(mj_lf* lf) {
+int lf_step(mj_lf* lf, const StreamDiag* dg = nullptr) {
   const bool prof = lf->profile && lf->ev_used + 3 <= (int)lf->ev.size() - 3 * kGraphSteps;
-  lf_step_launch<Real>(lf, lf->cur(), lf->next(), lf->step & 1, lf->stream, prof);
+  lf_step_launch<Real>(lf, lf->cur(), lf->next(), lf->step & 1, lf->stream, prof, dg);
   MJ_CUDA(cudaGetLastError());
   lf->cur_is_a = !lf->cur_is_a;  // new cur = old next; new next = overwritten old cur
   lf->step++;
@@ -788,8 +820,13 @@ int lf_capture(mj_lf* lf, bool prof, cudaGraphExec_t* out, bool diag = false) {
   for (int k = 0; k < kGraphSteps; k++) {
     void* cur = a ? lf->ua.ptr : lf->ub.ptr;
     void* nxt = a ? lf->ub.ptr : lf->ua.ptr;
-    if (diag) lf_diag_launch<Real>(lf, cur, nullptr, nullptr, 0, k, lf->diag_where.as<DiagDev>(), cs);
-    lf_step_launch<Real>(lf, cur, nxt, k & 1, cs, prof);
+    if (diag && lf_fused_diag(lf)) {  // the step writes its new iterate's column (k + 2)
+      const StreamDiag dg = lf_stream_diag(lf, lf->diag_where.as<DiagDev>(), DiagDev{}, k + 2);
+      lf_step_launch<Real>(lf, cur, nxt, k & 1, cs, prof, &dg);
+    } else {
+      if (diag) lf_diag_launch<Real>(lf, cur, nullptr, nullptr, 0, k, lf->diag_where.as<DiagDev>(), cs);
+      lf_step_launch<Real>(lf, cur, nxt, k & 1, cs, prof);
+    }
     a = !a;
   }
   if (diag) {
@@ -842,39 +879,60 @@ int lf_advance_impl(mj_lf* lf, int nsteps, double* norms, double* traces, int st
     }
     MJ_CUDA(cudaGetLastError());
   }
+  // Diagnostics: the norm and the traces of iterate s go to column s.  The
+  // state holds iterates s (handed out) and s+1, and step s produces s+2.
+  // With the fused form step s writes column s+2 (nothing past the call's
+  // columns), and iterates 0 and 1 have launches of their own.
+  const bool fused = (nd || td) && lf_fused_diag(lf);
+  const DiagDev direct = {nd, td, cols, 0, cols};
+  auto plain_step = [&](int s) -> int {
+    if (fused) {
+      const StreamDiag dg = lf_stream_diag(lf, nullptr, direct, s + 2);
+      return lf_step<Real>(lf, &dg);
+    }
+    if (nd || td) {
+      const int rc = lf_diag<Real>(lf, nd, s, td, cols, s);
+      if (rc) return rc;
+    }
+    return lf_step<Real>(lf);
+  };
+  if (fused)  // iterates 0 and 1 with the same arithmetic as the fused steps
+    for (int c = 0; c < std::min(cols, 2); c++) {
+      const StreamDiag dg = lf_stream_diag(lf, nullptr, direct, c);
+      k_stream_diag<<<lf->stream_grid_, kStreamThreads, 0, lf->stream>>>(
+          static_cast<const float*>(c == 0 ? lf->cur() : lf->next()), lf->stream_chunks.as<StreamChunk>(),
+          lf->n_stream_chunks, dg);
+      count_launch();
+    }
   if ((nd || td) && !lf->profile && lf->use_graph && nsteps >= kGraphSteps + 1) {
     // diagnosed steps: graph replays whose kernels read the arrays and the
     // column from diag_where
     if (lf->step & 1) {  // realign on an even step
-      int rc = lf_diag<Real>(lf, nd, 0, td, cols, 0);
-      if (rc) return rc;
-      rc = lf_step<Real>(lf);
+      const int rc = plain_step(0);
       if (rc) return rc;
       s0 = 1;
     }
     if (!lf->graph_diag) {
-      int rc = lf_capture<Real>(lf, false, &lf->graph_diag, true);
+      const int rc = lf_capture<Real>(lf, false, &lf->graph_diag, true);
       if (rc) return rc;
     }
-    const DiagDev where = {nd, td, cols, s0};
+    const DiagDev where = {nd, td, cols, s0, cols};
     k_diag_set<<<1, 1, 0, lf->stream>>>(lf->diag_where.as<DiagDev>(), where);
     count_launch();
     while (nsteps - s0 >= kGraphSteps) {
       MJ_CUDA(cudaGraphLaunch(lf->graph_diag, lf->stream));
-      count_launch((uint64_t)kGraphSteps * (lf_kernels_per_step(lf) + 1) + 1);
+      count_launch((uint64_t)kGraphSteps * (lf_kernels_per_step(lf) + (fused ? 0 : 1)) + 1);
       s0 += kGraphSteps;
       lf->step += kGraphSteps;
     }
     MJ_CUDA(cudaGetLastError());
   }
   for (int s = s0; s < nsteps; s++) {
-    int rc = lf_diag<Real>(lf, nd, s, td, cols, s);
-    if (rc) return rc;
-    rc = lf_step<Real>(lf);
+    const int rc = plain_step(s);
     if (rc) return rc;
   }
-  if (final_diag) {
-    int rc = lf_diag<Real>(lf, nd, nsteps, td, cols, nsteps);
+  if (final_diag && !fused) {
+    const int rc = lf_diag<Real>(lf, nd, nsteps, td, cols, nsteps);
     if (rc) return rc;
   }
   cudaStream_t s = lf->stream;
