@@ -122,6 +122,33 @@ __device__ __forceinline__ double source_at(const unsigned* __restrict__ mask, c
 // First gather of a step, pulse p = pulse[ctr[qc]]:
 //   EXACT (FP64): P = (-(A U^{n+1}) + p F) dt^2,  Z = invD P     (w <- P, z <- Z)
 //   FP32:         w = -(A U^{n+1}) + p F,         z = (dt^2/D) w
+// Sums of the contributions of V dofs d[v] of one thread straight from
+// global memory (dof-ordered CSR), each 0 + R[q0] + R[q0 + 1] + ... in CSR
+// order; the offsets and the first terms of all V dofs are loaded together
+// so their latencies overlap.
+template <typename Real, int V>
+__device__ __forceinline__ void contrib_sums_global(const Real* __restrict__ R, const int* __restrict__ ptr,
+                                                    const int (&d)[V], const bool (&on)[V], Real (&s)[V]) {
+  int qa[V], qb[V];
+  Real first[V];
+#pragma unroll
+  for (int v = 0; v < V; v++) {
+    qa[v] = on[v] ? __ldg(ptr + d[v]) : 0;
+    qb[v] = on[v] ? __ldg(ptr + d[v] + 1) : 0;
+  }
+#pragma unroll
+  for (int v = 0; v < V; v++) first[v] = qa[v] < qb[v] ? __ldg(R + qa[v]) : Real(0);
+#pragma unroll
+  for (int v = 0; v < V; v++) {
+    s[v] = Real(0);
+    if (qa[v] < qb[v]) s[v] += first[v];
+    for (int q = qa[v] + 1; q < qb[v]; q++) s[v] += __ldg(R + q);
+  }
+}
+
+// Dofs per thread and pass of the grid-stride gathers below.
+constexpr int kGatherV = 4;
+
 template <typename Real, bool EXACT>
 __global__ void k_gather_o4a(const Real* __restrict__ R, const int* __restrict__ ptr, const int* __restrict__ ctr,
                              int qc, const double* __restrict__ pulse, int n_pulse,
@@ -130,22 +157,34 @@ __global__ void k_gather_o4a(const Real* __restrict__ R, const int* __restrict__
                              Real* __restrict__ w, Real* __restrict__ z, int n_dof) {
   const int step = ctr[qc];
   const double p = step < n_pulse ? pulse[step] : 0.0;
-  for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < n_dof; d += gridDim.x * blockDim.x) {
-    Real s = 0;
-    const int q1 = __ldg(ptr + d + 1);
-    for (int q = __ldg(ptr + d); q < q1; q++) s += __ldg(R + q);
-    Real a = -s;
-    if (p != 0.0) {
-      const double f = source_at(mask, sidx, sval, nsrc, d);
-      if (f != 0.0) a = EXACT ? a + Real(p) * Real(f) : Real(double(a) + p * f);
+  constexpr int V = kGatherV;
+  for (int base = blockIdx.x * blockDim.x * V; base < n_dof; base += gridDim.x * blockDim.x * V) {
+    int dv[V];
+    bool on[V];
+    Real sv[V];
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+      dv[v] = base + v * blockDim.x + threadIdx.x;
+      on[v] = dv[v] < n_dof;
     }
-    if (EXACT) {
-      a *= dt2;
-      w[d] = a;
-      z[d] = a * __ldg(minv + d);
-    } else {
-      w[d] = a;
-      z[d] = __ldg(minv + d) * a;
+    contrib_sums_global<Real, V>(R, ptr, dv, on, sv);
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+      if (!on[v]) continue;
+      const int d = dv[v];
+      Real a = -sv[v];
+      if (p != 0.0) {
+        const double f = source_at(mask, sidx, sval, nsrc, d);
+        if (f != 0.0) a = EXACT ? a + Real(p) * Real(f) : Real(double(a) + p * f);
+      }
+      if (EXACT) {
+        a *= dt2;
+        w[d] = a;
+        z[d] = a * __ldg(minv + d);
+      } else {
+        w[d] = a;
+        z[d] = __ldg(minv + d) * a;
+      }
     }
   }
 }
@@ -164,24 +203,36 @@ __global__ void k_gather_o4b(const Real* __restrict__ R, const int* __restrict__
   if (blockIdx.x == 0 && threadIdx.x == 0) ctr[1 - qc] = ctr[qc] + 1;
   const int step = ctr[qc];
   const double p3 = step < n_pulse3 ? pulse3[step] : 0.0;
-  for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < n_dof; d += gridDim.x * blockDim.x) {
-    Real s = 0;
-    const int q1 = __ldg(ptr + d + 1);
-    for (int q = __ldg(ptr + d); q < q1; q++) s += __ldg(R + q);
-    Real y = -s;
-    if (p3 != 0.0) {
-      const double f = source_at(mask, sidx, sval, nsrc, d);
-      if (f != 0.0) y = EXACT ? y + Real(double(dt2) * p3) * Real(f) : Real(double(y) + double(dt2) * p3 * f);
+  constexpr int V = kGatherV;
+  for (int base = blockIdx.x * blockDim.x * V; base < n_dof; base += gridDim.x * blockDim.x * V) {
+    int dv[V];
+    bool on[V];
+    Real sv[V];
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+      dv[v] = base + v * blockDim.x + threadIdx.x;
+      on[v] = dv[v] < n_dof;
     }
-    if (EXACT) {
-      const Real Dd = __ldg(mass + d);
-      Real a = __ldg(w + d);
-      a += (dt2 / Real(12)) * y;
-      a += Real(2) * Dd * __ldg(u1 + d);
-      a += -Dd * u0[d];
-      u0[d] = a * __ldg(minv + d);
-    } else {
-      u0[d] = Real(2) * __ldg(u1 + d) - u0[d] + __ldg(minv + d) * (__ldg(w + d) + y * Real(1.0 / 12));
+    contrib_sums_global<Real, V>(R, ptr, dv, on, sv);
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+      if (!on[v]) continue;
+      const int d = dv[v];
+      Real y = -sv[v];
+      if (p3 != 0.0) {
+        const double f = source_at(mask, sidx, sval, nsrc, d);
+        if (f != 0.0) y = EXACT ? y + Real(double(dt2) * p3) * Real(f) : Real(double(y) + double(dt2) * p3 * f);
+      }
+      if (EXACT) {
+        const Real Dd = __ldg(mass + d);
+        Real a = __ldg(w + d);
+        a += (dt2 / Real(12)) * y;
+        a += Real(2) * Dd * __ldg(u1 + d);
+        a += -Dd * u0[d];
+        u0[d] = a * __ldg(minv + d);
+      } else {
+        u0[d] = Real(2) * __ldg(u1 + d) - u0[d] + __ldg(minv + d) * (__ldg(w + d) + y * Real(1.0 / 12));
+      }
     }
   }
 }
