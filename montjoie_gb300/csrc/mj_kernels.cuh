@@ -488,6 +488,101 @@ __global__ void __launch_bounds__(kStreamThreads, 8)  // 8 CTAs per SM: 32 regis
   if constexpr (DIAG) stream_diag_finish(nacc, dg, u0, G);
 }
 
+// The order-4 gathers of the FP32 form as streaming kernels, on the chunks,
+// buffers and grid of k_gather_leapfrog_stream:
+//   MODE 0 (first gather):  w = -(A U^{n+1}) + p F,  z = (dt^2/D) w;
+//   MODE 1 (second gather and update, advancing the step counter):
+//     U^{n+2} = 2 U^{n+1} - U^n + (dt^2/D)(w + Y/12),  Y = -(A Z) + dt^2 p'' F.
+// The same arithmetic as k_gather_o4a / k_gather_o4b<float, false>.
+template <int MODE>
+__global__ void __launch_bounds__(kStreamThreads, 8)
+    k_gather_o4_stream(const float* __restrict__ R, const int* __restrict__ ptr, int* __restrict__ ctr, int qc,
+                       const double* __restrict__ pulse, int n_pulse, const unsigned* __restrict__ mask,
+                       const int* __restrict__ sidx, const float* __restrict__ sval, int nsrc,
+                       float* __restrict__ u0, const float* __restrict__ u1, const float* __restrict__ m,
+                       float* __restrict__ w, float* __restrict__ z, const StreamChunk* __restrict__ chunks,
+                       int n_chunks, float dt2, int* __restrict__ err) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + kStreamNB * kStreamBuf);
+  const int t = threadIdx.x, G = gridDim.x;
+  if (MODE == 1 && blockIdx.x == 0 && t == 0) ctr[1 - qc] = ctr[qc] + 1;
+  const int step = ctr[qc];
+  const double p = step < n_pulse ? pulse[step] : 0.0;
+  auto issue = [&](int c, int b) {
+    if (c >= n_chunks) return;
+    const StreamChunk ch = chunks[c];
+    unsigned char* dst = smem + b * kStreamBuf;
+    const uint32_t sb = (uint32_t)(((ch.d1 - ch.d0 + 3) & ~3) * 4);
+    const uint32_t pb = (uint32_t)(((ch.d1 - ch.d0 + 1 + 3) & ~3) * 4);
+    const uint32_t rb = (uint32_t)((ch.q1 - ch.q0) * 4);
+    mbar_expect_tx(&bar[b], (MODE == 1 ? 3u : 1u) * sb + pb + rb);
+    if (MODE == 1) {
+      bulk_g2s(dst, u1 + ch.d0, sb, &bar[b]);
+      bulk_g2s(dst + kStreamDofs * 4, u0 + ch.d0, sb, &bar[b]);
+    }
+    bulk_g2s(dst + kStreamM, m + ch.d0, sb, &bar[b]);
+    bulk_g2s(dst + kStreamP, ptr + ch.d0, pb, &bar[b]);
+    bulk_g2s(dst + kStreamR, R + ch.q0, rb, &bar[b]);
+  };
+  if (t == 0) {
+    for (int b = 0; b < kStreamNB; b++) mbar_init(&bar[b], 1);
+    fence_mbar_init();
+    for (int b = 0; b < kStreamNB; b++) issue(blockIdx.x + b * G, b);
+  }
+  __syncthreads();
+  uint32_t ph = 0u;
+  int b = 0;
+  for (int c = blockIdx.x; c < n_chunks; c += G, b = (b + 1 == kStreamNB ? 0 : b + 1)) {
+    const StreamChunk ch = chunks[c];
+    const bool ok = mbar_wait_bounded(&bar[b], (ph >> b) & 1u);
+    if (__syncthreads_or(!ok)) {
+      if (t == 0) atomicExch(err, 1);
+      for (int i = 0, cb = b; i < kStreamNB; i++, cb = (cb + 1 == kStreamNB ? 0 : cb + 1))
+        if (c + i * G < n_chunks) mbar_wait_bounded(&bar[cb], (ph >> cb) & 1u);
+      return;
+    }
+    ph ^= 1u << b;
+    const unsigned char* buf = smem + b * kStreamBuf;
+    const float* su1 = reinterpret_cast<const float*>(buf);
+    const float* su0 = su1 + kStreamDofs;
+    const float* sm = reinterpret_cast<const float*>(buf + kStreamM);
+    const int* sp = reinterpret_cast<const int*>(buf + kStreamP);
+    const float* sR = reinterpret_cast<const float*>(buf + kStreamR);
+    constexpr int V = kStreamDofs / kStreamThreads;
+    int dls[V];
+    bool on[V];
+    float sums[V];
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+      dls[v] = v * kStreamThreads + t;
+      on[v] = ch.d0 + dls[v] < ch.d1;
+    }
+    contrib_sums<V>(sp, sR, ch.q0, dls, on, sums);
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+      if (!on[v]) continue;
+      const int dl = dls[v];
+      const int d = ch.d0 + dl;
+      float a = -sums[v];
+      if (p != 0.0 && ch.has_src) {
+        const double f = source_at(mask, sidx, sval, nsrc, d);
+        if (f != 0.0) a = MODE == 0 ? float(double(a) + p * f) : float(double(a) + double(dt2) * p * f);
+      }
+      if (MODE == 0) {
+        w[d] = a;
+        z[d] = sm[dl] * a;
+      } else {
+        u0[d] = 2.f * su1[dl] - su0[dl] + sm[dl] * (__ldg(w + d) + a * float(1.0 / 12));
+      }
+    }
+    __syncthreads();  // buffer b is free
+    if (t == 0) {
+      fence_proxy_async();
+      issue(c + kStreamNB * G, b);
+    }
+  }
+}
+
 // The fused diagnostics of a state u on their own (the iterates a call
 // starts from): the same chunks, grid, grouping and reduction as the
 // streaming gather's DIAG form, so every column has the same arithmetic.

@@ -698,16 +698,31 @@ void lf_step4_launch(mj_lf* lf, void* cur, const void* next, int qc, cudaStream_
   if (prof) cudaEventRecord(lf->ev[lf->ev_used], s);
   launch_k1<Real>(op, next, s);
   if (prof) cudaEventRecord(lf->ev[lf->ev_used + 1], s);
-  k_gather_o4a<Real, EXACT><<<stream_grid(n), 256, 0, s>>>(
-      op->R.as<Real>(), op->ptr.as<int>(), lf->ctr.as<int>(), qc, lf->pulse_d.as<double>(), lf->n_pulse,
-      lf->src_mask.as<unsigned>(), lf->src_sidx.as<int>(), lf->src_sval.as<Real>(), lf->n_src_sorted,
-      lf->minv.as<Real>(), dt2, lf->w4.as<Real>(), lf->z4.as<Real>(), n);
-  launch_k1<Real>(op, lf->z4.ptr, s);
-  k_gather_o4b<Real, EXACT><<<stream_grid(n), 256, 0, s>>>(
-      op->R.as<Real>(), op->ptr.as<int>(), lf->ctr.as<int>(), qc, lf->pulse3_d.as<double>(), lf->n_pulse3,
-      lf->src_mask.as<unsigned>(), lf->src_sidx.as<int>(), lf->src_sval.as<Real>(), lf->n_src_sorted,
-      lf->w4.as<Real>(), static_cast<Real*>(cur), static_cast<const Real*>(next),
-      EXACT ? lf->mass.as<Real>() : nullptr, lf->minv.as<Real>(), dt2, n);
+  if (!EXACT && lf->stream_grid_ > 0) {  // FP32: the streaming forms
+    const float* Rf = op->R.as<float>();
+    k_gather_o4_stream<0><<<lf->stream_grid_, kStreamThreads, kStreamSmem, s>>>(
+        Rf, op->ptr.as<int>(), lf->ctr.as<int>(), qc, lf->pulse_d.as<double>(), lf->n_pulse,
+        lf->src_mask.as<unsigned>(), lf->src_sidx.as<int>(), lf->src_sval.as<float>(), lf->n_src_sorted, nullptr,
+        nullptr, lf->minv.as<float>(), lf->w4.as<float>(), lf->z4.as<float>(), lf->stream_chunks.as<StreamChunk>(),
+        lf->n_stream_chunks, float(dt2), op->err.as<int>());
+    launch_k1<Real>(op, lf->z4.ptr, s);
+    k_gather_o4_stream<1><<<lf->stream_grid_, kStreamThreads, kStreamSmem, s>>>(
+        Rf, op->ptr.as<int>(), lf->ctr.as<int>(), qc, lf->pulse3_d.as<double>(), lf->n_pulse3,
+        lf->src_mask.as<unsigned>(), lf->src_sidx.as<int>(), lf->src_sval.as<float>(), lf->n_src_sorted,
+        static_cast<float*>(cur), static_cast<const float*>(next), lf->minv.as<float>(), lf->w4.as<float>(), nullptr,
+        lf->stream_chunks.as<StreamChunk>(), lf->n_stream_chunks, float(dt2), op->err.as<int>());
+  } else {
+    k_gather_o4a<Real, EXACT><<<stream_grid(n), 256, 0, s>>>(
+        op->R.as<Real>(), op->ptr.as<int>(), lf->ctr.as<int>(), qc, lf->pulse_d.as<double>(), lf->n_pulse,
+        lf->src_mask.as<unsigned>(), lf->src_sidx.as<int>(), lf->src_sval.as<Real>(), lf->n_src_sorted,
+        lf->minv.as<Real>(), dt2, lf->w4.as<Real>(), lf->z4.as<Real>(), n);
+    launch_k1<Real>(op, lf->z4.ptr, s);
+    k_gather_o4b<Real, EXACT><<<stream_grid(n), 256, 0, s>>>(
+        op->R.as<Real>(), op->ptr.as<int>(), lf->ctr.as<int>(), qc, lf->pulse3_d.as<double>(), lf->n_pulse3,
+        lf->src_mask.as<unsigned>(), lf->src_sidx.as<int>(), lf->src_sval.as<Real>(), lf->n_src_sorted,
+        lf->w4.as<Real>(), static_cast<Real*>(cur), static_cast<const Real*>(next),
+        EXACT ? lf->mass.as<Real>() : nullptr, lf->minv.as<Real>(), dt2, n);
+  }
   count_launch(2);
   if (prof) {
     cudaEventRecord(lf->ev[lf->ev_used + 2], s);
