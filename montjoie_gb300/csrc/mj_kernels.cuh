@@ -12,6 +12,32 @@
 
 namespace mj {
 
+// Sums of the contributions of V dofs d[v] of one thread straight from
+// global memory (dof-ordered CSR), each 0 + R[q0] + R[q0 + 1] + ... in CSR
+// order; the offsets and the first terms of all V dofs are loaded together
+// so their latencies overlap.
+template <typename Real, int V>
+__device__ __forceinline__ void contrib_sums_global(const Real* __restrict__ R, const int* __restrict__ ptr,
+                                                    const int (&d)[V], const bool (&on)[V], Real (&s)[V]) {
+  int qa[V], qb[V];
+  Real first[V];
+#pragma unroll
+  for (int v = 0; v < V; v++) {
+    qa[v] = on[v] ? __ldg(ptr + d[v]) : 0;
+    qb[v] = on[v] ? __ldg(ptr + d[v] + 1) : 0;
+  }
+#pragma unroll
+  for (int v = 0; v < V; v++) first[v] = qa[v] < qb[v] ? __ldg(R + qa[v]) : Real(0);
+#pragma unroll
+  for (int v = 0; v < V; v++) {
+    s[v] = Real(0);
+    if (qa[v] < qb[v]) s[v] += first[v];
+    for (int q = qa[v] + 1; q < qb[v]; q++) s[v] += __ldg(R + q);
+  }
+}
+
+// Dofs per thread and pass of the grid-stride gathers below.
+constexpr int kGatherV = 4;
 
 // ---------------------------------------------------------------------------
 // K2a: y <- beta*y + alpha * sum R[ptr[d] .. ptr[d+1])  (MltAdd).  The element
@@ -21,11 +47,20 @@ namespace mj {
 template <typename Real>
 __global__ void k_gather_mltadd(const Real* __restrict__ R, const int* __restrict__ ptr, Real alpha, Real beta,
                                 Real* __restrict__ y, int n_dof) {
-  for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < n_dof; d += gridDim.x * blockDim.x) {
-    Real s = 0;
-    const int q1 = __ldg(ptr + d + 1);
-    for (int q = __ldg(ptr + d); q < q1; q++) s += __ldg(R + q);
-    y[d] = (beta == Real(0)) ? alpha * s : beta * y[d] + alpha * s;
+  constexpr int V = kGatherV;
+  for (int base = blockIdx.x * blockDim.x * V; base < n_dof; base += gridDim.x * blockDim.x * V) {
+    int dv[V];
+    bool on[V];
+    Real sv[V];
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+      dv[v] = base + v * blockDim.x + threadIdx.x;
+      on[v] = dv[v] < n_dof;
+    }
+    contrib_sums_global<Real, V>(R, ptr, dv, on, sv);
+#pragma unroll
+    for (int v = 0; v < V; v++)
+      if (on[v]) y[dv[v]] = (beta == Real(0)) ? alpha * sv[v] : beta * y[dv[v]] + alpha * sv[v];
   }
 }
 
@@ -44,18 +79,30 @@ __global__ void k_gather_leapfrog(const Real* __restrict__ R, const int* __restr
                                   int qc, Real* __restrict__ u0, const Real* __restrict__ u1,
                                   const Real* __restrict__ mass, const Real* __restrict__ minv, Real dt2, int n_dof) {
   if (blockIdx.x == 0 && threadIdx.x == 0) ctr[1 - qc] = ctr[qc] + 1;
-  for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < n_dof; d += gridDim.x * blockDim.x) {
-    Real s = 0;
-    const int q1 = __ldg(ptr + d + 1);
-    for (int q = __ldg(ptr + d); q < q1; q++) s += __ldg(R + q);
-    const Real ah = -s;
-    if (EXACT) {
-      const Real Dd = __ldg(mass + d);
-      Real a = dt2 * ah - Dd * u0[d];
-      a += Real(2) * Dd * __ldg(u1 + d);
-      u0[d] = a * __ldg(minv + d);
-    } else {
-      u0[d] = Real(2) * __ldg(u1 + d) - u0[d] + __ldg(minv + d) * ah;
+  constexpr int V = kGatherV;
+  for (int base = blockIdx.x * blockDim.x * V; base < n_dof; base += gridDim.x * blockDim.x * V) {
+    int dv[V];
+    bool on[V];
+    Real sv[V];
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+      dv[v] = base + v * blockDim.x + threadIdx.x;
+      on[v] = dv[v] < n_dof;
+    }
+    contrib_sums_global<Real, V>(R, ptr, dv, on, sv);
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+      if (!on[v]) continue;
+      const int d = dv[v];
+      const Real ah = -sv[v];
+      if (EXACT) {
+        const Real Dd = __ldg(mass + d);
+        Real a = dt2 * ah - Dd * u0[d];
+        a += Real(2) * Dd * __ldg(u1 + d);
+        u0[d] = a * __ldg(minv + d);
+      } else {
+        u0[d] = Real(2) * __ldg(u1 + d) - u0[d] + __ldg(minv + d) * ah;
+      }
     }
   }
 }
@@ -122,32 +169,6 @@ __device__ __forceinline__ double source_at(const unsigned* __restrict__ mask, c
 // First gather of a step, pulse p = pulse[ctr[qc]]:
 //   EXACT (FP64): P = (-(A U^{n+1}) + p F) dt^2,  Z = invD P     (w <- P, z <- Z)
 //   FP32:         w = -(A U^{n+1}) + p F,         z = (dt^2/D) w
-// Sums of the contributions of V dofs d[v] of one thread straight from
-// global memory (dof-ordered CSR), each 0 + R[q0] + R[q0 + 1] + ... in CSR
-// order; the offsets and the first terms of all V dofs are loaded together
-// so their latencies overlap.
-template <typename Real, int V>
-__device__ __forceinline__ void contrib_sums_global(const Real* __restrict__ R, const int* __restrict__ ptr,
-                                                    const int (&d)[V], const bool (&on)[V], Real (&s)[V]) {
-  int qa[V], qb[V];
-  Real first[V];
-#pragma unroll
-  for (int v = 0; v < V; v++) {
-    qa[v] = on[v] ? __ldg(ptr + d[v]) : 0;
-    qb[v] = on[v] ? __ldg(ptr + d[v] + 1) : 0;
-  }
-#pragma unroll
-  for (int v = 0; v < V; v++) first[v] = qa[v] < qb[v] ? __ldg(R + qa[v]) : Real(0);
-#pragma unroll
-  for (int v = 0; v < V; v++) {
-    s[v] = Real(0);
-    if (qa[v] < qb[v]) s[v] += first[v];
-    for (int q = qa[v] + 1; q < qb[v]; q++) s[v] += __ldg(R + q);
-  }
-}
-
-// Dofs per thread and pass of the grid-stride gathers below.
-constexpr int kGatherV = 4;
 
 template <typename Real, bool EXACT>
 __global__ void k_gather_o4a(const Real* __restrict__ R, const int* __restrict__ ptr, const int* __restrict__ ctr,
