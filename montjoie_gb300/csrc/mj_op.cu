@@ -666,8 +666,7 @@ void lf_diag_launch(mj_lf* lf, const void* u, double* norms_d, double* traces_d,
 }
 
 template <typename Real>
-int lf_diag(mj_lf* lf, double* norms_d, int norm_col, double* traces_d, int stride, int col) {
-  (void)norm_col;  // the norm and the traces share the column
+int lf_diag(mj_lf* lf, double* norms_d, double* traces_d, int stride, int col) {
   lf_diag_launch<Real>(lf, lf->cur(), norms_d, traces_d, stride, col, nullptr, lf->stream);
   MJ_CUDA(cudaGetLastError());
   return MJ_OK;
@@ -906,7 +905,7 @@ int lf_advance_impl(mj_lf* lf, int nsteps, double* norms, double* traces, int st
       return lf_step<Real>(lf, &dg);
     }
     if (nd || td) {
-      const int rc = lf_diag<Real>(lf, nd, s, td, cols, s);
+      const int rc = lf_diag<Real>(lf, nd, td, cols, s);
       if (rc) return rc;
     }
     return lf_step<Real>(lf);
@@ -947,7 +946,7 @@ int lf_advance_impl(mj_lf* lf, int nsteps, double* norms, double* traces, int st
     if (rc) return rc;
   }
   if (final_diag && !fused) {
-    const int rc = lf_diag<Real>(lf, nd, nsteps, td, cols, nsteps);
+    const int rc = lf_diag<Real>(lf, nd, td, cols, nsteps);
     if (rc) return rc;
   }
   cudaStream_t s = lf->stream;
