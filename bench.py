@@ -1,7 +1,7 @@
 #!/usr/bin/env python
 """Benchmark: DOF-updates/s of the Q4 hexahedral acoustic leap-frog on one GB300.
 
-Workload (BASELINE configuration 2): unit cube, 64^3 hexahedra, vertices
+Workload: unit cube, 64^3 hexahedra, vertices
 perturbed uniformly by +-5% h (seeded), Q4 Gauss-Lobatto, c piecewise
 constant on 8^3 random blocks in [1,3], Ricker f0 = 5 at the centre (Gaussian
 R = 2h), Neumann, dt = 0.5 CFL.  One bench step = one leap-frog time step over
@@ -46,14 +46,15 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--no-extras", action="store_true", help="skip the configuration 3 and 4 legs")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the other workloads (Q8, sources, meshes, adjoint, order-4 scheme)")
     ap.add_argument("--extra-steps", type=int, default=500)
     ap.add_argument("--adjoint-steps", type=int, default=1000)
     ap.add_argument("--mb-orders", default="2,3,4,6,8",
-                    help="orders cycled over the heterogeneous batch (2,3,4,6,8 = the configuration)")
+                    help="orders cycled over the heterogeneous batch (default 2,3,4,6,8)")
     ap.add_argument("--mb-max-cells", type=int, default=40,
-                    help="largest mesh of the heterogeneous batch (40 = the configuration; smaller for profiling)")
-    ap.add_argument("--leg", default="all", choices=["all", "config3", "config4", "config4m", "config5", "order4"],
+                    help="largest mesh of the heterogeneous batch (default 40; smaller for profiling)")
+    ap.add_argument("--leg", default="all", choices=["all", "q8", "sources", "meshes", "adjoint", "order4"],
                     help="profiling aid: run one extra leg alone (no JSON line contract)")
     return ap.parse_args()
 
@@ -178,8 +179,8 @@ def timed_steps(torch, step_fn, steps):
     return start.elapsed_time(end)
 
 
-def leg_config3(args, torch, _lib):
-    """BASELINE configuration 3: 32^3 hexahedra, smooth sinusoidal vertex
+def leg_q8(args, torch, _lib):
+    """32^3 hexahedra, smooth sinusoidal vertex
     displacement 0.1h, Q8, c = 2 + 0.5 sin sin sin, FP32 state (factors stored
     FP64, cast to FP32), error stated against the FP64 plain path."""
     from montjoie_gb300 import mesh as M
@@ -216,8 +217,8 @@ def leg_config3(args, torch, _lib):
             "setup_seconds": setup_s}
 
 
-def leg_config4_sources(args, torch, _lib):
-    """BASELINE configuration 4, first half: 64 independent Ricker sources at
+def leg_sources(args, torch, _lib):
+    """64 independent Ricker sources at
     seeded random positions on one 32^3 Q4 mesh (c per element in [1,3]),
     FP32, advanced together, CUDA-graph replay."""
     from montjoie_gb300 import mesh as M
@@ -267,7 +268,8 @@ def leg_config4_sources(args, torch, _lib):
     u0_64 = lf.GetIterate()
     lf.close(); op64.close()
     n_elt, Q = pb.nodle.shape
-    # SURVEY 8d batched bytes per right-hand side and step, divided by the dofs
+    # batched bytes per right-hand side and step: factors and Nodle shared by the
+    # S runs, R written and read, the state rows; divided by the dofs
     bytes_step = (n_elt * Q * (6 * 4 + 4) / S + pb.n_dof * (3 * 4 + 4 / S)) / pb.n_dof
     value = pb.n_dof * S * K / (ms / 1e3)
     peak, _ = measured_peaks()
@@ -285,8 +287,8 @@ def leg_config4_sources(args, torch, _lib):
             "step_frac_of_hbm": value * bytes_step / 1e9 / peak}
 
 
-def leg_config4_meshes(args, torch, _lib):
-    """BASELINE configuration 4, second half: 24 meshes from 8^3 to 40^3
+def leg_meshes(args, torch, _lib):
+    """24 meshes from 8^3 to 40^3
     hexahedra (+-5% h perturbation, c per element in [1,3]) with orders
     cycling 2,3,4,6,8, each with its own Ricker source at the centre and its
     own dt = 0.5 CFL, FP32, all advanced by one cooperative kernel per step
@@ -356,7 +358,7 @@ def leg_config4_meshes(args, torch, _lib):
 
 def leg_order4(args, torch, _lib):
     """The order-4 modified-equation leap-frog (two stiffness products per
-    step, CFL constant 2 sqrt(3)) on the configuration-2 mesh, 64^3 Q4, at
+    step, CFL constant 2 sqrt(3)) on the 64^3 Q4 mesh of the headline workload, at
     dt = 0.5 CFL of that scheme: FP32 and FP64 step rates, FP32 error against
     FP64, and simulated time per second against the order-2 leap-frog."""
     cells, order, K = args.cells, args.order, args.extra_steps
@@ -395,8 +397,8 @@ def leg_order4(args, torch, _lib):
             "norm_history_rel_l2_vs_fp64": float(np.linalg.norm(n32 - n64) / max(np.linalg.norm(n64), 1e-300))}
 
 
-def leg_config5_adjoint(args, torch, _lib):
-    """BASELINE configuration 5: 32^3 Q4, per-element c as parameter (start
+def leg_adjoint(args, torch, _lib):
+    """32^3 Q4, per-element c as parameter (start
     U[1.5,2.5]), 16 sources x 64 receivers, FP32 steps, L2 misfit against
     traces of a seeded perturbed true c; gradient by the discrete adjoint with
     sqrt(N) checkpointing.  Timed at full size; the gradient is checked on a
@@ -601,7 +603,7 @@ def run_ours(args):
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
            "ms_per_step": ms32 / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "f32", "data": "synthetic (seeded perturbed mesh and media, BASELINE configuration 2 shapes)",
+           "dtype": "f32", "data": "synthetic (seeded perturbed 64^3 Q4 mesh, c on 8^3 random blocks)",
            "config": {"workload": workload_name(args.cells, args.order), "cells": args.cells, "order": args.order,
                       "n_dof": n_dof, "n_elt": n_elt, "dt": pb.setup.dt, "parallelism": f"replicas x{world}",
                       "l2_flush": "inputs larger than L2 (factors alone %.2f GB)" % (n_elt * Q * 24 / 1e9),
@@ -612,10 +614,10 @@ def run_ours(args):
            "roofline": roofline, "clocks": clk, "gpu_launches": launches, "e2e": e2e}
     if not args.no_extras:
         op32.close(); op64.close()
-        out["config3_q8"] = leg_config3(args, torch, _lib)
-        out["config4_sources"] = leg_config4_sources(args, torch, _lib)
-        out["config4_meshes"] = leg_config4_meshes(args, torch, _lib)
-        out["config5_adjoint"] = leg_config5_adjoint(args, torch, _lib)
+        out["q8_curved_32"] = leg_q8(args, torch, _lib)
+        out["sources64_32"] = leg_sources(args, torch, _lib)
+        out["meshes24"] = leg_meshes(args, torch, _lib)
+        out["adjoint_32"] = leg_adjoint(args, torch, _lib)
         o4 = leg_order4(args, torch, _lib)
         o4["simulated_time_per_second_order2_fp32"] = pb.setup.dt * K / (ms32 / 1e3)
         out["order4_scheme"] = o4
@@ -721,8 +723,8 @@ def main():
         import torch
         from montjoie_gb300 import _lib
         _lib.load(build_if_missing=False)
-        fn = {"config3": leg_config3, "config4": leg_config4_sources, "config4m": leg_config4_meshes,
-              "config5": leg_config5_adjoint, "order4": leg_order4}[args.leg]
+        fn = {"q8": leg_q8, "sources": leg_sources, "meshes": leg_meshes, "adjoint": leg_adjoint,
+              "order4": leg_order4}[args.leg]
         print(json.dumps({args.leg: fn(args, torch, _lib)}))
         return
     if args.impl == "reference":

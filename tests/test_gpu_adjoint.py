@@ -1,4 +1,4 @@
-"""GPU discrete adjoint (BASELINE configuration 5 pattern on a small mesh):
+"""GPU discrete adjoint (the 32^3 Q4 inverse problem's pattern on a small mesh):
 FP32 forward traces and the adjoint gradient against the FP64 CPU adjoint of
 the oracle, the torch.autograd.Function wrapper, and checkpointing that does
 not change the result."""

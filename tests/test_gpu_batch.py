@@ -1,4 +1,4 @@
-"""Many sources on one mesh (BASELINE configuration 4, first half): S leap-frog
+"""Many sources on one mesh (64 Ricker sources on 32^3 Q4 at full size): S leap-frog
 runs advanced together in FP32 must match S separate runs of the reference's
 scheme (the FP64 oracle) within the FP32 tolerance, 1e-4 relative L2 over
 the run; the captured-graph path must equal the plain launch path bit for bit."""

@@ -2,7 +2,7 @@
 
 FP64 plain form: relative L2 of the final iterate and of the norm history
 <= 1e-10 against the reference's own run (golden fixtures; 30-200 steps).
-The 16^3 Q4 case (BASELINE configuration 1, 200 steps) runs our whole
+The 16^3 Q4 parity case (200 steps) runs our whole
 set-up (numbering, geometry, mass, source, pulse, receivers) and compares
 the norm history, the 8 receiver traces and 512 probe values of u^200 with
 the reference's, <= 1e-10 relative.  FP32 errors are stated per test.
