@@ -8,7 +8,7 @@
  * by the reference itself (oracle/ref_dump.cc, tests/golden/make_golden.py).
  *
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
- * this library, always as the checker or the CPU baseline.
+ * this library, always for expected values or as the CPU baseline.
  *
  * Conventions (all from the reference):
  *  - reference cube [0,1]^3, GL weights summing to 1

@@ -3,7 +3,7 @@
 ctypes bindings to ``oracle/_build/liboracle.so`` (the plain-C FP64
 restatement of the reference's acoustic hot path, ``oracle/mj_oracle.c``) plus
 small numpy helpers.  Used by ``tests/``, ``__graft_entry__.smoke()`` and the
-CPU-baseline leg of ``bench.py`` as the checker, never as the measured path.
+CPU-baseline leg of ``bench.py`` as the source of expected values, never as the measured path.
 """
 from __future__ import annotations
 
