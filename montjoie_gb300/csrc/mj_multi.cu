@@ -19,11 +19,11 @@
 //   barrier  grid-wide, bounded (a cooperative launch guarantees that every
 //            CTA is resident, and every wait gives up after a time limit,
 //            reporting through the error flag);
-//   phase 2  dof chunks of all meshes, two buffers per CTA: the chunk's
-//            u^{n+1}, u^n, dt^2/D, CSR offsets and its contiguous range of R
-//            arrive by bulk copy (the next chunk's during this one), then
-//            each dof's sum, leap-frog update and source term (a per-dof bit
-//            mask marks source dofs).
+//   phase 2  dof chunks of all meshes, walked by each warp on its own with
+//            two buffers of its own: the chunk's u^{n+1}, u^n, dt^2/D, CSR
+//            offsets and its contiguous range of R arrive by bulk copy (the
+//            next chunk's during this one), then each dof's sum, leap-frog
+//            update and source term (a per-dof bit mask marks source dofs).
 // Two launch configurations are compiled (256 threads with large tiles, 128
 // threads with small tiles and more CTAs per SM); the first advance times
 // both on the batch itself and keeps the faster.  A batch whose meshes all
