@@ -146,6 +146,27 @@ def test_diagnosed_graph_replay_equals_plain_launches(config1, precision):
     assert np.array_equal(n1, n2) and np.array_equal(t1, t2) and np.array_equal(u1, u2)
 
 
+@pytest.mark.parametrize("nsteps", [0, 1, 2, 21, 22])
+def test_diagnosed_run_lengths_fp32_vs_fp64(config1, nsteps):
+    """Short and odd runs through the fused FP32 diagnostics (iterates 0 and 1
+    by their own launch, later ones by the steps): nsteps+1 columns, close to
+    the FP64 plain form's; Advance(0) records nothing."""
+    g, pb = config1
+    out = {}
+    for precision in ("fp64", "fp32"):
+        op = pb.operator(precision)
+        lf = pb.integrator(op)
+        uf, norms, traces = lf.Run(np.zeros(pb.n_dof), None, nsteps)
+        assert norms.shape == (nsteps + 1,) and traces.shape == (8, nsteps + 1)
+        n0, t0 = lf.Advance(0)
+        assert n0.shape == (0,) and t0.shape == (8, 0)
+        out[precision] = (uf, norms, traces)
+        lf.close(); op.close()
+    (u64, n64, t64), (u32, n32, t32) = out["fp64"], out["fp32"]
+    assert np.abs(n32 - n64).max() <= 1e-5 * max(np.abs(n64).max(), 1e-300)
+    assert np.abs(t32 - t64).max() <= 1e-5 * max(np.abs(t64).max(), 1e-300)
+
+
 def test_graph_replay_equals_plain_launches_single_source():
     g = load_golden("cube4_q4")
     for precision in ("fp64", "fp32"):
