@@ -178,9 +178,10 @@ __device__ __forceinline__ void store_tile(int n_rt, float* s_u, const float (&g
 // SAME: every tile of the batch has order N (the next tile's gather is
 // specialised to it).
 template <int T, int N, bool SAME>
-__device__ __forceinline__ bool tile_run(const MeshDev& m, int tile, const float* __restrict__ fac, float* s_u,
-                                         float* s_vx, float* s_vy, int nn, const float* xn, const int* nodn,
-                                         uint64_t* barn, uint32_t parn, bool prof, unsigned long long& wns) {
+__device__ __forceinline__ bool tile_run(float* R, const int* slot_e, int tile, const float* __restrict__ fac,
+                                         float* s_u, float* s_vx, float* s_vy, int nn, const float* xn,
+                                         const int* nodn, uint64_t* barn, uint32_t parn, bool prof,
+                                         unsigned long long& wns) {
   constexpr int E = MbCfg<T>::tile(N), NN = N * N, Q = N * NN, Qp = elem_slots(N);
   const float* __restrict__ Gm = c_gmat32[N];
   const int t = threadIdx.x;
@@ -241,7 +242,7 @@ __device__ __forceinline__ bool tile_run(const MeshDev& m, int tile, const float
       gri[a] = Gm[i * N + a];
       grj[a] = Gm[j * N + a];
     }
-    const int* __restrict__ st = m.slot_e + ((size_t)tile * E + el) * Qp + ij;
+    const int* __restrict__ st = slot_e + ((size_t)tile * E + el) * Qp + ij;
 #pragma unroll
     for (int k = 0; k < N; k++) {
       float rx[N], ry[N];
@@ -257,11 +258,34 @@ __device__ __forceinline__ bool tile_run(const MeshDev& m, int tile, const float
         y += grj[a] * ry[a];
         y += Gm[k * N + a] * vz[a];
       }
-      m.R[__ldg(st + k * NN)] = y;
+      R[__ldg(st + k * NN)] = y;
     }
   }
   if (nn) store_tile<T, SAME ? N : 0>(nn, s_u, g);
   return true;
+}
+
+// The tile product of order N as a function of its own, for the all-orders
+// kernel's orders up to n = 6 (Q5): out of line they no longer weigh on the
+// code of the costly high orders, which stay inline (measured on 24 meshes of
+// orders 2,3,4,6,8: 1.99 -> 1.88 ms per step; with only n = 9 inline, 1.94).
+// Shared memory is reached through the dynamic shared-memory symbol and
+// offsets.  Returns the stage-wait time, or ~0 on a timeout.
+template <int T, int N>
+__device__ __noinline__ unsigned long long tile_run_out(float* R, const int* slot_e, int tile, int stage, int nn,
+                                                        const float* xn, uint32_t parn, bool prof) {
+  using P = MbPlan<T>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  float* s_u = reinterpret_cast<float*>(smem + 2 * P::kStage);
+  float* s_vx = s_u + P::kWork;
+  float* s_vy = s_vx + P::kWork;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + P::kArea);
+  const float* fac = reinterpret_cast<const float*>(smem + stage * P::kStage);
+  const int* nodn = nn ? stage_nodle<T>(smem + (stage ^ 1) * P::kStage, nn) : nullptr;
+  unsigned long long wns = 0;
+  const bool ok = tile_run<T, N, false>(R, slot_e, tile, fac, s_u, s_vx, s_vy, nn, xn, nodn, &bar[stage ^ 1], parn,
+                                        prof, wns);
+  return ok ? wns : ~0ull;
 }
 
 // Position of d in the sorted source list (d is known to be present).
@@ -392,8 +416,15 @@ __global__ void __launch_bounds__(T, MbCfg<T>::min_ctas)
     // the tile's order as a compile-time constant; SAME when the batch has one order
     auto run = [&](auto order) {
       constexpr int N = decltype(order)::value;
-      return tile_run<T, N, (ONLY > 0)>(m, cur.tile, fac, s_u, s_vx, s_vy, nn, xn, nodn, &bar[s ^ 1], parn, prof,
-                                        wns1);
+      if constexpr (ONLY == 0 && N <= 6) {  // low orders out of line
+        const unsigned long long r = tile_run_out<T, N>(m.R, m.slot_e, cur.tile, s, nn, xn, parn, prof);
+        if (r == ~0ull) return false;
+        wns1 += r;
+        return true;
+      } else {
+        return tile_run<T, N, (ONLY > 0)>(m.R, m.slot_e, cur.tile, fac, s_u, s_vx, s_vy, nn, xn, nodn, &bar[s ^ 1],
+                                          parn, prof, wns1);
+      }
     };
     bool ok;
     if constexpr (ONLY > 0) {
