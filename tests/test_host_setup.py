@@ -55,6 +55,23 @@ def test_create_rejects_bad_arguments():
     assert L.mj_lf_advance(None, 1, None, None, 0) == _lib.MJ_ERR_ARG
 
 
+def test_batch_entry_points_reject_null_handles():
+    """The batch, many-source and adjoint entry points check their handles
+    before touching the device."""
+    L = _lib.load()
+    h = ctypes.c_void_p()
+    assert L.mj_mb_create(0, None, ctypes.byref(h)) == _lib.MJ_ERR_ARG
+    assert L.mj_mb_create(1, None, ctypes.byref(h)) == _lib.MJ_ERR_ARG
+    assert L.mj_mb_advance(None, 1, 1) == _lib.MJ_ERR_ARG
+    assert L.mj_mb_info(None, None, None, None, None, None, None) == _lib.MJ_ERR_ARG
+    assert L.mj_mb_phase_ms(None, None) == _lib.MJ_ERR_ARG
+    assert L.mj_mb_set_config(None, 128) == _lib.MJ_ERR_ARG
+    assert L.mj_mb_tuning(None, None, None) == _lib.MJ_ERR_ARG
+    assert L.mj_lfb_create(None, None, ctypes.byref(h)) == _lib.MJ_ERR_ARG
+    assert L.mj_adj_create(None, 10, 0, ctypes.byref(h)) == _lib.MJ_ERR_ARG
+    assert b"null" in L.mj_last_error()
+
+
 def test_numbering_is_the_reference_numbering_up_to_permutation(golden_case):
     name, g = golden_case
     r = int(g["order"])
