@@ -87,6 +87,13 @@ def workload_name(cells, order):
             f"Ricker f0=5 Gaussian R=2h at centre, Neumann, leap-frog dt=0.5 CFL")
 
 
+def workload_config(cells, order, n_dof):
+    """The `config` record, the same in both arms."""
+    return {"workload": workload_name(cells, order), "cells": cells, "order": order, "n_dof": n_dof,
+            "l2_flush": "none: inputs larger than L2 (the factors alone are %.2f GB or more per step)"
+                        % (cells ** 3 * (order + 1) ** 3 * 24 / 1e9)}
+
+
 def receivers():
     return np.random.default_rng(SEED + 3).uniform(0.1, 0.9, size=(8, 3))
 
@@ -604,10 +611,8 @@ def run_ours(args):
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
            "ms_per_step": ms32 / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f32", "data": "synthetic (seeded perturbed 64^3 Q4 mesh, c on 8^3 random blocks)",
-           "config": {"workload": workload_name(args.cells, args.order), "cells": args.cells, "order": args.order,
-                      "n_dof": n_dof, "n_elt": n_elt, "dt": pb.setup.dt, "parallelism": f"replicas x{world}",
-                      "l2_flush": "inputs larger than L2 (factors alone %.2f GB)" % (n_elt * Q * 24 / 1e9),
-                      "setup_seconds": setup_s},
+           "config": workload_config(args.cells, args.order, n_dof),
+           "parallelism": f"replicas x{world}", "n_elt": n_elt, "dt": pb.setup.dt, "setup_seconds": setup_s,
            "fp64": {"value": value64, "ms_per_step": ms64 / K64, "steps": K64, "elem_kernel_ms": k1_64,
                     "update_kernel_ms": k2_64, "fp32_over_fp64": value / world / value64},
            "error_fp32_vs_fp64": err,
@@ -622,7 +627,7 @@ def run_ours(args):
         o4["simulated_time_per_second_order2_fp32"] = pb.setup.dt * K / (ms32 / 1e3)
         out["order4_scheme"] = o4
     if rank == 0 and not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline(args, pb, u_check=None)
+        out["cpu_baseline"] = cpu_baseline(args)
     if rank == 0:
         print(json.dumps(out))
     if world > 1:
@@ -636,42 +641,81 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
-def cpu_baseline(args, pb=None, u_check=None, seconds=None):
+def port_workload(cells, order, nsteps, nodle=None):
+    """The headline workload set up by the oracle alone (no GPU): the seeded
+    mesh, FP64 factors and mass, the Gaussian source at the centre, dt from a
+    power iteration on the oracle operator and the pulse of nsteps steps.
+    `nodle` reuses a numbering made elsewhere (any numbering gives the same
+    work); by default the lattice numbering."""
+    from oracle import oracle as oc
+    m = workload_mesh(cells)
+    if nodle is None:
+        nodle = oc.structured_nodle(cells, order)
+    bh, jw, xq = oc.geometry(order, m.verts[m.hexes], m.elem_c ** 2)
+    ndof = int(nodle.max()) + 1
+    D = oc.lumped_mass(nodle, jw, ndof)
+    invD = 1.0 / D
+    colors = oc.structured_colors(cells)
+    F = oc.gaussian_source(nodle, jw, xq, ndof, np.array([0.5, 0.5, 0.5]), 2.0 / cells)
+    idx = np.nonzero(F)[0].astype(np.int32)
+    lam = oc.power_iteration_lambda_max(order, nodle, bh, invD, iters=8, colors=colors)
+    dt = 0.5 * 2.0 / np.sqrt(1.05 * lam)
+    pulse = oc.ricker_pulse(5.0, 0.0, dt, nsteps, 1e-15 * nsteps * dt)
+    return {"order": order, "nodle": nodle, "bh": bh, "D": D, "invD": invD, "colors": colors, "idx": idx,
+            "val": F[idx], "dt": dt, "pulse": pulse, "n_dof": ndof}
+
+
+def time_port_steps(w, steps, warmup=0, threads=None):
+    """Wall time of `steps` whole leap-frog steps of the oracle's restatement
+    in ONE call that continues from the state after `warmup` steps (no start
+    step inside the timed call).  threads: host threads (None: all)."""
+    from oracle import oracle as oc
+    before = oc.threads()
+    if threads:
+        oc.threads(threads)
+    u0, u1 = np.zeros(w["n_dof"]), np.zeros(w["n_dof"])
+    a = (w["order"], w["nodle"], w["bh"], w["D"], w["invD"], w["idx"], w["val"])
+    try:
+        if warmup:
+            oc.leapfrog_advance(*a, w["pulse"], w["dt"], warmup, u0, u1, colors=w["colors"])
+        t0 = time.perf_counter()
+        oc.leapfrog_advance(*a, w["pulse"][warmup:], w["dt"], steps, u0, u1, colors=w["colors"])
+        el = time.perf_counter() - t0
+    finally:
+        oc.threads(before)
+    return el
+
+
+def steps_for(seconds, per_step, cap):
+    return int(max(1, min(cap, seconds // max(per_step, 1e-9))))
+
+
+def cpu_baseline(args, seconds=None):
     """The oracle's C restatement (element loop in the reference's order,
     colour-parallel over the host cores) on a bounded sample of the workload:
-    whole leap-frog steps of the same mesh."""
-    from oracle import oracle as oc
+    whole leap-frog steps of the same mesh, timed as one call; also on one
+    core, the reference's own mode."""
     seconds = args.cpu_seconds if seconds is None else seconds
     cells, order = args.cells, args.order
-    if pb is None:
-        m = workload_mesh(cells)
-        nodle = oc.structured_nodle(cells, order)
-        verts_e = m.verts[m.hexes]
-        bh, jw, xq = oc.geometry(order, verts_e, m.elem_c ** 2)
-        ndof = (cells * order + 1) ** 3
-        D = oc.lumped_mass(nodle, jw, ndof)
-        dt = 1e-4
-    else:
-        nodle, bh, D, ndof, dt = pb.nodle, pb.factors, pb.mass, pb.n_dof, pb.setup.dt
-    colors = oc.structured_colors(cells)
-    invD = 1.0 / D
-    u0 = np.zeros(ndof)
-    empty_i, empty_d = np.zeros(0, dtype=np.int32), np.zeros(0)
-    t0 = time.perf_counter()
-    oc.leapfrog(order, nodle, bh, D, invD, empty_i, empty_d, None, dt, 1, u0, colors=colors)
-    t1 = time.perf_counter() - t0
-    steps = int(max(1, min(500, seconds / max(t1, 1e-6))))
-    t0 = time.perf_counter()
-    oc.leapfrog(order, nodle, bh, D, invD, empty_i, empty_d, None, dt, steps, u0, colors=colors)
-    el = time.perf_counter() - t0
-    # per step: (steps + 1) operator applications (initial step + steps)
-    return {"value": ndof * steps / el, "unit": UNIT, "cores": cpu_threads(), "kind": "port",
-            "sample": f"{steps} FP64 leap-frog steps of the same {cells}^3 Q{order} mesh ({ndof} dofs), "
-                      f"oracle C restatement, colour-parallel OpenMP, {el:.1f} s",
-            "seconds": el}
+    w = port_workload(cells, order, 600)
+    probe = time_port_steps(w, 1, warmup=2)
+    steps = steps_for(seconds, probe, 500)
+    el = time_port_steps(w, steps, warmup=2)
+    probe1 = time_port_steps(w, 1, warmup=2, threads=1)
+    steps1 = steps_for(seconds / 2, probe1, 100)
+    el1 = time_port_steps(w, steps1, warmup=2, threads=1)
+    nd = w["n_dof"]
+    return {"value": nd * steps / el, "unit": UNIT, "cores": cpu_threads(), "kind": "port",
+            "sample": f"{steps} FP64 leap-frog steps of the same {cells}^3 Q{order} mesh ({nd} dofs, source on) in "
+                      f"one call after 2 warm-up steps, oracle C restatement, colour-parallel OpenMP, {el:.1f} s",
+            "seconds": el,
+            "one_core": {"value": nd * steps1 / el1, "cores": 1, "steps": steps1, "seconds": el1}}
 
 
 def run_reference(args):
+    """The reference arm: the oracle's C restatement of the reference loop,
+    all host threads, the headline workload; K steps timed as ONE call after
+    W warm-up steps (capped to fit about two minutes), plus a one-core sample."""
     rank, world, local = dist_env()
     if rank != 0:
         return
@@ -679,40 +723,25 @@ def run_reference(args):
     oc.build()
     K, W = args.steps, args.warmup
     cells, order = args.cells, args.order
-    m = workload_mesh(cells)
-    nodle = oc.structured_nodle(cells, order)
-    bh, jw, xq = oc.geometry(order, m.verts[m.hexes], m.elem_c ** 2)
-    ndof = (cells * order + 1) ** 3
-    D = oc.lumped_mass(nodle, jw, ndof)
-    invD = 1.0 / D
-    colors = oc.structured_colors(cells)
-    dt = 0.5 * 2.0 / np.sqrt(1.02 * oc.power_iteration_lambda_max(order, nodle, bh, invD, iters=8, colors=colors))
-    u0 = np.zeros(ndof)
-    ei, ed = np.zeros(0, dtype=np.int32), np.zeros(0)
-    oc.leapfrog(order, nodle, bh, D, invD, ei, ed, None, dt, max(1, min(W, 3)), u0, colors=colors)
+    w = port_workload(cells, order, K + W + 10)
     budget = 120.0
-    t0 = time.perf_counter()
-    done = 0
-    chunk = 1
-    while done < K:
-        c = min(chunk, K - done)
-        oc.leapfrog(order, nodle, bh, D, invD, ei, ed, None, dt, c, u0, colors=colors)
-        done += c
-        el = time.perf_counter() - t0
-        if el > budget:
-            break
-        chunk = min(2 * chunk, 64)
-    el = time.perf_counter() - t0
-    value = ndof * done / el
-    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": done,
-           "requested_steps": K, "warmup": W, "ms_per_step": el / done * 1e3, "higher_is_better": True,
+    probe = time_port_steps(w, 1, warmup=min(W, 3))
+    steps = steps_for(budget, probe, K)
+    el = time_port_steps(w, steps, warmup=W)
+    value = w["n_dof"] * steps / el
+    probe1 = time_port_steps(w, 1, warmup=2, threads=1)
+    steps1 = steps_for(10.0, probe1, K)
+    el1 = time_port_steps(w, steps1, warmup=2, threads=1)
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
+           "requested_steps": K, "warmup": W, "ms_per_step": el / steps * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": workload_name(cells, order), "cells": cells, "order": order, "n_dof": ndof,
-                      "parallelism": "host cores"},
+           "config": workload_config(cells, order, w["n_dof"]), "parallelism": "host cores",
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu_threads(), "kind": "port",
-                            "sample": f"{done} FP64 leap-frog steps of the {cells}^3 Q{order} mesh (time-capped "
-                                      f"at {budget:.0f} s), oracle C restatement of the reference loop, "
-                                      f"colour-parallel OpenMP"},
+                            "sample": f"{steps} FP64 leap-frog steps of the {cells}^3 Q{order} mesh in one call after "
+                                      f"{W} warm-up steps, oracle C restatement of the reference loop, "
+                                      f"colour-parallel OpenMP",
+                            "one_core": {"value": w["n_dof"] * steps1 / el1, "cores": 1, "steps": steps1,
+                                         "seconds": el1}},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 

@@ -391,13 +391,15 @@ int mj_lumped_mass(int order, int n_elt, int n_dof, const int32_t* nodle, const 
  * (n_dof doubles).  The element-local scratch is a fixed array of
  * MJ_STATIC_SCRATCH_POINTS doubles (32 MiB) inside the library.  Every GPU
  * that loads the library holds it until the process exits.  Larger meshes are
- * rejected with MJ_ERR_ARG.  The first call on a device looks up that array's
- * device address, so make the first call on each device before any stream
- * capture.  All calls share the one array, so calls that overlap on the GPU
- * (other streams or host threads) race; serialise them.  The work is ordered
- * on `stream` (a cudaStream_t, NULL = legacy default stream) and the call
- * returns once it is done.  The scatter uses atomic additions, so the result
- * equals mj_op_mltadd's up to rounding order. */
+ * rejected with MJ_ERR_ARG.  Every call looks up that array's device address
+ * in the current device's context (no allocation); the first call on a device
+ * also loads the library's device code there, so make the first call on each
+ * device before any stream capture.  All calls share the one array and keep
+ * no state in it between calls, so calls that overlap on the GPU (other
+ * streams or host threads) race; serialise them.  The work is ordered on
+ * `stream` (a cudaStream_t, NULL = legacy default stream) and the call waits
+ * for it: it returns once the product is in y.  The scatter uses atomic
+ * additions, so the result equals mj_op_mltadd's up to rounding order. */
 int mj_stiffness_mltadd_static(int order, int n_elt, int n_dof, const int32_t* nodle, const double* factors,
                                double alpha, const double* x, double beta, double* y, void* stream);
 

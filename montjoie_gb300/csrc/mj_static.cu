@@ -10,9 +10,6 @@
 // allocated once per GPU when the library's code is loaded and kept until exit.
 #include <cuda_runtime.h>
 
-#include <mutex>
-#include <vector>
-
 #include "mj_common.cuh"
 
 namespace mj {
@@ -139,11 +136,6 @@ __global__ void k_static_scatter(const int* __restrict__ nodle, const double* __
 
 __global__ void k_static_clear_flag() { g_static_bad_index = 0; }
 
-std::mutex g_static_mutex;
-constexpr int kMaxDevices = 64;
-double* g_static_ptr[kMaxDevices] = {nullptr};
-int* g_static_flag_ptr[kMaxDevices] = {nullptr};
-
 template <int N>
 int static_launch(int n_elt, int n_dof, const int32_t* nodle, const double* factors, double alpha, const double* x,
                   double beta, double* y, cudaStream_t s, double* scratch) {
@@ -182,24 +174,19 @@ extern "C" int mj_stiffness_mltadd_static(int order, int n_elt, int n_dof, const
               " exceeds the static scratch of " + std::to_string(kStaticScratchPoints) + " values");
     return MJ_ERR_ARG;
   }
-  int dev = 0;
-  MJ_CUDA(cudaGetDevice(&dev));
-  MJ_CHECK_ARG(dev >= 0 && dev < kMaxDevices, "mj_stiffness_mltadd_static: device index too large");
-  {
-    // Once per device, with that device current: the device address of the
-    // scratch array (the host-side symbol is only a stand-in).
-    std::lock_guard<std::mutex> lock(g_static_mutex);
-    if (!g_static_ptr[dev]) {
-      void* p = nullptr;
-      void* f = nullptr;
-      MJ_CUDA(cudaGetSymbolAddress(&p, g_static_scratch));
-      MJ_CUDA(cudaGetSymbolAddress(&f, g_static_bad_index));
-      g_static_ptr[dev] = static_cast<double*>(p);
-      g_static_flag_ptr[dev] = static_cast<int*>(f);
-    }
-  }
+  // The device addresses of the scratch array and the flag in the current
+  // device's context (the host-side symbols are only stand-ins).  Looked up on
+  // every call: the lookup allocates nothing, and an address kept from an
+  // earlier call would dangle once that context is destroyed (cudaDeviceReset)
+  // and the library's device code is loaded again.  The first lookup on a
+  // device loads that code, which is why the first call comes before any
+  // stream capture.
+  void* p = nullptr;
+  void* f = nullptr;
+  MJ_CUDA(cudaGetSymbolAddress(&p, g_static_scratch));
+  MJ_CUDA(cudaGetSymbolAddress(&f, g_static_bad_index));
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  double* scratch = g_static_ptr[dev];
+  double* scratch = static_cast<double*>(p);
   int rc = MJ_OK;
   switch (order + 1) {
     case 2: rc = static_launch<2>(n_elt, n_dof, nodle, factors, alpha, x, beta, y, s, scratch); break;
@@ -214,7 +201,7 @@ extern "C" int mj_stiffness_mltadd_static(int order, int n_elt, int n_dof, const
   if (rc) return rc;
   MJ_CUDA(cudaStreamSynchronize(s));
   int bad = 0;
-  MJ_CUDA(cudaMemcpy(&bad, g_static_flag_ptr[dev], sizeof(int), cudaMemcpyDeviceToHost));
+  MJ_CUDA(cudaMemcpy(&bad, f, sizeof(int), cudaMemcpyDeviceToHost));
   if (bad) {
     set_error("mj_stiffness_mltadd_static: a Nodle entry is outside [0, n_dof); those entries were skipped");
     return MJ_ERR_ARG;

@@ -21,6 +21,7 @@
  */
 #define _GNU_SOURCE
 #include <math.h>
+#include <omp.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -455,6 +456,42 @@ void oc_leapfrog(int r, int ne, int ndof, const int* nodle, const int* num, cons
     }
   }
   free(ah);
+}
+
+/* The step loop of oc_leapfrog alone (Advance, ModifiedEquation.cxx:290-345)
+ * from a given state (U0, U1) = (u0, u1): nsteps steps, step s taking
+ * pulse[s]; no start step and no diagnostics.  The arithmetic of every dof is
+ * that of oc_leapfrog, so a trajectory continued in chunks equals one call.
+ * The per-dof passes run over the host threads; the element loop is
+ * colour-parallel when colours are given.  On return u0 = U^{n+nsteps},
+ * u1 = U^{n+nsteps+1}. */
+void oc_leapfrog_advance(int r, int ne, int ndof, const int* nodle, const int* num, const double* G,
+                         const double* bh, const double* D, const double* invD, int nsrc, const int* src_idx,
+                         const double* src_val, const double* pulse, double dt, int nsteps, double* u0,
+                         double* u1, int ncolors, const int* color_ptr, const int* color_elems) {
+  double dt2 = dt * dt;
+  double* ah = (double*)malloc(sizeof(double) * (size_t)ndof);
+  for (int s = 0; s < nsteps; s++) {
+    oc_stiffness_mltadd(r, ne, ndof, nodle, num, G, bh, -1.0, u1, 0.0, ah, ncolors, color_ptr, color_elems);
+    double p = pulse ? pulse[s] : 0.0;
+    if (p != 0.0)
+      for (int t = 0; t < nsrc; t++) ah[src_idx[t]] += p * src_val[t];
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < ndof; i++) {
+      double a = dt2 * ah[i] - D[i] * u0[i];
+      a += 2.0 * D[i] * u1[i];
+      u0[i] = u1[i];
+      u1[i] = a * invD[i];
+    }
+  }
+  free(ah);
+}
+
+/* Host threads of the OpenMP loops above (n <= 0: leave unchanged); returns
+ * the number in use. */
+int oc_threads(int n) {
+  if (n > 0) omp_set_num_threads(n);
+  return omp_get_max_threads();
 }
 
 /* Order-4 modified-equation leap-frog (ModifiedEquationIterator with

@@ -60,6 +60,11 @@ def lib():
         L.oc_leapfrog.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _I, _D, _D, _D, _D,
                                   ctypes.c_int, _I, _D, _D, ctypes.c_double, ctypes.c_int, _D, _D, _D,
                                   _D, _D, ctypes.c_int, _I, _D, _D, ctypes.c_int, _I, _I]
+        L.oc_leapfrog_advance.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _I, _D, _D, _D, _D,
+                                          ctypes.c_int, _I, _D, _D, ctypes.c_double, ctypes.c_int, _D, _D,
+                                          ctypes.c_int, _I, _I]
+        L.oc_threads.argtypes = [ctypes.c_int]
+        L.oc_threads.restype = ctypes.c_int
         L.oc_adjoint.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _I, _D, _D, _D, _D, _D,
                                  ctypes.c_int, ctypes.c_int, _I, _I, _D, _D, ctypes.c_double, ctypes.c_int,
                                  ctypes.c_int, _I, _D, _D, _D, _D]
@@ -222,6 +227,28 @@ def leapfrog(r, nodle, bh, D, invD, src_idx, src_val, pulse, dt, nsteps, u0, u1=
                       _p(traces), nc, _p(None if ptr is None else i32(ptr), _I),
                       _p(None if elems is None else i32(elems), _I))
     return u0, u1, norms, traces
+
+
+def leapfrog_advance(r, nodle, bh, D, invD, src_idx, src_val, pulse, dt, nsteps, u0, u1, colors=None):
+    """Continue the order-2 leap-frog from the state (u0, u1) = (U^n, U^{n+1})
+    in place for nsteps steps, step s taking pulse[s] (no start step, no
+    diagnostics).  Chunks of a trajectory equal one whole run."""
+    ne, Q = nodle.shape
+    assert u0.dtype == np.float64 and u1.dtype == np.float64 and u0.flags.c_contiguous and u1.flags.c_contiguous
+    G = grad_matrix(r).ravel().copy()
+    num = hex_numbering(r)
+    ptr, elems = (None, None) if colors is None else colors
+    nc = 0 if colors is None else len(ptr) - 1
+    lib().oc_leapfrog_advance(r, ne, D.size, _p(i32(nodle), _I), _p(num, _I), _p(G), _p(f64(bh)), _p(f64(D)),
+                              _p(f64(invD)), int(len(src_idx)), _p(i32(src_idx), _I), _p(f64(src_val)),
+                              _p(None if pulse is None else f64(pulse)), float(dt), int(nsteps), _p(u0), _p(u1), nc,
+                              _p(None if ptr is None else i32(ptr), _I), _p(None if elems is None else i32(elems), _I))
+    return u0, u1
+
+
+def threads(n: int = 0) -> int:
+    """Sets the host threads of the oracle's parallel loops (n > 0); returns the count in use."""
+    return int(lib().oc_threads(int(n)))
 
 
 def leapfrog4(r, nodle, bh, D, invD, src_idx, src_val, pulse, pulse3, dt, nsteps, u0, du0=None, jw=None,
