@@ -29,6 +29,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "DOF-updates/s (Q4/Q8 hex acoustic leap-frog), FP32 vs FP64 at stated L2 error"
+ORACLE_REF = "FP64 oracle (port): the C restatement of the reference loop, run on the host cores on the same arrays"
 UNIT = "DOF-updates/s"
 SEED = 20251203
 
@@ -46,6 +47,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-oracle", action="store_true",
+                    help="skip the full-size comparisons with the FP64 oracle (about 1.5 min of host time)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the other workloads (Q8, sources, meshes, adjoint, order-4 scheme)")
     ap.add_argument("--extra-steps", type=int, default=500)
@@ -175,6 +178,24 @@ def build_problem(cells, order, nsteps, mesh=None, time_order=2):
     return pb
 
 
+def oracle_run(pb, nsteps, snap_every=None, diag=False, src=None):
+    """The FP64 oracle (the C restatement of the reference loop, colour-
+    parallel on the host cores) on the problem's own arrays, from rest:
+    returns {"snaps": {step: u}, "u": U^nsteps} and, with diag, the norms and
+    receiver traces of iterates 0..nsteps.  src: (idx, val) instead of the
+    problem's source."""
+    from oracle import oracle as oc
+    idx, val = (pb.src_idx, pb.src_val) if src is None else src
+    rec = (pb.rec_idx, pb.rec_w) if (diag and pb.rec_idx is not None) else (None, None)
+    return oc.trajectory(pb.order, pb.nodle, pb.factors, pb.mass, 1.0 / pb.mass, idx, val, pb.pulse, pb.setup.dt,
+                         nsteps, np.zeros(pb.n_dof), jw=pb.jw if diag else None, rec_idx=rec[0], rec_w=rec[1],
+                         colors=oc.structured_colors(pb.mesh.n), snap_every=snap_every)
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), 1e-300))
+
+
 def timed_steps(torch, step_fn, steps):
     """Device time (ms) of step_fn(steps) with CUDA events on the legacy default stream."""
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -215,13 +236,18 @@ def leg_q8(args, torch, _lib):
     d32 = pb.integrator(op32)
     u32, n32, _ = d32.Run(zeros, None, K)
     d64.close(); d32.close(); op32.close(); op64.close()
+    err = {"steps": K, "reference": ORACLE_REF}
+    if not args.no_oracle:
+        t0 = time.perf_counter()
+        o = oracle_run(pb, K, diag=True)
+        err.update({"fp32_u_rel_l2": rel(u32, o["u"]), "fp64_u_rel_l2": rel(u64, o["u"]),
+                    "fp32_norm_history_rel_l2": rel(n32, o["norms"]), "fp64_norm_history_rel_l2": rel(n64, o["norms"]),
+                    "oracle_seconds": time.perf_counter() - t0})
     return {"workload": f"unit cube 32^3 hex Q8, 0.1h sinusoidal vertex displacement, c = 2 + 0.5 sin(2 pi x) sin(2 pi y) "
                         f"sin(2 pi z) per element, Ricker f0=5, Neumann, dt=0.5 CFL, FP32 state, {K} steps",
             "n_dof": pb.n_dof, "steps": K, "value": pb.n_dof * K / (ms32 / 1e3), "unit": UNIT,
             "ms_per_step": ms32 / K, "fp64_value": pb.n_dof * K64 / (ms64 / 1e3), "fp64_ms_per_step": ms64 / K64,
-            "u_rel_l2_vs_fp64": float(np.linalg.norm(u32 - u64) / max(np.linalg.norm(u64), 1e-300)),
-            "norm_history_rel_l2_vs_fp64": float(np.linalg.norm(n32 - n64) / max(np.linalg.norm(n64), 1e-300)),
-            "setup_seconds": setup_s}
+            "error_vs_oracle": err, "u_rel_l2_fp32_vs_fp64": rel(u32, u64), "setup_seconds": setup_s}
 
 
 def leg_sources(args, torch, _lib):
@@ -233,7 +259,8 @@ def leg_sources(args, torch, _lib):
     from montjoie_gb300.problem import gaussian_source
     cells, order, S, K = 32, 4, 64, args.extra_steps
     m = M.perturbed_cube(cells, seed=SEED + 40, amplitude=0.05, kind="random", c_mode="element")
-    pb = build_problem(cells, order, K + 40, mesh=m)
+    NE = max(K + 20, args.error_steps)
+    pb = build_problem(cells, order, max(K, NE) + 40, mesh=m)
     pos = np.random.default_rng(SEED + 41).uniform(0.1, 0.9, size=(S, 3))
     idx, rhs, val = [], [], []
     for s_, c in enumerate(pos):
@@ -254,6 +281,10 @@ def leg_sources(args, torch, _lib):
     b.advance(1)
     info["phase_ms_one_step"] = b.phase_ms()
     b.profile(False)
+    # run 0 after NE steps, against the FP64 oracle and a single-source run
+    b.init()
+    b.advance(NE)
+    u_ne, _ = b.state()
     # the same runs with two kernels per step (element kernel, then gather + update)
     b.set_fused(False)
     b.init()
@@ -261,19 +292,16 @@ def leg_sources(args, torch, _lib):
     ms_two = timed_steps(torch, b.advance, K)
     u_two, _ = b.state()
     b.close()
-    # run 0 against a single-source run of the same FP32 operator and
-    # against the FP64 plain form of that run
     lf = LeapFrogIteratorFor(pb, op, idx[0], val[0])
     lf.SetInitialConditionS(np.zeros(pb.n_dof))
     lf.Advance(K + 20)
     u0 = lf.GetIterate()
     lf.close(); op.close()
-    op64 = pb.operator("fp64")
-    lf = LeapFrogIteratorFor(pb, op64, idx[0], val[0])
-    lf.SetInitialConditionS(np.zeros(pb.n_dof))
-    lf.Advance(K + 20)
-    u0_64 = lf.GetIterate()
-    lf.close(); op64.close()
+    err = {"steps": NE, "run": 0, "reference": ORACLE_REF}
+    if not args.no_oracle:
+        t0 = time.perf_counter()
+        o = oracle_run(pb, NE, src=(idx[0], val[0]))
+        err.update({"fp32_u_rel_l2": rel(u_ne[:, 0], o["u"]), "oracle_seconds": time.perf_counter() - t0})
     n_elt, Q = pb.nodle.shape
     # batched bytes per right-hand side and step: factors and Nodle shared by the
     # S runs, R written and read, the state rows; divided by the dofs
@@ -287,9 +315,8 @@ def leg_sources(args, torch, _lib):
             "variant": info, "gpu_launches": launches,
             "two_kernel_ms_per_step": ms_two / K,
             "one_vs_two_kernel_rel_l2": float(np.linalg.norm(u - u_two) / max(np.linalg.norm(u_two), 1e-300)),
-            "run0_rel_l2_vs_single_source_run": float(np.linalg.norm(u[:, 0] - u0) / max(np.linalg.norm(u0), 1e-300)),
-            "run0_rel_l2_vs_fp64_plain_form": float(np.linalg.norm(u[:, 0] - u0_64) / max(np.linalg.norm(u0_64), 1e-300)),
-            "error_steps": K + 20,
+            "run0_rel_l2_vs_single_source_run_after_%d_steps" % (K + 20): rel(u[:, 0], u0),
+            "error_vs_oracle": err,
             "algorithmic_bytes_per_dof_update": bytes_step,
             "step_frac_of_hbm": value * bytes_step / 1e9 / peak}
 
@@ -392,6 +419,14 @@ def leg_order4(args, torch, _lib):
     d32 = pb.integrator(op32)
     u32, n32, _ = d32.Run(zeros, None, KE)
     d64.close(); d32.close(); op32.close(); op64.close()
+    err = {"steps": KE, "reference": ORACLE_REF.replace("reference loop", "reference's order-4 loop")}
+    if not args.no_oracle:
+        from oracle import oracle as oc
+        t0 = time.perf_counter()
+        uo, _, _, _ = oc.leapfrog4(order, pb.nodle, pb.factors, pb.mass, 1.0 / pb.mass, pb.src_idx, pb.src_val,
+                                   pb.pulse, pb.pulse_d2, pb.setup.dt, KE, zeros, colors=oc.structured_colors(cells))
+        err.update({"fp32_u_rel_l2": rel(u32, uo), "fp64_u_rel_l2": rel(u64, uo),
+                    "oracle_seconds": time.perf_counter() - t0})
     return {"workload": workload_name(cells, order).replace("leap-frog dt=0.5 CFL",
                                                            "order-4 modified-equation leap-frog dt=0.5 CFL(2 sqrt 3)")
             + f", FP32 state, {K} steps",
@@ -399,9 +434,7 @@ def leg_order4(args, torch, _lib):
             "ms_per_step": ms32 / K, "gpu_launches": launches,
             "fp64_value": pb.n_dof * K64 / (ms64 / 1e3), "fp64_ms_per_step": ms64 / K64,
             "simulated_time_per_second_fp32": pb.setup.dt * K / (ms32 / 1e3),
-            "error_steps": KE,
-            "u_rel_l2_vs_fp64": float(np.linalg.norm(u32 - u64) / max(np.linalg.norm(u64), 1e-300)),
-            "norm_history_rel_l2_vs_fp64": float(np.linalg.norm(n32 - n64) / max(np.linalg.norm(n64), 1e-300))}
+            "error_vs_oracle": err, "u_rel_l2_fp32_vs_fp64": rel(u32, u64)}
 
 
 def leg_adjoint(args, torch, _lib):
@@ -538,12 +571,12 @@ def run_ours(args):
     clocks = ClockSampler(local)
     clocks.start()
     ms32, k1_ms, k2_ms, launches = time_advance(torch, lf32, K, _lib, barrier=dist.barrier if world > 1 else None)
-    # ---- FP64 plain form, resident
+    # ---- FP64 plain form, resident (its own step count, after one graph's worth of warm-up)
     op64 = pb.operator("fp64")
     lf64 = pb.integrator(op64, diagnostics=False)
     lf64.SetInitialConditionS(zeros)
-    lf64.Advance(min(W, 3))
-    K64 = min(K, args.fp64_steps)
+    lf64.Advance(21)
+    K64 = args.fp64_steps
     ms64, k1_64, k2_64, _ = time_advance(torch, lf64, K64, _lib)
     clk = clocks.stop()
     if world > 1:
@@ -566,20 +599,28 @@ def run_ours(args):
     u32, n32, tr32 = lf32d.Run(u0_pin, None, args.error_steps, out=uf_pin)
     e2e_s = time.perf_counter() - t0
     lf32d.close()
-    # the same comparison every 100 steps (Advance in chunks; states read back)
-    series = []
+    # the FP32 and FP64 states every 100 steps (Advance in chunks; states read back)
+    NE = args.error_steps
+    snaps32, snaps64 = {}, {}
     a64, a32 = pb.integrator(op64, diagnostics=False), pb.integrator(op32, diagnostics=False)
     a64.SetInitialConditionS(zeros); a32.SetInitialConditionS(zeros)
-    for k in range(0, args.error_steps, 100):
-        a64.Advance(min(100, args.error_steps - k)); a32.Advance(min(100, args.error_steps - k))
-        v64, v32 = a64.GetIterate(), a32.GetIterate()
-        series.append([a64.n_time, float(np.linalg.norm(v32 - v64) / max(np.linalg.norm(v64), 1e-300))])
+    for k in range(0, NE, 100):
+        a64.Advance(min(100, NE - k)); a32.Advance(min(100, NE - k))
+        snaps64[a64.n_time], snaps32[a32.n_time] = a64.GetIterate(), a32.GetIterate()
     a64.close(); a32.close()
-    err = {"steps": args.error_steps, "u_rel_l2_every_100_steps": series,
-           "u_rel_l2": float(np.linalg.norm(u32 - u64) / max(np.linalg.norm(u64), 1e-300)),
-           "norm_history_rel_l2": float(np.linalg.norm(n32 - n64) / max(np.linalg.norm(n64), 1e-300)),
-           "traces_rel_max": float(np.abs(tr32 - tr64).max() / max(np.abs(tr64).max(), 1e-300)),
-           "reference": "FP64 plain GPU path (parity-pinned to the reference solver)"}
+    err = {"steps": NE, "reference": ORACLE_REF,
+           "fp32_vs_fp64_gpu_u_rel_l2": rel(u32, u64)}
+    if not args.no_oracle:
+        t0 = time.perf_counter()
+        o = oracle_run(pb, NE, snap_every=100, diag=True)
+        err.update({
+            "fp32_u_rel_l2_every_100_steps": [[k, rel(snaps32[k], o["snaps"][k])] for k in sorted(o["snaps"])],
+            "fp64_u_rel_l2_every_100_steps": [[k, rel(snaps64[k], o["snaps"][k])] for k in sorted(o["snaps"])],
+            "fp32_u_rel_l2": rel(u32, o["u"]), "fp64_u_rel_l2": rel(u64, o["u"]),
+            "fp32_norm_history_rel_l2": rel(n32, o["norms"]), "fp64_norm_history_rel_l2": rel(n64, o["norms"]),
+            "fp32_traces_rel_max": float(np.abs(tr32 - o["traces"]).max() / np.abs(o["traces"]).max()),
+            "fp64_traces_rel_max": float(np.abs(tr64 - o["traces"]).max() / np.abs(o["traces"]).max()),
+            "oracle_seconds": time.perf_counter() - t0})
     if not args.no_e2e:
         h2d = n_dof * 8  # u0 (du0 = NULL)
         d2h = n_dof * 8 + 8 * (args.error_steps + 1) * (1 + 8)  # u_final, norms, 8 traces
@@ -615,7 +656,7 @@ def run_ours(args):
            "parallelism": f"replicas x{world}", "n_elt": n_elt, "dt": pb.setup.dt, "setup_seconds": setup_s,
            "fp64": {"value": value64, "ms_per_step": ms64 / K64, "steps": K64, "elem_kernel_ms": k1_64,
                     "update_kernel_ms": k2_64, "fp32_over_fp64": value / world / value64},
-           "error_fp32_vs_fp64": err,
+           "error_vs_oracle": err,
            "roofline": roofline, "clocks": clk, "gpu_launches": launches, "e2e": e2e}
     if not args.no_extras:
         op32.close(); op64.close()

@@ -112,6 +112,20 @@ int mj_op_set_variant(mj_op* op, int tile_elems, int vector_lines);
 /* Number of kernels this library launched on the calling process since load. */
 uint64_t mj_kernel_launches(void);
 
+/* Test hook, no reference counterpart.  Every wait of the library's kernels
+ * is bounded: on a bulk copy (mbarrier), mbar_polls polls (default 2^22); on
+ * the other CTAs of a cooperative launch (grid barrier), barrier_polls polls
+ * (default 2^26) or barrier_ns nanoseconds (default 2 s), whichever comes
+ * first.  A wait that runs out makes the kernel report through its error flag
+ * after letting its own copies in flight land, and the entry point returns
+ * MJ_ERR_CUDA (single integrator, operator, many sources: element waits) or
+ * MJ_ERR_STATE (cooperative steps) with a message; the state is then invalid
+ * but the next call starts clean.  This call lowers the limits so a test can
+ * make waits run out (0: give up at the first poll); values above the
+ * defaults are clamped to them and negative values restore them.
+ * Process-wide. */
+int mj_debug_set_wait_limits(long long mbar_polls, long long barrier_polls, long long barrier_ns);
+
 /* ---- leap-frog time loop -------------------------------------------- */
 
 typedef struct {
@@ -198,6 +212,15 @@ int mj_lf_set_scheme(mj_lf* lf, int order, int n_pulse_d2, const double* pulse_d
  * copy; enable = 0 uses a gather kernel and a separate source kernel.  Both
  * give the same states bit for bit. */
 int mj_lf_set_stream_gather(mj_lf* lf, int enable);
+
+/* Divergence guard: mj_lf_advance / mj_lf_run return MJ_ERR_NONFINITE (with
+ * the offending value in mj_last_error) when a recorded norm exceeds
+ * norm_max in absolute value, or is not finite.  The reference checks
+ * |GetNormeSolution| against NormeMaxSolution (default 1e30, the default
+ * here too) and aborts (MONTJOIE/src/Instationary/VarInstationary.cxx:362-374,
+ * 2741-2745); here the call returns after its chunk of steps, the norms up to
+ * the offending step being valid.  Norms are only computed when asked for. */
+int mj_lf_set_norm_max(mj_lf* lf, double norm_max);
 
 /* Sets the CUDA stream (cudaStream_t) used by the integrator's launches. */
 int mj_lf_set_stream(mj_lf* lf, void* stream);

@@ -111,6 +111,8 @@ def load(build_if_missing: bool = True):
     L.mj_lf_set_graph.argtypes = [_VP, ctypes.c_int]
     L.mj_lf_set_scheme.argtypes = [_VP, ctypes.c_int, ctypes.c_int, _D]
     L.mj_lf_set_stream_gather.argtypes = [_VP, ctypes.c_int]
+    L.mj_lf_set_norm_max.argtypes = [_VP, ctypes.c_double]
+    L.mj_debug_set_wait_limits.argtypes = [ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong]
     L.mj_lf_profile.argtypes = [_VP, ctypes.c_int, _D, _D, ctypes.POINTER(ctypes.c_int)]
     L.mj_number_hex_mesh.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _I, ctypes.POINTER(ctypes.c_int)]
     L.mj_geometry.argtypes = [ctypes.c_int, ctypes.c_int, _D, _D, _D, _D, _D]

@@ -511,14 +511,7 @@ int mj_lfb_advance(mj_lfb* b, int nsteps, double* traces, int trace_stride, int 
     for (int r = 0; r < b->n_rec * b->S; r++)
       MJ_CUDA(cudaMemcpyAsync(traces + (size_t)r * trace_stride, b->traces_d.as<double>() + (size_t)r * nsteps,
                               sizeof(double) * nsteps, cudaMemcpyDeviceToHost, s));
-  int err = 0;
-  MJ_CUDA(cudaMemcpyAsync(&err, b->op->err.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
-  MJ_CUDA(cudaStreamSynchronize(s));
-  if (err) {
-    set_error("mj_lfb_advance: an element kernel wait timed out");
-    return MJ_ERR_CUDA;
-  }
-  return MJ_OK;
+  return take_kernel_error(b->op->err.ptr, s, "mj_lfb_advance");
 }
 
 int mj_lfb_get_state(mj_lfb* b, double* u_n, double* u_np1) {
@@ -827,12 +820,9 @@ int mj_adj_backward(mj_adj* a, const double* residual, const double* coef, doubl
   }
   std::vector<double> g(op->n_elt_pad);
   MJ_CUDA(cudaMemcpyAsync(g.data(), a->grad.ptr, sizeof(double) * g.size(), cudaMemcpyDeviceToHost, s));
-  int err = 0;
-  MJ_CUDA(cudaMemcpyAsync(&err, op->err.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
-  MJ_CUDA(cudaStreamSynchronize(s));
-  if (err) {
-    set_error("mj_adj_backward: an element kernel wait timed out");
-    return MJ_ERR_CUDA;
+  {
+    const int rc = take_kernel_error(op->err.ptr, s, "mj_adj_backward");
+    if (rc) return rc;
   }
   for (int e = 0; e < op->n_elt; e++) grad[e] = g[e];
   return MJ_OK;

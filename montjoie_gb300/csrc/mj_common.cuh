@@ -86,4 +86,9 @@ void gl_derivative_matrix(int r, const double* pts, double* g);
 
 int sm_count();
 
+// Reads a kernel's device error flag after the work on `s`; when it is set,
+// clears it (so the next call starts clean), records "<what>: <message>" and
+// returns MJ_ERR_CUDA.  Synchronises `s`.
+int take_kernel_error(void* dev_flag, cudaStream_t s, const char* what);
+
 }  // namespace mj

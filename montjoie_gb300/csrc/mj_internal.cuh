@@ -53,6 +53,7 @@ struct mj_lf {
   cudaGraphExec_t graph_diag = nullptr;  // steps with norm and receivers, columns read from diag_where
   bool use_graph = true;  // replay captured steps when no diagnostics are asked
   int n_src = 0, n_rec = 0, n_rec_w = 0;
+  double norm_max = 1e30;  // largest |norm| accepted (NormeMaxSolution; the reference's default)
   int step = 0;
   bool initialised = false;
   bool cur_is_a = true;

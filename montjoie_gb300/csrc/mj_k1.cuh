@@ -23,6 +23,8 @@
 
 #include <cstdint>
 
+#include "mj_wait.cuh"
+
 namespace mj {
 
 using ::uint32_t;
@@ -49,10 +51,12 @@ struct GConst<float> {
 
 // ---------------------------------------------------------------------------
 // Bulk-copy (TMA) and mbarrier helpers.  Every wait is bounded: after
-// kSpinLimit unsuccessful polls the waiter gives up and the kernel reports
-// the timeout through an error flag instead of hanging.
+// c_wait.mbar_polls unsuccessful polls (kSpinLimit unless a test lowered it)
+// the waiter gives up and the kernel reports the timeout through an error
+// flag instead of hanging.  Before returning, the CTA drains the copies it
+// still has in flight (mbar_wait_drain, always with the full kSpinLimit) so
+// that no copy lands in shared memory after the CTA has exited.
 // ---------------------------------------------------------------------------
-constexpr long kSpinLimit = 1L << 22;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -99,9 +103,17 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-  for (long it = 0; it < kSpinLimit; ++it)
+  const long limit = c_wait.mbar_polls;
+  for (long it = 0; it < limit; ++it)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
+}
+
+// Wait of a CTA that is giving up after a timed-out wait: lets a copy still in
+// flight into this stage complete (bounded by the full kSpinLimit).
+__device__ __forceinline__ void mbar_wait_drain(uint64_t* bar, uint32_t parity) {
+  for (long it = 0; it < kSpinLimit; ++it)
+    if (mbar_try_wait(bar, parity)) return;
 }
 
 // Sums of the staged contributions of V dofs of one thread (dof-ordered
@@ -248,7 +260,11 @@ __global__ void __launch_bounds__(E* N* N)
   if (tile < n_tiles) {
     const bool ok = mbar_wait_bounded(&bar[0], ph & 1u);
     if (__syncthreads_or(!ok)) {
-      if (t == 0) atomicExch(err, 1);
+      if (t == 0) {  // report; both stages may still have a copy in flight
+        atomicExch(err, 1);
+        mbar_wait_drain(&bar[0], 0u);
+        if (tile + g < n_tiles) mbar_wait_drain(&bar[1], 0u);
+      }
       return;
     }
     ph ^= 1u;
@@ -302,7 +318,10 @@ __global__ void __launch_bounds__(E* N* N)
       const int so = s ^ 1;
       const bool ok = mbar_wait_bounded(&bar[so], (ph >> so) & 1u);
       if (__syncthreads_or(!ok)) {
-        if (t == 0) atomicExch(err, 1);
+        if (t == 0) {  // report; stage so's copy may be in flight (stage s is not reissued yet)
+          atomicExch(err, 1);
+          mbar_wait_drain(&bar[so], (ph >> so) & 1u);
+        }
         return;
       }
       ph ^= 1u << so;
@@ -407,7 +426,11 @@ __global__ void __launch_bounds__(E * 32)
   if (tile < n_tiles) {
     const bool ok = mbar_wait_bounded(&bar[0], ph & 1u);
     if (__syncthreads_or(!ok)) {
-      if (t == 0) atomicExch(err, 1);
+      if (t == 0) {  // report; both stages may still have a copy in flight
+        atomicExch(err, 1);
+        mbar_wait_drain(&bar[0], 0u);
+        if (tile + g < n_tiles) mbar_wait_drain(&bar[1], 0u);
+      }
       return;
     }
     ph ^= 1u;
@@ -481,7 +504,10 @@ __global__ void __launch_bounds__(E * 32)
       }
     }
     if (__syncthreads_or(bad)) {  // stage s and the work arrays are free; any wait timed out?
-      if (t == 0) atomicExch(err, 1);
+      if (t == 0) {  // report; stage s^1's copy may be in flight (parity before the flip above)
+        atomicExch(err, 1);
+        mbar_wait_drain(&bar[s ^ 1], ((ph >> (s ^ 1)) & 1u) ^ 1u);
+      }
       return;
     }
     if (t == 0) fence_proxy_async();
@@ -562,7 +588,11 @@ __global__ void __launch_bounds__(E* N* N* L)
     float energy = 0.f;
     const bool ok = mbar_wait_bounded(&bar[s], (ph >> s) & 1u);
     if (__syncthreads_or(!ok)) {
-      if (threadIdx.x == 0) atomicExch(err, 1);
+      if (threadIdx.x == 0) {  // report; stage s and, if issued, stage s^1 may have copies in flight
+        atomicExch(err, 1);
+        mbar_wait_drain(&bar[s], (ph >> s) & 1u);
+        if (tile + g < n_tiles) mbar_wait_drain(&bar[s ^ 1], (ph >> (s ^ 1)) & 1u);
+      }
       return;
     }
     ph ^= 1u << s;

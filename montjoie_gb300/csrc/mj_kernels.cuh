@@ -463,7 +463,7 @@ __global__ void __launch_bounds__(kStreamThreads, 8)  // 8 CTAs per SM: 32 regis
       // still take part in the diagnostics' finished-CTA count
       if (t == 0) atomicExch(err, 1);
       for (int i = 0, cb = b; i < kStreamNB; i++, cb = (cb + 1 == kStreamNB ? 0 : cb + 1))
-        if (c + i * G < n_chunks) mbar_wait_bounded(&bar[cb], (ph >> cb) & 1u);
+        if (c + i * G < n_chunks) mbar_wait_drain(&bar[cb], (ph >> cb) & 1u);
       break;
     }
     ph ^= 1u << b;
@@ -559,7 +559,7 @@ __global__ void __launch_bounds__(kStreamThreads, 8)
     if (__syncthreads_or(!ok)) {
       if (t == 0) atomicExch(err, 1);
       for (int i = 0, cb = b; i < kStreamNB; i++, cb = (cb + 1 == kStreamNB ? 0 : cb + 1))
-        if (c + i * G < n_chunks) mbar_wait_bounded(&bar[cb], (ph >> cb) & 1u);
+        if (c + i * G < n_chunks) mbar_wait_drain(&bar[cb], (ph >> cb) & 1u);
       return;
     }
     ph ^= 1u << b;

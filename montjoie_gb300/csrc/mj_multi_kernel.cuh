@@ -389,7 +389,11 @@ __global__ void __launch_bounds__(T, MbCfg<T>::min_ctas)
     const bool ok = mbar_wait_bounded(&bar[0], 0u);
     if (prof) wns1 += global_ns() - w0;
     if (__syncthreads_or(!ok)) {
-      if (t == 0) atomicExch(err, 1);
+      if (t == 0) {  // report; both stages may still have a copy in flight
+        atomicExch(err, 1);
+        mbar_wait_drain(&bar[0], 0u);
+        if (nxt.mesh >= 0) mbar_wait_drain(&bar[1], 0u);
+      }
       return;
     }
     ph ^= 1u;
@@ -442,7 +446,10 @@ __global__ void __launch_bounds__(T, MbCfg<T>::min_ctas)
       }
     }
     if (!ok) {
-      if (t == 0) atomicExch(err, 1);
+      if (t == 0) {  // report; the next tile's stage may be in flight (stage s is not reissued yet)
+        atomicExch(err, 1);
+        if (nxt.mesh >= 0) mbar_wait_drain(&bar[s ^ 1], parn);
+      }
       return;
     }
     if (nxt.mesh >= 0) ph ^= 1u << (s ^ 1);
@@ -497,8 +504,8 @@ __global__ void __launch_bounds__(T, MbCfg<T>::min_ctas)
       if (__any_sync(0xffffffffu, !ok)) {
         // report, then wait (bounded) for this warp's copies still in flight
         if (lane == 0) atomicExch(err, 1);
-        mbar_wait_bounded(&wbar[b], (ph2 >> b) & 1u);
-        if (cnxt.mesh >= 0) mbar_wait_bounded(&wbar[b ^ 1], (ph2 >> (b ^ 1)) & 1u);
+        mbar_wait_drain(&wbar[b], (ph2 >> b) & 1u);
+        if (cnxt.mesh >= 0) mbar_wait_drain(&wbar[b ^ 1], (ph2 >> (b ^ 1)) & 1u);
         break;
       }
       ph2 ^= 1u << b;

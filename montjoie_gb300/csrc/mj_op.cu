@@ -13,6 +13,8 @@
 #include "mj_internal.cuh"
 #include "mj_kernels.cuh"
 
+#include <mutex>
+
 namespace mj {
 
 namespace {
@@ -147,6 +149,34 @@ int autotune_k1(mj_op* op) {
 }
 
 }  // namespace
+
+int mj::take_kernel_error(void* dev_flag, cudaStream_t s, const char* what) {
+  int herr = 0;
+  MJ_CUDA(cudaMemcpyAsync(&herr, dev_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MJ_CUDA(cudaStreamSynchronize(s));
+  if (!herr) return MJ_OK;
+  MJ_CUDA(cudaMemsetAsync(dev_flag, 0, sizeof(int), s));
+  MJ_CUDA(cudaStreamSynchronize(s));
+  set_error(std::string(what) + ": a bounded wait of a kernel on its bulk copies timed out (results invalid)");
+  return MJ_ERR_CUDA;
+}
+
+namespace {
+struct WaitLimitRegistry {
+  std::mutex m;
+  std::vector<mj::WaitLimitSetter> setters;
+};
+WaitLimitRegistry& wait_limit_registry() {
+  static WaitLimitRegistry r;
+  return r;
+}
+}  // namespace
+
+void mj::register_wait_limit_setter(mj::WaitLimitSetter f) {
+  WaitLimitRegistry& r = wait_limit_registry();
+  std::lock_guard<std::mutex> lock(r.m);
+  r.setters.push_back(f);
+}
 
 int mj::stream_grid(int n) {
   long g = (n + 255) / 256;
@@ -389,7 +419,22 @@ int mj_op_mltadd(mj_op* op, double alpha, const double* x, double beta, double* 
   if (rc) return rc;
   rc = download_vec(op, op->ybuf.ptr, y, stage, s);
   if (rc) return rc;
-  MJ_CUDA(cudaStreamSynchronize(s));
+  return take_kernel_error(op->err.ptr, s, "mj_op_mltadd");
+}
+
+int mj_debug_set_wait_limits(long long mbar_polls, long long barrier_polls, long long barrier_ns) {
+  mj::WaitLimits w;
+  w.mbar_polls = mbar_polls >= 0 ? (long)std::min<long long>(mbar_polls, mj::kSpinLimit) : mj::kSpinLimit;
+  w.barrier_polls =
+      barrier_polls >= 0 ? (long)std::min<long long>(barrier_polls, mj::kBarrierPolls) : mj::kBarrierPolls;
+  w.barrier_ns = barrier_ns >= 0 ? std::min<unsigned long long>(barrier_ns, mj::kBarrierNs) : mj::kBarrierNs;
+  WaitLimitRegistry& r = wait_limit_registry();
+  std::lock_guard<std::mutex> lock(r.m);
+  for (mj::WaitLimitSetter f : r.setters)
+    if (f(w)) {
+      set_error("mj_debug_set_wait_limits: cudaMemcpyToSymbol failed");
+      return MJ_ERR_CUDA;
+    }
   return MJ_OK;
 }
 
@@ -955,13 +1000,11 @@ int lf_advance_impl(mj_lf* lf, int nsteps, double* norms, double* traces, int st
     for (int k = 0; k < lf->n_rec; k++)
       MJ_CUDA(cudaMemcpyAsync(traces + (size_t)k * stride, td + (size_t)k * cols, sizeof(double) * cols,
                               cudaMemcpyDeviceToHost, s));
-  int flag = 0, kerr = 0;
+  int flag = 0;
   MJ_CUDA(cudaMemcpyAsync(&flag, lf->flag.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
-  MJ_CUDA(cudaMemcpyAsync(&kerr, lf->op->err.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
-  MJ_CUDA(cudaStreamSynchronize(s));
-  if (kerr) {
-    set_error("mj_lf_advance: an element kernel wait timed out");
-    return MJ_ERR_CUDA;
+  {
+    const int rc = take_kernel_error(lf->op->err.ptr, s, "mj_lf_advance");
+    if (rc) return rc;
   }
   if (replayed_prof) {  // per-kernel times of the last replay
     const int base = (int)lf->ev.size() - 3 * kGraphSteps;
@@ -983,6 +1026,19 @@ int lf_advance_impl(mj_lf* lf, int nsteps, double* norms, double* traces, int st
     lf->prof_steps++;
   }
   lf->ev_used = 0;
+  if (norms)  // the first recorded norm that is not finite or above the limit
+    for (int c = 0; c < cols; c++) {
+      if (!std::isfinite(norms[c])) {
+        set_error("mj_lf_advance: non-finite norm at column " + std::to_string(c) + " (unstable run?)");
+        return MJ_ERR_NONFINITE;
+      }
+      if (std::fabs(norms[c]) > lf->norm_max) {
+        // GetNormeSolution's guard (VarInstationary.cxx:2741-2745), which aborts there
+        set_error("mj_lf_advance: norm of the solution " + std::to_string(norms[c]) + " at column " +
+                  std::to_string(c) + " above the limit " + std::to_string(lf->norm_max) + " (unstable run?)");
+        return MJ_ERR_NONFINITE;
+      }
+    }
   if (flag) {
     set_error("mj_lf_advance: non-finite norm (unstable run?)");
     return MJ_ERR_NONFINITE;
@@ -1063,6 +1119,13 @@ int mj_lf_set_scheme(mj_lf* lf, int order, int n_pulse_d2, const double* pulse_d
     const int rc = lf_sorted_sources(lf);
     if (rc) return rc;
   }
+  return MJ_OK;
+}
+
+int mj_lf_set_norm_max(mj_lf* lf, double norm_max) {
+  MJ_CHECK_ARG(lf, "mj_lf_set_norm_max: null integrator");
+  MJ_CHECK_ARG(norm_max > 0.0, "mj_lf_set_norm_max: the limit must be positive");
+  lf->norm_max = norm_max;
   return MJ_OK;
 }
 

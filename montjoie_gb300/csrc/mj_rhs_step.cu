@@ -185,7 +185,11 @@ __global__ void __launch_bounds__(RsPlan<N, E, LB, V>::T, rs_min_ctas(RsPlan<N, 
     const int s = it & 1;
     const bool ok = mbar_wait_bounded(&bar[s], (ph >> s) & 1u);
     if (__syncthreads_or(!ok)) {
-      if (t == 0) atomicExch(err, 1);
+      if (t == 0) {  // report; stage s and, if issued, stage s^1 may have copies in flight
+        atomicExch(err, 1);
+        mbar_wait_drain(&bar[s], (ph >> s) & 1u);
+        if (tile + G < p.n_tiles) mbar_wait_drain(&bar[s ^ 1], (ph >> (s ^ 1)) & 1u);
+      }
       return;
     }
     ph ^= 1u << s;
@@ -301,7 +305,11 @@ __global__ void __launch_bounds__(RsPlan<N, E, LB, V>::T, rs_min_ctas(RsPlan<N, 
     const RsChunk ch = chunks[c];
     const bool ok = mbar_wait_bounded(&bar[2 + b], (ph2 >> b) & 1u);
     if (__syncthreads_or(!ok)) {
-      if (t == 0) atomicExch(err, 1);
+      if (t == 0) {  // report; buffer b and, if issued, buffer b^1 may have copies in flight
+        atomicExch(err, 1);
+        mbar_wait_drain(&bar[2 + b], (ph2 >> b) & 1u);
+        if (c + G < n_chunks) mbar_wait_drain(&bar[2 + (b ^ 1)], (ph2 >> (b ^ 1)) & 1u);
+      }
       return;
     }
     ph2 ^= 1u << b;

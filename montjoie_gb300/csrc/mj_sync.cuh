@@ -7,6 +7,8 @@
 
 #include <cuda_runtime.h>
 
+#include "mj_wait.cuh"
+
 namespace mj {
 
 struct SyncState {
@@ -28,8 +30,10 @@ __device__ __forceinline__ unsigned long long global_ns() {
 
 // Grid-wide barrier of a cooperative launch.  Thread 0 of each CTA arrives on
 // a counter; the last arrival resets it and bumps the generation the others
-// wait on.  The wait gives up after 2 s (or 2^26 polls): the CTA then sets
-// *err = 2 and the barrier reports failure.
+// wait on.  The wait gives up after c_wait.barrier_ns (2 s) or
+// c_wait.barrier_polls (2^26) polls, whichever comes first, unless a test
+// lowered them: the CTA then sets *err = 2 and the barrier reports failure.
+// The host resets the counter and generation after a failure.
 __device__ __forceinline__ bool grid_barrier(SyncState* s, int* err) {
   __shared__ int s_ok;
   __syncthreads();
@@ -44,7 +48,7 @@ __device__ __forceinline__ bool grid_barrier(SyncState* s, int* err) {
     } else {
       const unsigned long long t0 = global_ns();
       for (long it = 0; ld_acquire(&s->gen) == g0; ++it) {
-        if (it > (1L << 26) || global_ns() - t0 > 2000000000ull) {
+        if (it > c_wait.barrier_polls || global_ns() - t0 > c_wait.barrier_ns) {
           ok = 0;
           atomicExch(err, 2);
           break;

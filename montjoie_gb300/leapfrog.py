@@ -96,6 +96,12 @@ class LeapFrogIterator:
         gather kernel followed by the source kernel (bitwise the same states)."""
         _lib.check(_lib.load().mj_lf_set_stream_gather(self._h, int(bool(enable))))
 
+    def SetNormeMaxSolution(self, norm_max: float) -> None:
+        """Divergence guard (NormeMaxSolution, VarInstationary.cxx:362-374,2741-2745):
+        Advance / Run raise MontjoieError (MJ_ERR_NONFINITE) when a recorded
+        norm exceeds norm_max (default 1e30, as in the reference)."""
+        _lib.check(_lib.load().mj_lf_set_norm_max(self._h, float(norm_max)))
+
     def set_graph(self, enable: bool) -> None:
         """Replay captured CUDA graphs of 20 steps when no diagnostics are asked (default on)."""
         _lib.check(_lib.load().mj_lf_set_graph(self._h, int(bool(enable))))

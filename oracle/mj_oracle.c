@@ -458,20 +458,51 @@ void oc_leapfrog(int r, int ne, int ndof, const int* nodle, const int* num, cons
   free(ah);
 }
 
+/* Norm of oc_norm summed per block of 1024 elements (blocks in parallel,
+ * block sums added in block order): the same value whatever the thread count. */
+static double norm_blocked(int ne, int Q, const int* nodle, const double* jw, const double* u) {
+  const int nb = (ne + 1023) / 1024;
+  double* part = (double*)malloc(sizeof(double) * (size_t)nb);
+#pragma omp parallel for schedule(static)
+  for (int b = 0; b < nb; b++) {
+    double acc = 0.0;
+    const size_t o0 = (size_t)b * 1024 * Q;
+    const size_t o1 = (size_t)(b + 1 < nb ? (b + 1) * 1024 : ne) * Q;
+    for (size_t o = o0; o < o1; o++) acc += jw[o] * u[nodle[o]] * u[nodle[o]];
+    part[b] = acc;
+  }
+  double s = 0.0;
+  for (int b = 0; b < nb; b++) s += part[b];
+  free(part);
+  return s;
+}
+
 /* The step loop of oc_leapfrog alone (Advance, ModifiedEquation.cxx:290-345)
  * from a given state (U0, U1) = (u0, u1): nsteps steps, step s taking
- * pulse[s]; no start step and no diagnostics.  The arithmetic of every dof is
- * that of oc_leapfrog, so a trajectory continued in chunks equals one call.
- * The per-dof passes run over the host threads; the element loop is
- * colour-parallel when colours are given.  On return u0 = U^{n+nsteps},
- * u1 = U^{n+nsteps+1}. */
+ * pulse[s]; no start step.  The arithmetic of every dof is that of
+ * oc_leapfrog, so a trajectory continued in chunks equals one call.  When
+ * norms / traces are given, entry s (traces: k*trace_stride + s) receives the
+ * diagnostics of the iterate U0 before step s (the norm summed per block of
+ * elements, see norm_blocked).  The per-dof passes run over the host threads;
+ * the element loop is colour-parallel when colours are given.  On return
+ * u0 = U^{n+nsteps}, u1 = U^{n+nsteps+1}. */
 void oc_leapfrog_advance(int r, int ne, int ndof, const int* nodle, const int* num, const double* G,
                          const double* bh, const double* D, const double* invD, int nsrc, const int* src_idx,
                          const double* src_val, const double* pulse, double dt, int nsteps, double* u0,
-                         double* u1, int ncolors, const int* color_ptr, const int* color_elems) {
+                         double* u1, const double* jw, double* norms, int nrec, const int* rec_idx,
+                         const double* rec_w, double* traces, int trace_stride, int ncolors,
+                         const int* color_ptr, const int* color_elems) {
+  const int Q = (r + 1) * (r + 1) * (r + 1);
   double dt2 = dt * dt;
   double* ah = (double*)malloc(sizeof(double) * (size_t)ndof);
   for (int s = 0; s < nsteps; s++) {
+    if (norms) norms[s] = norm_blocked(ne, Q, nodle, jw, u0);
+    if (traces)
+      for (int k = 0; k < nrec; k++) {
+        double acc = 0.0;
+        for (int t = 0; t < Q; t++) acc += rec_w[(size_t)k * Q + t] * u0[rec_idx[(size_t)k * Q + t]];
+        traces[(size_t)k * trace_stride + s] = acc;
+      }
     oc_stiffness_mltadd(r, ne, ndof, nodle, num, G, bh, -1.0, u1, 0.0, ah, ncolors, color_ptr, color_elems);
     double p = pulse ? pulse[s] : 0.0;
     if (p != 0.0)

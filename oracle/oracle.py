@@ -62,6 +62,7 @@ def lib():
                                   _D, _D, ctypes.c_int, _I, _D, _D, ctypes.c_int, _I, _I]
         L.oc_leapfrog_advance.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _I, _D, _D, _D, _D,
                                           ctypes.c_int, _I, _D, _D, ctypes.c_double, ctypes.c_int, _D, _D,
+                                          _D, _D, ctypes.c_int, _I, _D, _D, ctypes.c_int,
                                           ctypes.c_int, _I, _I]
         L.oc_threads.argtypes = [ctypes.c_int]
         L.oc_threads.restype = ctypes.c_int
@@ -229,21 +230,57 @@ def leapfrog(r, nodle, bh, D, invD, src_idx, src_val, pulse, dt, nsteps, u0, u1=
     return u0, u1, norms, traces
 
 
-def leapfrog_advance(r, nodle, bh, D, invD, src_idx, src_val, pulse, dt, nsteps, u0, u1, colors=None):
+def leapfrog_advance(r, nodle, bh, D, invD, src_idx, src_val, pulse, dt, nsteps, u0, u1, colors=None, jw=None,
+                     rec_idx=None, rec_w=None):
     """Continue the order-2 leap-frog from the state (u0, u1) = (U^n, U^{n+1})
-    in place for nsteps steps, step s taking pulse[s] (no start step, no
-    diagnostics).  Chunks of a trajectory equal one whole run."""
+    in place for nsteps steps, step s taking pulse[s] (no start step).  With
+    jw / receivers, returns the norms (nsteps) and traces (nrec x nsteps) of
+    the iterates before each step, else None.  Chunks of a trajectory equal
+    one whole run."""
     ne, Q = nodle.shape
     assert u0.dtype == np.float64 and u1.dtype == np.float64 and u0.flags.c_contiguous and u1.flags.c_contiguous
     G = grad_matrix(r).ravel().copy()
     num = hex_numbering(r)
     ptr, elems = (None, None) if colors is None else colors
     nc = 0 if colors is None else len(ptr) - 1
+    norms = np.zeros(nsteps) if jw is not None else None
+    nrec = 0 if rec_idx is None else rec_idx.shape[0]
+    traces = np.zeros((nrec, nsteps)) if nrec else None
     lib().oc_leapfrog_advance(r, ne, D.size, _p(i32(nodle), _I), _p(num, _I), _p(G), _p(f64(bh)), _p(f64(D)),
                               _p(f64(invD)), int(len(src_idx)), _p(i32(src_idx), _I), _p(f64(src_val)),
-                              _p(None if pulse is None else f64(pulse)), float(dt), int(nsteps), _p(u0), _p(u1), nc,
+                              _p(None if pulse is None else f64(pulse)), float(dt), int(nsteps), _p(u0), _p(u1),
+                              _p(None if jw is None else f64(jw)), _p(norms), nrec,
+                              _p(None if rec_idx is None else i32(rec_idx), _I),
+                              _p(None if rec_w is None else f64(rec_w)), _p(traces), int(nsteps), nc,
                               _p(None if ptr is None else i32(ptr), _I), _p(None if elems is None else i32(elems), _I))
-    return u0, u1
+    return norms, traces
+
+
+def trajectory(r, nodle, bh, D, invD, src_idx, src_val, pulse, dt, nsteps, u0, jw=None, rec_idx=None, rec_w=None,
+               colors=None, snap_every=None):
+    """The order-2 run of `leapfrog` from (u0, du0 = 0), with the steps done by
+    `leapfrog_advance` (per-dof passes over the host threads): returns
+    {"u": U^nsteps, "snaps": {step: U^step every snap_every steps and at the
+    end}} and, with jw / receivers, "norms" / "traces" of iterates 0..nsteps."""
+    u0, u1, _, _ = leapfrog(r, nodle, bh, D, invD, src_idx, src_val, pulse, dt, 0, u0, colors=colors)
+    norms, traces, snaps, done = [], [], {}, 0
+    every = snap_every or nsteps
+    while done < nsteps:
+        k = min(every, nsteps - done)
+        nr, tr = leapfrog_advance(r, nodle, bh, D, invD, src_idx, src_val, None if pulse is None else pulse[done:],
+                                  dt, k, u0, u1, colors=colors, jw=jw, rec_idx=rec_idx, rec_w=rec_w)
+        if nr is not None:
+            norms.append(nr)
+        if tr is not None:
+            traces.append(tr)
+        done += k
+        snaps[done] = u0.copy()
+    out = {"snaps": snaps, "u": u0}
+    if jw is not None:
+        out["norms"] = np.concatenate(norms + [[norm(nodle, jw, u0)]])
+    if rec_idx is not None:
+        out["traces"] = np.concatenate(traces + [(rec_w * u0[rec_idx]).sum(axis=1)[:, None]], axis=1)
+    return out
 
 
 def threads(n: int = 0) -> int:
