@@ -358,6 +358,33 @@ typedef struct mj_adj mj_adj;
  * segment in the backward sweep.  No reference counterpart: the reference has
  * no time-domain adjoint.  `b` must have receivers. */
 int mj_adj_create(mj_lfb* b, int nsteps, int checkpoint_every, mj_adj** out);
+
+/* The same adjoint with binomial checkpointing (Griewank and Walther's
+ * revolve) under a budget of `snapshots` stored forward states (each a pair
+ * U^k, U^{k+1}; three more states are working buffers): the schedule that
+ * recomputes the fewest forward steps for that budget, planned at creation
+ * by dynamic programming (nsteps^2 x snapshots <= 4e8).  The forward sweep
+ * stores the schedule's first checkpoints as it passes them.  The gradient
+ * is bit for bit that of mj_adj_create: the same adjoint steps run on the
+ * same forward states in the same order.  No reference counterpart. */
+int mj_adj_create_revolve(mj_lfb* b, int nsteps, int snapshots, mj_adj** out);
+
+/* The binomial schedule of mj_adj_create_revolve, host only (no GPU): the
+ * chain of forward states x_k = (U^k, U^{k+1}), k = 1..nsteps-1, visited by
+ * the adjoint in the order x_{nsteps-1}, ..., x_1, with x_1 in snapshot slot
+ * 0.  actions (room for `capacity` triples, may be NULL) receive (kind, k,
+ * slot) with kind 0 = restore slot into the current state x_k, 1 = advance
+ * the current state to x_k, 2 = store the current state x_k in slot, 3 =
+ * visit x_k; *n_actions their count; *backward_steps the forward steps the
+ * whole schedule takes from x_1 (the minimum for that many snapshots). */
+int mj_revolve_schedule(int nsteps, int snapshots, int capacity, int* actions, int* n_actions,
+                        long long* backward_steps);
+
+/* Schedule facts: 1 for binomial checkpointing (else uniform), stored state
+ * pairs, forward steps of one forward + backward pass (nsteps + the steps the
+ * backward sweep recomputes) and the checkpoint memory in bytes (any output
+ * may be NULL). */
+int mj_adj_info(const mj_adj* a, int* revolve, int* snapshots, long long* forward_steps, size_t* device_bytes);
 int mj_adj_destroy(mj_adj* a);
 
 /* Forward run storing checkpoints; traces (host, may be NULL) receive the

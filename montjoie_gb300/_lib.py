@@ -125,6 +125,11 @@ def load(build_if_missing: bool = True):
     L.mj_lfb_info.argtypes = [_VP] + [ctypes.POINTER(ctypes.c_int)] * 5
     L.mj_op_set_element_scale.argtypes = [_VP, _D]
     L.mj_adj_create.argtypes = [_VP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_VP)]
+    L.mj_adj_create_revolve.argtypes = [_VP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_VP)]
+    L.mj_adj_info.argtypes = [_VP, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                              ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_size_t)]
+    L.mj_revolve_schedule.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, ctypes.POINTER(ctypes.c_int),
+                                      ctypes.POINTER(ctypes.c_longlong)]
     L.mj_adj_destroy.argtypes = [_VP]
     L.mj_adj_forward.argtypes = [_VP, _D]
     L.mj_adj_backward.argtypes = [_VP, _D, _D, _D]

@@ -5,8 +5,10 @@ many-source leap-frog.
 - Forward: S sources from rest, traces of K receivers for U^0..U^N.
 - Backward: the exact discrete adjoint of the leap-frog, a time-reversed
   leap-frog with the same symmetric operator.  Its adjoint sources are the
-  trace residuals.  Forward states are checkpointed every ~sqrt(N) steps and
-  replayed segment by segment.
+  trace residuals.  Forward states are checkpointed either every ~sqrt(N)
+  steps and replayed segment by segment, or by a binomial (revolve) schedule
+  under a budget of stored states, which recomputes the fewest forward steps
+  for that budget; both give the same gradient bit for bit.
 - Gradient: dJ/dc_e = -2 dt^2 / c_e sum_n lambda^{n+1}^T A_e U^n.
 All of it runs on the GPU through the C ABI (FP32 states, FP64 gradient
 accumulation).  ``misfit`` exposes J(c) as a ``torch.autograd.Function``.
@@ -27,7 +29,7 @@ class AcousticAdjoint:
 
     def __init__(self, order: int, nodle: np.ndarray, unit_factors: np.ndarray, n_dof: int, mass: np.ndarray,
                  dt: float, nsteps: int, n_runs: int, src_idx, src_rhs, src_val, pulse, rec_idx, rec_w,
-                 checkpoint_every: int = 0):
+                 checkpoint_every: int = 0, snapshots: int | None = None):
         L = _lib.load()
         self.dt, self.N, self.S = float(dt), int(nsteps), int(n_runs)
         self.op = FemMatrixFreeOperator(order, nodle, unit_factors, n_dof, "fp32")
@@ -35,9 +37,21 @@ class AcousticAdjoint:
         self.batch = BatchLeapFrog(self.op, dt, n_runs, mass, None, src_idx, src_rhs, src_val, pulse, rec_idx, rec_w)
         self.n_rec = int(np.asarray(rec_idx).shape[0])
         h = ctypes.c_void_p()
-        _lib.check(L.mj_adj_create(self.batch.handle, self.N, int(checkpoint_every), ctypes.byref(h)))
+        if snapshots:
+            _lib.check(L.mj_adj_create_revolve(self.batch.handle, self.N, int(snapshots), ctypes.byref(h)))
+        else:
+            _lib.check(L.mj_adj_create(self.batch.handle, self.N, int(checkpoint_every), ctypes.byref(h)))
         self._h = h
         self._c = None
+
+    def schedule(self) -> dict:
+        """Checkpoint schedule: revolve or uniform, stored state pairs, forward
+        steps of one forward + backward pass, checkpoint bytes on the device."""
+        rv, sn, fs, nb = ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong(), ctypes.c_size_t()
+        _lib.check(_lib.load().mj_adj_info(self._h, ctypes.byref(rv), ctypes.byref(sn), ctypes.byref(fs),
+                                           ctypes.byref(nb)))
+        return {"revolve": bool(rv.value), "snapshots": sn.value, "forward_steps": fs.value,
+                "checkpoint_bytes": nb.value}
 
     def set_speed(self, c: np.ndarray) -> None:
         c = np.ascontiguousarray(c, dtype=np.float64)
@@ -78,6 +92,55 @@ class AcousticAdjoint:
             self.close()
         except Exception:
             pass
+
+
+class Fp64Misfit:
+    """J(c) of AcousticAdjoint computed by the FP64 plain form: one FP64
+    single-source integrator run per source (mj_lf_run with receivers), on
+    unit-mu factors scaled by c^2 (mj_op_set_element_scale).  Slower than the
+    FP32 batch; it serves as the reference of finite-difference checks of the
+    adjoint gradient."""
+
+    def __init__(self, order, nodle, unit_factors, n_dof, mass, dt, nsteps, n_runs, src_idx, src_rhs, src_val,
+                 pulse, rec_idx, rec_w):
+        from .leapfrog import LeapFrogIterator
+        self.N, self.S, self.n_dof = int(nsteps), int(n_runs), int(n_dof)
+        self.op = FemMatrixFreeOperator(order, nodle, unit_factors, n_dof, "fp64")
+        src_idx, src_rhs, src_val = np.asarray(src_idx), np.asarray(src_rhs), np.asarray(src_val)
+        self.runs = []
+        for s in range(self.S):
+            m = src_rhs == s
+            self.runs.append(LeapFrogIterator(self.op, dt, mass, None, src_idx[m], src_val[m], pulse, None,
+                                              rec_idx, rec_w))
+
+    def traces(self, c: np.ndarray) -> np.ndarray:
+        """(n_rec, S, N+1) traces of U^0..U^N for wave speed c."""
+        c = np.ascontiguousarray(c, dtype=np.float64)
+        self.op.set_element_scale(c * c)
+        out = [lf.Run(np.zeros(self.n_dof), None, self.N)[2] for lf in self.runs]
+        return np.stack(out, axis=1)
+
+    def __call__(self, c: np.ndarray, data: np.ndarray) -> float:
+        res = self.traces(c) - data
+        return 0.5 * float((res * res).sum())
+
+    def close(self) -> None:
+        for lf in self.runs:
+            lf.close()
+        self.runs = []
+        self.op.close()
+
+
+def central_differences(J, c: np.ndarray, elements, rel_step: float = 1e-4) -> np.ndarray:
+    """(J(c + h e_k) - J(c - h e_k)) / 2h, h = rel_step * c_k, for k in elements."""
+    out = []
+    for e in elements:
+        h = rel_step * c[e]
+        cp, cm = c.copy(), c.copy()
+        cp[e] += h
+        cm[e] -= h
+        out.append((J(cp) - J(cm)) / (2.0 * h))
+    return np.array(out)
 
 
 def _torch_function():

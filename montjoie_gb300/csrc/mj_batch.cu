@@ -579,6 +579,15 @@ int mj_lfb_info(const mj_lfb* b, int* n_rhs, int* tile_elems, int* lanes, int* g
 // Discrete adjoint of the many-source leap-frog (no reference counterpart).
 // ---------------------------------------------------------------------------
 
+// One action of a binomial (revolve) checkpoint schedule over the chain of
+// forward states P_k = (U^k, U^{k+1}), k = 1..N-1, whose adjoint visits
+// P_{N-1}, ..., P_1 in that order (adjoint step m = k+1 needs U^k).
+struct RevAction {
+  enum Kind { RESTORE, ADVANCE, STORE, VISIT } kind;
+  int step;  // RESTORE/STORE: the state's k; ADVANCE: target k; VISIT: k
+  int slot;  // RESTORE/STORE: snapshot slot
+};
+
 struct mj_adj {
   mj_lfb* b = nullptr;
   int N = 0, K = 0, J = 0;           // steps, checkpoint interval, checkpoints
@@ -591,6 +600,15 @@ struct mj_adj {
   DevBuf rdof, rptr, rk, rw;         // receiver injection CSR
   int n_rd = 0;
   bool have_forward = false;
+  // binomial (revolve) schedule: snaps snapshot slots of one state pair each
+  bool revolve = false;
+  int snaps = 0;
+  std::vector<RevAction> plan;       // whole schedule; plan[first_visit] is the first VISIT
+  size_t first_visit = 0;
+  std::vector<std::pair<int, int>> sweep_stores;  // (k, slot) stored by the forward sweep
+  DevBuf slots;                      // snaps x 2 states
+  DevBuf work;                       // 3 states: the current pair and the next state
+  long long backward_steps = 0;      // forward steps recomputed by the backward sweep
 };
 
 namespace {
@@ -621,6 +639,94 @@ int adj_forward_step(mj_adj* a, const float* u0, const float* u1, float* out, in
                                                         b->n_pulse, b->ctr.as<int>(), 0, b->m.as<float>(), out, b->S);
     count_launch();
   }
+  MJ_CUDA(cudaGetLastError());
+  return MJ_OK;
+}
+
+// Binomial checkpointing (Griewank and Walther's revolve): the fewest
+// forward steps that visit the chain states x_{b-1}, ..., x_a in reverse
+// order, x_a being held in a snapshot and s more snapshots free, by dynamic
+// programming: cost(l, 0) = l(l-1)/2 (every state recomputed from x_a) and
+// cost(l, s) = min_c [c + cost(l-c, s-1) + cost(c, s)] (advance c steps,
+// store, reverse the right part with one snapshot fewer, then the left part).
+struct RevolvePlanner {
+  int L, S;
+  std::vector<long long> cost;
+  std::vector<int> arg;
+  std::vector<RevAction>* out;
+  std::vector<int> free_slots;
+  RevolvePlanner(int L_, int S_) : L(L_), S(S_), cost((size_t)(L_ + 1) * (S_ + 1)), arg((size_t)(L_ + 1) * (S_ + 1)) {
+    for (int l = 0; l <= L; l++) C(l, 0) = (long long)l * (l - 1) / 2;
+    for (int s = 1; s <= S; s++) {
+      C(0, s) = C(1, s) = 0;
+      for (int l = 2; l <= L; l++) {
+        long long best = -1;
+        int bc = 1;
+        for (int c = 1; c < l; c++) {
+          const long long v = c + C(l - c, s - 1) + C(c, s);
+          if (best < 0 || v < best) { best = v; bc = c; }
+        }
+        C(l, s) = best;
+        A(l, s) = bc;
+      }
+    }
+  }
+  long long& C(int l, int s) { return cost[(size_t)l * (S + 1) + s]; }
+  int& A(int l, int s) { return arg[(size_t)l * (S + 1) + s]; }
+  void reverse(int a, int b, int s, int slot_a) {
+    const int l = b - a;
+    if (l <= 0) return;
+    if (l == 1) {
+      out->push_back({RevAction::RESTORE, a, slot_a});
+      out->push_back({RevAction::VISIT, a, -1});
+      return;
+    }
+    if (s == 0) {
+      for (int k = b - 1; k >= a; k--) {
+        out->push_back({RevAction::RESTORE, a, slot_a});
+        if (k > a) out->push_back({RevAction::ADVANCE, k, -1});
+        out->push_back({RevAction::VISIT, k, -1});
+      }
+      return;
+    }
+    const int c = A(l, s);
+    const int t = free_slots.back();
+    free_slots.pop_back();
+    out->push_back({RevAction::RESTORE, a, slot_a});
+    out->push_back({RevAction::ADVANCE, a + c, -1});
+    out->push_back({RevAction::STORE, a + c, t});
+    reverse(a + c, b, s - 1, t);
+    free_slots.push_back(t);
+    reverse(a, a + c, s, slot_a);
+  }
+};
+
+// Adjoint step m = k + 1 with U^k in `uk`: lambda^m from lambda^{m+1},
+// lambda^{m+2} and the residual of column m, then the gradient term
+// lambda^m^T A_e U^k (one kernel each).
+int adj_visit(mj_adj* a, const float* uk, int m, float*& lam1, float*& lam2, cudaStream_t s) {
+  mj_lfb* b = a->b;
+  mj_op* op = b->op;
+  const int S = b->S, N = a->N;
+  if (b->fused) {  // lambda^m = 2 lambda^{m+1} - lambda^{m+2} + m (-A lambda^{m+1}), one kernel
+    const int rc = lfb_fused_step_on(b, lam2, lam1, lam2, false, s);
+    if (rc) return rc;
+  } else {
+    lfb_k1(b, lam1, s);
+    const long long total = (long long)a->rows;
+    k_gather_leapfrog_rhs<<<grid_for(total), 256, 0, s>>>(b->R.as<float>(), op->ptr.as<int>(), nullptr, 0, lam2,
+                                                          lam1, lam2, b->m.as<float>(), b->n_dof, S);
+    count_launch();
+  }
+  const int inj_blocks = (a->n_rd * S + 127) / 128;
+  k_inject_rhs<<<inj_blocks, 128, 0, s>>>(a->rdof.as<int>(), a->rptr.as<int>(), a->rk.as<int>(), a->rw.as<double>(),
+                                          a->n_rd, a->res.as<double>(), N + 1, m, b->inv_mass64.as<double>(), lam2,
+                                          S);
+  count_launch();
+  std::swap(lam1, lam2);  // lam1 = lambda^m, lam2 = lambda^{m+1}
+  energy_launch(op->n, b->E, b->L, b->grid, uk, op->nodle_e.as<int>(), op->fac_e.as<float>(), b->n_tiles, S,
+                op->err.as<int>(), lam1, a->grad.as<double>(), a->coef.as<double>(), s);
+  count_launch();
   MJ_CUDA(cudaGetLastError());
   return MJ_OK;
 }
@@ -657,20 +763,14 @@ int mj_op_set_element_scale(mj_op* op, const double* scale) {
   return MJ_OK;
 }
 
-int mj_adj_create(mj_lfb* b, int nsteps, int checkpoint_every, mj_adj** out) {
-  MJ_CHECK_ARG(b && out, "mj_adj_create: null argument");
-  *out = nullptr;
-  MJ_CHECK_ARG(nsteps >= 2, "mj_adj_create: at least 2 steps");
-  MJ_CHECK_ARG(b->n_rec > 0, "mj_adj_create: the integrator needs receivers");
-  std::unique_ptr<mj_adj> a(new mj_adj());
-  a->b = b;
-  a->N = nsteps;
-  a->K = checkpoint_every > 0 ? checkpoint_every : std::max(2, (int)std::ceil(std::sqrt((double)nsteps)));
-  MJ_CHECK_ARG(a->K >= 2, "mj_adj_create: checkpoint interval must be >= 2");
-  a->J = (nsteps + a->K - 1) / a->K;
-  a->rows = (size_t)b->n_dof * b->S;
-  MJ_CUDA(a->ckpt.alloc(sizeof(float) * a->rows * 2 * a->J));
-  MJ_CUDA(a->seg.alloc(sizeof(float) * a->rows * a->K));
+}  // extern "C"
+
+namespace {
+
+// Buffers and receiver tables shared by both checkpoint schedules.
+int adj_common_init(mj_adj* a) {
+  mj_lfb* b = a->b;
+  const int nsteps = a->N;
   MJ_CUDA(a->la.alloc(sizeof(float) * a->rows));
   MJ_CUDA(a->lb.alloc(sizeof(float) * a->rows));
   const size_t tr = (size_t)b->n_rec * b->S * (nsteps + 1);
@@ -707,9 +807,109 @@ int mj_adj_create(mj_lfb* b, int nsteps, int checkpoint_every, mj_adj** out) {
   MJ_CUDA(cudaMemcpy(a->rptr.ptr, rptr.data(), sizeof(int) * rptr.size(), cudaMemcpyHostToDevice));
   MJ_CUDA(cudaMemcpy(a->rk.ptr, rk.data(), sizeof(int) * rk.size(), cudaMemcpyHostToDevice));
   MJ_CUDA(cudaMemcpy(a->rw.ptr, rw.data(), sizeof(double) * rw.size(), cudaMemcpyHostToDevice));
-  int rc = energy_prepare(op->n, b->E, b->L);
+  return energy_prepare(op->n, b->E, b->L);
+}
+
+}  // namespace
+
+extern "C" {
+
+int mj_adj_create(mj_lfb* b, int nsteps, int checkpoint_every, mj_adj** out) {
+  MJ_CHECK_ARG(b && out, "mj_adj_create: null argument");
+  *out = nullptr;
+  MJ_CHECK_ARG(nsteps >= 2, "mj_adj_create: at least 2 steps");
+  MJ_CHECK_ARG(b->n_rec > 0, "mj_adj_create: the integrator needs receivers");
+  std::unique_ptr<mj_adj> a(new mj_adj());
+  a->b = b;
+  a->N = nsteps;
+  a->K = checkpoint_every > 0 ? checkpoint_every : std::max(2, (int)std::ceil(std::sqrt((double)nsteps)));
+  MJ_CHECK_ARG(a->K >= 2, "mj_adj_create: checkpoint interval must be >= 2");
+  a->J = (nsteps + a->K - 1) / a->K;
+  a->rows = (size_t)b->n_dof * b->S;
+  MJ_CUDA(a->ckpt.alloc(sizeof(float) * a->rows * 2 * a->J));
+  MJ_CUDA(a->seg.alloc(sizeof(float) * a->rows * a->K));
+  for (int j = 0; j < a->J; j++) {  // replays: U^{n0+2} .. U^{n1-1} of every segment
+    const int n0 = j * a->K, n1 = std::min(n0 + a->K, nsteps);
+    a->backward_steps += std::max(0, n1 - n0 - 2);
+  }
+  const int rc = adj_common_init(a.get());
   if (rc) return rc;
   *out = a.release();
+  return MJ_OK;
+}
+
+int mj_adj_create_revolve(mj_lfb* b, int nsteps, int snapshots, mj_adj** out) {
+  MJ_CHECK_ARG(b && out, "mj_adj_create_revolve: null argument");
+  *out = nullptr;
+  MJ_CHECK_ARG(nsteps >= 2, "mj_adj_create_revolve: at least 2 steps");
+  MJ_CHECK_ARG(snapshots >= 1, "mj_adj_create_revolve: at least one snapshot");
+  MJ_CHECK_ARG(b->n_rec > 0, "mj_adj_create_revolve: the integrator needs receivers");
+  const int L = nsteps - 1;  // chain x_1 .. x_{N-1}
+  const int S = std::min(snapshots, std::max(1, L)) - 1;  // free slots besides the one holding x_1
+  MJ_CHECK_ARG((double)L * L * (S + 1) <= 4e8,
+               "mj_adj_create_revolve: schedule too large to plan (steps^2 x snapshots above 4e8)");
+  std::unique_ptr<mj_adj> a(new mj_adj());
+  a->b = b;
+  a->N = nsteps;
+  a->revolve = true;
+  a->snaps = S + 1;
+  a->rows = (size_t)b->n_dof * b->S;
+  RevolvePlanner pl(L, S);
+  pl.out = &a->plan;
+  for (int t = S; t >= 1; t--) pl.free_slots.push_back(t);
+  pl.reverse(1, nsteps, S, 0);
+  // The forward sweep does the plan's leading restores, advances and stores
+  // itself (it passes every state in order) and ends on x_{N-1}, the first
+  // state visited: the backward sweep starts at the first VISIT.
+  a->sweep_stores.push_back({1, 0});
+  while (a->first_visit < a->plan.size() && a->plan[a->first_visit].kind != RevAction::VISIT) {
+    const RevAction& x = a->plan[a->first_visit++];
+    if (x.kind == RevAction::STORE) a->sweep_stores.push_back({x.step, x.slot});
+  }
+  int cur = -1;
+  for (size_t i = a->first_visit; i < a->plan.size(); i++) {
+    const RevAction& x = a->plan[i];
+    if (x.kind == RevAction::RESTORE) cur = x.step;
+    if (x.kind == RevAction::ADVANCE) { a->backward_steps += x.step - cur; cur = x.step; }
+  }
+  MJ_CUDA(a->slots.alloc(sizeof(float) * a->rows * 2 * a->snaps));
+  MJ_CUDA(a->work.alloc(sizeof(float) * a->rows * 3));
+  const int rc = adj_common_init(a.get());
+  if (rc) return rc;
+  *out = a.release();
+  return MJ_OK;
+}
+
+int mj_revolve_schedule(int nsteps, int snapshots, int capacity, int* actions, int* n_actions,
+                        long long* backward_steps) {
+  MJ_CHECK_ARG(nsteps >= 2 && snapshots >= 1, "mj_revolve_schedule: nsteps >= 2 and snapshots >= 1");
+  const int L = nsteps - 1;
+  const int S = std::min(snapshots, std::max(1, L)) - 1;
+  MJ_CHECK_ARG((double)L * L * (S + 1) <= 4e8, "mj_revolve_schedule: schedule too large to plan");
+  std::vector<RevAction> plan;
+  RevolvePlanner pl(L, S);
+  pl.out = &plan;
+  for (int t = S; t >= 1; t--) pl.free_slots.push_back(t);
+  pl.reverse(1, nsteps, S, 0);
+  if (n_actions) *n_actions = (int)plan.size();
+  if (actions) {
+    MJ_CHECK_ARG(capacity >= (int)plan.size(), "mj_revolve_schedule: action buffer too small");
+    for (size_t i = 0; i < plan.size(); i++) {
+      actions[3 * i] = (int)plan[i].kind;
+      actions[3 * i + 1] = plan[i].step;
+      actions[3 * i + 2] = plan[i].slot;
+    }
+  }
+  if (backward_steps) *backward_steps = pl.C(L, S);
+  return MJ_OK;
+}
+
+int mj_adj_info(const mj_adj* a, int* revolve, int* snapshots, long long* forward_steps, size_t* device_bytes) {
+  MJ_CHECK_ARG(a, "mj_adj_info: null argument");
+  if (revolve) *revolve = a->revolve ? 1 : 0;
+  if (snapshots) *snapshots = a->revolve ? a->snaps : a->J;
+  if (forward_steps) *forward_steps = (long long)a->N + a->backward_steps;
+  if (device_bytes) *device_bytes = a->ckpt.bytes + a->seg.bytes + a->slots.bytes + a->work.bytes;
   return MJ_OK;
 }
 
@@ -725,14 +925,24 @@ int mj_adj_forward(mj_adj* a, double* traces) {
   int rc = mj_lfb_init(b, nullptr, nullptr);  // zero initial conditions
   if (rc) return rc;
   const size_t bytes = sizeof(float) * a->rows;
-  float* ck = a->ckpt.as<float>();
+  float* ck = a->revolve ? a->slots.as<float>() : a->ckpt.as<float>();
+  size_t next_store = 0;  // revolve: the next (k, slot) of sweep_stores (increasing k)
   for (int n = 0; n <= a->N; n++) {
     adj_receivers(a, b->cur(), n, s);
     if (n == a->N) break;
-    if (n % a->K == 0) {
-      float* dst = ck + (size_t)(n / a->K) * 2 * a->rows;
+    int slot = -1;
+    if (!a->revolve && n % a->K == 0) slot = n / a->K;
+    if (a->revolve && next_store < a->sweep_stores.size() && a->sweep_stores[next_store].first == n)
+      slot = a->sweep_stores[next_store++].second;
+    if (slot >= 0) {
+      float* dst = ck + (size_t)slot * 2 * a->rows;
       MJ_CUDA(cudaMemcpyAsync(dst, b->cur(), bytes, cudaMemcpyDeviceToDevice, s));
       MJ_CUDA(cudaMemcpyAsync(dst + a->rows, b->next(), bytes, cudaMemcpyDeviceToDevice, s));
+    }
+    if (a->revolve && n == a->N - 1) {  // x_{N-1}, the first state the backward sweep visits
+      float* w = a->work.as<float>();
+      MJ_CUDA(cudaMemcpyAsync(w, b->cur(), bytes, cudaMemcpyDeviceToDevice, s));
+      MJ_CUDA(cudaMemcpyAsync(w + a->rows, b->next(), bytes, cudaMemcpyDeviceToDevice, s));
     }
     if (b->fused) {
       const int rc = lfb_fused_step(b, s);
@@ -776,10 +986,37 @@ int mj_adj_backward(mj_adj* a, const double* residual, const double* coef, doubl
   MJ_CUDA(cudaMemsetAsync(a->lb.ptr, 0, bytes, s));
   float* lam1 = a->la.as<float>();  // lambda^{m+1}
   float* lam2 = a->lb.as<float>();  // lambda^{m+2}
+  if (a->revolve) {
+    // current pair (U^k, U^{k+1}) in w[0], w[1]; w[2] receives U^{k+2}
+    float* w[3] = {a->work.as<float>(), a->work.as<float>() + rows, a->work.as<float>() + 2 * rows};
+    float* sl = a->slots.as<float>();
+    int cur = a->N - 1;  // the forward sweep left x_{N-1} in w[0], w[1]
+    for (size_t i = a->first_visit; i < a->plan.size(); i++) {
+      const RevAction& x = a->plan[i];
+      if (x.kind == RevAction::RESTORE) {
+        if (cur == x.step) continue;  // already the current pair
+        MJ_CUDA(cudaMemcpyAsync(w[0], sl + (size_t)x.slot * 2 * rows, bytes, cudaMemcpyDeviceToDevice, s));
+        MJ_CUDA(cudaMemcpyAsync(w[1], sl + (size_t)x.slot * 2 * rows + rows, bytes, cudaMemcpyDeviceToDevice, s));
+        cur = x.step;
+      } else if (x.kind == RevAction::ADVANCE) {
+        for (; cur < x.step; cur++) {
+          const int rc = adj_forward_step(a, w[0], w[1], w[2], cur, s);
+          if (rc) return rc;
+          float* t = w[0];
+          w[0] = w[1]; w[1] = w[2]; w[2] = t;
+        }
+      } else if (x.kind == RevAction::STORE) {
+        MJ_CUDA(cudaMemcpyAsync(sl + (size_t)x.slot * 2 * rows, w[0], bytes, cudaMemcpyDeviceToDevice, s));
+        MJ_CUDA(cudaMemcpyAsync(sl + (size_t)x.slot * 2 * rows + rows, w[1], bytes, cudaMemcpyDeviceToDevice, s));
+      } else {  // VISIT x_k: adjoint step m = k + 1 with U^k
+        const int rc = adj_visit(a, w[0], x.step + 1, lam1, lam2, s);
+        if (rc) return rc;
+      }
+    }
+  }
   float* seg = a->seg.as<float>();
   const float* ck = a->ckpt.as<float>();
-  const int inj_blocks = (a->n_rd * S + 127) / 128;
-  for (int j = a->J - 1; j >= 0; j--) {
+  for (int j = a->revolve ? -1 : a->J - 1; j >= 0; j--) {
     const int n0 = j * K, n1 = std::min(n0 + K, N);
     // replay U^{n0} .. U^{n1-1} of the segment from its checkpoint
     MJ_CUDA(cudaMemcpyAsync(seg, ck + (size_t)j * 2 * rows, bytes, cudaMemcpyDeviceToDevice, s));
@@ -792,26 +1029,8 @@ int mj_adj_backward(mj_adj* a, const double* residual, const double* coef, doubl
     }
     // adjoint steps m = n1 .. max(n0+1, 2), then the gradient term with U^{m-1}
     for (int m = n1; m >= std::max(n0 + 1, 2); m--) {
-      if (b->fused) {  // lambda^m = 2 lambda^{m+1} - lambda^{m+2} + m (-A lambda^{m+1}), one kernel
-        const int rc = lfb_fused_step_on(b, lam2, lam1, lam2, false, s);
-        if (rc) return rc;
-      } else {
-        lfb_k1(b, lam1, s);
-        const long long total = (long long)rows;
-        k_gather_leapfrog_rhs<<<grid_for(total), 256, 0, s>>>(b->R.as<float>(), op->ptr.as<int>(), nullptr, 0,
-                                                              lam2, lam1, lam2, b->m.as<float>(), b->n_dof, S);
-        count_launch();
-      }
-      k_inject_rhs<<<inj_blocks, 128, 0, s>>>(a->rdof.as<int>(), a->rptr.as<int>(), a->rk.as<int>(),
-                                              a->rw.as<double>(), a->n_rd, a->res.as<double>(), N + 1, m,
-                                              b->inv_mass64.as<double>(), lam2, S);
-      count_launch();
-      std::swap(lam1, lam2);  // lam1 = lambda^m, lam2 = lambda^{m+1}
-      energy_launch(op->n, b->E, b->L, b->grid, seg + (size_t)(m - 1 - n0) * rows, op->nodle_e.as<int>(),
-                    op->fac_e.as<float>(), b->n_tiles, S, op->err.as<int>(), lam1, a->grad.as<double>(),
-                    a->coef.as<double>(), s);
-      count_launch();
-      MJ_CUDA(cudaGetLastError());
+      const int rc = adj_visit(a, seg + (size_t)(m - 1 - n0) * rows, m, lam1, lam2, s);
+      if (rc) return rc;
     }
   }
   if (b->fused) {
