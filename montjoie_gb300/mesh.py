@@ -1,10 +1,13 @@
-"""Hexahedral meshes of the unit cube, Medit ``.mesh`` output and acoustic decks.
+"""Hexahedral meshes of the unit cube, Medit ``.mesh`` files and acoustic decks.
 
 The reference reads meshes in the Medit ``.mesh`` format (vertices, hexahedra,
-boundary quadrilaterals, each with an integer reference) and data decks of
-``Keyword = values`` lines (``MONTJOIE/src/Instationary/VarInstationary.cxx:79-378``,
-``MONTJOIE/src/Mesh/MeshBase.cxx:424``).  This module writes both, so that one
-seeded mesh drives the reference solver and this library alike.
+boundary quadrilaterals, each with an integer reference;
+``Mesh<Dimension3>::Read``, ``MONTJOIE/src/Mesh/Mesh3D.cxx:1027-1054,3561-3638``)
+and data decks of ``Keyword = values`` lines (``ReadInputFile``,
+``MONTJOIE/src/Output/CommonInputOutput.cxx:1793-1858``; the acoustic keywords
+in ``MONTJOIE/src/Instationary/VarInstationary.cxx:79-378``).  This module
+writes and reads both, so that one seeded mesh and deck drive the reference
+solver and this library alike.
 
 Vertex order of a hexahedron is the reference cube's
 (``MONTJOIE/src/Quadrature/HexahedronQuadrature.cxx:78-86``):
@@ -165,19 +168,23 @@ class AcousticSetup:
     nsteps: int = 200
     print_level: int = 0
     time_order: int = 2   # 2: leap-frog; 4: modified-equation leap-frog (OrderTimeScheme = 4 LEAP_FROG)
+    t_end: float | None = None  # the deck's final time when read from one
 
     @property
     def tf(self) -> float:
+        if self.t_end is not None:
+            return self.t_end
         # ceil((tf - t0)/dt) must give exactly nsteps
         return self.t0 + (self.nsteps - 0.5) * self.dt
 
 
-def write_deck(path: str, mesh_file: str, mesh: HexMesh, setup: AcousticSetup) -> None:
+def write_deck(path: str, mesh_file: str, mesh: HexMesh, setup: AcousticSetup, receivers=None) -> None:
     """Data deck for the reference's ``acous3D`` solver on ``mesh_file``.
 
     ``rho = 1`` and ``mu = c^2`` per medium (``MateriauDielec = ref ISOTROPE rho mu sigma``,
     ``MONTJOIE/src/Elliptic/Helmholtz/VarHelmholtz.cxx:1179-1197``); Neumann on all
-    faces; Gaussian volume source with a Ricker pulse; explicit time step.
+    faces; Gaussian volume source with a Ricker pulse; explicit time step;
+    optional ``SismoPoint`` receivers.
     """
     lines = [
         "TypeElement = HEXAHEDRON_LOBATTO",
@@ -203,5 +210,123 @@ def write_deck(path: str, mesh_file: str, mesh: HexMesh, setup: AcousticSetup) -
         f"OrderTimeScheme = {setup.time_order} LEAP_FROG",
         f"PrintLevel = {setup.print_level}",
     ]
+    for p in receivers if receivers is not None else ():
+        lines.append(f"SismoPoint = {p[0]:.17g} {p[1]:.17g} {p[2]:.17g}")
     with open(path, "w") as f:
         f.write("\n".join(lines) + "\n")
+
+
+def read_medit(path: str) -> HexMesh:
+    """Reads a Medit ``.mesh`` file the way the reference does
+    (Mesh3D.cxx:3561-3638): a line holding a section keyword (``Vertices``,
+    ``Edges``, ``Triangles``, ``Quadrilaterals``, ``Tetrahedra``,
+    ``Hexahedra``) is followed by a count and that many whitespace-separated
+    records, 1-based vertex numbers and an integer reference last; lines
+    starting with ``#`` are comments.  Returns the hexahedra (reference-cube
+    vertex order, as the file gives them) with their references, and the
+    boundary quadrilaterals.  Meshes of other elements (tetrahedra, or
+    degenerate hexahedra: pyramids and wedges) are outside the hexahedral
+    Gauss-Lobatto path and raise ValueError.  ``media_c`` is left empty: the
+    media come from the deck (``MateriauDielec``)."""
+    with open(path) as f:
+        lines = f.read().splitlines()
+    verts = hexes = elem_ref = None
+    quads = []
+    i = 0
+
+    def records(start, count, width):
+        toks = []
+        j = start
+        while len(toks) < count * width:
+            if j >= len(lines):
+                raise ValueError(f"{path}: truncated section")
+            toks.extend(lines[j].split())
+            j += 1
+        return np.array(toks[:count * width], dtype=np.float64).reshape(count, width), j
+
+    while i < len(lines):
+        line = lines[i]
+        i += 1
+        if not line or line[0] == "#":
+            continue
+        key = next((k for k in ("Vertices", "Edges", "Triangles", "Quadrilaterals", "Tetrahedra", "Hexahedra")
+                    if k in line), None)
+        if key is None:
+            continue
+        while not lines[i].split():
+            i += 1
+        count = int(lines[i].split()[0])
+        rest = lines[i].split()[1:]
+        if rest:  # records start on the count's line
+            lines[i] = " ".join(rest)
+        else:
+            i += 1
+        width = {"Vertices": 4, "Edges": 3, "Triangles": 4, "Quadrilaterals": 5, "Tetrahedra": 5, "Hexahedra": 9}[key]
+        rec, i = records(i, count, width)
+        if key == "Vertices":
+            verts = rec[:, :3].copy()
+        elif key == "Quadrilaterals":
+            quads.append(rec[:, :4].astype(np.int64) - 1)
+        elif key == "Tetrahedra" and count:
+            raise ValueError(f"{path}: tetrahedra are not supported (hexahedral Gauss-Lobatto elements only)")
+        elif key == "Hexahedra":
+            h = rec[:, :8].astype(np.int64)
+            if np.any(h[:, 7] == h[:, 6]):
+                raise ValueError(f"{path}: degenerate hexahedra (pyramids or wedges) are not supported")
+            hexes = (h - 1).astype(np.int32)
+            elem_ref = rec[:, 8].astype(np.int32)
+    if verts is None or hexes is None:
+        raise ValueError(f"{path}: no Vertices or no Hexahedra section")
+    if hexes.min() < 0 or hexes.max() >= verts.shape[0]:
+        raise ValueError(f"{path}: vertex number out of range")
+    bfaces = np.concatenate(quads).astype(np.int32) if quads else np.zeros((0, 4), dtype=np.int32)
+    return HexMesh(verts=verts, hexes=hexes, elem_ref=elem_ref, media_c=np.zeros(0), bfaces=bfaces, n=0)
+
+
+def _tokens(line: str):
+    """Words of a deck line: split on blanks and tabs outside parentheses,
+    empty words dropped (StringTokenize, MONTJOIE/src/Share/CommonMontjoie.cxx:70-97)."""
+    out, cur, level = [], "", 0
+    for ch in line:
+        level += (ch == "(") - (ch == ")")
+        if ch in " \t" and level == 0:
+            if cur:
+                out.append(cur)
+            cur = ""
+        else:
+            cur += ch
+    if cur:
+        out.append(cur)
+    return out
+
+
+def read_deck(path: str) -> dict:
+    """Reads a data deck as ``ReadInputFile`` does (CommonInputOutput.cxx:1793-1858):
+    lines starting with ``#`` are comments; a line is split on blanks and tabs,
+    its first word is the keyword and the words after the second (``=``) its
+    parameters (parenthesised groups stay one word); a last word ending in a
+    backslash continues the parameters on
+    the next line; a keyword without parameters is ignored.  Returns
+    ``{keyword: [parameters of each occurrence]}`` in file order (keywords
+    such as ``MateriauDielec`` and ``SismoPoint`` repeat)."""
+    with open(path) as f:
+        lines = f.read().splitlines()
+    out = {}
+    n = 0
+    while n < len(lines):
+        line = lines[n]
+        n += 1
+        if not line or line[0] == "#":
+            continue
+        words = _tokens(line)
+        if len(words) <= 2:
+            continue
+        params = words[2:]
+        while params and params[-1].endswith("\\") and n < len(lines):
+            params[-1] = params[-1][:-1]
+            if not params[-1]:
+                params.pop()
+            params += _tokens(lines[n])
+            n += 1
+        out.setdefault(words[0], []).append(params)
+    return out

@@ -258,17 +258,25 @@ def lumped_mass(order: int, nodle: np.ndarray, jw: np.ndarray, n_dof: int, rho=N
 
 
 class AcousticProblem:
-    """All arrays of one leap-frog run, built by this library from a mesh."""
+    """All arrays of one leap-frog run, built by this library from a mesh.
 
-    def __init__(self, mesh: HexMesh, setup: AcousticSetup, receivers=None, defer_time: bool = False):
+    The medium of element e is rho_e = 1, mu_e = c_e^2 (``mesh.elem_c``)
+    unless per-element ``rho`` and ``mu`` are given (``from_deck`` passes the
+    deck's ``MateriauDielec`` values): mass D_i = sum rho J w
+    (TimeAcoustic.cxx:889-965), factors B = (J w) DF^-1 mu DF^-T
+    (VarHelmholtz.cxx:95-123), norm weight sum J w (VarInstationary.cxx:2696-2745)."""
+
+    def __init__(self, mesh: HexMesh, setup: AcousticSetup, receivers=None, defer_time: bool = False, rho=None,
+                 mu=None):
         r = setup.order
         self.mesh, self.setup, self.order = mesh, setup, r
         self.verts_e = mesh.verts[mesh.hexes]
         self.nodle, self.n_dof = number_mesh(r, mesh.hexes, mesh.verts.shape[0])
-        mu = mesh.elem_c ** 2
+        mu = mesh.elem_c ** 2 if mu is None else np.asarray(mu, dtype=np.float64)
         self.factors, self.jw, self.xq = geometry(r, self.verts_e, mu)
-        self.mass = lumped_mass(r, self.nodle, self.jw, self.n_dof)
-        self.norm_weight = self.mass.copy()  # rho = 1: D_i is also the sum of J w
+        self.norm_weight = lumped_mass(r, self.nodle, self.jw, self.n_dof)
+        self.mass = self.norm_weight.copy() if rho is None else lumped_mass(r, self.nodle, self.jw, self.n_dof, rho)
+        self.norm_max = 1e30
         self.src_idx, self.src_val = gaussian_source(self.nodle, self.jw, self.xq, self.n_dof,
                                                      setup.src_center, setup.src_radius)
         self.pulse = None
@@ -290,14 +298,97 @@ class AcousticProblem:
             self.pulse_d2 = ricker_pulse(self.setup.f0, self.setup.t0, self.setup.dt, self.setup.nsteps, eps_time,
                                          nb_deriv=3)
 
+    @classmethod
+    def from_deck(cls, deck_path: str, defer_time: bool = False) -> "AcousticProblem":
+        """The run a reference data deck describes, read from disk with its
+        Medit mesh (the subset of keywords this path has; anything else in the
+        deck, such as output settings, is ignored):
+
+        - ``TypeElement = HEXAHEDRON_LOBATTO``, ``OrderDiscretization = r``;
+        - ``MeshPath`` (optional) and ``FileMesh``: the Medit ``.mesh`` file;
+        - ``MateriauDielec = ref ISOTROPE rho mu sigma`` per medium reference
+          (VarHelmholtz.cxx:1179-1197; sigma must be 0);
+        - ``ConditionReference = ref NEUMANN`` (the only condition of this path);
+        - ``TypeSource = SRC_VOLUME GAUSSIAN x y z R``, ``Frequency = f0``,
+          ``TemporalSource = RICKER``;
+        - ``TimeStep = dt`` (explicit: ``AUTO`` needs an eigensolver),
+          ``TimeInterval = t0 tf`` (ceil((tf - t0)/dt) steps,
+          ModifiedEquation.cxx:23-24), ``OrderTimeScheme = 2|4 LEAP_FROG``;
+        - ``SismoPoint = x y z`` receivers (GridInterpolation.cxx:836-850);
+        - ``NormeMaxSolution = value`` (VarInstationary.cxx:362-374).
+        Unsupported values raise ValueError naming the keyword."""
+        import os
+
+        from .mesh import read_deck, read_medit
+        kw = read_deck(deck_path)
+
+        def one(key, default=None):
+            if key not in kw:
+                if default is None:
+                    raise ValueError(f"{deck_path}: keyword {key} missing")
+                return default
+            return kw[key][-1]
+
+        if one("TypeElement")[0] != "HEXAHEDRON_LOBATTO":
+            raise ValueError(f"TypeElement {one('TypeElement')[0]}: only HEXAHEDRON_LOBATTO is on this path")
+        order = int(one("OrderDiscretization")[0])
+        mesh_dir = one("MeshPath", [os.path.dirname(os.path.abspath(deck_path))])[0]
+        mesh_file = one("FileMesh")[0]
+        if not os.path.isabs(mesh_file):
+            mesh_file = os.path.join(mesh_dir, mesh_file)
+        if not os.path.exists(mesh_file):  # a deck moved with its mesh
+            mesh_file = os.path.join(os.path.dirname(os.path.abspath(deck_path)), os.path.basename(mesh_file))
+        mesh = read_medit(mesh_file)
+        media = {}
+        for p in kw.get("MateriauDielec", []):
+            if p[1] != "ISOTROPE" or float(p[4] if len(p) > 4 else 0.0) != 0.0:
+                raise ValueError(f"MateriauDielec {' '.join(p)}: only ISOTROPE media without damping")
+            media[int(p[0])] = (float(p[2]), float(p[3]))
+        missing = sorted(set(np.unique(mesh.elem_ref).tolist()) - set(media))
+        if missing:
+            raise ValueError(f"MateriauDielec missing for references {missing}")
+        for p in kw.get("ConditionReference", []):
+            if p[1] != "NEUMANN":
+                raise ValueError(f"ConditionReference {' '.join(p)}: only NEUMANN is on this path")
+        rho = np.array([media[int(r_)][0] for r_ in mesh.elem_ref])
+        mu = np.array([media[int(r_)][1] for r_ in mesh.elem_ref])
+        refs = sorted(media)
+        mesh.media_c = np.array([np.sqrt(media[r_][1] / media[r_][0]) for r_ in refs])
+        mesh.elem_ref = np.searchsorted(refs, mesh.elem_ref).astype(np.int32) + 1
+        src = one("TypeSource")
+        if src[0] != "SRC_VOLUME" or src[1] != "GAUSSIAN":
+            raise ValueError(f"TypeSource {' '.join(src)}: only SRC_VOLUME GAUSSIAN is on this path")
+        if one("TemporalSource", ["RICKER"])[0] != "RICKER":
+            raise ValueError("TemporalSource: only RICKER is on this path")
+        if one("TimeStep")[0] == "AUTO":
+            raise ValueError("TimeStep = AUTO needs an eigensolver; give an explicit time step")
+        dt = float(one("TimeStep")[0])
+        t0, tf = (float(v) for v in one("TimeInterval")[:2])
+        scheme = one("OrderTimeScheme", ["2", "LEAP_FROG"])
+        if len(scheme) > 1 and scheme[1] != "LEAP_FROG":
+            raise ValueError(f"OrderTimeScheme {' '.join(scheme)}: only LEAP_FROG is on this path")
+        setup = AcousticSetup(order=order, f0=float(one("Frequency")[0]),
+                              src_center=tuple(float(v) for v in src[2:5]), src_radius=float(src[5]), dt=dt, t0=t0,
+                              nsteps=int(math.ceil((tf - t0) / dt)), time_order=int(scheme[0]), t_end=tf)
+        receivers = np.array([[float(v) for v in p[:3]] for p in kw.get("SismoPoint", [])]).reshape(-1, 3)
+        pb = cls(mesh, setup, receivers=receivers if len(receivers) else None, defer_time=True,
+                 rho=None if np.all(rho == 1.0) else rho, mu=mu)
+        pb.norm_max = float(one("NormeMaxSolution", ["1e30"])[0])
+        if not defer_time:
+            pb.set_time_step(dt, setup.nsteps)
+        return pb
+
     def operator(self, precision: str = "fp64") -> FemMatrixFreeOperator:
         return FemMatrixFreeOperator(self.order, self.nodle, self.factors, self.n_dof, precision)
 
     def integrator(self, op: FemMatrixFreeOperator, diagnostics: bool = True) -> LeapFrogIterator:
-        return LeapFrogIterator(op, self.setup.dt, self.mass, None, self.src_idx, self.src_val, self.pulse,
-                                self.norm_weight if diagnostics else None,
-                                self.rec_idx if diagnostics else None, self.rec_w if diagnostics else None,
-                                time_order=self.setup.time_order, pulse_d2=self.pulse_d2)
+        lf = LeapFrogIterator(op, self.setup.dt, self.mass, None, self.src_idx, self.src_val, self.pulse,
+                              self.norm_weight if diagnostics else None,
+                              self.rec_idx if diagnostics else None, self.rec_w if diagnostics else None,
+                              time_order=self.setup.time_order, pulse_d2=self.pulse_d2)
+        if self.norm_max != 1e30:
+            lf.SetNormeMaxSolution(self.norm_max)
+        return lf
 
 
 def cfl_time_step(pb: AcousticProblem, safety: float = 0.5, iters: int = 40, seed: int = 0) -> float:

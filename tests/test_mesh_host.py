@@ -89,3 +89,114 @@ def test_medit_and_deck(tmp_path):
     # ceil((tf - t0) / dt) is the step count the reference will run
     t0, tf = (float(x) for x in [ln for ln in deck if ln.startswith("TimeInterval")][0].split()[2:4])
     assert int(np.ceil((tf - t0) / s.dt)) == s.nsteps
+
+
+def test_medit_round_trip(tmp_path):
+    """write_medit then read_medit gives back the mesh exactly (17 digits)."""
+    m = M.perturbed_cube(5, seed=9, amplitude=0.1, kind="sin", c_mode="blocks", c_blocks=2)
+    path = str(tmp_path / "m.mesh")
+    M.write_medit(path, m)
+    r = M.read_medit(path)
+    assert np.array_equal(r.verts, m.verts)
+    assert np.array_equal(r.hexes, m.hexes) and np.array_equal(r.elem_ref, m.elem_ref)
+    assert np.array_equal(r.bfaces, m.bfaces)
+
+
+def test_medit_reader_follows_the_reference_layout(tmp_path):
+    """Comments, blank lines, records spread over lines, sections in any
+    order and unknown sections, as the reference's stream reader accepts."""
+    path = tmp_path / "hand.mesh"
+    path.write_text("""MeshVersionFormatted 2
+# a comment
+Dimension 3
+
+Hexahedra
+1
+1 2 3 4
+5 6 7 8 7
+
+Corners
+0
+
+Vertices
+8
+0 0 0 0   1 0 0 0
+1 1 0 0
+0 1 0 0
+0 0 1 0
+1 0 1 0
+1 1 1 0
+0 1 1 0
+Quadrilaterals
+1
+1 4 3 2 1
+End
+""")
+    r = M.read_medit(str(path))
+    assert r.verts.shape == (8, 3) and np.array_equal(r.verts[6], [1.0, 1.0, 1.0])
+    assert np.array_equal(r.hexes, [[0, 1, 2, 3, 4, 5, 6, 7]]) and np.array_equal(r.elem_ref, [7])
+    assert np.array_equal(r.bfaces, [[0, 3, 2, 1]])
+    tet = tmp_path / "tet.mesh"
+    tet.write_text("Vertices\n4\n0 0 0 0\n1 0 0 0\n0 1 0 0\n0 0 1 0\nTetrahedra\n1\n1 2 3 4 1\n")
+    with pytest.raises(ValueError, match="tetrahedra"):
+        M.read_medit(str(tet))
+
+
+def test_deck_reader_follows_the_reference_rules(tmp_path):
+    """ReadInputFile's rules: # comments, words after '=' as parameters, a
+    trailing backslash continues the line, repeated keywords kept in order,
+    keywords without parameters ignored, blanks inside parentheses kept."""
+    path = tmp_path / "d.ini"
+    path.write_text("""# deck
+TypeElement = HEXAHEDRON_LOBATTO
+OrderDiscretization = 4
+MateriauDielec = 1 ISOTROPE 1.0 4.0 0.0
+MateriauDielec = 2 ISOTROPE 2.0 \\
+   8.0 0.0
+SismoPoint = 0.1 0.2 0.3
+SismoPoint = 0.4 0.5 0.6
+Empty =
+\tTimeStep\t=\t0.001
+Function = (a b) c
+""")
+    d = M.read_deck(str(path))
+    assert d["TypeElement"] == [["HEXAHEDRON_LOBATTO"]] and d["OrderDiscretization"] == [["4"]]
+    assert d["MateriauDielec"] == [["1", "ISOTROPE", "1.0", "4.0", "0.0"], ["2", "ISOTROPE", "2.0", "8.0", "0.0"]]
+    assert d["SismoPoint"] == [["0.1", "0.2", "0.3"], ["0.4", "0.5", "0.6"]]
+    assert "Empty" not in d
+    assert d["TimeStep"] == [["0.001"]]  # empty words (leading tab) are dropped
+    assert d["Function"] == [["(a b)", "c"]]
+
+
+def test_written_deck_reads_back(tmp_path):
+    m = M.perturbed_cube(3, seed=2, amplitude=0.05, kind="random", c_mode="element")
+    s = M.AcousticSetup(order=3, dt=1.25e-3, nsteps=40, src_radius=0.3, time_order=4)
+    rec = np.array([[0.2, 0.3, 0.4], [0.6, 0.5, 0.7]])
+    M.write_medit(str(tmp_path / "c.mesh"), m)
+    M.write_deck(str(tmp_path / "c.ini"), str(tmp_path / "c.mesh"), m, s, receivers=rec)
+    d = M.read_deck(str(tmp_path / "c.ini"))
+    assert float(d["TimeStep"][0][0]) == s.dt
+    assert [float(v) for v in d["TimeInterval"][0]] == [s.t0, s.tf]
+    assert d["OrderTimeScheme"] == [["4", "LEAP_FROG"]]
+    assert np.array_equal(np.array(d["SismoPoint"], dtype=float), rec)
+    mu = np.array([float(p[3]) for p in d["MateriauDielec"]])
+    assert np.array_equal(mu, m.media_c ** 2)
+
+
+@pytest.mark.parametrize("edit,match", [
+    (("TimeStep = ", "TimeStep = AUTO"), "AUTO"),
+    (("ConditionReference = 1 NEUMANN", "ConditionReference = 1 DIRICHLET"), "NEUMANN"),
+    (("TypeElement = HEXAHEDRON_LOBATTO", "TypeElement = TETRAHEDRON_CLASSICAL"), "HEXAHEDRON_LOBATTO"),
+    (("TemporalSource = RICKER", "TemporalSource = GAUSSIAN"), "RICKER"),
+])
+def test_deck_outside_the_path_is_refused(tmp_path, edit, match):
+    """Keywords this path does not cover raise before any GPU work."""
+    from montjoie_gb300.problem import AcousticProblem
+    m = M.perturbed_cube(2, seed=2, amplitude=0.05, kind="random", c_mode="element")
+    M.write_medit(str(tmp_path / "c.mesh"), m)
+    M.write_deck(str(tmp_path / "c.ini"), str(tmp_path / "c.mesh"), m, M.AcousticSetup(order=2))
+    text = (tmp_path / "c.ini").read_text().splitlines()
+    text = [edit[1] if line.startswith(edit[0]) else line for line in text]
+    (tmp_path / "c.ini").write_text("\n".join(text) + "\n")
+    with pytest.raises(ValueError, match=match):
+        AcousticProblem.from_deck(str(tmp_path / "c.ini"))
