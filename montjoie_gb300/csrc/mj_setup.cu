@@ -5,7 +5,6 @@
 #include <array>
 #include <cmath>
 #include <cstring>
-#include <unordered_map>
 #include <vector>
 
 #include "mj_common.cuh"
@@ -177,21 +176,36 @@ using namespace mj;
 
 namespace {
 
-struct EdgeKey {
-  int a, b;
-  bool operator==(const EdgeKey& o) const { return a == o.a && b == o.b; }
-};
-struct EdgeHash {
-  size_t operator()(const EdgeKey& k) const { return std::hash<long long>()(((long long)k.a << 32) ^ (unsigned)k.b); }
-};
-struct FaceKey {
-  int a, b, c;  // origin corner, first-axis neighbour, second-axis neighbour (canonical)
-  bool operator==(const FaceKey& o) const { return a == o.a && b == o.b && c == o.c; }
-};
-struct FaceHash {
-  size_t operator()(const FaceKey& k) const {
-    size_t h = std::hash<long long>()(((long long)k.a << 32) ^ (unsigned)k.b);
-    return h ^ (std::hash<int>()(k.c) * 0x9e3779b97f4a7c15ULL);
+// Open-addressing table from an entity key (an edge: its two vertices; a
+// face: three of its vertices in canonical order) to the offset of the
+// entity's interior node ids in a flat pool (ids -1 until numbered).  A key
+// starts probing at 16 x its smallest vertex, so the entities of nearby
+// vertices (those of consecutive elements) sit together in memory; a regular
+// vertex of a hexahedral mesh is the smallest vertex of at most 6 edges and
+// 12 faces, so its keys mostly fit its own 16 slots.
+struct EntityTable {
+  static constexpr int kPerVertex = 16;
+  std::vector<uint64_t> khi;
+  std::vector<uint32_t> klo;
+  std::vector<int64_t> off;  // -1: empty slot
+  size_t cap = 0;
+  explicit EntityTable(size_t n_vert) : cap(n_vert * kPerVertex + 64) {
+    khi.assign(cap, 0);
+    klo.assign(cap, 0);
+    off.assign(cap, -1);
+  }
+  // Offset of the key's ids; a new key takes `width` fresh ids (-1) at the end of the pool.
+  int64_t find_or_add(uint32_t minv, uint64_t hi, uint32_t lo, std::vector<int>& pool, int width) {
+    for (size_t i = (size_t)minv * kPerVertex;; i = (i + 1 == cap) ? 0 : i + 1) {
+      if (off[i] < 0) {
+        khi[i] = hi;
+        klo[i] = lo;
+        off[i] = (int64_t)pool.size();
+        pool.resize(pool.size() + width, -1);
+        return off[i];
+      }
+      if (khi[i] == hi && klo[i] == lo) return off[i];
+    }
   }
 };
 
@@ -207,11 +221,46 @@ int mj_number_hex_mesh(int order, int n_elt, int n_vert, const int32_t* hexes, i
   for (long long t = 0; t < 8LL * n_elt; t++)
     MJ_CHECK_ARG(hexes[t] >= 0 && hexes[t] < n_vert, "mj_number_hex_mesh: vertex index out of range");
   std::vector<int> vdof(n_vert, -1);
-  // edge / face -> ids of its interior nodes in canonical order (-1: not yet numbered)
-  std::unordered_map<EdgeKey, std::vector<int>, EdgeHash> edges;
-  std::unordered_map<FaceKey, std::vector<int>, FaceHash> faces;
-  edges.reserve((size_t)n_elt * 3 + 16);
-  faces.reserve((size_t)n_elt * 3 + 16);
+  // edge / face -> offset of its interior node ids (canonical order) in a pool
+  EntityTable edges((size_t)n_vert), faces((size_t)n_vert);
+  std::vector<int> epool, fpool;
+  epool.reserve((size_t)n_elt * 3 * std::max(m, 0) + 16);
+  fpool.reserve((size_t)n_elt * 3 * std::max(m * m, 0) + 16);
+  int corner_of[2][2][2];
+  for (int c = 0; c < 8; c++) corner_of[kCorner[c][0]][kCorner[c][1]][kCorner[c][2]] = c;
+  // Every node of the reference element, in the order nodes are numbered:
+  // tensor order (i fastest, then j, then k), so consecutive nodes along x
+  // of an element mostly get consecutive numbers (coalesced gathers).  kind
+  // 0: vertex (corner a); 1: edge along axis a at the other coordinates
+  // (b, c) in {0,1}^2, node l along it; 2: face fixed along axis a on side
+  // b, node (c, l) on its two varying axes; 3: interior.
+  struct NodeDesc { int ql, kind, a, b, c, l; };
+  std::vector<NodeDesc> nodes;
+  for (int k = 0; k < n; k++)
+    for (int j = 0; j < n; j++)
+      for (int i = 0; i < n; i++) {
+        const int cc[3] = {i, j, k};
+        NodeDesc nd{num[(i * n + j) * n + k], 3, 0, 0, 0, 0};
+        int nb = 0;
+        for (int d = 0; d < 3; d++) nb += (cc[d] == 0 || cc[d] == r);
+        if (nb == 3) {
+          nd.kind = 0;
+          nd.a = corner_of[i / r][j / r][k / r];
+        } else if (nb == 2) {
+          int ax = 0;
+          for (int d = 0; d < 3; d++)
+            if (cc[d] != 0 && cc[d] != r) ax = d;
+          const int o1 = ax == 0 ? 1 : 0, o2 = ax == 2 ? 1 : 2;
+          nd = {nd.ql, 1, ax, cc[o1] / r, cc[o2] / r, cc[ax]};
+        } else if (nb == 1) {
+          int fx = 0;
+          for (int d = 0; d < 3; d++)
+            if (cc[d] == 0 || cc[d] == r) fx = d;
+          const int pa = (fx == 0) ? 1 : 0, qa = (fx == 2) ? 1 : 2;
+          nd = {nd.ql, 2, fx, cc[fx] / r, cc[pa], cc[qa]};
+        }
+        nodes.push_back(nd);
+      }
   long long next = 0;
   auto fresh = [&](int& id) {
     if (id < 0) id = (int)next++;
@@ -219,74 +268,77 @@ int mj_number_hex_mesh(int order, int n_elt, int n_vert, const int32_t* hexes, i
   };
   for (int e = 0; e < n_elt; e++) {
     const int32_t* hv = hexes + 8LL * e;
-    auto gvert = [&](int ci, int cj, int ck) {  // global vertex at corner (ci,cj,ck) in {0,1}^3
-      for (int c = 0; c < 8; c++)
-        if (kCorner[c][0] == ci && kCorner[c][1] == cj && kCorner[c][2] == ck) return (int)hv[c];
-      return -1;
-    };
-    int32_t* out = nodle_out + (size_t)e * Q;
-    // Nodes are visited in tensor order (i fastest, then j, then k) and every
-    // dof gets the next number when first met, so consecutive nodes along x
-    // of an element mostly get consecutive numbers (coalesced gathers).
-    for (int k = 0; k < n; k++)
-      for (int j = 0; j < n; j++)
-        for (int i = 0; i < n; i++) {
-          const int ql = num[(i * n + j) * n + k];
-          const int c[3] = {i, j, k};
-          int nb = 0;
-          for (int d = 0; d < 3; d++) nb += (c[d] == 0 || c[d] == r);
-          int dof = -1;
-          if (nb == 3) {
-            dof = fresh(vdof[gvert(i / r, j / r, k / r)]);
-          } else if (nb == 2) {
-            int ax = 0;
-            for (int d = 0; d < 3; d++)
-              if (c[d] != 0 && c[d] != r) ax = d;
-            int lo[3] = {c[0] / r, c[1] / r, c[2] / r}, hi[3] = {c[0] / r, c[1] / r, c[2] / r};
+    auto gvert = [&](int ci, int cj, int ck) { return (int)hv[corner_of[ci][cj][ck]]; };
+    // the element's 12 edges (axis, the other two coordinates) and 6 faces
+    // (fixed axis, side): pool offset and orientation, one lookup each
+    int64_t ebase[3][2][2] = {};
+    bool efwd[3][2][2] = {};
+    int64_t fbase[3][2] = {};
+    int fos[3][2] = {}, foq[3][2] = {};
+    bool fswap[3][2] = {};
+    if (m > 0) {
+      for (int ax = 0; ax < 3; ax++)
+        for (int a = 0; a < 2; a++)
+          for (int b = 0; b < 2; b++) {
+            int lo[3], hi[3];
+            const int o1 = ax == 0 ? 1 : 0, o2 = ax == 2 ? 1 : 2;
+            lo[o1] = hi[o1] = a;
+            lo[o2] = hi[o2] = b;
             lo[ax] = 0;
             hi[ax] = 1;
             const int ga = gvert(lo[0], lo[1], lo[2]), gb = gvert(hi[0], hi[1], hi[2]);
-            const int l = c[ax];
-            std::vector<int>& ids = edges.try_emplace(EdgeKey{std::min(ga, gb), std::max(ga, gb)}, m, -1).first->second;
-            dof = fresh(ids[((ga < gb) ? l : r - l) - 1]);
-          } else if (nb == 1) {
-            int fx = 0;
-            for (int d = 0; d < 3; d++)
-              if (c[d] == 0 || c[d] == r) fx = d;
-            const int pa = (fx == 0) ? 1 : 0, qa = (fx == 2) ? 1 : 2;  // the two varying axes
-            const int side = c[fx] / r;
-            auto corner = [&](int sp, int sq) {
-              int cc[3];
-              cc[fx] = side;
-              cc[pa] = sp;
-              cc[qa] = sq;
-              return gvert(cc[0], cc[1], cc[2]);
-            };
-            const int g[2][2] = {{corner(0, 0), corner(0, 1)}, {corner(1, 0), corner(1, 1)}};
-            // canonical frame: origin = smallest vertex; first axis towards its
-            // smaller neighbour.
-            int os = 0, oq = 0;
-            for (int a = 0; a < 2; a++)
-              for (int b = 0; b < 2; b++)
-                if (g[a][b] < g[os][oq]) { os = a; oq = b; }
-            const int nP = g[1 - os][oq], nQ = g[os][1 - oq];
-            const bool swap = nQ < nP;  // first canonical axis is q
-            int p = c[pa], q = c[qa];
-            if (os) p = r - p;
-            if (oq) q = r - q;
-            const int u = swap ? q : p, v = swap ? p : q;
-            std::vector<int>& ids =
-                faces.try_emplace(FaceKey{g[os][oq], swap ? nQ : nP, swap ? nP : nQ}, m * m, -1).first->second;
-            dof = fresh(ids[(u - 1) * m + (v - 1)]);
-          } else {
-            dof = (int)next++;
+            const uint64_t key = ((uint64_t)(uint32_t)std::min(ga, gb) << 32) | (uint32_t)std::max(ga, gb);
+            ebase[ax][a][b] = edges.find_or_add((uint32_t)std::min(ga, gb), key, 0xFFFFFFFFu, epool, m);
+            efwd[ax][a][b] = ga < gb;
           }
-          if (next > INT32_MAX) {
-            set_error("mj_number_hex_mesh: too many dofs for int32");
-            return MJ_ERR_ARG;
-          }
-          out[ql] = dof;
+      for (int fx = 0; fx < 3; fx++)
+        for (int side = 0; side < 2; side++) {
+          const int pa = (fx == 0) ? 1 : 0, qa = (fx == 2) ? 1 : 2;  // the two varying axes
+          auto corner = [&](int sp, int sq) {
+            int cc[3];
+            cc[fx] = side;
+            cc[pa] = sp;
+            cc[qa] = sq;
+            return gvert(cc[0], cc[1], cc[2]);
+          };
+          const int g[2][2] = {{corner(0, 0), corner(0, 1)}, {corner(1, 0), corner(1, 1)}};
+          // canonical frame: origin = smallest vertex; first axis towards its
+          // smaller neighbour.
+          int os = 0, oq = 0;
+          for (int a = 0; a < 2; a++)
+            for (int b = 0; b < 2; b++)
+              if (g[a][b] < g[os][oq]) { os = a; oq = b; }
+          const int nP = g[1 - os][oq], nQ = g[os][1 - oq];
+          const bool swap = nQ < nP;  // first canonical axis is q
+          const uint64_t hi = ((uint64_t)(uint32_t)g[os][oq] << 32) | (uint32_t)(swap ? nQ : nP);
+          fbase[fx][side] = faces.find_or_add((uint32_t)g[os][oq], hi, (uint32_t)(swap ? nP : nQ), fpool, m * m);
+          fos[fx][side] = os;
+          foq[fx][side] = oq;
+          fswap[fx][side] = swap;
         }
+    }
+    int32_t* out = nodle_out + (size_t)e * Q;
+    for (const NodeDesc& nd : nodes) {
+      int dof;
+      switch (nd.kind) {
+        case 0: dof = fresh(vdof[hv[nd.a]]); break;
+        case 1: dof = fresh(epool[ebase[nd.a][nd.b][nd.c] + (efwd[nd.a][nd.b][nd.c] ? nd.l : r - nd.l) - 1]); break;
+        case 2: {
+          int p = nd.c, q = nd.l;
+          if (fos[nd.a][nd.b]) p = r - p;
+          if (foq[nd.a][nd.b]) q = r - q;
+          const int u = fswap[nd.a][nd.b] ? q : p, v = fswap[nd.a][nd.b] ? p : q;
+          dof = fresh(fpool[fbase[nd.a][nd.b] + (u - 1) * m + (v - 1)]);
+          break;
+        }
+        default: dof = (int)next++;
+      }
+      if (next > INT32_MAX) {
+        set_error("mj_number_hex_mesh: too many dofs for int32");
+        return MJ_ERR_ARG;
+      }
+      out[nd.ql] = dof;
+    }
   }
   *n_dof = (int)next;
   return MJ_OK;
