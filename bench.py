@@ -262,11 +262,11 @@ def leg_sources(args, torch, _lib):
     NE = max(K + 20, args.error_steps)
     pb = build_problem(cells, order, max(K, NE) + 40, mesh=m)
     pos = np.random.default_rng(SEED + 41).uniform(0.1, 0.9, size=(S, 3))
-    idx, rhs, val = [], [], []
-    for s_, c in enumerate(pos):
-        i_, v_ = gaussian_source(pb.nodle, pb.jw, pb.xq, pb.n_dof, c, 2.0 / cells)
-        idx.append(i_); val.append(v_); rhs.append(np.full(i_.size, s_))
     op = pb.operator("fp32")
+    idx, rhs, val = [], [], []
+    for s_, c in enumerate(pos):  # each source assembled on the device
+        i_, v_ = op.gaussian_source(c, 2.0 / cells)
+        idx.append(i_); val.append(v_); rhs.append(np.full(i_.size, s_))
     b = BatchLeapFrog(op, pb.setup.dt, S, pb.mass, None, np.concatenate(idx), np.concatenate(rhs),
                       np.concatenate(val), pb.pulse)
     b.init()

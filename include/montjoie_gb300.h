@@ -75,6 +75,46 @@ typedef struct {
  * problem's Nodle and Glob_matMass_Bh). precision: MJ_FP64 or MJ_FP32. */
 int mj_op_create(const mj_mesh_desc* mesh, const mj_geom_desc* geom, int precision, mj_op** out);
 
+/* Creates the same operator from the mesh's geometry instead of host factors:
+ * the FP64 stiffness factors B = (J w) DF^-1 mu_e DF^-T of straight-sided
+ * (trilinear) hexahedra are computed on the device directly in the
+ * operator's layout (VarGeometryProblem.cxx:685-759, VarHelmholtz.cxx:54-131;
+ * the arithmetic of mj_geometry, so the factors are the same bits), and the
+ * vertices stay on the device for mj_op_lumped_mass and mj_op_gaussian_source.
+ * verts: n_elt x 8 x 3 host (reference-cube vertex order); mu: n_elt host.
+ * MJ_ERR_GEOMETRY when a Jacobian is not positive.  No reference counterpart
+ * as one call: it replaces the setup of Glob_matMass_Bh plus
+ * FemMatrixFreeClass construction. */
+int mj_op_create_geometry(const mj_mesh_desc* mesh, const double* verts, const double* mu, int precision,
+                          mj_op** out);
+
+/* Lumped mass D_i = sum over the points on dof i of rho_e J w, assembled on
+ * the device in element order (the reference's assembly order,
+ * ContinuousMassMatrixAcoustic::Init, TimeAcoustic.cxx:889-965, so the sums
+ * round as the host loop's; the same bits as mj_lumped_mass for rho = 1).
+ * rho: n_elt host values, or NULL (1; then D is also the norm weight sum of
+ * J w of GetNormeSolution).  mass_out: n_dof host.  Operators from
+ * mj_op_create_geometry only (MJ_ERR_STATE otherwise). */
+int mj_op_lumped_mass(mj_op* op, const double* rho, double* mass_out);
+
+/* Gaussian volume source F_i = sum over the points on dof i of J w g(x),
+ * g = beta exp(-alpha r^2) for r = |x - center| < radius, alpha =
+ * -ln(1e-6)/radius^2, beta = sqrt(alpha/pi) (GaussianSource::GetAmplitude,
+ * MONTJOIE/src/Source/SourceSpatiale.cxx:78-90; the right-hand side of
+ * VarInstationary.cxx:620-676), assembled on the device in element order.
+ * Returns the non-zero entries in increasing dof order: *n_out of them, the
+ * first `capacity` in idx_out / val_out (both may be NULL to count only;
+ * MJ_ERR_ARG when they do not fit).  Operators from mj_op_create_geometry. */
+int mj_op_gaussian_source(mj_op* op, const double* center, double radius, int capacity, int32_t* idx_out,
+                          double* val_out, int* n_out);
+
+/* Largest eigenvalue of D^-1 A by power iteration on the device, for the
+ * explicit time step dt = C / sqrt(lambda) (the reference's TimeStep = AUTO
+ * needs ARPACK/SLEPc, EvaluationCflWave.cxx:729-741): x_0 = x0 (host, n_dof),
+ * y = D^-1 A x_k in the operator's precision (as mj_op_mltadd computes it),
+ * lambda = |y| / |x_k|, x_{k+1} = y / |y|, iters times. */
+int mj_op_power_iteration(mj_op* op, const double* inv_mass, const double* x0, int iters, double* lambda_max);
+
 /* Releases every device buffer of the operator. NULL is accepted. */
 int mj_op_destroy(mj_op* op);
 

@@ -92,6 +92,10 @@ def load(build_if_missing: bool = True):
     L.mj_version.restype = ctypes.c_char_p
     L.mj_kernel_launches.restype = ctypes.c_uint64
     L.mj_op_create.argtypes = [ctypes.POINTER(MeshDesc), ctypes.POINTER(GeomDesc), ctypes.c_int, ctypes.POINTER(_VP)]
+    L.mj_op_create_geometry.argtypes = [ctypes.POINTER(MeshDesc), _D, _D, ctypes.c_int, ctypes.POINTER(_VP)]
+    L.mj_op_lumped_mass.argtypes = [_VP, _D, _D]
+    L.mj_op_gaussian_source.argtypes = [_VP, _D, ctypes.c_double, ctypes.c_int, _I, _D, ctypes.POINTER(ctypes.c_int)]
+    L.mj_op_power_iteration.argtypes = [_VP, _D, _D, ctypes.c_int, _D]
     L.mj_op_destroy.argtypes = [_VP]
     L.mj_op_mltadd.argtypes = [_VP, ctypes.c_double, _D, ctypes.c_double, _D]
     L.mj_op_mltadd_device.argtypes = [_VP, ctypes.c_double, _VP, ctypes.c_double, _VP, _VP]

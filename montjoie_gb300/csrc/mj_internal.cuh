@@ -19,6 +19,7 @@ struct mj_op {
   mj::DevBuf nodle_e, fac_e, slot_e, R, ptr;
   mj::DevBuf err;                       // device error flag (bounded-wait timeouts)
   mj::DevBuf fac_orig;                  // factors before mj_op_set_element_scale (kept on first use)
+  mj::DevBuf verts;                     // n_elt x 8 x 3 vertices (operators built from geometry)
   std::vector<int> h_ptr;               // CSR of incidences per dof (host copy)
   double gradphi[mj::kMaxN * mj::kMaxN];
   mj::DevBuf xbuf, ybuf;                // staging for host-vector MltAdd
@@ -27,7 +28,7 @@ struct mj_op {
   std::vector<int> tune_E, tune_vec;
   size_t device_bytes() const {
     return nodle_e.bytes + fac_e.bytes + fac_orig.bytes + slot_e.bytes + R.bytes + ptr.bytes + xbuf.bytes +
-           ybuf.bytes;
+           ybuf.bytes + verts.bytes;
   }
 };
 
@@ -159,6 +160,20 @@ std::vector<RhsVariant> k1_rhs_candidates(int n);
 int k1_set_gmat_rhs(int n, const double* g);
 
 int stream_grid(int n);
+
+// Setup on the device (mj_setup.cu).  geometry_elem_major: FP64 J w, stiffness
+// factors B = (J w) DF^-1 mu DF^-T and positions of every quadrature point of
+// straight-sided hexahedra (verts: device n_elt x 8 x 3, mu: device n_elt) in
+// the element-major layout of the operators (outputs may be NULL; factors in
+// FP64 or FP32); *bad (device) counts non-positive Jacobians.
+// assemble_points: out[d] = sum over the dof's incidences, in element order,
+// of rho_e J w (center == NULL: lumped mass, rho NULL = 1) or of J w g(x)
+// (the Gaussian source of `center` and `radius`); tmp: n_inc doubles.
+int geometry_elem_major(int order, int n_elt, int Qp, const double* verts, const double* mu, double* fac64,
+                        float* fac32, double* jw, double* xq, int* bad, cudaStream_t s);
+int assemble_points(int order, int n_elt, int Qp, const double* jw, const double* xq, const double* rho,
+                    const int* slot, const int* ptr, int n_dof, const double* center, double radius, double* tmp,
+                    double* out, cudaStream_t s);
 
 // One cooperative kernel per step for S right-hand sides (mj_rhs_step.cu):
 // variant choice at creation, and the advance used by mj_lfb_advance.

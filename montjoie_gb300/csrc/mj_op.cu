@@ -46,6 +46,27 @@ __global__ void k_cast_to_f64(const Real* __restrict__ a, double* __restrict__ b
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = double(a[i]);
 }
 
+// Power-iteration helpers (mj_op_power_iteration): per-block sums of squares
+// (the host adds the block sums in block order), y *= w, x = y / s.
+__global__ void k_sumsq_blocks(const double* __restrict__ a, int n, double* __restrict__ partial) {
+  __shared__ double sh[256];
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) acc += a[i] * a[i];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+__global__ void k_mul(double* __restrict__ y, const double* __restrict__ w, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) y[i] *= w[i];
+}
+__global__ void k_div(const double* __restrict__ y, double s, double* __restrict__ x, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] = y[i] / s;
+}
+
 }  // namespace mj
 
 using namespace mj;
@@ -237,49 +258,49 @@ const char* mj_version(void) { return "montjoie_gb300 0.1 (sm_103a)"; }
 
 uint64_t mj_kernel_launches(void) { return launch_counter().load(); }
 
-int mj_op_create(const mj_mesh_desc* mesh, const mj_geom_desc* geom, int precision, mj_op** out) {
-  MJ_CHECK_ARG(mesh && geom && out, "mj_op_create: null argument");
-  *out = nullptr;
+}  // extern "C"
+
+namespace {
+
+// Element-major connectivity, incidence slots and CSR of an operator from the
+// reference-layout Nodle (host), uploaded; the factors are left to the caller
+// (host factors: mj_op_create; device geometry: mj_op_create_geometry).
+int op_layout(mj_op* op, const mj_mesh_desc* mesh, const double* gradphi, int precision, const char* who) {
   const int r = mesh->order;
-  MJ_CHECK_ARG(r >= 1 && r <= kMaxOrder, "mj_op_create: order must be in [1, 8]");
-  MJ_CHECK_ARG(mesh->n_elt > 0 && mesh->n_dof > 0, "mj_op_create: empty mesh");
-  MJ_CHECK_ARG(mesh->nodle && geom->factors, "mj_op_create: nodle and factors are required");
-  MJ_CHECK_ARG(precision == MJ_FP64 || precision == MJ_FP32, "mj_op_create: precision must be MJ_FP64 or MJ_FP32");
+  MJ_CHECK_ARG(r >= 1 && r <= kMaxOrder, std::string(who) + ": order must be in [1, 8]");
+  MJ_CHECK_ARG(mesh->n_elt > 0 && mesh->n_dof > 0, std::string(who) + ": empty mesh");
+  MJ_CHECK_ARG(mesh->nodle, std::string(who) + ": nodle is required");
+  MJ_CHECK_ARG(precision == MJ_FP64 || precision == MJ_FP32, std::string(who) + ": precision must be MJ_FP64 or MJ_FP32");
   const int n = r + 1, Q = n * n * n, NN = n * n;
   const long long total_pts = (long long)mesh->n_elt * Q;
-  MJ_CHECK_ARG(total_pts < (1LL << 31) - 1, "mj_op_create: n_elt*(r+1)^3 exceeds int32 indexing");
-
-  std::unique_ptr<mj_op> op(new mj_op());
+  MJ_CHECK_ARG(total_pts < (1LL << 31) - 1, std::string(who) + ": n_elt*(r+1)^3 exceeds int32 indexing");
   op->order = r; op->n = n; op->Q = Q; op->n_elt = mesh->n_elt; op->n_dof = mesh->n_dof;
   op->precision = precision;
   op->Qp = elem_slots(n);
   op->n_elt_pad = (mesh->n_elt + kElemPad - 1) / kElemPad * kElemPad;
   op->r_len = (size_t)op->n_elt_pad * op->Qp;
-  MJ_CHECK_ARG(op->r_len < (size_t)INT32_MAX - 1, "mj_op_create: mesh too large for int32 incidences");
-
-  // derivative matrix
-  if (geom->gradphi) {
-    for (int a = 0; a < NN; a++) op->gradphi[a] = geom->gradphi[a];
+  MJ_CHECK_ARG(op->r_len < (size_t)INT32_MAX - 1, std::string(who) + ": mesh too large for int32 incidences");
+  if (gradphi) {
+    for (int a = 0; a < NN; a++) op->gradphi[a] = gradphi[a];
   } else {
     double pts[kMaxN], wts[kMaxN];
     gauss_lobatto(r, pts, wts);
     gl_derivative_matrix(r, pts, op->gradphi);
   }
   for (int a = 0; a < NN; a++)
-    MJ_CHECK_ARG(std::isfinite(op->gradphi[a]), "mj_op_create: non-finite derivative matrix");
+    MJ_CHECK_ARG(std::isfinite(op->gradphi[a]), std::string(who) + ": non-finite derivative matrix");
 
   const std::vector<int> num = hex_local_numbering(r);
   const size_t Qp = (size_t)op->Qp;
-  // element-major connectivity and factors, and CSR incidences
   std::vector<int> nodle_e(op->r_len, 0);
   std::vector<int> count(op->n_dof + 1, 0);
   for (long long t = 0; t < total_pts; t++) {
     const int d = mesh->nodle[t];
-    MJ_CHECK_ARG(d >= 0 && d < mesh->n_dof, "mj_op_create: Nodle entry out of [0, n_dof)");
+    MJ_CHECK_ARG(d >= 0 && d < mesh->n_dof, std::string(who) + ": Nodle entry out of [0, n_dof)");
     count[d + 1]++;
   }
   for (int d = 0; d < op->n_dof; d++)
-    MJ_CHECK_ARG(count[d + 1] > 0, "mj_op_create: a dof belongs to no element");
+    MJ_CHECK_ARG(count[d + 1] > 0, std::string(who) + ": a dof belongs to no element");
   op->h_ptr.assign(op->n_dof + 1, 0);
   for (int d = 0; d < op->n_dof; d++) op->h_ptr[d + 1] = op->h_ptr[d] + count[d + 1];
   op->n_inc = (size_t)total_pts;
@@ -287,38 +308,25 @@ int mj_op_create(const mj_mesh_desc* mesh, const mj_geom_desc* geom, int precisi
   // list; padding points write to the spare entry R[n_inc]
   std::vector<int> slot_e(op->r_len, (int)op->n_inc);
   std::vector<int> fill(op->h_ptr.begin(), op->h_ptr.end() - 1);
-
-  const size_t esz = elem_size(precision);
-  std::vector<unsigned char> fac_bytes((size_t)op->n_elt_pad * 6 * Qp * esz, 0);
-  double* fac64 = reinterpret_cast<double*>(fac_bytes.data());
-  float* fac32 = reinterpret_cast<float*>(fac_bytes.data());
+  std::vector<int> ql_of(Q);  // element-major slot p -> local index
+  for (int k = 0; k < n; k++)
+    for (int j = 0; j < n; j++)
+      for (int i = 0; i < n; i++) ql_of[(k * n + j) * n + i] = num[(i * n + j) * n + k];
   // Walk R slots in increasing order so each dof's incidences come out sorted.
-  for (int e = 0; e < mesh->n_elt; e++)
-    for (int k = 0; k < n; k++)
-      for (int j = 0; j < n; j++)
-        for (int i = 0; i < n; i++) {
-          const int p = (k * n + j) * n + i;
-          const size_t rp = (size_t)e * Qp + p;
-          const int ql = num[(i * n + j) * n + k];
-          const size_t src = (size_t)e * Q + ql;
-          const int d = mesh->nodle[src];
-          nodle_e[rp] = d;
-          slot_e[rp] = fill[d]++;
-          for (int c = 0; c < 6; c++) {
-            const double v = geom->factors[src * 6 + c];
-            if (!std::isfinite(v)) {
-              set_error("mj_op_create: non-finite stiffness factor");
-              return MJ_ERR_NONFINITE;
-            }
-            const size_t fp = ((size_t)e * 6 + c) * Qp + p;
-            if (precision == MJ_FP64) fac64[fp] = v;
-            else fac32[fp] = (float)v;
-          }
-        }
-
+  for (int e = 0; e < mesh->n_elt; e++) {
+    const int32_t* row = mesh->nodle + (size_t)e * Q;
+    int* ne = nodle_e.data() + (size_t)e * Qp;
+    int* se = slot_e.data() + (size_t)e * Qp;
+    for (int p = 0; p < Q; p++) {
+      const int d = row[ql_of[p]];
+      ne[p] = d;
+      se[p] = fill[d]++;
+    }
+  }
+  const size_t esz = elem_size(precision);
   MJ_CUDA(op->nodle_e.alloc(sizeof(int) * op->r_len));
   MJ_CUDA(op->slot_e.alloc(sizeof(int) * op->r_len));
-  MJ_CUDA(op->fac_e.alloc(fac_bytes.size()));
+  MJ_CUDA(op->fac_e.alloc((size_t)op->n_elt_pad * 6 * Qp * esz));
   // 3 spare entries past the dummy slot: 16-byte rounded bulk copies of a
   // dof range of R stay inside the buffer
   MJ_CUDA(op->R.alloc(esz * (op->n_inc + 4)));
@@ -326,23 +334,232 @@ int mj_op_create(const mj_mesh_desc* mesh, const mj_geom_desc* geom, int precisi
   MJ_CUDA(cudaMemset(op->ptr.ptr, 0, sizeof(int) * (op->n_dof + 8)));
   MJ_CUDA(cudaMemcpy(op->nodle_e.ptr, nodle_e.data(), sizeof(int) * op->r_len, cudaMemcpyHostToDevice));
   MJ_CUDA(cudaMemcpy(op->slot_e.ptr, slot_e.data(), sizeof(int) * op->r_len, cudaMemcpyHostToDevice));
-  MJ_CUDA(cudaMemcpy(op->fac_e.ptr, fac_bytes.data(), fac_bytes.size(), cudaMemcpyHostToDevice));
   MJ_CUDA(cudaMemcpy(op->ptr.ptr, op->h_ptr.data(), sizeof(int) * (op->n_dof + 1), cudaMemcpyHostToDevice));
   MJ_CUDA(cudaMemset(op->R.ptr, 0, esz * (op->n_inc + 4)));
   MJ_CUDA(op->err.alloc(sizeof(int)));
   MJ_CUDA(cudaMemset(op->err.ptr, 0, sizeof(int)));
-  {
-    // derivative matrix of this order into the constant-memory slot n of
-    // every unit that launches element kernels
-    int rc = precision == MJ_FP64 ? k1_set_gmat_f64(n, op->gradphi) : k1_set_gmat_f32(n, op->gradphi);
-    if (rc) return rc;
+  return MJ_OK;
+}
+
+// Derivative matrix into constant memory and the element-kernel autotuner.
+int op_finish(mj_op* op) {
+  int rc = op->precision == MJ_FP64 ? k1_set_gmat_f64(op->n, op->gradphi) : k1_set_gmat_f32(op->n, op->gradphi);
+  if (rc) return rc;
+  return autotune_k1(op);
+}
+
+}  // namespace
+
+extern "C" {
+
+int mj_op_create(const mj_mesh_desc* mesh, const mj_geom_desc* geom, int precision, mj_op** out) {
+  MJ_CHECK_ARG(mesh && geom && out, "mj_op_create: null argument");
+  *out = nullptr;
+  MJ_CHECK_ARG(geom->factors, "mj_op_create: nodle and factors are required");
+  if (mesh->order >= 1 && mesh->order <= kMaxOrder && mesh->n_elt > 0) {
+    const size_t nf = (size_t)mesh->n_elt * (mesh->order + 1) * (mesh->order + 1) * (mesh->order + 1) * 6;
+    for (size_t t = 0; t < nf; t++)
+      if (!std::isfinite(geom->factors[t])) {
+        set_error("mj_op_create: non-finite stiffness factor");
+        return MJ_ERR_NONFINITE;
+      }
   }
-  {
-    int rc = autotune_k1(op.get());
-    if (rc) return rc;
-  }
+  std::unique_ptr<mj_op> op(new mj_op());
+  int rc = op_layout(op.get(), mesh, geom->gradphi, precision, "mj_op_create");
+  if (rc) return rc;
+  const int n = op->n, Q = op->Q;
+  const size_t Qp = (size_t)op->Qp;
+  const std::vector<int> num = hex_local_numbering(op->order);
+  std::vector<unsigned char> fac_bytes(op->fac_e.bytes, 0);
+  double* fac64 = reinterpret_cast<double*>(fac_bytes.data());
+  float* fac32 = reinterpret_cast<float*>(fac_bytes.data());
+  for (int e = 0; e < op->n_elt; e++)
+    for (int k = 0; k < n; k++)
+      for (int j = 0; j < n; j++)
+        for (int i = 0; i < n; i++) {
+          const int p = (k * n + j) * n + i;
+          const size_t src = (size_t)e * Q + num[(i * n + j) * n + k];
+          for (int c = 0; c < 6; c++) {
+            const double v = geom->factors[src * 6 + c];
+            const size_t fp = ((size_t)e * 6 + c) * Qp + p;
+            if (precision == MJ_FP64) fac64[fp] = v;
+            else fac32[fp] = (float)v;
+          }
+        }
+  MJ_CUDA(cudaMemcpy(op->fac_e.ptr, fac_bytes.data(), fac_bytes.size(), cudaMemcpyHostToDevice));
+  rc = op_finish(op.get());
+  if (rc) return rc;
   *out = op.release();
   return MJ_OK;
+}
+
+int mj_op_create_geometry(const mj_mesh_desc* mesh, const double* verts, const double* mu, int precision,
+                          mj_op** out) {
+  MJ_CHECK_ARG(mesh && verts && mu && out, "mj_op_create_geometry: null argument");
+  *out = nullptr;
+  for (int e = 0; e < mesh->n_elt; e++)
+    MJ_CHECK_ARG(std::isfinite(mu[e]) && mu[e] >= 0, "mj_op_create_geometry: mu must be finite and >= 0");
+  std::unique_ptr<mj_op> op(new mj_op());
+  int rc = op_layout(op.get(), mesh, nullptr, precision, "mj_op_create_geometry");
+  if (rc) return rc;
+  cudaStream_t s = op->stream;
+  MJ_CUDA(op->verts.alloc(sizeof(double) * 24 * op->n_elt));
+  MJ_CUDA(cudaMemcpyAsync(op->verts.ptr, verts, sizeof(double) * 24 * op->n_elt, cudaMemcpyHostToDevice, s));
+  DevBuf dmu, bad;
+  MJ_CUDA(dmu.alloc(sizeof(double) * op->n_elt));
+  MJ_CUDA(cudaMemcpyAsync(dmu.ptr, mu, sizeof(double) * op->n_elt, cudaMemcpyHostToDevice, s));
+  MJ_CUDA(bad.alloc(sizeof(int)));
+  MJ_CUDA(cudaMemsetAsync(bad.ptr, 0, sizeof(int), s));
+  MJ_CUDA(cudaMemsetAsync(op->fac_e.ptr, 0, op->fac_e.bytes, s));  // padding elements and slots
+  rc = geometry_elem_major(op->order, op->n_elt, op->Qp, op->verts.as<double>(), dmu.as<double>(),
+                           precision == MJ_FP64 ? op->fac_e.as<double>() : nullptr,
+                           precision == MJ_FP32 ? op->fac_e.as<float>() : nullptr, nullptr, nullptr, bad.as<int>(), s);
+  if (rc) return rc;
+  int hbad = 0;
+  MJ_CUDA(cudaMemcpyAsync(&hbad, bad.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MJ_CUDA(cudaStreamSynchronize(s));
+  if (hbad) {
+    set_error("mj_op_create_geometry: " + std::to_string(hbad) + " quadrature points with non-positive Jacobian");
+    return MJ_ERR_GEOMETRY;
+  }
+  rc = op_finish(op.get());
+  if (rc) return rc;
+  *out = op.release();
+  return MJ_OK;
+}
+
+namespace {
+// rho J w (center == NULL) or J w g(x) summed per dof on the device, into `d_out` (device, n_dof).
+int op_assemble(mj_op* op, const double* rho, const double* center, double radius, double* d_out, const char* who) {
+  if (!op->verts.ptr) {
+    set_error(std::string(who) + ": the operator was not built from its geometry (mj_op_create_geometry)");
+    return MJ_ERR_STATE;
+  }
+  cudaStream_t s = op->stream;
+  const size_t pts = op->r_len;
+  DevBuf jw, xq, tmp, drho, bad;
+  MJ_CUDA(jw.alloc(sizeof(double) * pts));
+  if (center) MJ_CUDA(xq.alloc(sizeof(double) * 3 * pts));
+  MJ_CUDA(tmp.alloc(sizeof(double) * (op->n_inc + 1)));
+  MJ_CUDA(bad.alloc(sizeof(int)));
+  MJ_CUDA(cudaMemsetAsync(bad.ptr, 0, sizeof(int), s));
+  if (rho) {
+    MJ_CUDA(drho.alloc(sizeof(double) * op->n_elt));
+    MJ_CUDA(cudaMemcpyAsync(drho.ptr, rho, sizeof(double) * op->n_elt, cudaMemcpyHostToDevice, s));
+  }
+  int rc = geometry_elem_major(op->order, op->n_elt, op->Qp, op->verts.as<double>(), nullptr, nullptr, nullptr,
+                               jw.as<double>(), center ? xq.as<double>() : nullptr, bad.as<int>(), s);
+  if (rc) return rc;
+  return assemble_points(op->order, op->n_elt, op->Qp, jw.as<double>(), xq.as<double>(), drho.as<double>(),
+                         op->slot_e.as<int>(), op->ptr.as<int>(), op->n_dof, center, radius, tmp.as<double>(), d_out,
+                         s);
+}
+}  // namespace
+
+int mj_op_lumped_mass(mj_op* op, const double* rho, double* mass_out) {
+  MJ_CHECK_ARG(op && mass_out, "mj_op_lumped_mass: null argument");
+  if (rho)
+    for (int e = 0; e < op->n_elt; e++)
+      MJ_CHECK_ARG(std::isfinite(rho[e]) && rho[e] > 0, "mj_op_lumped_mass: rho must be finite and > 0");
+  DevBuf d;
+  MJ_CUDA(d.alloc(sizeof(double) * op->n_dof));
+  int rc = op_assemble(op, rho, nullptr, 0.0, d.as<double>(), "mj_op_lumped_mass");
+  if (rc) return rc;
+  MJ_CUDA(cudaMemcpyAsync(mass_out, d.ptr, sizeof(double) * op->n_dof, cudaMemcpyDeviceToHost, op->stream));
+  MJ_CUDA(cudaStreamSynchronize(op->stream));
+  return MJ_OK;
+}
+
+int mj_op_gaussian_source(mj_op* op, const double* center, double radius, int capacity, int32_t* idx_out,
+                          double* val_out, int* n_out) {
+  MJ_CHECK_ARG(op && center && n_out, "mj_op_gaussian_source: null argument");
+  MJ_CHECK_ARG(radius > 0 && std::isfinite(radius), "mj_op_gaussian_source: radius must be positive");
+  DevBuf d;
+  MJ_CUDA(d.alloc(sizeof(double) * op->n_dof));
+  int rc = op_assemble(op, nullptr, center, radius, d.as<double>(), "mj_op_gaussian_source");
+  if (rc) return rc;
+  std::vector<double> F(op->n_dof);
+  MJ_CUDA(cudaMemcpyAsync(F.data(), d.ptr, sizeof(double) * op->n_dof, cudaMemcpyDeviceToHost, op->stream));
+  MJ_CUDA(cudaStreamSynchronize(op->stream));
+  int cnt = 0;
+  for (int i = 0; i < op->n_dof; i++)
+    if (F[i] != 0.0) {
+      if (idx_out && val_out && cnt < capacity) {
+        idx_out[cnt] = i;
+        val_out[cnt] = F[i];
+      }
+      cnt++;
+    }
+  *n_out = cnt;
+  if ((idx_out || val_out) && cnt > capacity) {
+    set_error("mj_op_gaussian_source: " + std::to_string(cnt) + " source dofs exceed the capacity " +
+              std::to_string(capacity));
+    return MJ_ERR_ARG;
+  }
+  return MJ_OK;
+}
+
+int mj_op_power_iteration(mj_op* op, const double* inv_mass, const double* x0, int iters, double* lambda_max) {
+  MJ_CHECK_ARG(op && inv_mass && x0 && lambda_max && iters > 0, "mj_op_power_iteration: bad argument");
+  const int n = op->n_dof;
+  cudaStream_t s = op->stream;
+  const size_t esz = elem_size(op->precision);
+  DevBuf x64, y64, w, xo, yo, part;
+  constexpr int kBlocks = 1024;
+  MJ_CUDA(x64.alloc(sizeof(double) * n));
+  MJ_CUDA(y64.alloc(sizeof(double) * n));
+  MJ_CUDA(w.alloc(sizeof(double) * n));
+  MJ_CUDA(part.alloc(sizeof(double) * kBlocks));
+  if (op->precision == MJ_FP32) {
+    MJ_CUDA(xo.alloc(esz * n));
+    MJ_CUDA(yo.alloc(esz * n));
+  }
+  MJ_CUDA(cudaMemcpyAsync(x64.ptr, x0, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  MJ_CUDA(cudaMemcpyAsync(w.ptr, inv_mass, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  std::vector<double> hp(kBlocks);
+  auto norm = [&](const DevBuf& v, double* out) -> int {
+    k_sumsq_blocks<<<kBlocks, 256, 0, s>>>(v.as<double>(), n, part.as<double>());
+    count_launch();
+    MJ_CUDA(cudaMemcpyAsync(hp.data(), part.ptr, sizeof(double) * kBlocks, cudaMemcpyDeviceToHost, s));
+    MJ_CUDA(cudaStreamSynchronize(s));
+    double t = 0.0;
+    for (double v2 : hp) t += v2;
+    *out = std::sqrt(t);
+    return MJ_OK;
+  };
+  const int g = stream_grid(n);
+  double lam = 0.0;
+  for (int it = 0; it < iters; it++) {
+    // y = A x in the operator's precision (the host MltVector's arithmetic), then D^-1 y in FP64
+    if (op->precision == MJ_FP32) {
+      k_cast_from_f64<float><<<g, 256, 0, s>>>(x64.as<double>(), xo.as<float>(), n);
+      count_launch();
+      int rc = mltadd_impl<float>(op, 1.0, xo.ptr, 0.0, yo.ptr, s);
+      if (rc) return rc;
+      k_cast_to_f64<float><<<g, 256, 0, s>>>(yo.as<float>(), y64.as<double>(), n);
+      count_launch();
+    } else {
+      int rc = mltadd_impl<double>(op, 1.0, x64.ptr, 0.0, y64.ptr, s);
+      if (rc) return rc;
+    }
+    k_mul<<<g, 256, 0, s>>>(y64.as<double>(), w.as<double>(), n);
+    count_launch();
+    double ny = 0.0, nx = 0.0;
+    int rc = norm(y64, &ny);
+    if (rc) return rc;
+    rc = norm(x64, &nx);
+    if (rc) return rc;
+    if (!(ny > 0.0) || !(nx > 0.0)) {
+      set_error("mj_op_power_iteration: the iterate vanished or is not finite");
+      return MJ_ERR_NONFINITE;
+    }
+    lam = ny / nx;
+    k_div<<<g, 256, 0, s>>>(y64.as<double>(), ny, x64.as<double>(), n);
+    count_launch();
+  }
+  MJ_CUDA(cudaGetLastError());
+  *lambda_max = lam;
+  return take_kernel_error(op->err.ptr, s, "mj_op_power_iteration");
 }
 
 int mj_op_destroy(mj_op* op) {

@@ -110,15 +110,29 @@ struct GeomParams {
 
 __constant__ unsigned char c_coord[kMaxN * kMaxN * kMaxN * 3];  // local index -> (i,j,k)
 
+// Output layout of k_geometry.  Reference layout (Qp = 0): point t = e*Q + q
+// in local (NumDofs3D) order, factors fac[6t + c], jw[t], xq[3t + d].
+// Element-major layout (Qp > 0, the operators' layout): slot
+// p = (k*n + j)*n + i of element e, factors fac[(e*6 + c)*Qp + p] (FP64, or
+// FP32 in fac32), jw[e*Qp + p], xq[(e*3 + d)*Qp + p].  Both layouts come from
+// the same arithmetic, so every setup path gives the same bits.
+struct GeomOut {
+  int Qp;
+  double* fac;
+  float* fac32;
+  double* jw;
+  double* xq;
+};
+
 __global__ void k_geometry(const double* __restrict__ verts, const double* __restrict__ mu, int n_elt,
-                           const GeomParams P, double* __restrict__ fac, double* __restrict__ jw,
-                           double* __restrict__ xq, int* __restrict__ bad) {
+                           const GeomParams P, const GeomOut out, int* __restrict__ bad) {
   const long long total = (long long)n_elt * P.Q;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x) {
     const int e = (int)(t / P.Q);
     const int q = (int)(t - (long long)e * P.Q);
     const int ci = c_coord[3 * q], cj = c_coord[3 * q + 1], ck = c_coord[3 * q + 2];
+    const long long pe = out.Qp ? (long long)e * out.Qp + (ck * P.n + cj) * P.n + ci : t;  // this point's slot
     const double x = P.pts[ci], y = P.pts[cj], z = P.pts[ck];
     const double w = P.wts[ci] * P.wts[cj] * P.wts[ck];
     const double* v = verts + (size_t)e * 24;
@@ -156,17 +170,69 @@ __global__ void k_geometry(const double* __restrict__ verts, const double* __res
     inv[1][2] = (DF[0][2] * DF[1][0] - DF[0][0] * DF[1][2]) * iJ;
     inv[2][2] = (DF[0][0] * DF[1][1] - DF[0][1] * DF[1][0]) * iJ;
     const double jwq = J * w;
-    if (jw) jw[t] = jwq;
-    if (xq) { xq[3 * t] = F[0]; xq[3 * t + 1] = F[1]; xq[3 * t + 2] = F[2]; }
-    if (fac) {
+    if (out.jw) out.jw[pe] = jwq;
+    if (out.xq)
+#pragma unroll
+      for (int d = 0; d < 3; d++) out.xq[out.Qp ? ((long long)e * 3 + d) * out.Qp + (pe - (long long)e * out.Qp)
+                                                : 3 * t + d] = F[d];
+    if (out.fac || out.fac32) {
       const double s = jwq * mu[e];
       const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
 #pragma unroll
       for (int c = 0; c < 6; c++) {
         const int a = ia[c], b = ib[c];
-        fac[6 * t + c] = s * (inv[a][0] * inv[b][0] + inv[a][1] * inv[b][1] + inv[a][2] * inv[b][2]);
+        const double v = s * (inv[a][0] * inv[b][0] + inv[a][1] * inv[b][1] + inv[a][2] * inv[b][2]);
+        const long long fi = out.Qp ? ((long long)e * 6 + c) * out.Qp + (pe - (long long)e * out.Qp) : 6 * t + c;
+        if (out.fac) out.fac[fi] = v;
+        else out.fac32[fi] = (float)v;
       }
     }
+  }
+}
+
+// Values of the element-major points scattered to their incidence slots:
+// tmp[slot_e[e*Qp + p]] = v(e, p), for the lumped mass (v = rho_e J w) or the
+// Gaussian source (v = J w g(|x - c|) inside the ball, 0 outside, with the
+// distance rounded as sqrt((dx*dx + dy*dy) + dz*dz), no fused multiply-add).
+struct SlotValues {
+  int n_elt, Q, Qp, n;
+  const double* jw;    // element-major J w
+  const double* xq;    // element-major positions (source only)
+  const double* rho;   // per element, or NULL (mass)
+  const int* slot;
+  double cx, cy, cz, R, alpha, beta;
+  int gauss;
+};
+
+__global__ void k_slot_values(const SlotValues a, double* __restrict__ tmp) {
+  const long long total = (long long)a.n_elt * a.Q;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int e = (int)(t / a.Q);
+    const int p = (int)(t - (long long)e * a.Q);  // p < Q: a real point of the element (p = (k*n + j)*n + i)
+    const long long pe = (long long)e * a.Qp + p;
+    double v;
+    if (a.gauss) {
+      const double dx = a.xq[((long long)e * 3) * a.Qp + p] - a.cx;
+      const double dy = a.xq[((long long)e * 3 + 1) * a.Qp + p] - a.cy;
+      const double dz = a.xq[((long long)e * 3 + 2) * a.Qp + p] - a.cz;
+      const double rr = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+      v = rr < a.R ? __dmul_rn(__dmul_rn(a.jw[pe], a.beta), exp(-a.alpha * __dmul_rn(rr, rr))) : 0.0;
+    } else {
+      v = a.rho ? __dmul_rn(a.rho[e], a.jw[pe]) : a.jw[pe];
+    }
+    tmp[a.slot[pe]] = v;
+  }
+}
+
+// out[d] = 0 + tmp[ptr[d]] + tmp[ptr[d] + 1] + ... (the dof's incidences in
+// element order: the order of the reference's element-by-element assembly).
+__global__ void k_csr_sum(const double* __restrict__ tmp, const int* __restrict__ ptr, int n_dof,
+                          double* __restrict__ out) {
+  for (int d = blockIdx.x * blockDim.x + threadIdx.x; d < n_dof; d += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int q = ptr[d]; q < ptr[d + 1]; q++) s = __dadd_rn(s, tmp[q]);
+    out[d] = s;
   }
 }
 
@@ -379,8 +445,8 @@ int mj_geometry(int order, int n_elt, const double* verts, const double* mu, dou
   MJ_CUDA(dbad.alloc(sizeof(int)));
   MJ_CUDA(cudaMemset(dbad.ptr, 0, sizeof(int)));
   const int blocks = (int)std::min<size_t>((pts + 255) / 256, (size_t)sm_count() * 32);
-  k_geometry<<<blocks, 256>>>(dv.as<double>(), dmu.as<double>(), n_elt, P, dfac.as<double>(), djw.as<double>(),
-                              dxq.as<double>(), dbad.as<int>());
+  const GeomOut go{0, dfac.as<double>(), nullptr, djw.as<double>(), dxq.as<double>()};
+  k_geometry<<<blocks, 256>>>(dv.as<double>(), dmu.as<double>(), n_elt, P, go, dbad.as<int>());
   count_launch();
   MJ_CUDA(cudaGetLastError());
   int bad = 0;
@@ -394,6 +460,83 @@ int mj_geometry(int order, int n_elt, const double* verts, const double* mu, dou
   }
   return MJ_OK;
 }
+
+}  // extern "C"
+
+namespace mj {
+
+namespace {
+int geom_params(int order, GeomParams* P) {
+  const int r = order, n = r + 1;
+  *P = GeomParams{};
+  P->n = n;
+  P->Q = n * n * n;
+  gauss_lobatto(r, P->pts, P->wts);
+  const std::vector<int> num = hex_local_numbering(r);
+  std::vector<unsigned char> coord(P->Q * 3);
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++)
+      for (int k = 0; k < n; k++) {
+        const int q = num[(i * n + j) * n + k];
+        coord[3 * q] = (unsigned char)i;
+        coord[3 * q + 1] = (unsigned char)j;
+        coord[3 * q + 2] = (unsigned char)k;
+      }
+  MJ_CUDA(cudaMemcpyToSymbol(c_coord, coord.data(), coord.size()));
+  return MJ_OK;
+}
+}  // namespace
+
+int geometry_elem_major(int order, int n_elt, int Qp, const double* verts, const double* mu, double* fac64,
+                        float* fac32, double* jw, double* xq, int* bad, cudaStream_t s) {
+  GeomParams P;
+  int rc = geom_params(order, &P);
+  if (rc) return rc;
+  const size_t pts = (size_t)n_elt * P.Q;
+  const int blocks = (int)std::min<size_t>((pts + 255) / 256, (size_t)sm_count() * 32);
+  const GeomOut go{Qp, fac64, fac32, jw, xq};
+  k_geometry<<<blocks, 256, 0, s>>>(verts, mu, n_elt, P, go, bad);
+  count_launch();
+  MJ_CUDA(cudaGetLastError());
+  return MJ_OK;
+}
+
+int assemble_points(int order, int n_elt, int Qp, const double* jw, const double* xq, const double* rho,
+                    const int* slot, const int* ptr, int n_dof, const double* center, double radius, double* tmp,
+                    double* out, cudaStream_t s) {
+  SlotValues a{};
+  a.n_elt = n_elt;
+  a.n = order + 1;
+  a.Q = a.n * a.n * a.n;
+  a.Qp = Qp;
+  a.jw = jw;
+  a.xq = xq;
+  a.rho = rho;
+  a.slot = slot;
+  a.gauss = center != nullptr;
+  if (a.gauss) {
+    // g(x) = beta exp(-alpha r^2) for r < R, alpha = -ln(1e-6)/R^2, beta = sqrt(alpha/pi)
+    // (GaussianSource::GetAmplitude, MONTJOIE/src/Source/SourceSpatiale.cxx:78-90)
+    a.cx = center[0];
+    a.cy = center[1];
+    a.cz = center[2];
+    a.R = radius;
+    a.alpha = -std::log(1e-6) / (radius * radius);
+    a.beta = std::sqrt(a.alpha / M_PI);
+  }
+  const size_t pts = (size_t)n_elt * a.Q;
+  const int blocks = (int)std::min<size_t>((pts + 255) / 256, (size_t)sm_count() * 32);
+  k_slot_values<<<blocks, 256, 0, s>>>(a, tmp);
+  k_csr_sum<<<(int)std::min<size_t>(((size_t)n_dof + 255) / 256, (size_t)sm_count() * 32), 256, 0, s>>>(tmp, ptr,
+                                                                                                       n_dof, out);
+  count_launch(2);
+  MJ_CUDA(cudaGetLastError());
+  return MJ_OK;
+}
+
+}  // namespace mj
+
+extern "C" {
 
 int mj_lumped_mass(int order, int n_elt, int n_dof, const int32_t* nodle, const double* jw, const double* rho,
                    double* mass_out) {

@@ -19,27 +19,69 @@ from . import _lib
 
 
 class FemMatrixFreeOperator:
-    def __init__(self, order: int, nodle: np.ndarray, factors: np.ndarray, n_dof: int,
-                 precision: str = "fp64", gradphi: np.ndarray | None = None):
+    def __init__(self, order: int, nodle: np.ndarray, factors: np.ndarray | None, n_dof: int,
+                 precision: str = "fp64", gradphi: np.ndarray | None = None, verts_e: np.ndarray | None = None,
+                 mu: np.ndarray | None = None):
+        """From the reference's arrays (Nodle and the stiffness factors), or,
+        with factors = None, from the geometry (element vertices verts_e,
+        n_elt x 8 x 3, and mu per element): the factors are then computed on
+        the device (mj_op_create_geometry) and the operator can also assemble
+        the lumped mass and Gaussian sources there."""
         L = _lib.load()
         self.order = int(order)
         self.n_dof = int(n_dof)
         nodle = np.ascontiguousarray(nodle, dtype=np.int32)
-        factors = np.ascontiguousarray(factors, dtype=np.float64)
         Q = (self.order + 1) ** 3
         if nodle.ndim != 2 or nodle.shape[1] != Q:
             raise ValueError(f"nodle must be (n_elt, {Q})")
         self.n_elt = nodle.shape[0]
-        if factors.size != self.n_elt * Q * 6:
-            raise ValueError(f"factors must hold n_elt*{Q}*6 values")
         self.precision = {"fp64": _lib.MJ_FP64, "fp32": _lib.MJ_FP32}[precision]
         self.dtype = np.float64 if self.precision == _lib.MJ_FP64 else np.float32
-        g = None if gradphi is None else np.ascontiguousarray(gradphi, dtype=np.float64)
         mesh = _lib.MeshDesc(self.order, self.n_elt, self.n_dof, _lib.iptr(nodle))
-        geom = _lib.GeomDesc(_lib.dptr(factors), _lib.dptr(g))
         handle = ctypes.c_void_p()
-        _lib.check(L.mj_op_create(ctypes.byref(mesh), ctypes.byref(geom), self.precision, ctypes.byref(handle)))
+        if factors is None:
+            verts_e = np.ascontiguousarray(verts_e, dtype=np.float64)
+            mu = np.ascontiguousarray(mu, dtype=np.float64)
+            if verts_e.shape != (self.n_elt, 8, 3) or mu.shape != (self.n_elt,):
+                raise ValueError("from geometry: verts_e (n_elt, 8, 3) and mu (n_elt,) are required")
+            _lib.check(L.mj_op_create_geometry(ctypes.byref(mesh), _lib.dptr(verts_e), _lib.dptr(mu),
+                                               self.precision, ctypes.byref(handle)))
+        else:
+            factors = np.ascontiguousarray(factors, dtype=np.float64)
+            if factors.size != self.n_elt * Q * 6:
+                raise ValueError(f"factors must hold n_elt*{Q}*6 values")
+            g = None if gradphi is None else np.ascontiguousarray(gradphi, dtype=np.float64)
+            geom = _lib.GeomDesc(_lib.dptr(factors), _lib.dptr(g))
+            _lib.check(L.mj_op_create(ctypes.byref(mesh), ctypes.byref(geom), self.precision, ctypes.byref(handle)))
         self._h = handle
+
+    def lumped_mass(self, rho: np.ndarray | None = None) -> np.ndarray:
+        """D_i = sum rho_e J w over the points on dof i, assembled on the device
+        (operators built from geometry)."""
+        out = np.zeros(self.n_dof)
+        r = None if rho is None else np.ascontiguousarray(rho, dtype=np.float64)
+        _lib.check(_lib.load().mj_op_lumped_mass(self._h, _lib.dptr(r), _lib.dptr(out)))
+        return out
+
+    def gaussian_source(self, center, radius: float):
+        """(idx, val): the Gaussian volume source F_i = sum J w g(x), assembled
+        on the device (operators built from geometry)."""
+        L = _lib.load()
+        c = np.ascontiguousarray(center, dtype=np.float64)
+        n = ctypes.c_int()
+        _lib.check(L.mj_op_gaussian_source(self._h, _lib.dptr(c), float(radius), 0, None, None, ctypes.byref(n)))
+        idx, val = np.zeros(n.value, dtype=np.int32), np.zeros(n.value)
+        _lib.check(L.mj_op_gaussian_source(self._h, _lib.dptr(c), float(radius), n.value, _lib.iptr(idx),
+                                           _lib.dptr(val), ctypes.byref(n)))
+        return idx, val
+
+    def power_iteration(self, inv_mass: np.ndarray, x0: np.ndarray, iters: int) -> float:
+        """lambda_max(D^-1 A) by power iteration on the device."""
+        lam = ctypes.c_double()
+        _lib.check(_lib.load().mj_op_power_iteration(self._h, _lib.dptr(np.ascontiguousarray(inv_mass, np.float64)),
+                                                     _lib.dptr(np.ascontiguousarray(x0, np.float64)), int(iters),
+                                                     ctypes.byref(lam)))
+        return float(lam.value)
 
     @property
     def handle(self):

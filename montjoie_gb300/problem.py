@@ -136,21 +136,37 @@ def ricker_pulse(f0: float, t_init: float, dt: float, nsteps: int, eps_time: flo
         tlimit = 2.5 / f0
     pts, _ = gauss_lobatto(24)
     G = derivative_matrix(pts)
-    t0, t1 = t_init, t_init + 0.5 / f0
-    der = None
-    out = np.zeros(nsteps)
+    n = pts.size
+    # the window of every step (a window covers [t0, t1] and moves on when
+    # t > t1 + eps_time), then each window's steps at once
+    times = t_init + np.arange(nsteps) * dt + dt
+    win = np.zeros(nsteps, dtype=np.int64)
+    starts = [(t_init, t_init + 0.5 / f0)]
+    t0, t1 = starts[0]
     for s in range(nsteps):
-        t = t_init + s * dt + dt
+        t = times[s]
         if t > t1 + eps_time and t1 > t0:
             while t > t1 + eps_time:
                 t0, t1 = t1, t1 + (t1 - t0)
-            der = None
-        if der is None:
-            der = ricker_primitive(f0, (1.0 - pts) * t0 + pts * t1)
-            for _ in range(nb_deriv):
-                der = (G.T @ der) * (1.0 / (t1 - t0))
-        p = float(lagrange_values(pts, (t - t0) / (t1 - t0)) @ der)
-        out[s] = 0.0 if t >= tlimit else p
+            starts.append((t0, t1))
+        win[s] = len(starts) - 1
+    out = np.zeros(nsteps)
+    for w, (t0, t1) in enumerate(starts):
+        sel = np.nonzero(win == w)[0]
+        if sel.size == 0:
+            continue
+        der = ricker_primitive(f0, (1.0 - pts) * t0 + pts * t1)
+        for _ in range(nb_deriv):
+            der = (G.T @ der) * (1.0 / (t1 - t0))
+        x = (times[sel] - t0) / (t1 - t0)
+        L = np.ones((sel.size, n))  # Lagrange values, factors multiplied in the order of lagrange_values
+        with np.errstate(divide="ignore", invalid="ignore"):
+            for b in range(n):
+                f = (x[:, None] - pts[b]) / (pts[None, :] - pts[b])
+                f[:, b] = 1.0
+                L *= f
+        out[sel] = L @ der
+    out[times >= tlimit] = 0.0
     return out
 
 
@@ -272,13 +288,18 @@ class AcousticProblem:
         self.mesh, self.setup, self.order = mesh, setup, r
         self.verts_e = mesh.verts[mesh.hexes]
         self.nodle, self.n_dof = number_mesh(r, mesh.hexes, mesh.verts.shape[0])
-        mu = mesh.elem_c ** 2 if mu is None else np.asarray(mu, dtype=np.float64)
-        self.factors, self.jw, self.xq = geometry(r, self.verts_e, mu)
-        self.norm_weight = lumped_mass(r, self.nodle, self.jw, self.n_dof)
-        self.mass = self.norm_weight.copy() if rho is None else lumped_mass(r, self.nodle, self.jw, self.n_dof, rho)
+        self.mu = mesh.elem_c ** 2 if mu is None else np.asarray(mu, dtype=np.float64)
+        self.rho = None if rho is None else np.asarray(rho, dtype=np.float64)
+        # On the device: the FP32 operator's factors from the geometry, then the
+        # lumped mass, the norm weights and the Gaussian source, each assembled
+        # in element order (the host arrays of the reference layout, factors,
+        # jw and xq, are computed only when asked for)
+        self._op = self._make_operator("fp32")
+        self.norm_weight = self._op.lumped_mass(None)  # sum of J w (GetNormeSolution)
+        self.mass = self.norm_weight.copy() if self.rho is None else self._op.lumped_mass(self.rho)
         self.norm_max = 1e30
-        self.src_idx, self.src_val = gaussian_source(self.nodle, self.jw, self.xq, self.n_dof,
-                                                     setup.src_center, setup.src_radius)
+        self.src_idx, self.src_val = self._op.gaussian_source(setup.src_center, setup.src_radius)
+        self._geom = None
         self.pulse = None
         if not defer_time:
             self.set_time_step(setup.dt, setup.nsteps)
@@ -378,8 +399,42 @@ class AcousticProblem:
             pb.set_time_step(dt, setup.nsteps)
         return pb
 
+    def _make_operator(self, precision: str) -> FemMatrixFreeOperator:
+        return FemMatrixFreeOperator(self.order, self.nodle, None, self.n_dof, precision, verts_e=self.verts_e,
+                                     mu=self.mu)
+
+    def _geometry(self):
+        if self._geom is None:
+            self._geom = geometry(self.order, self.verts_e, self.mu)
+        return self._geom
+
+    @property
+    def factors(self) -> np.ndarray:
+        """Stiffness factors in the reference layout (n_elt, Q, 6), host (computed on first use)."""
+        return self._geometry()[0]
+
+    @property
+    def jw(self) -> np.ndarray:
+        """J w of every quadrature point (n_elt, Q), host (computed on first use)."""
+        return self._geometry()[1]
+
+    @property
+    def xq(self) -> np.ndarray:
+        """Physical quadrature points (n_elt, Q, 3), host (computed on first use)."""
+        return self._geometry()[2]
+
     def operator(self, precision: str = "fp64") -> FemMatrixFreeOperator:
-        return FemMatrixFreeOperator(self.order, self.nodle, self.factors, self.n_dof, precision)
+        """A new operator owned by the caller; the first FP32 one is the
+        operator the set-up already built."""
+        if precision == "fp32" and self._op is not None:
+            op, self._op = self._op, None
+            return op
+        return self._make_operator(precision)
+
+    def close(self) -> None:
+        if getattr(self, "_op", None) is not None:
+            self._op.close()
+            self._op = None
 
     def integrator(self, op: FemMatrixFreeOperator, diagnostics: bool = True) -> LeapFrogIterator:
         lf = LeapFrogIterator(op, self.setup.dt, self.mass, None, self.src_idx, self.src_val, self.pulse,
@@ -394,20 +449,12 @@ class AcousticProblem:
 def cfl_time_step(pb: AcousticProblem, safety: float = 0.5, iters: int = 40, seed: int = 0) -> float:
     """dt = safety * C / sqrt(lambda_max(D^-1 A)) with the scheme's CFL
     constant C = 2 (order 2) or 2 sqrt(3) (order 4) (ModifiedEquation.cxx:217-225);
-    lambda_max by power iteration with the GPU operator (the reference needs
-    ARPACK/SLEPc for TimeStep = AUTO)."""
-    op = pb.operator("fp32")
-    rng = np.random.default_rng(seed)
-    x = rng.uniform(-1.0, 1.0, pb.n_dof)
-    y = np.zeros(pb.n_dof)
-    inv = 1.0 / pb.mass
-    lam = 0.0
-    for _ in range(iters):
-        op.MltVector(x, y)
-        y *= inv
-        nrm = np.linalg.norm(y)
-        lam = nrm / np.linalg.norm(x)
-        x = y / nrm
-    op.close()
+    lambda_max by power iteration on the device with the FP32 operator (the
+    reference needs ARPACK/SLEPc for TimeStep = AUTO)."""
+    op = pb._op if pb._op is not None else pb.operator("fp32")
+    x0 = np.random.default_rng(seed).uniform(-1.0, 1.0, pb.n_dof)
+    lam = op.power_iteration(1.0 / pb.mass, x0, iters)
+    if op is not pb._op:
+        op.close()
     c = 2.0 if pb.setup.time_order == 2 else 2.0 * math.sqrt(3.0)
     return safety * c / math.sqrt(lam * 1.05)
