@@ -351,6 +351,7 @@ def leg_meshes(args, torch, _lib):
     launches = _lib.kernel_launches() - l0
     info = mb.info()
     info["tuning"] = mb.tuning()
+    info["grouping"] = mb.grouping()
     u_batch = [x[4].GetIterate() for x in runs]
     mb.profile(True)  # phase times of one extra step (per-CTA time stamps)
     mb.advance(1)

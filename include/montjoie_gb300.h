@@ -153,17 +153,22 @@ int mj_op_set_variant(mj_op* op, int tile_elems, int vector_lines);
 uint64_t mj_kernel_launches(void);
 
 /* Test hook, no reference counterpart.  Every wait of the library's kernels
- * is bounded: on a bulk copy (mbarrier), mbar_polls polls (default 2^22); on
- * the other CTAs of a cooperative launch (grid barrier), barrier_polls polls
- * (default 2^26) or barrier_ns nanoseconds (default 2 s), whichever comes
- * first.  A wait that runs out makes the kernel report through its error flag
- * after letting its own copies in flight land, and the entry point returns
- * MJ_ERR_CUDA (single integrator, operator, many sources: element waits) or
- * MJ_ERR_STATE (cooperative steps) with a message; the state is then invalid
- * but the next call starts clean.  This call lowers the limits so a test can
- * make waits run out (0: give up at the first poll); values above the
- * defaults are clamped to them and negative values restore them.
- * Process-wide. */
+ * is bounded: on a bulk copy (mbarrier), 2^22 polls; on the other CTAs of a
+ * cooperative launch (grid barrier), barrier_polls polls (default 2^26) or
+ * barrier_ns nanoseconds (default 2 s), whichever comes first.  A wait that
+ * runs out makes the kernel report through its error flag after letting its
+ * own copies in flight land, and the entry point returns MJ_ERR_CUDA (element
+ * kernels) or MJ_ERR_STATE (cooperative steps) with a message; the state is
+ * then invalid but the next call starts clean.  This call lets a test make
+ * waits run out: mbar_polls = 0 switches two element-kernel variants (FP32
+ * one element per warp, order 4, 2 elements per CTA; FP64 compact, order 4,
+ * 4 elements per CTA; see mj_op_set_variant) to instances compiled with a
+ * bulk-copy wait limit of 0 (the bound is a compile-time constant in the
+ * kernels), any other value switches them back; barrier_polls and
+ * barrier_ns lower the grid barrier's limits (0: give up after the first
+ * poll; values above the defaults are clamped to them; negative values
+ * restore them).  Process-wide; captured CUDA graphs keep the kernels they
+ * were captured with. */
 int mj_debug_set_wait_limits(long long mbar_polls, long long barrier_polls, long long barrier_ns);
 
 /* ---- leap-frog time loop -------------------------------------------- */
@@ -377,9 +382,20 @@ int mj_mb_phase_ms(const mj_mb* mb, double* out);
  * may be NULL).  At most 48 runs per batch. */
 int mj_mb_tuning(const mj_mb* mb, int* threads, double* candidate_ms);
 
-/* Forces the launch configuration (threads = 128 or 256), or 0 to time both
- * again at the next advance. */
+/* Forces the launch configuration (threads = 128 or 256: one kernel of all
+ * orders per step; -1: grouped by order, below), or 0 to time them again at
+ * the next advance. */
 int mj_mb_set_config(mj_mb* mb, int threads);
+
+/* A batch of several orders also holds one sub-batch per order, each running
+ * the kernel instance of its order alone; a step can then be one cooperative
+ * launch per order (in increasing order) instead of one launch of the
+ * all-orders kernel.  The first advance times this grouped form beside the
+ * two configurations of the all-orders kernel (runs restored afterwards) and
+ * keeps the fastest.  Reports whether the grouped form is in use, the number
+ * of order groups (0 for a batch of one order) and its timed ms per step
+ * (any output may be NULL).  No reference counterpart. */
+int mj_mb_grouping(const mj_mb* mb, int* grouped, int* n_groups, double* grouped_ms);
 
 /* ---- media update and adjoint ------------------------------------------ */
 

@@ -152,6 +152,15 @@ int k1_prepare_w_f32(int n, int E, int* ctas_per_sm);
 void k1_launch_w_f32(int n, int E, int grid, const void* x, const int* nodle_e, const void* fac_e, void* R,
                      const int* slot_e, int n_tiles, int* err, cudaStream_t s);
 
+// Test instances of two variants compiled with a bulk-copy wait limit of 0
+// (the test hook of mj_debug_set_wait_limits): FP32 one element per warp with
+// n = 5, E = 2, and FP64 compact with n = 5, E = 4.  Return false (nothing
+// launched) for any other variant.
+bool k1_launch_w_f32_waits_out(int n, int E, int grid, const void* x, const int* nodle_e, const void* fac_e,
+                               void* R, const int* slot_e, int n_tiles, int* err, cudaStream_t s);
+bool k1_launch_f64_waits_out(int n, int E, int grid, const void* x, const int* nodle_e, const void* fac_e,
+                             void* R, const int* slot_e, int n_tiles, int* err, cudaStream_t s);
+
 // Many right-hand sides (FP32 only, mj_batch.cu).
 struct RhsVariant {
   int E, L;

@@ -50,12 +50,12 @@ struct GConst<float> {
 };
 
 // ---------------------------------------------------------------------------
-// Bulk-copy (TMA) and mbarrier helpers.  Every wait is bounded: after
-// c_wait.mbar_polls unsuccessful polls (kSpinLimit unless a test lowered it)
-// the waiter gives up and the kernel reports the timeout through an error
-// flag instead of hanging.  Before returning, the CTA drains the copies it
-// still has in flight (mbar_wait_drain, always with the full kSpinLimit) so
-// that no copy lands in shared memory after the CTA has exited.
+// Bulk-copy (TMA) and mbarrier helpers.  Every wait is bounded: after LIMIT
+// unsuccessful polls (kSpinLimit; 0 in the test instances) the waiter gives
+// up and the kernel reports the timeout through an error flag instead of
+// hanging.  Before returning, the CTA drains the copies it still has in
+// flight (mbar_wait_drain, always with the full kSpinLimit) so that no copy
+// lands in shared memory after the CTA has exited.
 // ---------------------------------------------------------------------------
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
@@ -102,16 +102,18 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
+template <long LIMIT = kSpinLimit>
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-  const long limit = c_wait.mbar_polls;
-  for (long it = 0; it < limit; ++it)
+  for (long it = 0; it < LIMIT; ++it)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
 
 // Wait of a CTA that is giving up after a timed-out wait: lets a copy still in
-// flight into this stage complete (bounded by the full kSpinLimit).
-__device__ __forceinline__ void mbar_wait_drain(uint64_t* bar, uint32_t parity) {
+// flight into this stage complete (bounded by the full kSpinLimit).  Out of
+// line, so that the rarely taken failure path leaves the kernels' register
+// allocation as it is.
+static __device__ __noinline__ void mbar_wait_drain(uint64_t* bar, uint32_t parity) {
   for (long it = 0; it < kSpinLimit; ++it)
     if (mbar_try_wait(bar, parity)) return;
 }
@@ -200,7 +202,7 @@ struct K1Plan {
 // compact copy of u, vx, vy ([el][k][j][i]; y lines read with stride n);
 // VEC = true keeps x-lines and y-lines as separate padded copies so every
 // line is read with 16-byte loads (more shared memory, fewer instructions).
-template <typename Real, int N, int E, bool VEC = false>
+template <typename Real, int N, int E, bool VEC = false, long SPIN = kSpinLimit>
 __global__ void __launch_bounds__(E* N* N)
     k_local_stiffness(const Real* __restrict__ x, const int* __restrict__ nodle_e,
                       const Real* __restrict__ fac_e, Real* __restrict__ R, const int* __restrict__ slot_e,
@@ -258,7 +260,7 @@ __global__ void __launch_bounds__(E* N* N)
   uint32_t ph = 0u;  // bit st: parity of the next completion of stage st
   Real u[N];
   if (tile < n_tiles) {
-    const bool ok = mbar_wait_bounded(&bar[0], ph & 1u);
+    const bool ok = mbar_wait_bounded<SPIN>(&bar[0], ph & 1u);
     if (__syncthreads_or(!ok)) {
       if (t == 0) {  // report; both stages may still have a copy in flight
         atomicExch(err, 1);
@@ -316,7 +318,7 @@ __global__ void __launch_bounds__(E* N* N)
     const int nt = tile + g;
     if (nt < n_tiles) {
       const int so = s ^ 1;
-      const bool ok = mbar_wait_bounded(&bar[so], (ph >> so) & 1u);
+      const bool ok = mbar_wait_bounded<SPIN>(&bar[so], (ph >> so) & 1u);
       if (__syncthreads_or(!ok)) {
         if (t == 0) {  // report; stage so's copy may be in flight (stage s is not reissued yet)
           atomicExch(err, 1);
@@ -368,7 +370,7 @@ __global__ void __launch_bounds__(E* N* N)
 // release, which also carries the timeout vote of the warps' bounded stage
 // waits).  Same operation order as k_local_stiffness.
 // ---------------------------------------------------------------------------
-template <typename Real, int N, int E>
+template <typename Real, int N, int E, long SPIN = kSpinLimit>
 __global__ void __launch_bounds__(E * 32)
     k_local_stiffness_w(const Real* __restrict__ x, const int* __restrict__ nodle_e,
                         const Real* __restrict__ fac_e, Real* __restrict__ R, const int* __restrict__ slot_e,
@@ -424,7 +426,7 @@ __global__ void __launch_bounds__(E * 32)
   uint32_t ph = 0u;
   Real u[N];
   if (tile < n_tiles) {
-    const bool ok = mbar_wait_bounded(&bar[0], ph & 1u);
+    const bool ok = mbar_wait_bounded<SPIN>(&bar[0], ph & 1u);
     if (__syncthreads_or(!ok)) {
       if (t == 0) {  // report; both stages may still have a copy in flight
         atomicExch(err, 1);
@@ -480,7 +482,7 @@ __global__ void __launch_bounds__(E * 32)
     bool bad = false;
     if (nt < n_tiles) {
       const int so = s ^ 1;
-      const bool ok = mbar_wait_bounded(&bar[so], (ph >> so) & 1u);
+      const bool ok = mbar_wait_bounded<SPIN>(&bar[so], (ph >> so) & 1u);
       bad = __any_sync(0xffffffffu, !ok);
       ph ^= 1u << so;
       if (!bad && act) {

@@ -35,6 +35,18 @@ void launch_w_one(int grid, const void* x, const int* nodle_e, const void* fac_e
 }
 }  // namespace
 
+bool k1_launch_w_f32_waits_out(int n, int E, int grid, const void* x, const int* nodle_e, const void* fac_e,
+                               void* R, const int* slot_e, int n_tiles, int* err, cudaStream_t s) {
+  if (n != 5 || E != 2) return false;
+  using P = K1Plan<float, 5, 2, 1, false>;
+  auto* k = k_local_stiffness_w<float, 5, 2, 0>;
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::total) != cudaSuccess)
+    return false;
+  k<<<grid, 2 * 32, P::total, s>>>(static_cast<const float*>(x), nodle_e, static_cast<const float*>(fac_e),
+                                    static_cast<float*>(R), slot_e, n_tiles, err);
+  return true;
+}
+
 std::vector<int> k1_warp_tile_candidates(int n) {
   return n == 5 ? std::vector<int>{1, 2, 3, 4, 5, 6, 8, 10} : std::vector<int>{};
 }

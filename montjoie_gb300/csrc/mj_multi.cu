@@ -54,7 +54,7 @@ struct mj_mb {
   MbLists cfg[2];   // 0: 256 threads, 1: 128 threads
   int only = 0;     // the order n of every mesh (single-order kernels), or 0
   int use = -1;     // configuration in use (-1: not tuned yet)
-  double tune_ms[2] = {0, 0};
+  double tune_ms[3] = {0, 0, 0};  // one kernel (256, 128 threads), grouped by order
   // launch parity of the uploaded table: per run (cur_is_a, step & 1) at upload
   std::vector<int> base_cur, base_qc;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // 20 steps starting at k = 0 or k = 1
@@ -62,6 +62,10 @@ struct mj_mb {
   DevBuf stamps;        // per-CTA phase time stamps when profiling (plain launches only)
   bool profile = false;
   cudaStream_t stream = nullptr;
+  // Mixed orders: one sub-batch per order (each runs its single-order
+  // instance), the alternative to the all-orders kernel.  use == 2 selects it:
+  // a step is then one cooperative launch per order, in a fixed order.
+  std::vector<std::unique_ptr<mj_mb>> groups;
   ~mj_mb() {
     for (auto& g : graph)
       if (g) cudaGraphExecDestroy(g);
@@ -102,6 +106,13 @@ int mb_launch_t(mj_mb* mb, const MbLists& L, int k, cudaStream_t s) {
 }
 
 int mb_launch(mj_mb* mb, int which, int k, cudaStream_t s) {
+  if (which == 2) {  // one single-order launch per order group
+    for (auto& g : mb->groups) {
+      const int rc = mb_launch(g.get(), g->use, k, s);
+      if (rc) return rc;
+    }
+    return MJ_OK;
+  }
   return which == 0 ? mb_launch_t<256>(mb, mb->cfg[0], k, s) : mb_launch_t<128>(mb, mb->cfg[1], k, s);
 }
 
@@ -172,6 +183,7 @@ void mb_upload(mj_mb* mb) {
       cudaGraphExecDestroy(g);
       g = nullptr;
     }
+  for (auto& g : mb->groups) mb_upload(g.get());
 }
 
 // Offset (0 or 1) of the runs' current roles from the uploaded table, or -1
@@ -191,8 +203,15 @@ int mb_offset(const mj_mb* mb) {
 
 int mb_check_err(mj_mb* mb, cudaStream_t s) {
   int herr = 0;
-  MJ_CUDA(cudaMemcpyAsync(&herr, mb->err.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+  for (auto& g : mb->groups) {
+    const int rc = mb_check_err(g.get(), s);
+    if (rc == MJ_ERR_STATE) herr = 1;
+    else if (rc) return rc;
+  }
+  int own = 0;
+  MJ_CUDA(cudaMemcpyAsync(&own, mb->err.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
   MJ_CUDA(cudaStreamSynchronize(s));
+  herr |= own;
   if (herr) {
     cudaMemset(mb->err.ptr, 0, sizeof(int));
     cudaMemset(mb->sync.ptr, 0, sizeof(SyncState));
@@ -224,7 +243,18 @@ int mb_autotune(mj_mb* mb, int off, cudaStream_t s) {
   MJ_CUDA(cudaEventCreate(&e1));
   const uint64_t before = launch_counter().load();
   int best = 0;
-  for (int c = 0; c < 2; c++) {
+  const int n_modes = mb->groups.empty() ? 2 : 3;
+  for (int c = 0; c < n_modes; c++) {
+    if (c == 2)  // each order group picks its own launch configuration first
+      for (auto& g : mb->groups)
+        if (g->use < 0) {
+          const int rc = mb_autotune(g.get(), off, s);
+          if (rc) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return rc;
+          }
+        }
     int rc = mb_launch(mb, c, off, s);
     if (!rc) rc = cudaEventRecord(e0, s) == cudaSuccess ? MJ_OK : MJ_ERR_CUDA;
     for (int i = 1; !rc && i <= 3; i++) rc = mb_launch(mb, c, off + i, s);
@@ -256,14 +286,9 @@ int mb_autotune(mj_mb* mb, int off, cudaStream_t s) {
   return MJ_OK;
 }
 
-}  // namespace
-
-extern "C" {
-
-int mj_mb_create(int n_runs, mj_lf* const* runs, mj_mb** out) {
-  MJ_CHECK_ARG(out && runs && n_runs > 0, "mj_mb_create: null argument or no runs");
-  MJ_CHECK_ARG(n_runs <= kMaxRuns, "mj_mb_create: at most 48 runs per batch");
-  *out = nullptr;
+// A batch of the given runs; with split, a batch of several orders also gets
+// one sub-batch per order (the grouped alternative its autotuner times).
+int mb_create(int n_runs, mj_lf* const* runs, bool split, std::unique_ptr<mj_mb>* result) {
   std::unique_ptr<mj_mb> mb(new mj_mb());
   mb->runs.assign(runs, runs + n_runs);
   std::vector<const mj_op*> ops;
@@ -372,7 +397,35 @@ int mj_mb_create(int n_runs, mj_lf* const* runs, mj_mb** out) {
   MJ_CUDA(mb->stamps.alloc(sizeof(unsigned long long) * kStamps *
                            std::max(mb->cfg[0].grid, mb->cfg[1].grid)));
   mb->stream = runs[0]->stream;
+  if (split && !mb->only) {
+    for (int n = 2; n <= kMaxNK; n++) {
+      if (!have_g[n]) continue;
+      std::vector<mj_lf*> sub;
+      for (int r = 0; r < n_runs; r++)
+        if (runs[r]->op->n == n) sub.push_back(runs[r]);
+      std::unique_ptr<mj_mb> g;
+      const int rc = mb_create((int)sub.size(), sub.data(), false, &g);
+      if (rc) return rc;
+      mb->groups.push_back(std::move(g));
+    }
+  }
   mb_upload(mb.get());
+  *result = std::move(mb);
+  return MJ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mj_mb_create(int n_runs, mj_lf* const* runs, mj_mb** out) {
+  MJ_CHECK_ARG(out && runs && n_runs > 0, "mj_mb_create: null argument or no runs");
+  MJ_CHECK_ARG(n_runs <= kMaxRuns, "mj_mb_create: at most 48 runs per batch");
+  *out = nullptr;
+  for (int r = 0; r < n_runs; r++) MJ_CHECK_ARG(runs[r], "mj_mb_create: null run");
+  std::unique_ptr<mj_mb> mb;
+  const int rc = mb_create(n_runs, runs, true, &mb);
+  if (rc) return rc;
   *out = mb.release();
   return MJ_OK;
 }
@@ -403,6 +456,12 @@ int mj_mb_advance(mj_mb* mb, int nsteps, int use_graph) {
     const int rc = mb_autotune(mb, off, s);
     if (rc) return rc;
   }
+  if (mb->use == 2)  // grouped by order (forced): every group needs its configuration
+    for (auto& g : mb->groups)
+      if (g->use < 0) {
+        const int rc = mb_autotune(g.get(), off, s);
+        if (rc) return rc;
+      }
   mb->last_graph = false;
   int done = 0;
   if (use_graph && !mb->profile && nsteps >= kGraphStepsMb) {
@@ -447,12 +506,23 @@ int mj_mb_advance(mj_mb* mb, int nsteps, int use_graph) {
 int mj_mb_profile(mj_mb* mb, int enable) {
   MJ_CHECK_ARG(mb, "mj_mb_profile: null batch");
   mb->profile = enable != 0;
+  for (auto& g : mb->groups) g->profile = mb->profile;
   return MJ_OK;
 }
 
 int mj_mb_phase_ms(const mj_mb* mb, double* out) {
   MJ_CHECK_ARG(mb && out, "mj_mb_phase_ms: null argument");
   MJ_CHECK_ARG(mb->use >= 0, "mj_mb_phase_ms: no step has run");
+  if (mb->use == 2) {  // grouped by order: each phase summed over the groups' launches
+    for (int i = 0; i < 6; i++) out[i] = 0.0;
+    for (auto& g : mb->groups) {
+      double o[6];
+      const int rc = mj_mb_phase_ms(g.get(), o);
+      if (rc) return rc;
+      for (int i = 0; i < 6; i++) out[i] += o[i];
+    }
+    return MJ_OK;
+  }
   const int grid = mb->cfg[mb->use].grid;
   std::vector<unsigned long long> st(kStamps * (size_t)grid);
   MJ_CUDA(cudaMemcpy(st.data(), mb->stamps.ptr, sizeof(unsigned long long) * st.size(), cudaMemcpyDeviceToHost));
@@ -481,7 +551,8 @@ int mj_mb_phase_ms(const mj_mb* mb, double* out) {
 int mj_mb_info(const mj_mb* mb, int* grid, int* ctas_per_sm, int* n_tiles, int* n_chunks, int* graph,
                int* single_order) {
   MJ_CHECK_ARG(mb, "mj_mb_info: null batch");
-  const MbLists& L = mb->cfg[mb->use < 0 ? 0 : mb->use];
+  const MbLists& L = mb->use == 2 ? mb->groups[0]->cfg[std::max(0, mb->groups[0]->use)]
+                                   : mb->cfg[mb->use < 0 ? 0 : mb->use];
   if (grid) *grid = L.grid;
   if (ctas_per_sm) *ctas_per_sm = L.ctas_per_sm;
   if (n_tiles) *n_tiles = L.n_work;
@@ -493,8 +564,11 @@ int mj_mb_info(const mj_mb* mb, int* grid, int* ctas_per_sm, int* n_tiles, int* 
 
 int mj_mb_set_config(mj_mb* mb, int threads) {
   MJ_CHECK_ARG(mb, "mj_mb_set_config: null batch");
-  MJ_CHECK_ARG(threads == 0 || threads == 128 || threads == 256, "mj_mb_set_config: threads must be 0, 128 or 256");
-  mb->use = threads == 0 ? -1 : threads == 256 ? 0 : 1;
+  MJ_CHECK_ARG(threads == 0 || threads == 128 || threads == 256 || threads == -1,
+               "mj_mb_set_config: threads must be 0, 128, 256 or -1");
+  MJ_CHECK_ARG(threads != -1 || !mb->groups.empty(), "mj_mb_set_config: the batch has one order (no groups)");
+  mb->use = threads == 0 ? -1 : threads == 256 ? 0 : threads == 128 ? 1 : 2;
+  for (auto& g : mb->groups) g->use = -1;  // groups tune again at the next advance
   for (auto& g : mb->graph)
     if (g) {
       cudaGraphExecDestroy(g);
@@ -503,9 +577,20 @@ int mj_mb_set_config(mj_mb* mb, int threads) {
   return MJ_OK;
 }
 
+int mj_mb_grouping(const mj_mb* mb, int* grouped, int* n_groups, double* grouped_ms) {
+  MJ_CHECK_ARG(mb, "mj_mb_grouping: null batch");
+  if (grouped) *grouped = mb->use == 2 ? 1 : 0;
+  if (n_groups) *n_groups = (int)mb->groups.size();
+  if (grouped_ms) *grouped_ms = mb->tune_ms[2];
+  return MJ_OK;
+}
+
 int mj_mb_tuning(const mj_mb* mb, int* threads, double* candidate_ms) {
   MJ_CHECK_ARG(mb, "mj_mb_tuning: null batch");
-  if (threads) *threads = mb->use < 0 ? 0 : mb->cfg[mb->use].threads;
+  if (threads)
+    *threads = mb->use < 0 ? 0
+               : mb->use == 2 ? mb->groups[0]->cfg[std::max(0, mb->groups[0]->use)].threads
+                              : mb->cfg[mb->use].threads;
   if (candidate_ms) {
     candidate_ms[0] = mb->tune_ms[0];
     candidate_ms[1] = mb->tune_ms[1];

@@ -74,8 +74,23 @@ using namespace mj;
 
 namespace {
 
-// One launch of the element kernel with the operator's tuned variant.
+// One launch of the element kernel with the operator's tuned variant (its
+// instance compiled with a bulk-copy wait limit of 0 while the test hook
+// mj_debug_set_wait_limits asks for it and one exists).
 void launch_k1(mj_op* op, const void* x, cudaStream_t s) {
+  if (k1_waits_run_out()) {
+    const bool done =
+        op->warp ? k1_launch_w_f32_waits_out(op->n, op->E, op->grid_k1, x, op->nodle_e.as<int>(), op->fac_e.ptr,
+                                            op->R.ptr, op->slot_e.as<int>(), op->n_tiles, op->err.as<int>(), s)
+        : op->precision == MJ_FP64 && !op->vec
+            ? k1_launch_f64_waits_out(op->n, op->E, op->grid_k1, x, op->nodle_e.as<int>(), op->fac_e.ptr, op->R.ptr,
+                                      op->slot_e.as<int>(), op->n_tiles, op->err.as<int>(), s)
+            : false;
+    if (done) {
+      count_launch();
+      return;
+    }
+  }
   if (op->warp) {
     k1_launch_w_f32(op->n, op->E, op->grid_k1, x, op->nodle_e.as<int>(), op->fac_e.ptr, op->R.ptr,
                     op->slot_e.as<int>(), op->n_tiles, op->err.as<int>(), s);
@@ -192,6 +207,11 @@ WaitLimitRegistry& wait_limit_registry() {
   return r;
 }
 }  // namespace
+
+bool& mj::k1_waits_run_out() {
+  static bool on = false;
+  return on;
+}
 
 void mj::register_wait_limit_setter(mj::WaitLimitSetter f) {
   WaitLimitRegistry& r = wait_limit_registry();
@@ -640,8 +660,8 @@ int mj_op_mltadd(mj_op* op, double alpha, const double* x, double beta, double* 
 }
 
 int mj_debug_set_wait_limits(long long mbar_polls, long long barrier_polls, long long barrier_ns) {
+  mj::k1_waits_run_out() = mbar_polls == 0;
   mj::WaitLimits w;
-  w.mbar_polls = mbar_polls >= 0 ? (long)std::min<long long>(mbar_polls, mj::kSpinLimit) : mj::kSpinLimit;
   w.barrier_polls =
       barrier_polls >= 0 ? (long)std::min<long long>(barrier_polls, mj::kBarrierPolls) : mj::kBarrierPolls;
   w.barrier_ns = barrier_ns >= 0 ? std::min<unsigned long long>(barrier_ns, mj::kBarrierNs) : mj::kBarrierNs;

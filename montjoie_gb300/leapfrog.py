@@ -267,7 +267,8 @@ def RunSecondOrderScheme(t_begin: float, t_end: float, dt: float, U0: np.ndarray
 class MeshBatch:
     """Leap-frog runs on meshes of different size and order (each a
     ``LeapFrogIterator`` on its own FP32 operator) advanced together by one
-    cooperative persistent kernel per time step.  The reference advances such
+    cooperative persistent kernel per time step (or, when the autotuner finds
+    it faster, one per order group).  The reference advances such
     runs one after the other (``ModifiedEquation.cxx:290-345`` per run).
     Each run stays usable on its own (``SetInitialConditionS``,
     ``GetIterate``, ``Advance``) between calls."""
@@ -303,9 +304,17 @@ class MeshBatch:
         return {"threads": th.value, "candidate_ms": {"256": ms[0], "128": ms[1]}}
 
     def set_config(self, threads: int) -> None:
-        """Forces the launch configuration (128 or 256 threads per CTA), or 0
-        to time both again at the next advance."""
+        """Forces the launch configuration (128 or 256 threads per CTA: one
+        kernel of all orders per step; -1: one launch per order group), or 0
+        to time them again at the next advance."""
         _lib.check(_lib.load().mj_mb_set_config(self._h, int(threads)))
+
+    def grouping(self) -> dict:
+        """Whether steps run one launch per order group, the number of groups
+        and the grouped form's timed ms per step."""
+        g, n, ms = ctypes.c_int(), ctypes.c_int(), np.zeros(1)
+        _lib.check(_lib.load().mj_mb_grouping(self._h, ctypes.byref(g), ctypes.byref(n), _lib.dptr(ms)))
+        return {"grouped": bool(g.value), "groups": n.value, "grouped_ms": float(ms[0])}
 
     def profile(self, enable: bool) -> None:
         """Plain launches with per-CTA time stamps (no graph) while enabled."""

@@ -1,11 +1,12 @@
 """Failure paths, made to happen on purpose without faulting or hanging the GPU.
 
-- Bounded waits.  mj_debug_set_wait_limits lowers the poll and time limits of
-  every bounded wait (mbarrier waits on bulk copies, the grid barrier of the
-  cooperative steps).  With a limit of 0 the waits give up at once: the
-  kernels report through their error flag after letting their own copies in
-  flight land, the entry point returns an error status with a message, and
-  the next call (limits restored) gives the same result as before.
+- Bounded waits.  mj_debug_set_wait_limits makes waits run out: the element
+  kernel's bulk-copy waits (two variants switched to instances compiled with
+  a wait limit of 0; the variant is forced here) and the grid barrier of the
+  cooperative steps (its limits lowered to 0).  The kernels report through
+  their error flag after letting their own copies in flight land, the entry
+  point returns an error status with a message, and the next call (limits
+  restored) gives the same result as before.
 - Divergence guard.  An unstable time step (well above the CFL limit) makes
   the norm grow past NormeMaxSolution (1e30 by default, as in the reference,
   MONTJOIE/src/Instationary/VarInstationary.cxx:2741-2745) and, with no limit,
@@ -45,11 +46,17 @@ def _problem(cells=12, order=4, seed=3):
     return pb
 
 
+# the element-kernel variants that have instances with a wait limit of 0:
+# (elements per CTA, layout) for each precision
+WAITS_OUT_VARIANT = {"fp32": (2, 2), "fp64": (4, 0)}
+
+
 @pytest.mark.parametrize("precision", ["fp32", "fp64"])
 def test_element_kernel_wait_runs_out_and_next_call_works(lowered_waits, precision):
     from montjoie_gb300._lib import MJ_ERR_CUDA, MontjoieError
     pb = _problem()
     op = pb.operator(precision)
+    op.set_variant(*WAITS_OUT_VARIANT[precision])
     x = np.random.default_rng(0).uniform(-1, 1, pb.n_dof)
     y_ok = np.zeros(pb.n_dof)
     op.MltAddVector(1.0, x, 0.0, y_ok)
@@ -65,11 +72,13 @@ def test_element_kernel_wait_runs_out_and_next_call_works(lowered_waits, precisi
 
 
 def test_leapfrog_waits_run_out_and_next_run_works(lowered_waits):
-    """FP32 order-2 steps (element kernel and streaming gather, graph replays)."""
+    """FP32 order-2 steps launched one by one (a captured graph keeps its kernels)."""
     from montjoie_gb300._lib import MJ_ERR_CUDA, MontjoieError
     pb = _problem()
     op = pb.operator("fp32")
+    op.set_variant(*WAITS_OUT_VARIANT["fp32"])
     lf = pb.integrator(op, diagnostics=False)
+    lf.set_graph(False)
     zeros = np.zeros(pb.n_dof)
     lf.SetInitialConditionS(zeros)
     lf.Advance(45)
@@ -101,8 +110,7 @@ def _batch_runs():
     return runs
 
 
-@pytest.mark.parametrize("which", ["grid_barrier", "bulk_copies"])
-def test_mesh_batch_waits_run_out_and_next_advance_works(lowered_waits, which):
+def test_mesh_batch_waits_run_out_and_next_advance_works(lowered_waits):
     from montjoie_gb300._lib import MJ_ERR_STATE, MontjoieError
     from montjoie_gb300.leapfrog import MeshBatch
     runs = _batch_runs()
@@ -111,10 +119,7 @@ def test_mesh_batch_waits_run_out_and_next_advance_works(lowered_waits, which):
     u_ok = [lf.GetIterate() for _, lf in runs]
     for _, lf in runs:
         lf.SetInitialConditionS(np.zeros(lf.op.n_dof))
-    if which == "grid_barrier":
-        lowered_waits(barrier_polls=0, barrier_ns=0)
-    else:
-        lowered_waits(mbar_polls=0, barrier_polls=0, barrier_ns=0)
+    lowered_waits(barrier_polls=0, barrier_ns=0)
     with pytest.raises(MontjoieError) as exc:
         mb.advance(25)
     assert exc.value.code == MJ_ERR_STATE and "timed out" in str(exc.value)
@@ -130,8 +135,7 @@ def test_mesh_batch_waits_run_out_and_next_advance_works(lowered_waits, which):
         op.close()
 
 
-@pytest.mark.parametrize("which", ["grid_barrier", "bulk_copies"])
-def test_many_source_step_waits_run_out_and_next_advance_works(lowered_waits, which):
+def test_many_source_step_waits_run_out_and_next_advance_works(lowered_waits):
     from montjoie_gb300._lib import MJ_ERR_STATE, MontjoieError
     from montjoie_gb300.leapfrog import BatchLeapFrog
     g = load_golden("cube3_q4")
@@ -147,10 +151,7 @@ def test_many_source_step_waits_run_out_and_next_advance_works(lowered_waits, wh
     b.advance(25)
     u_ok, _ = b.state()
     b.init()
-    if which == "grid_barrier":
-        lowered_waits(barrier_polls=0, barrier_ns=0)
-    else:
-        lowered_waits(mbar_polls=0, barrier_polls=0, barrier_ns=0)
+    lowered_waits(barrier_polls=0, barrier_ns=0)
     with pytest.raises(MontjoieError) as exc:
         b.advance(25)
     assert exc.value.code == MJ_ERR_STATE and "timed out" in str(exc.value)

@@ -35,9 +35,10 @@ def snapshot(g, step):
     return g["snaps"][steps.index(step)] if step in steps else None
 
 
-@pytest.mark.parametrize("threads", [0, 128, 256])
+@pytest.mark.parametrize("threads", [0, 128, 256, -1])
 def test_batch_matches_reference_and_single_runs(threads):
-    """threads = 0: the autotuned launch configuration; 128 / 256: forced."""
+    """threads = 0: the autotuned launch configuration; 128 / 256: one kernel
+    of all orders per step, forced; -1: one launch per order group, forced."""
     from montjoie_gb300.leapfrog import MeshBatch
     gs = [load_golden(c) for c in CASES]
     batch_runs = [run_fp32(g) for g in gs]
@@ -50,7 +51,12 @@ def test_batch_matches_reference_and_single_runs(threads):
     assert info["single_order"] == 0  # several orders: the all-orders kernel
     mb.advance(30)  # one 20-step graph + 10 launches
     assert mb.info()["graph"] == 1
-    assert mb.tuning()["threads"] == (threads or mb.tuning()["threads"]) and mb.tuning()["threads"] in (128, 256)
+    assert mb.grouping()["groups"] == len({int(g["order"]) for g in gs})
+    if threads == -1:
+        assert mb.grouping()["grouped"]
+    elif threads:
+        assert mb.tuning()["threads"] == threads and not mb.grouping()["grouped"]
+    assert mb.tuning()["threads"] in (128, 256)
     for g, (_, lf), (_, ls) in zip(gs, batch_runs, single_runs):
         ls.Advance(30)
         u = lf.GetIterate()
