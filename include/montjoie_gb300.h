@@ -362,7 +362,9 @@ int mj_mb_advance(mj_mb* mb, int nsteps, int use_graph);
 /* Launch shape of the batch kernel: CTAs, CTAs per SM, element tiles and dof
  * chunks per step, 1 if the last advance replayed a graph, and the order
  * index n = r+1 when every mesh has that order (the batch then runs the
- * kernel instance of that order alone), else 0.  Any output may be NULL. */
+ * kernel instance of that order alone), else 0.  Grouped by order
+ * (mj_mb_grouping): tiles and chunks of all groups, CTAs of the largest
+ * group.  Any output may be NULL. */
 int mj_mb_info(const mj_mb* mb, int* grid, int* ctas_per_sm, int* n_tiles, int* n_chunks, int* graph,
                int* single_order);
 

@@ -551,12 +551,29 @@ int mj_mb_phase_ms(const mj_mb* mb, double* out) {
 int mj_mb_info(const mj_mb* mb, int* grid, int* ctas_per_sm, int* n_tiles, int* n_chunks, int* graph,
                int* single_order) {
   MJ_CHECK_ARG(mb, "mj_mb_info: null batch");
-  const MbLists& L = mb->use == 2 ? mb->groups[0]->cfg[std::max(0, mb->groups[0]->use)]
-                                   : mb->cfg[mb->use < 0 ? 0 : mb->use];
-  if (grid) *grid = L.grid;
-  if (ctas_per_sm) *ctas_per_sm = L.ctas_per_sm;
-  if (n_tiles) *n_tiles = L.n_work;
-  if (n_chunks) *n_chunks = L.n_chunks;
+  if (mb->use == 2) {  // grouped by order: the groups' totals, the launch shape of the largest group
+    int tiles = 0, chunks = 0, best = 0;
+    for (size_t i = 0; i < mb->groups.size(); i++) {
+      const mj_mb* g = mb->groups[i].get();
+      const MbLists& L = g->cfg[std::max(0, g->use)];
+      tiles += L.n_work;
+      chunks += L.n_chunks;
+      const mj_mb* b = mb->groups[best].get();
+      if (L.n_work > b->cfg[std::max(0, b->use)].n_work) best = (int)i;
+    }
+    const mj_mb* b = mb->groups[best].get();
+    const MbLists& L = b->cfg[std::max(0, b->use)];
+    if (grid) *grid = L.grid;
+    if (ctas_per_sm) *ctas_per_sm = L.ctas_per_sm;
+    if (n_tiles) *n_tiles = tiles;
+    if (n_chunks) *n_chunks = chunks;
+  } else {
+    const MbLists& L = mb->cfg[mb->use < 0 ? 0 : mb->use];
+    if (grid) *grid = L.grid;
+    if (ctas_per_sm) *ctas_per_sm = L.ctas_per_sm;
+    if (n_tiles) *n_tiles = L.n_work;
+    if (n_chunks) *n_chunks = L.n_chunks;
+  }
   if (graph) *graph = mb->last_graph ? 1 : 0;
   if (single_order) *single_order = mb->only;
   return MJ_OK;

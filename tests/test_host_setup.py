@@ -132,3 +132,61 @@ def test_receiver_weights_match_oracle():
         e = int(np.nonzero((g["nodle"] == idx[k]).all(axis=1))[0][0])
         wo, xi, inside = oc.point_weights(r, g["verts_e"][e], p)
         assert inside and np.abs(wo - w[k]).max() < 1e-12
+
+
+def _cpp_blocks(markdown):
+    out, cur = [], None
+    for line in markdown.splitlines():
+        if line.startswith("```cpp"):
+            cur = []
+        elif line.startswith("```") and cur is not None:
+            out.append(cur)
+            cur = None
+        elif cur is not None:
+            cur.append(line)
+    return out
+
+
+def test_integration_code_is_the_compiled_dropin():
+    """Every C++ block of INTEGRATION.md sections 1-2 (the operator subclass,
+    its installation, the order-2 loop and its order-4 variant) appears line
+    for line in oracle/dropin.cc, the file the drop-in build compiles."""
+    md = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    sections = md.split("## 2b.")[0]
+    src = [l.strip() for l in open(os.path.join(ROOT, "oracle", "dropin.cc")).read().splitlines() if l.strip()]
+    blocks = _cpp_blocks(sections)
+    assert len(blocks) == 4
+    for block in blocks:
+        lines = [l.strip() for l in block if l.strip()]
+        while lines and lines[0].startswith("//"):  # a context comment above the code
+            lines.pop(0)
+        starts = [i for i, l in enumerate(src) if l == lines[0]]
+        assert any(src[i:i + len(lines)] == lines for i in starts), lines[0]
+
+
+def test_dropin_links_with_the_library():
+    """oracle/_ref/dropin (built by __graft_entry__.build() where the reference
+    checkout is present): the binding compiled against the reference's
+    headers, whose mj_ symbols all resolve from libmontjoie_gb300.so."""
+    import shutil
+    import subprocess
+    exe = os.path.join(ROOT, "oracle", "_ref", "dropin")
+    if not os.path.exists(exe):
+        import __graft_entry__ as ge
+        ref = ge.reference_root()
+        if not os.path.isdir(os.path.join(ref, "MONTJOIE", "src")):
+            pytest.skip("no reference checkout here: the drop-in is built where the reference is")
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "dropin", f"REF={ref}"], check=True)
+    if not shutil.which("nm") or not shutil.which("ldd"):
+        pytest.skip("binutils absent")
+    ldd = subprocess.run(["ldd", exe], capture_output=True, text=True).stdout
+    lib_line = [l for l in ldd.splitlines() if "libmontjoie_gb300.so" in l]
+    assert lib_line and "not found" not in lib_line[0]
+    und = subprocess.run(["nm", "-D", "--undefined-only", exe], capture_output=True, text=True).stdout
+    used = {l.split()[-1] for l in und.splitlines() if l.split() and l.split()[-1].startswith("mj_")}
+    # mj_op_mltadd is called from the overriding MltAddFree, which the vtable keeps
+    assert {"mj_op_create", "mj_op_mltadd", "mj_op_destroy", "mj_lf_create", "mj_lf_run", "mj_lf_destroy",
+            "mj_lf_set_scheme", "mj_last_error"} <= used
+    exported = subprocess.run(["nm", "-D", "--defined-only", _lib.library_path()], capture_output=True,
+                              text=True).stdout
+    assert used <= {l.split()[-1] for l in exported.splitlines() if l.split()}
