@@ -679,8 +679,9 @@ def run_ours(args):
     achieved = bytes_k1 / (k1_ms / 1e3) / 1e9
     per_elt = ncu_traffic_per_element(f"k_local_stiffness_fp32_q{args.order}.md")
     step_bytes = n_elt * Q * (6 * 4 + 4) + n_dof * (3 * 4 + 4)
-    kname = ("k_local_stiffness_w<float,%d,%d>" % (args.order + 1, tuning32["tile_elems"])
-             if tuning32["layout"] == "warp_per_element" else
+    kname = ("k_local_stiffness_w<float,%d,%d%s>" % (args.order + 1, tuning32["tile_elems"],
+                                                    ",packed" if tuning32["layout"].endswith("packed") else "")
+             if tuning32["layout"].startswith("warp_per_element") else
              "k_local_stiffness<float,%d,%d,%s>" % (args.order + 1, tuning32["tile_elems"],
                                                    "vec" if tuning32["layout"] == "vector_lines" else "compact"))
     roofline = {"bound": "hbm", "kernel": kname + " (element kernel, autotuned)",

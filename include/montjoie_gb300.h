@@ -136,7 +136,10 @@ int mj_op_info(const mj_op* op, int* order, int* n_elt, int* n_dof, int* precisi
                size_t* device_bytes);
 
 /* Element-kernel variant chosen by the autotuner at creation: elements per
- * CTA, work layout (0 compact, 1 vector lines, 2 one element per warp), grid; and the timings (ms per launch,
+ * CTA, work layout (0 compact, 1 vector lines, 2 one element per warp, 3 one
+ * element per warp reading the packed connectivity: each point's dof with its
+ * rank among the dof's elements, so the result slot is the dof's CSR offset
+ * plus the rank and no slot array is read), grid; and the timings (ms per launch,
  * or a negative occupancy score on meshes too small to time) of the
  * candidates tried (candidate_ms may be NULL, else room for 64 values). */
 int mj_op_tuning(const mj_op* op, int* tile_elems, int* vector_lines, int* grid, int* n_candidates,
@@ -144,8 +147,10 @@ int mj_op_tuning(const mj_op* op, int* tile_elems, int* vector_lines, int* grid,
 
 /* Forces the element-kernel variant instead of the autotuner's choice:
  * tile_elems elements per CTA and the work layout (vector_lines: 0 compact,
- * 1 vector lines, 2 one element per warp; 1 and 2 are FP32 only, 2 exists
- * for order 4); MJ_ERR_ARG when no such variant exists for the order.  Integrators bound to the operator
+ * 1 vector lines, 2 one element per warp, 3 the same with packed
+ * connectivity; 1, 2 and 3 are FP32 only, 2 and 3 exist for order 4, 3 for
+ * meshes of fewer than 2^27 dofs each shared by at most 32 elements);
+ * MJ_ERR_ARG when no such variant exists for the order.  Integrators bound to the operator
  * keep captured CUDA graphs of the old variant until re-created. */
 int mj_op_set_variant(mj_op* op, int tile_elems, int vector_lines);
 

@@ -14,9 +14,11 @@ struct mj_op {
   int E = 1, n_tiles = 0, grid_k1 = 1;  // tile size and grid of the element kernel (autotuned)
   bool vec = false;                     // work layout of the element kernel (autotuned)
   bool warp = false;                    // warp-per-element layout (FP32, order 4; autotuned)
+  bool packed = false;                  // that layout with packed connectivity (nodle_pk; autotuned)
   size_t r_len = 0;                     // element-major slots (n_elt_pad * Qp)
   size_t n_inc = 0;                     // incidences (n_elt * Q); R has n_inc + 1 entries
   mj::DevBuf nodle_e, fac_e, slot_e, R, ptr;
+  mj::DevBuf nodle_pk;                  // packed connectivity: dof | rank << 27 (FP32 order 4), or empty
   mj::DevBuf err;                       // device error flag (bounded-wait timeouts)
   mj::DevBuf fac_orig;                  // factors before mj_op_set_element_scale (kept on first use)
   mj::DevBuf verts;                     // n_elt x 8 x 3 vertices (operators built from geometry)
@@ -28,7 +30,7 @@ struct mj_op {
   std::vector<int> tune_E, tune_vec;
   size_t device_bytes() const {
     return nodle_e.bytes + fac_e.bytes + fac_orig.bytes + slot_e.bytes + R.bytes + ptr.bytes + xbuf.bytes +
-           ybuf.bytes + verts.bytes;
+           ybuf.bytes + verts.bytes + nodle_pk.bytes;
   }
 };
 
@@ -147,10 +149,12 @@ void k1_launch_f64(int n, int E, bool vec, int grid, const void* x, const int* n
 void k1_launch_f32(int n, int E, bool vec, int grid, const void* x, const int* nodle_e, const void* fac_e, void* R,
                    const int* slot_e, int n_tiles, int* err, cudaStream_t s);
 // Warp-per-element layout (FP32; orders with (r+1)^2 <= 32 that are instantiated).
+// packed: the variant reading the packed connectivity (nodle_e = nodle_pk,
+// slot_e = the CSR offsets ptr; see kPkDofBits).
 std::vector<int> k1_warp_tile_candidates(int n);
-int k1_prepare_w_f32(int n, int E, int* ctas_per_sm);
-void k1_launch_w_f32(int n, int E, int grid, const void* x, const int* nodle_e, const void* fac_e, void* R,
-                     const int* slot_e, int n_tiles, int* err, cudaStream_t s);
+int k1_prepare_w_f32(int n, int E, bool packed, int* ctas_per_sm);
+void k1_launch_w_f32(int n, int E, bool packed, int grid, const void* x, const int* nodle_e, const void* fac_e,
+                     void* R, const int* slot_e, int n_tiles, int* err, cudaStream_t s);
 
 // Test instances of two variants compiled with a bulk-copy wait limit of 0
 // (the test hook of mj_debug_set_wait_limits): FP32 one element per warp with

@@ -370,11 +370,20 @@ __global__ void __launch_bounds__(E* N* N)
 // release, which also carries the timeout vote of the warps' bounded stage
 // waits).  Same operation order as k_local_stiffness.
 // ---------------------------------------------------------------------------
-template <typename Real, int N, int E, long SPIN = kSpinLimit>
+// Packed connectivity (PK): an entry of nodle_pk holds the dof in its low
+// kPkDofBits bits and, above them, the element's rank among the dof's
+// elements, so the result slot is ptr[dof] + rank: the slot array stream is
+// replaced by a gather of ptr at the dofs already gathered for u.  Padding
+// entries name the spare dof n_dof (slot ptr[n_dof] = the dummy slot).
+constexpr int kPkDofBits = 27;
+constexpr int kPkMaxRank = (1 << (32 - kPkDofBits)) - 1;  // 31
+
+template <typename Real, int N, int E, long SPIN = kSpinLimit, bool PK = false>
 __global__ void __launch_bounds__(E * 32)
     k_local_stiffness_w(const Real* __restrict__ x, const int* __restrict__ nodle_e,
                         const Real* __restrict__ fac_e, Real* __restrict__ R, const int* __restrict__ slot_e,
                         int n_tiles, int* __restrict__ err) {
+  // PK: nodle_e is the packed connectivity and slot_e the CSR offsets ptr
   static_assert(N * N <= 32, "one element per warp");
   using P = K1Plan<Real, N, E, 1, false>;
   constexpr int NN = P::NN, Q = P::Q, Qp = P::Qp;
@@ -425,6 +434,7 @@ __global__ void __launch_bounds__(E * 32)
   issue(1, tile + g);
   uint32_t ph = 0u;
   Real u[N];
+  int slot[N];  // PK: result slots of the gathered tile's points
   if (tile < n_tiles) {
     const bool ok = mbar_wait_bounded<SPIN>(&bar[0], ph & 1u);
     if (__syncthreads_or(!ok)) {
@@ -439,7 +449,12 @@ __global__ void __launch_bounds__(E * 32)
     const int* nd = s_nod(0) + pe;
     if (act) {
 #pragma unroll
-      for (int k = 0; k < N; k++) u[k] = __ldg(x + nd[k * NN]);
+      for (int k = 0; k < N; k++) {
+        const int w = nd[k * NN];
+        const int d = PK ? (w & ((1 << kPkDofBits) - 1)) : w;
+        u[k] = __ldg(x + d);
+        if constexpr (PK) slot[k] = __ldg(slot_e + d) + (int)((unsigned)w >> kPkDofBits);
+      }
     }
   }
   for (int it = 0; tile < n_tiles; tile += g, ++it) {
@@ -480,6 +495,7 @@ __global__ void __launch_bounds__(E * 32)
     // flight during the divergence
     const int nt = tile + g;
     bool bad = false;
+    int nslot[N];  // PK: the next tile's result slots
     if (nt < n_tiles) {
       const int so = s ^ 1;
       const bool ok = mbar_wait_bounded<SPIN>(&bar[so], (ph >> so) & 1u);
@@ -488,7 +504,12 @@ __global__ void __launch_bounds__(E * 32)
       if (!bad && act) {
         const int* nd = s_nod(so) + pe;
 #pragma unroll
-        for (int k = 0; k < N; k++) u[k] = __ldg(x + nd[k * NN]);
+        for (int k = 0; k < N; k++) {
+          const int w = nd[k * NN];
+          const int d = PK ? (w & ((1 << kPkDofBits) - 1)) : w;
+          u[k] = __ldg(x + d);
+          if constexpr (PK) nslot[k] = __ldg(slot_e + d) + (int)((unsigned)w >> kPkDofBits);
+        }
       }
     }
     if (act) {
@@ -502,8 +523,13 @@ __global__ void __launch_bounds__(E * 32)
           y += grj[a] * s_vy[ly + k * NN + a * N];
           y += Gm[k * N + a] * vz[a];
         }
-        R[__ldg(st + k * NN)] = y;
+        if constexpr (PK) R[slot[k]] = y;
+        else R[__ldg(st + k * NN)] = y;
       }
+    }
+    if constexpr (PK) {
+#pragma unroll
+      for (int k = 0; k < N; k++) slot[k] = nslot[k];
     }
     if (__syncthreads_or(bad)) {  // stage s and the work arrays are free; any wait timed out?
       if (t == 0) {  // report; stage s^1's copy may be in flight (parity before the flip above)

@@ -13,25 +13,25 @@ void k1_launch_f32(int n, int E, bool vec, int grid, const void* x, const int* n
 
 // warp-per-element layout, order 4 (n = 5): E warps per CTA
 namespace {
-template <int E>
+template <int E, bool PK>
 int prepare_w_one(int* ctas) {
   using P = K1Plan<float, 5, E, 1, false>;
-  MJ_CUDA(cudaFuncSetAttribute(k_local_stiffness_w<float, 5, E>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)P::total));
-  MJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas, k_local_stiffness_w<float, 5, E>, E * 32, P::total));
+  auto* k = k_local_stiffness_w<float, 5, E, kSpinLimit, PK>;
+  MJ_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::total));
+  MJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas, k, E * 32, P::total));
   if (*ctas < 1) {
     set_error("element kernel variant cannot be resident");
     return MJ_ERR_ARG;
   }
   return MJ_OK;
 }
-template <int E>
+template <int E, bool PK>
 void launch_w_one(int grid, const void* x, const int* nodle_e, const void* fac_e, void* R, const int* slot_e,
                   int n_tiles, int* err, cudaStream_t s) {
   using P = K1Plan<float, 5, E, 1, false>;
-  k_local_stiffness_w<float, 5, E><<<grid, E * 32, P::total, s>>>(static_cast<const float*>(x), nodle_e,
-                                                                   static_cast<const float*>(fac_e),
-                                                                   static_cast<float*>(R), slot_e, n_tiles, err);
+  k_local_stiffness_w<float, 5, E, kSpinLimit, PK><<<grid, E * 32, P::total, s>>>(
+      static_cast<const float*>(x), nodle_e, static_cast<const float*>(fac_e), static_cast<float*>(R), slot_e,
+      n_tiles, err);
 }
 }  // namespace
 
@@ -51,30 +51,29 @@ std::vector<int> k1_warp_tile_candidates(int n) {
   return n == 5 ? std::vector<int>{1, 2, 3, 4, 5, 6, 8, 10} : std::vector<int>{};
 }
 
-int k1_prepare_w_f32(int n, int E, int* ctas) {
-  if (n == 5 && E == 1) return prepare_w_one<1>(ctas);
-  if (n == 5 && E == 2) return prepare_w_one<2>(ctas);
-  if (n == 5 && E == 3) return prepare_w_one<3>(ctas);
-  if (n == 5 && E == 4) return prepare_w_one<4>(ctas);
-  if (n == 5 && E == 5) return prepare_w_one<5>(ctas);
-  if (n == 5 && E == 6) return prepare_w_one<6>(ctas);
-  if (n == 5 && E == 8) return prepare_w_one<8>(ctas);
-  if (n == 5 && E == 10) return prepare_w_one<10>(ctas);
+#define MJ_W_TILES(X) X(1) X(2) X(3) X(4) X(5) X(6) X(8) X(10)
+
+int k1_prepare_w_f32(int n, int E, bool packed, int* ctas) {
+#define MJ_X(EV)                                                                 \
+  if (n == 5 && E == EV) return packed ? prepare_w_one<EV, true>(ctas) : prepare_w_one<EV, false>(ctas);
+  MJ_W_TILES(MJ_X)
+#undef MJ_X
   set_error("no warp-per-element kernel variant for this order and tile size");
   return MJ_ERR_ARG;
 }
 
-void k1_launch_w_f32(int n, int E, int grid, const void* x, const int* nodle_e, const void* fac_e, void* R,
-                     const int* slot_e, int n_tiles, int* err, cudaStream_t s) {
-  if (n == 5 && E == 1) launch_w_one<1>(grid, x, nodle_e, fac_e, R, slot_e, n_tiles, err, s);
-  if (n == 5 && E == 2) launch_w_one<2>(grid, x, nodle_e, fac_e, R, slot_e, n_tiles, err, s);
-  if (n == 5 && E == 3) launch_w_one<3>(grid, x, nodle_e, fac_e, R, slot_e, n_tiles, err, s);
-  if (n == 5 && E == 4) launch_w_one<4>(grid, x, nodle_e, fac_e, R, slot_e, n_tiles, err, s);
-  if (n == 5 && E == 5) launch_w_one<5>(grid, x, nodle_e, fac_e, R, slot_e, n_tiles, err, s);
-  if (n == 5 && E == 6) launch_w_one<6>(grid, x, nodle_e, fac_e, R, slot_e, n_tiles, err, s);
-  if (n == 5 && E == 8) launch_w_one<8>(grid, x, nodle_e, fac_e, R, slot_e, n_tiles, err, s);
-  if (n == 5 && E == 10) launch_w_one<10>(grid, x, nodle_e, fac_e, R, slot_e, n_tiles, err, s);
+void k1_launch_w_f32(int n, int E, bool packed, int grid, const void* x, const int* nodle_e, const void* fac_e,
+                     void* R, const int* slot_e, int n_tiles, int* err, cudaStream_t s) {
+#define MJ_X(EV)                                                                                      \
+  if (n == 5 && E == EV) {                                                                            \
+    if (packed) launch_w_one<EV, true>(grid, x, nodle_e, fac_e, R, slot_e, n_tiles, err, s);          \
+    else launch_w_one<EV, false>(grid, x, nodle_e, fac_e, R, slot_e, n_tiles, err, s);                \
+    return;                                                                                           \
+  }
+  MJ_W_TILES(MJ_X)
+#undef MJ_X
 }
+#undef MJ_W_TILES
 
 std::vector<int> k1_tile_candidates(int n) {
   switch (n) {

@@ -78,7 +78,7 @@ namespace {
 // instance compiled with a bulk-copy wait limit of 0 while the test hook
 // mj_debug_set_wait_limits asks for it and one exists).
 void launch_k1(mj_op* op, const void* x, cudaStream_t s) {
-  if (k1_waits_run_out()) {
+  if (k1_waits_run_out() && !op->packed) {
     const bool done =
         op->warp ? k1_launch_w_f32_waits_out(op->n, op->E, op->grid_k1, x, op->nodle_e.as<int>(), op->fac_e.ptr,
                                             op->R.ptr, op->slot_e.as<int>(), op->n_tiles, op->err.as<int>(), s)
@@ -92,8 +92,9 @@ void launch_k1(mj_op* op, const void* x, cudaStream_t s) {
     }
   }
   if (op->warp) {
-    k1_launch_w_f32(op->n, op->E, op->grid_k1, x, op->nodle_e.as<int>(), op->fac_e.ptr, op->R.ptr,
-                    op->slot_e.as<int>(), op->n_tiles, op->err.as<int>(), s);
+    k1_launch_w_f32(op->n, op->E, op->packed, op->grid_k1, x, (op->packed ? op->nodle_pk : op->nodle_e).as<int>(),
+                    op->fac_e.ptr, op->R.ptr, (op->packed ? op->ptr : op->slot_e).as<int>(), op->n_tiles,
+                    op->err.as<int>(), s);
     count_launch();
     return;
   }
@@ -128,14 +129,14 @@ int autotune_k1(mj_op* op) {
   MJ_CUDA(cudaEventCreate(&e1));
   double best = 1e300;
   int bestE = -1, bestGrid = 1;
-  bool bestVec = false, bestWarp = false;
+  bool bestVec = false, bestWarp = false, bestPacked = false;
   const bool time_it = (long long)op->n_elt * op->Q >= 2000000;
-  const int n_layouts = op->precision == MJ_FP32 ? 3 : 1;
+  const int n_layouts = op->precision == MJ_FP32 ? (op->nodle_pk.ptr ? 4 : 3) : 1;
   for (int lay = 0; lay < n_layouts; lay++)
-    for (int E : (lay == 2 ? k1_warp_tile_candidates(op->n) : cands)) {
-      const bool vec = lay == 1, warp = lay == 2;
+    for (int E : (lay >= 2 ? k1_warp_tile_candidates(op->n) : cands)) {
+      const bool vec = lay == 1, warp = lay >= 2, packed = lay == 3;
       int ctas = 0;
-      const int rc = warp ? k1_prepare_w_f32(op->n, E, &ctas)
+      const int rc = warp ? k1_prepare_w_f32(op->n, E, packed, &ctas)
                           : op->precision == MJ_FP64 ? k1_prepare_f64(op->n, E, vec, &ctas)
                                                      : k1_prepare_f32(op->n, E, vec, &ctas);
       if (rc != MJ_OK) continue;
@@ -143,7 +144,7 @@ int autotune_k1(mj_op* op) {
       const int grid = std::max(1, std::min(tiles, ctas * sms));
       double ms = 0.0;
       if (time_it) {
-        op->E = E; op->vec = vec; op->warp = warp; op->grid_k1 = grid; op->n_tiles = tiles;
+        op->E = E; op->vec = vec; op->warp = warp; op->packed = packed; op->grid_k1 = grid; op->n_tiles = tiles;
         launch_k1(op, x.ptr, op->stream);
         MJ_CUDA(cudaEventRecord(e0, op->stream));
         for (int rep = 0; rep < 3; rep++) launch_k1(op, x.ptr, op->stream);
@@ -153,12 +154,13 @@ int autotune_k1(mj_op* op) {
         MJ_CUDA(cudaEventElapsedTime(&f, e0, e1));
         ms = f / 3.0;
       } else {
-        ms = -double(ctas) * E * op->n * op->n + (vec ? 0.5 : 0.0) + (warp ? 0.75 : 0.0);  // most resident threads first
+        ms = -double(ctas) * E * op->n * op->n + (vec ? 0.5 : 0.0) + (warp ? 0.75 : 0.0) +
+             (packed ? 0.1 : 0.0);  // most resident threads first
       }
       op->tune_E.push_back(E);
       op->tune_vec.push_back(lay);
       op->tune_ms.push_back(ms);
-      if (ms < best) { best = ms; bestE = E; bestGrid = grid; bestVec = vec; bestWarp = warp; }
+      if (ms < best) { best = ms; bestE = E; bestGrid = grid; bestVec = vec; bestWarp = warp; bestPacked = packed; }
     }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -169,11 +171,12 @@ int autotune_k1(mj_op* op) {
   op->E = bestE;
   op->vec = bestVec;
   op->warp = bestWarp;
+  op->packed = bestPacked;
   op->grid_k1 = bestGrid;
   // the chosen variant's shared-memory attribute must be the one set last
   {
     int ctas = 0;
-    const int rc = bestWarp ? k1_prepare_w_f32(op->n, bestE, &ctas)
+    const int rc = bestWarp ? k1_prepare_w_f32(op->n, bestE, bestPacked, &ctas)
                             : op->precision == MJ_FP64 ? k1_prepare_f64(op->n, bestE, bestVec, &ctas)
                                                        : k1_prepare_f32(op->n, bestE, bestVec, &ctas);
     if (rc) return rc;
@@ -342,6 +345,22 @@ int op_layout(mj_op* op, const mj_mesh_desc* mesh, const double* gradphi, int pr
       ne[p] = d;
       se[p] = fill[d]++;
     }
+  }
+  // packed connectivity for the FP32 warp-per-element kernel: dof | rank << kPkDofBits
+  // (rank = the slot's place among the dof's incidences), padding -> the spare dof n_dof
+  int max_deg = 0;
+  for (int d = 0; d < op->n_dof; d++) max_deg = std::max(max_deg, count[d + 1]);
+  if (precision == MJ_FP32 && !k1_warp_tile_candidates(n).empty() && op->n_dof < (1 << kPkDofBits) &&
+      max_deg <= kPkMaxRank + 1) {
+    std::vector<int> pk(op->r_len, op->n_dof);
+    for (int e = 0; e < mesh->n_elt; e++)
+      for (int p = 0; p < Q; p++) {
+        const size_t rp = (size_t)e * Qp + p;
+        const int d = nodle_e[rp];
+        pk[rp] = (int)((unsigned)d | ((unsigned)(slot_e[rp] - op->h_ptr[d]) << kPkDofBits));
+      }
+    MJ_CUDA(op->nodle_pk.alloc(sizeof(int) * op->r_len));
+    MJ_CUDA(cudaMemcpy(op->nodle_pk.ptr, pk.data(), sizeof(int) * op->r_len, cudaMemcpyHostToDevice));
   }
   const size_t esz = elem_size(precision);
   MJ_CUDA(op->nodle_e.alloc(sizeof(int) * op->r_len));
@@ -601,7 +620,7 @@ int mj_op_tuning(const mj_op* op, int* tile_elems, int* vector_lines, int* grid,
                  double* candidate_ms) {
   MJ_CHECK_ARG(op, "mj_op_tuning: null operator");
   if (tile_elems) *tile_elems = op->E;
-  if (vector_lines) *vector_lines = op->warp ? 2 : op->vec ? 1 : 0;
+  if (vector_lines) *vector_lines = op->packed ? 3 : op->warp ? 2 : op->vec ? 1 : 0;
   if (grid) *grid = op->grid_k1;
   if (n_candidates) *n_candidates = (int)op->tune_ms.size();
   if (candidate_ms)
@@ -611,21 +630,23 @@ int mj_op_tuning(const mj_op* op, int* tile_elems, int* vector_lines, int* grid,
 
 int mj_op_set_variant(mj_op* op, int tile_elems, int vector_lines) {
   MJ_CHECK_ARG(op, "mj_op_set_variant: null operator");
-  MJ_CHECK_ARG(vector_lines >= 0 && vector_lines <= 2, "mj_op_set_variant: layout must be 0, 1 or 2");
-  const bool warp = vector_lines == 2, vec = vector_lines == 1;
+  MJ_CHECK_ARG(vector_lines >= 0 && vector_lines <= 3, "mj_op_set_variant: layout must be 0, 1, 2 or 3");
+  MJ_CHECK_ARG(vector_lines != 3 || op->nodle_pk.ptr, "mj_op_set_variant: no packed connectivity for this operator");
+  const bool warp = vector_lines >= 2, vec = vector_lines == 1, packed = vector_lines == 3;
   const std::vector<int> cands = warp ? k1_warp_tile_candidates(op->n) : k1_tile_candidates(op->n);
   MJ_CHECK_ARG(std::find(cands.begin(), cands.end(), tile_elems) != cands.end(),
                "mj_op_set_variant: no element kernel with this tile size and layout for this order");
   MJ_CHECK_ARG(vector_lines == 0 || op->precision == MJ_FP32,
                "mj_op_set_variant: vector-line and warp layouts are FP32 only");
   int ctas = 0;
-  const int rc = warp ? k1_prepare_w_f32(op->n, tile_elems, &ctas)
+  const int rc = warp ? k1_prepare_w_f32(op->n, tile_elems, packed, &ctas)
                       : op->precision == MJ_FP64 ? k1_prepare_f64(op->n, tile_elems, false, &ctas)
                                                  : k1_prepare_f32(op->n, tile_elems, vec, &ctas);
   if (rc) return rc;
   op->E = tile_elems;
   op->vec = vec;
   op->warp = warp;
+  op->packed = packed;
   op->n_tiles = op->n_elt_pad / tile_elems;
   op->grid_k1 = std::max(1, std::min(op->n_tiles, ctas * sm_count()));
   return MJ_OK;

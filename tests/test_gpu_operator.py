@@ -116,18 +116,21 @@ K1_TILES = {1: (30, 60), 2: (12, 24), 3: (8, 16), 4: (4, 5, 8, 10), 5: (3, 4, 6)
 def test_every_element_kernel_variant(case):
     """Every instantiated element-kernel variant (tile size x work layout),
     forced in turn, against the reference's MltAdd: FP64 (compact) <= 1e-12,
-    FP32 (compact and vector lines) <= 2e-5 relative L2."""
+    FP32 (compact, vector lines, one element per warp with the slot array or
+    with the packed connectivity) <= 2e-5 relative L2; the two warp forms
+    give the same result bit for bit."""
     from montjoie_gb300.operator import FemMatrixFreeOperator
     g = load_golden(case)
     r = int(g["order"])
     n_dof = g["massD"].size
     from montjoie_gb300._lib import MontjoieError
-    for precision, layouts, tol in (("fp64", (0,), 1e-12), ("fp32", (0, 1, 2), 2e-5)):
+    for precision, layouts, tol in (("fp64", (0,), 1e-12), ("fp32", (0, 1, 2, 3), 2e-5)):
         op = FemMatrixFreeOperator(r, g["nodle"], g["bh"], n_dof, precision, gradphi=g["gradphi"])
         tried = set()
+        warp_y = {}
         for E in sorted(set(K1_TILES[r]) | ({1, 2, 3, 4, 5, 6, 8, 10} if r == 4 else set())):
             for vec in layouts:
-                if vec == 2 and (r != 4 or E not in (1, 2, 3, 4, 5, 6, 8, 10)):
+                if vec >= 2 and (r != 4 or E not in (1, 2, 3, 4, 5, 6, 8, 10)):
                     continue
                 try:
                     op.set_variant(E, vec)
@@ -138,5 +141,9 @@ def test_every_element_kernel_variant(case):
                 y = g["y0"].copy()
                 op.MltAddVector(float(g["alpha"]), g["x"], float(g["beta"]), y)
                 assert rel_l2(y, g["kh_y"]) < tol, (precision, E, vec)
-        assert tried == (set(layouts) if r == 4 else set(layouts) - {2})
+                if vec >= 2:
+                    warp_y.setdefault(E, []).append(y)
+        assert tried == (set(layouts) if r == 4 else set(layouts) - {2, 3})
+        for ys in warp_y.values():
+            assert len(ys) == 2 and np.array_equal(ys[0], ys[1])
         op.close()
