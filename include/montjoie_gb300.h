@@ -399,10 +399,20 @@ int mj_mb_set_config(mj_mb* mb, int threads);
  * launch per order (in increasing order) instead of one launch of the
  * all-orders kernel.  The first advance times this grouped form beside the
  * two configurations of the all-orders kernel (runs restored afterwards) and
- * keeps the fastest.  Reports whether the grouped form is in use, the number
- * of order groups (0 for a batch of one order) and its timed ms per step
- * (any output may be NULL).  No reference counterpart. */
+ * keeps the fastest.  Within the grouped form each group is timed both ways:
+ * its batch kernel, or its runs' own step kernels (those of mj_lf_advance)
+ * one run after the other, and keeps the faster (large meshes of high order
+ * run well on their own kernels, many small ones batched).  Reports whether
+ * the grouped form is in use, the number of order groups (0 for a batch of
+ * one order) and its timed ms per step (any output may be NULL).  No
+ * reference counterpart. */
 int mj_mb_grouping(const mj_mb* mb, int* grouped, int* n_groups, double* grouped_ms);
+
+/* Group `group` (0 .. n_groups-1, in increasing order): its order, runs,
+ * 1 when it steps with its runs' own kernels, and the timed ms per step of
+ * both forms (any output may be NULL). */
+int mj_mb_group_info(const mj_mb* mb, int group, int* order, int* n_runs, int* own_kernels, double* batch_ms,
+                     double* own_ms);
 
 /* ---- media update and adjoint ------------------------------------------ */
 

@@ -198,6 +198,11 @@ int lfb_fused_step_on(mj_lfb* b, float* u0, float* u1, float* out, bool sources,
 int lfb_fused_step(mj_lfb* b, cudaStream_t s);
 int lfb_fused_check(mj_lfb* b, cudaStream_t s);
 
+// One time step of a run with its own kernels (the ones mj_lf_advance
+// launches), on the given buffers (cur = U^n, overwritten by U^{n+2}; next =
+// U^{n+1}) and pulse-counter parity qc, on stream s (capturable).
+int lf_step_on(mj_lf* lf, void* cur, const void* next, int qc, cudaStream_t s);
+
 // Single-order instances of the many-mesh batch kernel (mj_multi_one.cu):
 // the kernel for `threads` per CTA and order n (2..9), and the FP32
 // derivative matrix of order n in that translation unit's constant bank.

@@ -66,6 +66,10 @@ struct mj_mb {
   // instance), the alternative to the all-orders kernel.  use == 2 selects it:
   // a step is then one cooperative launch per order, in a fixed order.
   std::vector<std::unique_ptr<mj_mb>> groups;
+  // A group may instead step its runs with their own kernels, one run after
+  // the other, when that is faster for its meshes (chosen by timing).
+  bool seq = false;
+  double seq_ms = 0, batch_ms = 0;
   ~mj_mb() {
     for (auto& g : graph)
       if (g) cudaGraphExecDestroy(g);
@@ -105,10 +109,24 @@ int mb_launch_t(mj_mb* mb, const MbLists& L, int k, cudaStream_t s) {
   return MJ_OK;
 }
 
+// Step k (relative to the uploaded table) of every run of the batch with the
+// runs' own kernels, one run after the other.
+int mb_launch_seq(mj_mb* mb, int k, cudaStream_t s) {
+  for (size_t r = 0; r < mb->runs.size(); r++) {
+    mj_lf* lf = mb->runs[r];
+    const MeshDev& m = mb->h_mesh[r];
+    float* cur = ((k + m.cur_par) & 1) == 0 ? m.ua : m.ub;  // U^n, overwritten by U^{n+2}
+    const float* next = ((k + m.cur_par) & 1) == 0 ? m.ub : m.ua;
+    const int rc = lf_step_on(lf, cur, next, (k + m.qc_par) & 1, s);
+    if (rc) return rc;
+  }
+  return MJ_OK;
+}
+
 int mb_launch(mj_mb* mb, int which, int k, cudaStream_t s) {
-  if (which == 2) {  // one single-order launch per order group
+  if (which == 2) {  // one launch per order group (or its runs' own kernels)
     for (auto& g : mb->groups) {
-      const int rc = mb_launch(g.get(), g->use, k, s);
+      const int rc = g->seq ? mb_launch_seq(g.get(), k, s) : mb_launch(g.get(), g->use, k, s);
       if (rc) return rc;
     }
     return MJ_OK;
@@ -207,6 +225,9 @@ int mb_check_err(mj_mb* mb, cudaStream_t s) {
     const int rc = mb_check_err(g.get(), s);
     if (rc == MJ_ERR_STATE) herr = 1;
     else if (rc) return rc;
+    if (g->seq)  // runs stepped with their own kernels report through their operators
+      for (mj_lf* lf : g->runs)
+        if (take_kernel_error(lf->op->err.ptr, s, "mj_mb_advance")) herr = 1;
   }
   int own = 0;
   MJ_CUDA(cudaMemcpyAsync(&own, mb->err.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -245,16 +266,28 @@ int mb_autotune(mj_mb* mb, int off, cudaStream_t s) {
   int best = 0;
   const int n_modes = mb->groups.empty() ? 2 : 3;
   for (int c = 0; c < n_modes; c++) {
-    if (c == 2)  // each order group picks its own launch configuration first
-      for (auto& g : mb->groups)
-        if (g->use < 0) {
-          const int rc = mb_autotune(g.get(), off, s);
-          if (rc) {
-            cudaEventDestroy(e0);
-            cudaEventDestroy(e1);
-            return rc;
-          }
+    if (c == 2)  // each order group picks its launch configuration, then batched or its runs' own kernels
+      for (auto& g : mb->groups) {
+        int rc = g->use < 0 ? mb_autotune(g.get(), off, s) : MJ_OK;
+        for (int form = 0; !rc && form < 2; form++) {
+          g->seq = form == 1;
+          rc = mb_launch(mb, 2, off, s) == MJ_OK ? MJ_OK : MJ_ERR_CUDA;  // warm-up of the whole grouped step
+          if (!rc) rc = cudaEventRecord(e0, s) == cudaSuccess ? MJ_OK : MJ_ERR_CUDA;
+          for (int i = 1; !rc && i <= 3; i++)
+            rc = g->seq ? mb_launch_seq(g.get(), off + i, s) : mb_launch(g.get(), g->use, off + i, s);
+          if (!rc) rc = cudaEventRecord(e1, s) == cudaSuccess ? MJ_OK : MJ_ERR_CUDA;
+          if (!rc) rc = mb_check_err(mb, s);
+          float ms = 0.f;
+          if (!rc) rc = cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess ? MJ_OK : MJ_ERR_CUDA;
+          (form ? g->seq_ms : g->batch_ms) = ms / 3.0;
         }
+        if (rc) {
+          cudaEventDestroy(e0);
+          cudaEventDestroy(e1);
+          return rc;
+        }
+        g->seq = g->seq_ms < g->batch_ms;
+      }
     int rc = mb_launch(mb, c, off, s);
     if (!rc) rc = cudaEventRecord(e0, s) == cudaSuccess ? MJ_OK : MJ_ERR_CUDA;
     for (int i = 1; !rc && i <= 3; i++) rc = mb_launch(mb, c, off + i, s);
@@ -485,9 +518,15 @@ int mj_mb_advance(mj_mb* mb, int nsteps, int use_graph) {
       cudaGraphDestroy(g);
       cudaStreamDestroy(cs);
     }
+    // kernels per step: one, or one per order group (two per run of a group on its runs' own kernels)
+    uint64_t per_step = 1;
+    if (mb->use == 2) {
+      per_step = 0;
+      for (auto& g : mb->groups) per_step += g->seq ? 2 * g->runs.size() : 1;
+    }
     while (nsteps - done >= kGraphStepsMb) {
       MJ_CUDA(cudaGraphLaunch(mb->graph[off], s));
-      count_launch(kGraphStepsMb);
+      count_launch(kGraphStepsMb * per_step);
       done += kGraphStepsMb;
     }
     mb->last_graph = true;
@@ -599,6 +638,18 @@ int mj_mb_grouping(const mj_mb* mb, int* grouped, int* n_groups, double* grouped
   if (grouped) *grouped = mb->use == 2 ? 1 : 0;
   if (n_groups) *n_groups = (int)mb->groups.size();
   if (grouped_ms) *grouped_ms = mb->tune_ms[2];
+  return MJ_OK;
+}
+
+int mj_mb_group_info(const mj_mb* mb, int group, int* order, int* n_runs, int* own_kernels, double* batch_ms,
+                     double* own_ms) {
+  MJ_CHECK_ARG(mb && group >= 0 && group < (int)mb->groups.size(), "mj_mb_group_info: no such group");
+  const mj_mb* g = mb->groups[group].get();
+  if (order) *order = g->runs[0]->op->order;
+  if (n_runs) *n_runs = (int)g->runs.size();
+  if (own_kernels) *own_kernels = g->seq ? 1 : 0;
+  if (batch_ms) *batch_ms = g->batch_ms;
+  if (own_ms) *own_ms = g->seq_ms;
   return MJ_OK;
 }
 

@@ -1434,3 +1434,10 @@ int mj_lf_device_state(mj_lf* lf, void** u_n, void** u_np1, int* step) {
 }
 
 }  // extern "C"
+
+int mj::lf_step_on(mj_lf* lf, void* cur, const void* next, int qc, cudaStream_t s) {
+  if (lf->op->precision == MJ_FP64) lf_step_launch<double>(lf, cur, next, qc, s, false);
+  else lf_step_launch<float>(lf, cur, next, qc, s, false);
+  MJ_CUDA(cudaGetLastError());
+  return MJ_OK;
+}

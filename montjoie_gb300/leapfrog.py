@@ -312,9 +312,17 @@ class MeshBatch:
     def grouping(self) -> dict:
         """Whether steps run one launch per order group, the number of groups
         and the grouped form's timed ms per step."""
+        L = _lib.load()
         g, n, ms = ctypes.c_int(), ctypes.c_int(), np.zeros(1)
-        _lib.check(_lib.load().mj_mb_grouping(self._h, ctypes.byref(g), ctypes.byref(n), _lib.dptr(ms)))
-        return {"grouped": bool(g.value), "groups": n.value, "grouped_ms": float(ms[0])}
+        _lib.check(L.mj_mb_grouping(self._h, ctypes.byref(g), ctypes.byref(n), _lib.dptr(ms)))
+        groups = []
+        for i in range(n.value):
+            o, nr, own, bms, oms = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), np.zeros(1), np.zeros(1)
+            _lib.check(L.mj_mb_group_info(self._h, i, ctypes.byref(o), ctypes.byref(nr), ctypes.byref(own),
+                                          _lib.dptr(bms), _lib.dptr(oms)))
+            groups.append({"order": o.value, "runs": nr.value, "own_kernels": bool(own.value),
+                           "batch_ms": float(bms[0]), "own_ms": float(oms[0])})
+        return {"grouped": bool(g.value), "groups": n.value, "grouped_ms": float(ms[0]), "per_group": groups}
 
     def profile(self, enable: bool) -> None:
         """Plain launches with per-CTA time stamps (no graph) while enabled."""
