@@ -57,6 +57,8 @@ def parse():
                     help="orders cycled over the heterogeneous batch (default 2,3,4,6,8)")
     ap.add_argument("--mb-max-cells", type=int, default=40,
                     help="largest mesh of the heterogeneous batch (default 40; smaller for profiling)")
+    ap.add_argument("--fp32-only", action="store_true",
+                    help="profiling aid: only the FP32 set-up and timed steps of the workload (no JSON line contract)")
     ap.add_argument("--leg", default="all", choices=["all", "q8", "sources", "meshes", "adjoint", "order4"],
                     help="profiling aid: run one extra leg alone (no JSON line contract)")
     return ap.parse_args()
@@ -614,6 +616,12 @@ def run_ours(args):
     clocks = ClockSampler(local)
     clocks.start()
     ms32, k1_ms, k2_ms, launches = time_advance(torch, lf32, K, _lib, barrier=dist.barrier if world > 1 else None)
+    if args.fp32_only:
+        clocks.stop()
+        print(json.dumps({"fp32_only": True, "cells": args.cells, "order": args.order, "ms_per_step": ms32 / K,
+                          "element_kernel_ms": k1_ms, "update_kernel_ms": k2_ms, "tuning": tuning32,
+                          "setup_seconds": setup_s}))
+        return
     # ---- FP64 plain form, resident (its own step count, after one graph's worth of warm-up)
     op64 = pb.operator("fp64")
     lf64 = pb.integrator(op64, diagnostics=False)
