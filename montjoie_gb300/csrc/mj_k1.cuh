@@ -641,19 +641,20 @@ __global__ void __launch_bounds__(E* N* N* L)
       float vz[N];
 #pragma unroll
       for (int k = 0; k < N; k++) {
+        // explicit FMAs in the order of k_rhs_step, so both forms round alike
         float gx = 0, gy = 0, gz = 0;
 #pragma unroll
         for (int a = 0; a < N; a++) {
-          gz += Gm[a * N + k] * u[a];
-          gx += gci[a] * s_u[(s_line_x + k * NN + a) * L + lane];
-          gy += gcj[a] * s_u[(s_line_y + k * NN + a * N) * L + lane];
+          gz = fmaf(Gm[a * N + k], u[a], gz);
+          gx = fmaf(gci[a], s_u[(s_line_x + k * NN + a) * L + lane], gx);
+          gy = fmaf(gcj[a], s_u[(s_line_y + k * NN + a * N) * L + lane], gy);
         }
         const float* fk = f + k * NN;
         const float bxx = fk[0], bxy = fk[Qp], bxz = fk[2 * Qp];
         const float byy = fk[3 * Qp], byz = fk[4 * Qp], bzz = fk[5 * Qp];
-        s_vx[(s_base + k * NN + ij) * L + lane] = bxx * gx + bxy * gy + bxz * gz;
-        s_vy[(s_base + k * NN + ij) * L + lane] = bxy * gx + byy * gy + byz * gz;
-        vz[k] = bxz * gx + byz * gy + bzz * gz;
+        s_vx[(s_base + k * NN + ij) * L + lane] = fmaf(bxz, gz, fmaf(bxy, gy, bxx * gx));
+        s_vy[(s_base + k * NN + ij) * L + lane] = fmaf(byz, gz, fmaf(byy, gy, bxy * gx));
+        vz[k] = fmaf(bzz, gz, fmaf(byz, gy, bxz * gx));
       }
       __syncthreads();
       const int* st = slot_e + ((size_t)tile * E + el) * Qp + ij;
@@ -662,9 +663,9 @@ __global__ void __launch_bounds__(E* N* N* L)
         float y = 0;
 #pragma unroll
         for (int a = 0; a < N; a++) {
-          y += gri[a] * s_vx[(s_line_x + k * NN + a) * L + lane];
-          y += grj[a] * s_vy[(s_line_y + k * NN + a * N) * L + lane];
-          y += Gm[k * N + a] * vz[a];
+          y = fmaf(gri[a], s_vx[(s_line_x + k * NN + a) * L + lane], y);
+          y = fmaf(grj[a], s_vy[(s_line_y + k * NN + a * N) * L + lane], y);
+          y = fmaf(Gm[k * N + a], vz[a], y);
         }
         if (ENERGY) energy += y * __ldg(lam + (size_t)dofs[k] * S + col);
         else R[(size_t)__ldg(st + k * NN) * S + col] = y;

@@ -70,6 +70,41 @@ __device__ __forceinline__ void vstore(float* p, const float (&r)[V]) {
   }
 }
 
+// acc[v] = fma(c, x[v], acc[v]) for the V right-hand sides of a thread, two
+// at a time by the paired FP32 FMA of sm_100+ (__ffma2_rn: each lane rounds
+// as fmaf, so the results are those of V scalar FMAs with half the issued
+// instructions); mul: acc[v] = c * x[v].
+template <int V>
+__device__ __forceinline__ void fma_v(float (&acc)[V], float c, const float (&x)[V]) {
+  if constexpr (V % 2 == 0) {
+    const float2 c2 = make_float2(c, c);
+#pragma unroll
+    for (int v = 0; v < V; v += 2) {
+      const float2 r = __ffma2_rn(c2, make_float2(x[v], x[v + 1]), make_float2(acc[v], acc[v + 1]));
+      acc[v] = r.x;
+      acc[v + 1] = r.y;
+    }
+  } else {
+#pragma unroll
+    for (int v = 0; v < V; v++) acc[v] = fmaf(c, x[v], acc[v]);
+  }
+}
+template <int V>
+__device__ __forceinline__ void mul_v(float (&acc)[V], float c, const float (&x)[V]) {
+  if constexpr (V % 2 == 0) {
+    const float2 c2 = make_float2(c, c);
+#pragma unroll
+    for (int v = 0; v < V; v += 2) {
+      const float2 r = __fmul2_rn(c2, make_float2(x[v], x[v + 1]));
+      acc[v] = r.x;
+      acc[v + 1] = r.y;
+    }
+  } else {
+#pragma unroll
+    for (int v = 0; v < V; v++) acc[v] = c * x[v];
+  }
+}
+
 template <int N, int E, int LB, int V>
 struct RsPlan {
   static constexpr int NN = N * N, Q = N * NN, Qp = elem_slots(N);
@@ -208,6 +243,8 @@ __global__ void __launch_bounds__(RsPlan<N, E, LB, V>::T, rs_min_ctas(RsPlan<N, 
         vstore<V>(s_u + wix(k * NN + ij), u[k]);
       }
       __syncthreads();
+      // the operation order of k_local_stiffness_rhs, written out as explicit
+      // FMAs so both forms round alike
       float vz[N][V];
 #pragma unroll
       for (int k = 0; k < N; k++) {
@@ -219,24 +256,23 @@ __global__ void __launch_bounds__(RsPlan<N, E, LB, V>::T, rs_min_ctas(RsPlan<N, 
           float rx[V], ry[V];
           vload<V>(s_u + wix(k * NN + j * N + a), rx);
           vload<V>(s_u + wix(k * NN + a * N + i), ry);
-          const float gza = Gm[a * N + k];
-#pragma unroll
-          for (int v = 0; v < V; v++) {
-            gz[v] += gza * u[a][v];
-            gx[v] += gci[a] * rx[v];
-            gy[v] += gcj[a] * ry[v];
-          }
+          fma_v<V>(gz, Gm[a * N + k], u[a]);
+          fma_v<V>(gx, gci[a], rx);
+          fma_v<V>(gy, gcj[a], ry);
         }
         const float* fk = f + k * NN;
         const float bxx = fk[0], bxy = fk[Qp], bxz = fk[2 * Qp];
         const float byy = fk[3 * Qp], byz = fk[4 * Qp], bzz = fk[5 * Qp];
         float ox[V], oy[V];
-#pragma unroll
-        for (int v = 0; v < V; v++) {
-          ox[v] = bxx * gx[v] + bxy * gy[v] + bxz * gz[v];
-          oy[v] = bxy * gx[v] + byy * gy[v] + byz * gz[v];
-          vz[k][v] = bxz * gx[v] + byz * gy[v] + bzz * gz[v];
-        }
+        mul_v<V>(ox, bxx, gx);
+        fma_v<V>(ox, bxy, gy);
+        fma_v<V>(ox, bxz, gz);
+        mul_v<V>(oy, bxy, gx);
+        fma_v<V>(oy, byy, gy);
+        fma_v<V>(oy, byz, gz);
+        mul_v<V>(vz[k], bxz, gx);
+        fma_v<V>(vz[k], byz, gy);
+        fma_v<V>(vz[k], bzz, gz);
         vstore<V>(s_vx + wix(k * NN + ij), ox);
         vstore<V>(s_vy + wix(k * NN + ij), oy);
       }
@@ -251,13 +287,9 @@ __global__ void __launch_bounds__(RsPlan<N, E, LB, V>::T, rs_min_ctas(RsPlan<N, 
           float rx[V], ry[V];
           vload<V>(s_vx + wix(k * NN + j * N + a), rx);
           vload<V>(s_vy + wix(k * NN + a * N + i), ry);
-          const float gka = Gm[k * N + a];
-#pragma unroll
-          for (int v = 0; v < V; v++) {
-            y[v] += gri[a] * rx[v];
-            y[v] += grj[a] * ry[v];
-            y[v] += gka * vz[a][v];
-          }
+          fma_v<V>(y, gri[a], rx);
+          fma_v<V>(y, grj[a], ry);
+          fma_v<V>(y, Gm[k * N + a], vz[a]);
         }
         vstore<V>(p.R + (size_t)__ldg(st + k * NN) * S + col, y);
       }
