@@ -360,8 +360,9 @@ int mj_mb_create(int n_runs, mj_lf* const* runs, mj_mb** out);
 int mj_mb_destroy(mj_mb* mb);
 
 /* Advances every run by nsteps steps; every run must have been initialised
- * (mj_lf_init).  use_graph != 0 replays a captured CUDA graph of 20 steps
- * (one kernel per step). */
+ * (mj_lf_init).  use_graph != 0 replays a captured CUDA graph of 20 steps.
+ * Every run needs the order-2 scheme (not mj_lf_set_scheme order 4).  The
+ * batch must be destroyed before its runs. */
 int mj_mb_advance(mj_mb* mb, int nsteps, int use_graph);
 
 /* Launch shape of the batch kernel: CTAs, CTAs per SM, element tiles and dof
@@ -369,7 +370,8 @@ int mj_mb_advance(mj_mb* mb, int nsteps, int use_graph);
  * index n = r+1 when every mesh has that order (the batch then runs the
  * kernel instance of that order alone), else 0.  Grouped by order
  * (mj_mb_grouping): tiles and chunks of all groups, CTAs of the largest
- * group.  Any output may be NULL. */
+ * group.  A union (mj_mb_union_info): its element kernel's CTAs and tiles
+ * and its streaming gather's chunks.  Any output may be NULL. */
 int mj_mb_info(const mj_mb* mb, int* grid, int* ctas_per_sm, int* n_tiles, int* n_chunks, int* graph,
                int* single_order);
 
@@ -382,16 +384,18 @@ int mj_mb_info(const mj_mb* mb, int* grid, int* ctas_per_sm, int* n_tiles, int* 
 int mj_mb_profile(mj_mb* mb, int enable);
 int mj_mb_phase_ms(const mj_mb* mb, double* out);
 
-/* Launch configuration chosen by timing both candidates on the batch at its
- * first advance (run states are restored afterwards): threads per CTA (256:
- * large tiles, 128: small tiles, more CTAs per SM; 0 before the first
- * advance) and the two candidates' ms per step (candidate_ms: room for 2,
- * may be NULL).  At most 48 runs per batch. */
+/* Launch configuration of the batch kernel, timed on the batch at its first
+ * advance (run states are restored afterwards): threads per CTA (256: large
+ * tiles, 128: small tiles, more CTAs per SM; 0 before the first advance) of
+ * the configuration in use, or of the faster one when another form runs
+ * (grouped: of the first group), and the two candidates' ms per step
+ * (candidate_ms: room for 2, may be NULL).  At most 48 runs per batch. */
 int mj_mb_tuning(const mj_mb* mb, int* threads, double* candidate_ms);
 
-/* Forces the launch configuration (threads = 128 or 256: one kernel of all
- * orders per step; -1: grouped by order, below), or 0 to time them again at
- * the next advance. */
+/* Forces the form of a step (threads = 128 or 256: one kernel of all orders
+ * per step; -1: grouped by order, below; -2: unions, below: of the whole
+ * batch when it has one order, else of every order group), or 0 to time the
+ * forms again at the next advance. */
 int mj_mb_set_config(mj_mb* mb, int threads);
 
 /* A batch of several orders also holds one sub-batch per order, each running
@@ -413,6 +417,22 @@ int mj_mb_grouping(const mj_mb* mb, int* grouped, int* n_groups, double* grouped
  * both forms (any output may be NULL). */
 int mj_mb_group_info(const mj_mb* mb, int group, int* order, int* n_runs, int* own_kernels, double* batch_ms,
                      double* own_ms);
+
+/* Union form.  The runs of one order (the whole batch, or an order group)
+ * can also step as ONE operator over the disjoint union of their meshes:
+ * dofs, elements and incidences concatenated in run order (every dof keeps
+ * its elements and its sum order, so results are bitwise those of the runs'
+ * own kernels), one autotuned element kernel and one streaming gather over
+ * all of them, then one launch applying each run's source with its own pulse,
+ * counter and dt.  The batch copies the runs' states into the union at the
+ * start of an advance and back at its end; factors changed since
+ * (mj_op_set_element_scale) are copied again at the next advance.  The
+ * autotuner times it beside the batch kernel (and, in a group, beside the
+ * runs' own kernels).  group = -1: the batch itself, else an order group.
+ * Reports whether that union steps the runs, its timed ms per step, its
+ * element kernel's tile size and its dofs (0 when the runs are too large for
+ * one union's int32 indexing and have none).  Any output may be NULL. */
+int mj_mb_union_info(const mj_mb* mb, int group, int* in_use, double* union_ms, int* tile_elems, int* n_dof);
 
 /* ---- media update and adjoint ------------------------------------------ */
 

@@ -151,6 +151,8 @@ def load(build_if_missing: bool = True):
     L.mj_mb_set_config.argtypes = [_VP, ctypes.c_int]
     L.mj_mb_grouping.argtypes = [_VP, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), _D]
     L.mj_mb_group_info.argtypes = [_VP, ctypes.c_int] + [ctypes.POINTER(ctypes.c_int)] * 3 + [_D, _D]
+    L.mj_mb_union_info.argtypes = [_VP, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _D,
+                                   ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     L.mj_stiffness_mltadd_static.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP, ctypes.c_double,
                                              _VP, ctypes.c_double, _VP, _VP]
     _lib = L

@@ -760,6 +760,7 @@ int mj_op_set_element_scale(mj_op* op, const double* scale) {
   count_launch();
   MJ_CUDA(cudaGetLastError());
   MJ_CUDA(cudaStreamSynchronize(op->stream));
+  op->fac_version++;
   return MJ_OK;
 }
 

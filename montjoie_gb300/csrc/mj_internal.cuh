@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <memory>
 #include <vector>
 
 #include "mj_common.cuh"
@@ -21,6 +22,7 @@ struct mj_op {
   mj::DevBuf nodle_pk;                  // packed connectivity: dof | rank << 27 (FP32 order 4), or empty
   mj::DevBuf err;                       // device error flag (bounded-wait timeouts)
   mj::DevBuf fac_orig;                  // factors before mj_op_set_element_scale (kept on first use)
+  int fac_version = 0;                  // bumped whenever fac_e changes after creation
   mj::DevBuf verts;                     // n_elt x 8 x 3 vertices (operators built from geometry)
   std::vector<int> h_ptr;               // CSR of incidences per dof (host copy)
   double gradphi[mj::kMaxN * mj::kMaxN];
@@ -202,6 +204,18 @@ int lfb_fused_check(mj_lfb* b, cudaStream_t s);
 // launches), on the given buffers (cur = U^n, overwritten by U^{n+2}; next =
 // U^{n+1}) and pulse-counter parity qc, on stream s (capturable).
 int lf_step_on(mj_lf* lf, void* cur, const void* next, int qc, cudaStream_t s);
+
+// The union of several FP32 order-2 runs of one order (mesh batch,
+// mj_multi.cu): one operator over the disjoint union of their meshes (dofs,
+// elements and incidences concatenated in run order, so every dof keeps its
+// elements and its sum order) with a tuned element kernel, and an integrator
+// state over the union's dofs (dt^2/D and 1/D of each run at its offset, no
+// sources: the batch applies each run's own).  dof_off/elt_off: each run's
+// first dof and element in the union.  union_copy_factors: the factors of run
+// operator op into the union at element elt_off (after a change of op's).
+int lf_union_create(const std::vector<mj_lf*>& runs, std::unique_ptr<mj_op>* uop, std::unique_ptr<mj_lf>* ulf,
+                    std::vector<int>* dof_off, std::vector<int>* elt_off);
+int union_copy_factors(mj_op* uop, const mj_op* op, int elt_off, cudaStream_t s);
 
 // Single-order instances of the many-mesh batch kernel (mj_multi_one.cu):
 // the kernel for `threads` per CTA and order n (2..9), and the FP32

@@ -45,6 +45,57 @@
 
 using namespace mj;
 
+namespace mj {
+
+// Per-run source state of a union group (kernel parameter): each run keeps
+// its own pulse, step counters and dt; qc_par is the run's counter parity at
+// the uploaded table (step k of the batch reads ctr[(k + qc_par) & 1]).
+struct UnionRun {
+  int* ctr;
+  const double* pulse;
+  double dt2;
+  int n_pulse, qc_par;
+};
+struct UnionRuns {
+  UnionRun r[kMaxRuns];
+  int n;
+};
+
+// Sources of a union group's step k, after its streaming gather: every run's
+// entries with that run's pulse, in the arithmetic of the source term of the
+// run's own streaming gather (u = u + dt^2 (1/D) p f in FP64, rounded once),
+// so the union steps bitwise like the runs' own kernels.  Block 0 advances
+// every run's counters as the run's own gather does.
+static __global__ void k_union_sources(const __grid_constant__ UnionRuns runs, int k, const int* __restrict__ sdof,
+                                const int* __restrict__ srun, const float* __restrict__ sval, int n_src,
+                                const double* __restrict__ inv_mass, float* __restrict__ u) {
+  if (blockIdx.x == 0 && threadIdx.x < runs.n) {
+    const UnionRun& q = runs.r[threadIdx.x];
+    const int qc = (k + q.qc_par) & 1;
+    q.ctr[1 - qc] = q.ctr[qc] + 1;
+  }
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n_src; e += gridDim.x * blockDim.x) {
+    const UnionRun& q = runs.r[srun[e]];
+    const int step = q.ctr[(k + q.qc_par) & 1];
+    const float f = sval[e];
+    if (step >= q.n_pulse || f == 0.f) continue;
+    const int d = sdof[e];
+    u[d] = float(double(u[d]) + q.dt2 * inv_mass[d] * q.pulse[step] * double(f));
+  }
+}
+
+// A group's runs stepped as one union operator (lf_union_create).
+struct UnionGroup {
+  std::unique_ptr<mj_op> op;
+  std::unique_ptr<mj_lf> lf;
+  std::vector<int> dof_off, elt_off, fac_version;
+  DevBuf sdof, srun, sval;
+  int n_src = 0;
+  UnionRuns table{};
+};
+
+}  // namespace mj
+
 struct mj_mb {
   std::vector<mj_lf*> runs;
   DevBuf sync, err;
@@ -54,7 +105,7 @@ struct mj_mb {
   MbLists cfg[2];   // 0: 256 threads, 1: 128 threads
   int only = 0;     // the order n of every mesh (single-order kernels), or 0
   int use = -1;     // configuration in use (-1: not tuned yet)
-  double tune_ms[3] = {0, 0, 0};  // one kernel (256, 128 threads), grouped by order
+  double tune_ms[4] = {0, 0, 0, 0};  // one kernel (256, 128 threads), grouped by order, union
   // launch parity of the uploaded table: per run (cur_is_a, step & 1) at upload
   std::vector<int> base_cur, base_qc;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // 20 steps starting at k = 0 or k = 1
@@ -70,6 +121,12 @@ struct mj_mb {
   // the other, when that is faster for its meshes (chosen by timing).
   bool seq = false;
   double seq_ms = 0, batch_ms = 0;
+  // A batch of one order may also step its runs as one union operator
+  // (use == 3): one tuned element kernel, one streaming gather and one source
+  // launch per step over all its meshes, on copies of the runs' states taken
+  // at the start of each advance and handed back at its end.
+  std::unique_ptr<UnionGroup> uni;
+  bool force_union = false;  // mj_mb_set_config(-2)
   ~mj_mb() {
     for (auto& g : graph)
       if (g) cudaGraphExecDestroy(g);
@@ -123,15 +180,130 @@ int mb_launch_seq(mj_mb* mb, int k, cudaStream_t s) {
   return MJ_OK;
 }
 
-int mb_launch(mj_mb* mb, int which, int k, cudaStream_t s) {
-  if (which == 2) {  // one launch per order group (or its runs' own kernels)
+// Step k of a union batch, i steps after the runs' states were copied into
+// the union: the union's two state buffers swap roles with the parity of i.
+int mb_launch_union(mj_mb* mb, int k, int i, cudaStream_t s) {
+  UnionGroup* u = mb->uni.get();
+  mj_lf* lf = u->lf.get();
+  float* cur = (i & 1) ? lf->ub.as<float>() : lf->ua.as<float>();
+  const float* next = (i & 1) ? lf->ua.as<float>() : lf->ub.as<float>();
+  if (int rc = lf_step_on(lf, cur, next, i & 1, s)) return rc;
+  const int blocks = std::max(1, std::min((u->n_src + 255) / 256, 1024));
+  k_union_sources<<<blocks, 256, 0, s>>>(u->table, k, u->sdof.as<int>(), u->srun.as<int>(), u->sval.as<float>(),
+                                         u->n_src, lf->inv_mass64.as<double>(), cur);
+  count_launch();
+  MJ_CUDA(cudaGetLastError());
+  return MJ_OK;
+}
+
+// Step k of the batch in form `which` (0/1: one kernel of 256/128 threads;
+// 2: one launch per order group; 3: the union), i steps into the advance.
+int mb_launch(mj_mb* mb, int which, int k, int i, cudaStream_t s) {
+  if (which == 2) {  // one launch per order group (or its runs' own kernels, or its union)
     for (auto& g : mb->groups) {
-      const int rc = g->seq ? mb_launch_seq(g.get(), k, s) : mb_launch(g.get(), g->use, k, s);
+      const int rc = g->seq ? mb_launch_seq(g.get(), k, s) : mb_launch(g.get(), g->use, k, i, s);
       if (rc) return rc;
     }
     return MJ_OK;
   }
+  if (which == 3) return mb_launch_union(mb, k, i, s);
   return which == 0 ? mb_launch_t<256>(mb, mb->cfg[0], k, s) : mb_launch_t<128>(mb, mb->cfg[1], k, s);
+}
+
+// Kernel launches of one step in the batch's chosen form.
+uint64_t mb_launches_per_step(const mj_mb* mb) {
+  if (mb->use == 3) return 3;  // element kernel, streaming gather, sources
+  if (mb->use != 2) return 1;
+  uint64_t n = 0;
+  for (auto& g : mb->groups) n += g->seq ? 2 * g->runs.size() : mb_launches_per_step(g.get());
+  return n;
+}
+
+// The union copies of the runs' states: in, before the steps of an advance
+// (U^n, U^{n+1} of every run at its offset); out, after `steps` steps and the
+// runs' role update, back into each run's own buffers.
+int union_copy(mj_mb* mb, bool in, int steps, cudaStream_t s) {
+  UnionGroup* u = mb->uni.get();
+  float* A = u->lf->ua.as<float>();
+  float* B = u->lf->ub.as<float>();
+  float* ucur = (steps & 1) ? B : A;
+  float* unext = (steps & 1) ? A : B;
+  for (size_t r = 0; r < mb->runs.size(); r++) {
+    mj_lf* lf = mb->runs[r];
+    const size_t bytes = sizeof(float) * lf->n_dof;
+    float* c = ucur + u->dof_off[r];
+    float* x = unext + u->dof_off[r];
+    if (in) {
+      MJ_CUDA(cudaMemcpyAsync(c, lf->cur(), bytes, cudaMemcpyDeviceToDevice, s));
+      MJ_CUDA(cudaMemcpyAsync(x, lf->next(), bytes, cudaMemcpyDeviceToDevice, s));
+    } else {
+      MJ_CUDA(cudaMemcpyAsync(lf->cur(), c, bytes, cudaMemcpyDeviceToDevice, s));
+      MJ_CUDA(cudaMemcpyAsync(lf->next(), x, bytes, cudaMemcpyDeviceToDevice, s));
+    }
+  }
+  return MJ_OK;
+}
+
+// union_copy for every union the batch's chosen form steps.
+int mb_union_copy(mj_mb* mb, bool in, int steps, cudaStream_t s) {
+  if (mb->use == 3) return union_copy(mb, in, steps, s);
+  if (mb->use == 2)
+    for (auto& g : mb->groups)
+      if (!g->seq && g->use == 3)
+        if (int rc = union_copy(g.get(), in, steps, s)) return rc;
+  return MJ_OK;
+}
+
+// Factors of a run's operator changed since they were copied into the union
+// (mj_op_set_element_scale): copy them again.
+int mb_union_refresh(mj_mb* mb, cudaStream_t s) {
+  for (auto& g : mb->groups)
+    if (int rc = mb_union_refresh(g.get(), s)) return rc;
+  UnionGroup* u = mb->uni.get();
+  if (!u) return MJ_OK;
+  for (size_t r = 0; r < mb->runs.size(); r++) {
+    const mj_op* op = mb->runs[r]->op;
+    if (u->fac_version[r] == op->fac_version) continue;
+    if (int rc = union_copy_factors(u->op.get(), op, u->elt_off[r], s)) return rc;
+    u->fac_version[r] = op->fac_version;
+  }
+  return MJ_OK;
+}
+
+// The union of a batch of one order, with every run's sources at the run's
+// offset; a batch too large for one union's int32 indexing gets none.
+int mb_union_create(mj_mb* mb) {
+  std::unique_ptr<UnionGroup> u(new UnionGroup());
+  const int rc = lf_union_create(mb->runs, &u->op, &u->lf, &u->dof_off, &u->elt_off);
+  if (rc == MJ_ERR_ARG) return MJ_OK;
+  if (rc) return rc;
+  std::vector<int> sdof, srun;
+  std::vector<float> sval;
+  for (size_t r = 0; r < mb->runs.size(); r++) {
+    mj_lf* lf = mb->runs[r];
+    u->fac_version.push_back(lf->op->fac_version);
+    if (!lf->n_src) continue;
+    std::vector<int> idx(lf->n_src);
+    std::vector<float> val(lf->n_src);
+    MJ_CUDA(cudaMemcpy(idx.data(), lf->src_idx.ptr, sizeof(int) * lf->n_src, cudaMemcpyDeviceToHost));
+    MJ_CUDA(cudaMemcpy(val.data(), lf->src_val.ptr, sizeof(float) * lf->n_src, cudaMemcpyDeviceToHost));
+    for (int t = 0; t < lf->n_src; t++) {
+      sdof.push_back(u->dof_off[r] + idx[t]);
+      srun.push_back((int)r);
+      sval.push_back(val[t]);
+    }
+  }
+  u->n_src = (int)sdof.size();
+  MJ_CUDA(u->sdof.alloc(sizeof(int) * std::max<size_t>(1, sdof.size())));
+  MJ_CUDA(u->srun.alloc(sizeof(int) * std::max<size_t>(1, srun.size())));
+  MJ_CUDA(u->sval.alloc(sizeof(float) * std::max<size_t>(1, sval.size())));
+  if (u->n_src) {
+    MJ_CUDA(cudaMemcpy(u->sdof.ptr, sdof.data(), sizeof(int) * sdof.size(), cudaMemcpyHostToDevice));
+    MJ_CUDA(cudaMemcpy(u->srun.ptr, srun.data(), sizeof(int) * srun.size(), cudaMemcpyHostToDevice));
+    MJ_CUDA(cudaMemcpy(u->sval.ptr, sval.data(), sizeof(float) * sval.size(), cudaMemcpyHostToDevice));
+  }
+  mb->uni = std::move(u);
+  return MJ_OK;
 }
 
 // Tile and chunk lists of configuration T: tiles sorted by decreasing cost
@@ -194,8 +366,12 @@ void mb_upload(mj_mb* mb) {
     mb->base_cur[r] = lf->cur_is_a ? 1 : 0;
     mb->base_qc[r] = lf->step & 1;
     mb->table.m[r] = mb->h_mesh[r];
+    if (mb->uni)
+      mb->uni->table.r[r] = {lf->ctr.as<int>(), lf->pulse_d.as<double>(), lf->dt * lf->dt, lf->n_pulse,
+                             mb->h_mesh[r].qc_par};
   }
   mb->table.n = (int)n;
+  if (mb->uni) mb->uni->table.n = (int)n;
   for (auto& g : mb->graph)
     if (g) {
       cudaGraphExecDestroy(g);
@@ -229,6 +405,7 @@ int mb_check_err(mj_mb* mb, cudaStream_t s) {
       for (mj_lf* lf : g->runs)
         if (take_kernel_error(lf->op->err.ptr, s, "mj_mb_advance")) herr = 1;
   }
+  if (mb->uni && take_kernel_error(mb->uni->op->err.ptr, s, "mj_mb_advance")) herr = 1;
   int own = 0;
   MJ_CUDA(cudaMemcpyAsync(&own, mb->err.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
   MJ_CUDA(cudaStreamSynchronize(s));
@@ -242,8 +419,11 @@ int mb_check_err(mj_mb* mb, cudaStream_t s) {
   return MJ_OK;
 }
 
-// Times both launch configurations on the batch itself (3 steps each after
-// one warm-up) and keeps the faster.  The runs' states and step counters are
+// Times the batch's forms on the batch itself (3 steps each after one
+// warm-up) and keeps the fastest: one kernel of 256 or 128 threads; for
+// several orders, one launch per order group (each group batched, on its
+// runs' own kernels or as its union, whichever its own timing favours); for
+// one order, the union of its runs.  The runs' states and step counters are
 // saved before and restored after, so tuning leaves no trace.
 int mb_autotune(mj_mb* mb, int off, cudaStream_t s) {
   const size_t n = mb->runs.size();
@@ -264,33 +444,34 @@ int mb_autotune(mj_mb* mb, int off, cudaStream_t s) {
   MJ_CUDA(cudaEventCreate(&e1));
   const uint64_t before = launch_counter().load();
   int best = 0;
-  const int n_modes = mb->groups.empty() ? 2 : 3;
-  for (int c = 0; c < n_modes; c++) {
-    if (c == 2)  // each order group picks its launch configuration, then batched or its runs' own kernels
+  std::vector<int> forms = {0, 1};
+  if (!mb->groups.empty()) forms.push_back(2);
+  if (mb->uni) forms.push_back(3);
+  for (int c : forms) {
+    int rc = MJ_OK;
+    if (c == 3) rc = union_copy(mb, true, 0, s);  // the union steps from the runs' states
+    if (c == 2)  // each order group picks its form, then batched or its runs' own kernels
       for (auto& g : mb->groups) {
-        int rc = g->use < 0 ? mb_autotune(g.get(), off, s) : MJ_OK;
+        if (!rc && g->use < 0) rc = mb_autotune(g.get(), off, s);
+        if (!rc && g->use == 3) rc = union_copy(g.get(), true, 0, s);
         for (int form = 0; !rc && form < 2; form++) {
           g->seq = form == 1;
-          rc = mb_launch(mb, 2, off, s) == MJ_OK ? MJ_OK : MJ_ERR_CUDA;  // warm-up of the whole grouped step
+          rc = mb_launch(mb, 2, off, 0, s) == MJ_OK ? MJ_OK : MJ_ERR_CUDA;  // warm-up of the whole grouped step
           if (!rc) rc = cudaEventRecord(e0, s) == cudaSuccess ? MJ_OK : MJ_ERR_CUDA;
           for (int i = 1; !rc && i <= 3; i++)
-            rc = g->seq ? mb_launch_seq(g.get(), off + i, s) : mb_launch(g.get(), g->use, off + i, s);
+            rc = g->seq ? mb_launch_seq(g.get(), off + i, s) : mb_launch(g.get(), g->use, off + i, i, s);
           if (!rc) rc = cudaEventRecord(e1, s) == cudaSuccess ? MJ_OK : MJ_ERR_CUDA;
           if (!rc) rc = mb_check_err(mb, s);
           float ms = 0.f;
           if (!rc) rc = cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess ? MJ_OK : MJ_ERR_CUDA;
           (form ? g->seq_ms : g->batch_ms) = ms / 3.0;
         }
-        if (rc) {
-          cudaEventDestroy(e0);
-          cudaEventDestroy(e1);
-          return rc;
-        }
+        if (rc) break;
         g->seq = g->seq_ms < g->batch_ms;
       }
-    int rc = mb_launch(mb, c, off, s);
+    if (!rc) rc = mb_launch(mb, c, off, 0, s);
     if (!rc) rc = cudaEventRecord(e0, s) == cudaSuccess ? MJ_OK : MJ_ERR_CUDA;
-    for (int i = 1; !rc && i <= 3; i++) rc = mb_launch(mb, c, off + i, s);
+    for (int i = 1; !rc && i <= 3; i++) rc = mb_launch(mb, c, off + i, i, s);
     if (!rc) rc = cudaEventRecord(e1, s) == cudaSuccess ? MJ_OK : MJ_ERR_CUDA;
     if (!rc) rc = mb_check_err(mb, s);
     float ms = 0.f;
@@ -332,6 +513,7 @@ int mb_create(int n_runs, mj_lf* const* runs, bool split, std::unique_ptr<mj_mb>
     MJ_CHECK_ARG(lf, "mj_mb_create: null run");
     const mj_op* op = lf->op;
     MJ_CHECK_ARG(op->precision == MJ_FP32, "mj_mb_create: every run needs an MJ_FP32 operator");
+    MJ_CHECK_ARG(lf->time_order == 2, "mj_mb_create: every run needs the order-2 leap-frog");
     MJ_CHECK_ARG(op->n >= 2 && op->n <= kMaxNK, "mj_mb_create: order out of range");
     MJ_CHECK_ARG(std::find(ops.begin(), ops.end(), op) == ops.end(), "mj_mb_create: runs share an operator");
     ops.push_back(op);
@@ -430,6 +612,8 @@ int mb_create(int n_runs, mj_lf* const* runs, bool split, std::unique_ptr<mj_mb>
   MJ_CUDA(mb->stamps.alloc(sizeof(unsigned long long) * kStamps *
                            std::max(mb->cfg[0].grid, mb->cfg[1].grid)));
   mb->stream = runs[0]->stream;
+  if (mb->only)
+    if (int rc = mb_union_create(mb.get())) return rc;
   if (split && !mb->only) {
     for (int n = 2; n <= kMaxNK; n++) {
       if (!have_g[n]) continue;
@@ -485,6 +669,7 @@ int mj_mb_advance(mj_mb* mb, int nsteps, int use_graph) {
     mb_upload(mb);
     off = 0;
   }
+  if (int rc = mb_union_refresh(mb, s)) return rc;
   if (mb->use < 0) {
     const int rc = mb_autotune(mb, off, s);
     if (rc) return rc;
@@ -495,6 +680,7 @@ int mj_mb_advance(mj_mb* mb, int nsteps, int use_graph) {
         const int rc = mb_autotune(g.get(), off, s);
         if (rc) return rc;
       }
+  if (int rc = mb_union_copy(mb, true, 0, s)) return rc;
   mb->last_graph = false;
   int done = 0;
   if (use_graph && !mb->profile && nsteps >= kGraphStepsMb) {
@@ -505,7 +691,7 @@ int mj_mb_advance(mj_mb* mb, int nsteps, int use_graph) {
       const uint64_t before = launch_counter().load();
       MJ_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
       for (int k = 0; k < kGraphStepsMb; k++) {
-        const int rc = mb_launch(mb, mb->use, off + k, cs);
+        const int rc = mb_launch(mb, mb->use, off + k, k, cs);
         if (rc) {
           cudaStreamEndCapture(cs, &g);
           cudaStreamDestroy(cs);
@@ -518,12 +704,7 @@ int mj_mb_advance(mj_mb* mb, int nsteps, int use_graph) {
       cudaGraphDestroy(g);
       cudaStreamDestroy(cs);
     }
-    // kernels per step: one, or one per order group (two per run of a group on its runs' own kernels)
-    uint64_t per_step = 1;
-    if (mb->use == 2) {
-      per_step = 0;
-      for (auto& g : mb->groups) per_step += g->seq ? 2 * g->runs.size() : 1;
-    }
+    const uint64_t per_step = mb_launches_per_step(mb);
     while (nsteps - done >= kGraphStepsMb) {
       MJ_CUDA(cudaGraphLaunch(mb->graph[off], s));
       count_launch(kGraphStepsMb * per_step);
@@ -532,13 +713,14 @@ int mj_mb_advance(mj_mb* mb, int nsteps, int use_graph) {
     mb->last_graph = true;
   }
   for (; done < nsteps; done++) {
-    const int rc = mb_launch(mb, mb->use, off + done, s);
+    const int rc = mb_launch(mb, mb->use, off + done, done, s);
     if (rc) return rc;
   }
   for (mj_lf* lf : mb->runs) {
     lf->step += nsteps;
     if (nsteps & 1) lf->cur_is_a = !lf->cur_is_a;
   }
+  if (int rc = mb_union_copy(mb, false, nsteps, s)) return rc;
   return mb_check_err(mb, s);
 }
 
@@ -552,9 +734,14 @@ int mj_mb_profile(mj_mb* mb, int enable) {
 int mj_mb_phase_ms(const mj_mb* mb, double* out) {
   MJ_CHECK_ARG(mb && out, "mj_mb_phase_ms: null argument");
   MJ_CHECK_ARG(mb->use >= 0, "mj_mb_phase_ms: no step has run");
-  if (mb->use == 2) {  // grouped by order: each phase summed over the groups' launches
+  if (mb->use == 3) {  // the union's kernels carry no phase stamps
+    for (int i = 0; i < 6; i++) out[i] = 0.0;
+    return MJ_OK;
+  }
+  if (mb->use == 2) {  // grouped by order: each phase summed over the groups' batch-kernel launches
     for (int i = 0; i < 6; i++) out[i] = 0.0;
     for (auto& g : mb->groups) {
+      if (g->seq) continue;
       double o[6];
       const int rc = mj_mb_phase_ms(g.get(), o);
       if (rc) return rc;
@@ -590,29 +777,44 @@ int mj_mb_phase_ms(const mj_mb* mb, double* out) {
 int mj_mb_info(const mj_mb* mb, int* grid, int* ctas_per_sm, int* n_tiles, int* n_chunks, int* graph,
                int* single_order) {
   MJ_CHECK_ARG(mb, "mj_mb_info: null batch");
-  if (mb->use == 2) {  // grouped by order: the groups' totals, the launch shape of the largest group
-    int tiles = 0, chunks = 0, best = 0;
-    for (size_t i = 0; i < mb->groups.size(); i++) {
-      const mj_mb* g = mb->groups[i].get();
-      const MbLists& L = g->cfg[std::max(0, g->use)];
-      tiles += L.n_work;
-      chunks += L.n_chunks;
-      const mj_mb* b = mb->groups[best].get();
-      if (L.n_work > b->cfg[std::max(0, b->use)].n_work) best = (int)i;
+  // the launch shape of a form: a batch kernel's lists, or the union's element
+  // kernel (its tiles) and streaming gather (its chunks)
+  auto shape = [](const mj_mb* b, int* gr, int* cps, int* tiles, int* chunks) {
+    if (b->use == 3) {
+      const mj_op* op = b->uni->op.get();
+      *gr = op->grid_k1;
+      *cps = std::max(1, op->grid_k1 / sm_count());
+      *tiles = op->n_tiles;
+      *chunks = b->uni->lf->n_stream_chunks;
+      return;
     }
-    const mj_mb* b = mb->groups[best].get();
-    const MbLists& L = b->cfg[std::max(0, b->use)];
-    if (grid) *grid = L.grid;
-    if (ctas_per_sm) *ctas_per_sm = L.ctas_per_sm;
-    if (n_tiles) *n_tiles = tiles;
-    if (n_chunks) *n_chunks = chunks;
+    const MbLists& L = b->cfg[std::max(0, std::min(1, b->use))];
+    *gr = L.grid;
+    *cps = L.ctas_per_sm;
+    *tiles = L.n_work;
+    *chunks = L.n_chunks;
+  };
+  int gr = 0, cps = 0, tiles = 0, chunks = 0;
+  if (mb->use == 2) {  // grouped by order: the groups' totals, the launch shape of the largest group
+    int best_tiles = -1;
+    for (const auto& g : mb->groups) {
+      int g1, c1, t1, k1;
+      shape(g.get(), &g1, &c1, &t1, &k1);
+      tiles += t1;
+      chunks += k1;
+      if (t1 > best_tiles) {
+        best_tiles = t1;
+        gr = g1;
+        cps = c1;
+      }
+    }
   } else {
-    const MbLists& L = mb->cfg[mb->use < 0 ? 0 : mb->use];
-    if (grid) *grid = L.grid;
-    if (ctas_per_sm) *ctas_per_sm = L.ctas_per_sm;
-    if (n_tiles) *n_tiles = L.n_work;
-    if (n_chunks) *n_chunks = L.n_chunks;
+    shape(mb, &gr, &cps, &tiles, &chunks);
   }
+  if (grid) *grid = gr;
+  if (ctas_per_sm) *ctas_per_sm = cps;
+  if (n_tiles) *n_tiles = tiles;
+  if (n_chunks) *n_chunks = chunks;
   if (graph) *graph = mb->last_graph ? 1 : 0;
   if (single_order) *single_order = mb->only;
   return MJ_OK;
@@ -620,11 +822,25 @@ int mj_mb_info(const mj_mb* mb, int* grid, int* ctas_per_sm, int* n_tiles, int* 
 
 int mj_mb_set_config(mj_mb* mb, int threads) {
   MJ_CHECK_ARG(mb, "mj_mb_set_config: null batch");
-  MJ_CHECK_ARG(threads == 0 || threads == 128 || threads == 256 || threads == -1,
-               "mj_mb_set_config: threads must be 0, 128, 256 or -1");
+  MJ_CHECK_ARG(threads == 0 || threads == 128 || threads == 256 || threads == -1 || threads == -2,
+               "mj_mb_set_config: threads must be 0, 128, 256, -1 or -2");
   MJ_CHECK_ARG(threads != -1 || !mb->groups.empty(), "mj_mb_set_config: the batch has one order (no groups)");
-  mb->use = threads == 0 ? -1 : threads == 256 ? 0 : threads == 128 ? 1 : 2;
-  for (auto& g : mb->groups) g->use = -1;  // groups tune again at the next advance
+  if (threads == -2) {  // the union: of the whole batch (one order) or of every order group
+    if (mb->groups.empty()) {
+      MJ_CHECK_ARG(mb->uni, "mj_mb_set_config: the batch is too large for one union");
+      mb->use = 3;
+    } else {
+      for (auto& g : mb->groups) MJ_CHECK_ARG(g->uni, "mj_mb_set_config: a group is too large for one union");
+      mb->use = 2;
+      for (auto& g : mb->groups) {
+        g->use = 3;
+        g->seq = false;
+      }
+    }
+  } else {
+    mb->use = threads == 0 ? -1 : threads == 256 ? 0 : threads == 128 ? 1 : 2;
+    for (auto& g : mb->groups) g->use = -1;  // groups tune again at the next advance
+  }
   for (auto& g : mb->graph)
     if (g) {
       cudaGraphExecDestroy(g);
@@ -655,14 +871,29 @@ int mj_mb_group_info(const mj_mb* mb, int group, int* order, int* n_runs, int* o
 
 int mj_mb_tuning(const mj_mb* mb, int* threads, double* candidate_ms) {
   MJ_CHECK_ARG(mb, "mj_mb_tuning: null batch");
-  if (threads)
-    *threads = mb->use < 0 ? 0
-               : mb->use == 2 ? mb->groups[0]->cfg[std::max(0, mb->groups[0]->use)].threads
-                              : mb->cfg[mb->use].threads;
+  if (threads) {
+    // the batch kernel's configuration: the one in use, else the faster of
+    // the two timed (of the first group when grouped)
+    const mj_mb* b = mb->use == 2 ? mb->groups[0].get() : mb;
+    int c = b->use;
+    if (c != 0 && c != 1) c = (b->tune_ms[1] > 0 && b->tune_ms[1] < b->tune_ms[0]) ? 1 : 0;
+    *threads = mb->use < 0 ? 0 : b->cfg[c].threads;
+  }
   if (candidate_ms) {
     candidate_ms[0] = mb->tune_ms[0];
     candidate_ms[1] = mb->tune_ms[1];
   }
+  return MJ_OK;
+}
+
+int mj_mb_union_info(const mj_mb* mb, int group, int* in_use, double* union_ms, int* tile_elems, int* n_dof) {
+  MJ_CHECK_ARG(mb, "mj_mb_union_info: null batch");
+  MJ_CHECK_ARG(group >= -1 && group < (int)mb->groups.size(), "mj_mb_union_info: no such group");
+  const mj_mb* b = group < 0 ? mb : mb->groups[group].get();
+  if (in_use) *in_use = (group < 0 ? mb->use == 3 : (mb->use == 2 && !b->seq && b->use == 3)) ? 1 : 0;
+  if (union_ms) *union_ms = b->tune_ms[3];
+  if (tile_elems) *tile_elems = b->uni ? b->uni->op->E : 0;
+  if (n_dof) *n_dof = b->uni ? b->uni->op->n_dof : 0;
   return MJ_OK;
 }
 

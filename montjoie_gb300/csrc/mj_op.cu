@@ -1441,3 +1441,141 @@ int mj::lf_step_on(mj_lf* lf, void* cur, const void* next, int qc, cudaStream_t 
   MJ_CUDA(cudaGetLastError());
   return MJ_OK;
 }
+
+// ---- union of several runs of one order (mesh batch) ------------------------
+
+namespace mj {
+
+// Element-major connectivity and slots of one run, shifted into the union:
+// points of the element get the run's dof and incidence offsets, padding
+// points the union's spare dof 0 and spare slot.
+static __global__ void k_union_remap(const int* __restrict__ nodle, const int* __restrict__ slot, long long n, int Qp,
+                              int Q, int dof_off, int inc_off, int pad_slot, int* __restrict__ onodle,
+                              int* __restrict__ oslot) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    if ((int)(t % Qp) < Q) {
+      onodle[t] = nodle[t] + dof_off;
+      oslot[t] = slot[t] + inc_off;
+    } else {
+      onodle[t] = 0;
+      oslot[t] = pad_slot;
+    }
+  }
+}
+
+static __global__ void k_fill_int(int* __restrict__ a, long long n, int v) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+    a[t] = v;
+}
+
+static int grid_for_len(long long n) { return (int)std::max(1LL, std::min<long long>((n + 255) / 256, 4096)); }
+
+}  // namespace mj
+
+int mj::union_copy_factors(mj_op* uop, const mj_op* op, int elt_off, cudaStream_t s) {
+  const size_t per = (size_t)6 * op->Qp * sizeof(float);
+  MJ_CUDA(cudaMemcpyAsync(uop->fac_e.as<char>() + (size_t)elt_off * per, op->fac_e.ptr, (size_t)op->n_elt * per,
+                          cudaMemcpyDeviceToDevice, s));
+  return MJ_OK;
+}
+
+int mj::lf_union_create(const std::vector<mj_lf*>& runs, std::unique_ptr<mj_op>* uop_out,
+                        std::unique_ptr<mj_lf>* ulf_out, std::vector<int>* dof_off, std::vector<int>* elt_off) {
+  MJ_CHECK_ARG(!runs.empty(), "union: no runs");
+  const mj_op* op0 = runs[0]->op;
+  long long n_elt = 0, n_dof = 0, n_inc = 0;
+  dof_off->clear();
+  elt_off->clear();
+  for (mj_lf* lf : runs) {
+    const mj_op* op = lf->op;
+    MJ_CHECK_ARG(op->precision == MJ_FP32 && op->n == op0->n && lf->time_order == 2,
+                 "union: the runs need FP32 operators of one order and the order-2 scheme");
+    for (int a = 0; a < op->n * op->n; a++)
+      MJ_CHECK_ARG(op->gradphi[a] == op0->gradphi[a], "union: the runs use different derivative matrices");
+    dof_off->push_back((int)n_dof);
+    elt_off->push_back((int)n_elt);
+    n_elt += op->n_elt;
+    n_dof += op->n_dof;
+    n_inc += (long long)op->n_inc;
+  }
+  const int Qp = op0->Qp, Q = op0->Q;
+  const long long n_elt_pad = (n_elt + kElemPad - 1) / kElemPad * kElemPad;
+  MJ_CHECK_ARG(n_dof < INT32_MAX - 8 && n_inc < INT32_MAX - 8 && n_elt_pad * Qp < INT32_MAX - 1 &&
+                   n_elt * Q < (1LL << 31) - 1,
+               "union: the runs together exceed int32 indexing");
+  std::unique_ptr<mj_op> u(new mj_op());
+  u->order = op0->order; u->n = op0->n; u->Q = Q; u->Qp = Qp;
+  u->n_elt = (int)n_elt; u->n_elt_pad = (int)n_elt_pad; u->n_dof = (int)n_dof; u->precision = MJ_FP32;
+  u->r_len = (size_t)n_elt_pad * Qp;
+  u->n_inc = (size_t)n_inc;
+  std::copy(op0->gradphi, op0->gradphi + op0->n * op0->n, u->gradphi);
+  u->h_ptr.assign((size_t)n_dof + 1, 0);
+  for (size_t r = 0; r < runs.size(); r++) {
+    const mj_op* op = runs[r]->op;
+    const int base = op->h_ptr[0];  // 0
+    const int inc0 = u->h_ptr[(*dof_off)[r]];
+    for (int d = 0; d < op->n_dof; d++) u->h_ptr[(size_t)(*dof_off)[r] + d + 1] = inc0 + op->h_ptr[d + 1] - base;
+  }
+  cudaStream_t s = u->stream;
+  MJ_CUDA(u->nodle_e.alloc(sizeof(int) * u->r_len));
+  MJ_CUDA(u->slot_e.alloc(sizeof(int) * u->r_len));
+  MJ_CUDA(u->fac_e.alloc((size_t)n_elt_pad * 6 * Qp * sizeof(float)));
+  MJ_CUDA(u->R.alloc(sizeof(float) * (u->n_inc + 4)));
+  MJ_CUDA(u->ptr.alloc(sizeof(int) * ((size_t)n_dof + 8)));
+  MJ_CUDA(u->err.alloc(sizeof(int)));
+  MJ_CUDA(cudaMemsetAsync(u->err.ptr, 0, sizeof(int), s));
+  MJ_CUDA(cudaMemsetAsync(u->ptr.ptr, 0, sizeof(int) * ((size_t)n_dof + 8), s));
+  MJ_CUDA(cudaMemsetAsync(u->R.ptr, 0, sizeof(float) * (u->n_inc + 4), s));
+  MJ_CUDA(cudaMemsetAsync(u->fac_e.ptr, 0, u->fac_e.bytes, s));
+  MJ_CUDA(cudaMemsetAsync(u->nodle_e.ptr, 0, u->nodle_e.bytes, s));
+  k_fill_int<<<grid_for_len((long long)u->r_len), 256, 0, s>>>(u->slot_e.as<int>(), (long long)u->r_len,
+                                                                (int)u->n_inc);
+  count_launch();
+  for (size_t r = 0; r < runs.size(); r++) {
+    const mj_op* op = runs[r]->op;
+    const long long len = (long long)op->n_elt * Qp;
+    const size_t at = (size_t)(*elt_off)[r] * Qp;
+    k_union_remap<<<grid_for_len(len), 256, 0, s>>>(op->nodle_e.as<int>(), op->slot_e.as<int>(), len, Qp, Q,
+                                                    (*dof_off)[r], u->h_ptr[(*dof_off)[r]], (int)u->n_inc,
+                                                    u->nodle_e.as<int>() + at, u->slot_e.as<int>() + at);
+    count_launch();
+    if (int rc = union_copy_factors(u.get(), op, (*elt_off)[r], s)) return rc;
+  }
+  MJ_CUDA(cudaMemcpyAsync(u->ptr.ptr, u->h_ptr.data(), sizeof(int) * ((size_t)n_dof + 1), cudaMemcpyHostToDevice, s));
+  MJ_CUDA(cudaStreamSynchronize(s));
+  MJ_CUDA(cudaGetLastError());
+  if (int rc = op_finish(u.get())) return rc;
+
+  // the union's integrator state: dt^2/D and 1/D of every run at its offset,
+  // no sources (applied per run by the batch), its own step counters
+  std::unique_ptr<mj_lf> lf(new mj_lf());
+  lf->op = u.get(); lf->dt = 1.0; lf->n_dof = (int)n_dof; lf->stream = s;
+  MJ_CUDA(lf->minv.alloc(sizeof(float) * ((size_t)n_dof + 4)));
+  MJ_CUDA(cudaMemsetAsync(lf->minv.ptr, 0, lf->minv.bytes, s));
+  MJ_CUDA(lf->inv_mass64.alloc(sizeof(double) * (size_t)n_dof));
+  MJ_CUDA(lf->ua.alloc(sizeof(float) * ((size_t)n_dof + 4)));
+  MJ_CUDA(lf->ub.alloc(sizeof(float) * ((size_t)n_dof + 4)));
+  MJ_CUDA(cudaMemsetAsync(lf->ua.ptr, 0, lf->ua.bytes, s));
+  MJ_CUDA(cudaMemsetAsync(lf->ub.ptr, 0, lf->ub.bytes, s));
+  for (size_t r = 0; r < runs.size(); r++) {
+    const mj_lf* src = runs[r];
+    const size_t off = (size_t)(*dof_off)[r];
+    MJ_CUDA(cudaMemcpyAsync(lf->minv.as<float>() + off, src->minv.ptr, sizeof(float) * src->n_dof,
+                            cudaMemcpyDeviceToDevice, s));
+    MJ_CUDA(cudaMemcpyAsync(lf->inv_mass64.as<double>() + off, src->inv_mass64.ptr, sizeof(double) * src->n_dof,
+                            cudaMemcpyDeviceToDevice, s));
+  }
+  MJ_CUDA(lf->ctr.alloc(sizeof(int) * 2));
+  MJ_CUDA(cudaMemsetAsync(lf->ctr.ptr, 0, sizeof(int) * 2, s));
+  MJ_CUDA(lf->pulse_d.alloc(sizeof(double)));
+  MJ_CUDA(cudaMemsetAsync(lf->pulse_d.ptr, 0, sizeof(double), s));
+  lf->n_pulse = 0;
+  lf->n_src = 0;
+  lf->stream_gather = true;
+  lf->initialised = true;
+  MJ_CUDA(cudaStreamSynchronize(s));
+  if (int rc = lf_stream_setup(lf.get())) return rc;
+  *uop_out = std::move(u);
+  *ulf_out = std::move(lf);
+  return MJ_OK;
+}

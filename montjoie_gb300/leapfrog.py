@@ -267,8 +267,9 @@ def RunSecondOrderScheme(t_begin: float, t_end: float, dt: float, U0: np.ndarray
 class MeshBatch:
     """Leap-frog runs on meshes of different size and order (each a
     ``LeapFrogIterator`` on its own FP32 operator) advanced together by one
-    cooperative persistent kernel per time step (or, when the autotuner finds
-    it faster, one per order group).  The reference advances such
+    cooperative persistent kernel per time step, or, when the autotuner finds
+    it faster, one launch per order group, or the runs of one order stepped
+    as one union operator (``union_info``).  The reference advances such
     runs one after the other (``ModifiedEquation.cxx:290-345`` per run).
     Each run stays usable on its own (``SetInitialConditionS``,
     ``GetIterate``, ``Advance``) between calls."""
@@ -304,14 +305,26 @@ class MeshBatch:
         return {"threads": th.value, "candidate_ms": {"256": ms[0], "128": ms[1]}}
 
     def set_config(self, threads: int) -> None:
-        """Forces the launch configuration (128 or 256 threads per CTA: one
-        kernel of all orders per step; -1: one launch per order group), or 0
-        to time them again at the next advance."""
+        """Forces the form of a step (128 or 256 threads per CTA: one kernel
+        of all orders per step; -1: one launch per order group; -2: unions,
+        of the whole batch when it has one order, else of every order group),
+        or 0 to time them again at the next advance."""
         _lib.check(_lib.load().mj_mb_set_config(self._h, int(threads)))
 
+    def union_info(self, group: int = -1) -> dict:
+        """The union form (one operator over the disjoint union of the runs'
+        meshes) of the batch (group -1) or of an order group: whether it steps
+        the runs, its timed ms per step, its element kernel's tile size and
+        its dofs (0: no union, the runs are too large for one)."""
+        use, tile, nd, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), np.zeros(1)
+        _lib.check(_lib.load().mj_mb_union_info(self._h, int(group), ctypes.byref(use), _lib.dptr(ms),
+                                                ctypes.byref(tile), ctypes.byref(nd)))
+        return {"in_use": bool(use.value), "union_ms": float(ms[0]), "tile_elems": tile.value, "n_dof": nd.value}
+
     def grouping(self) -> dict:
-        """Whether steps run one launch per order group, the number of groups
-        and the grouped form's timed ms per step."""
+        """Whether steps run one launch per order group, the number of groups,
+        the grouped form's timed ms per step and, per group, its form (batch
+        kernel, its runs' own kernels, or its union) with the timings."""
         L = _lib.load()
         g, n, ms = ctypes.c_int(), ctypes.c_int(), np.zeros(1)
         _lib.check(L.mj_mb_grouping(self._h, ctypes.byref(g), ctypes.byref(n), _lib.dptr(ms)))
@@ -320,8 +333,10 @@ class MeshBatch:
             o, nr, own, bms, oms = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), np.zeros(1), np.zeros(1)
             _lib.check(L.mj_mb_group_info(self._h, i, ctypes.byref(o), ctypes.byref(nr), ctypes.byref(own),
                                           _lib.dptr(bms), _lib.dptr(oms)))
+            u = self.union_info(i)
             groups.append({"order": o.value, "runs": nr.value, "own_kernels": bool(own.value),
-                           "batch_ms": float(bms[0]), "own_ms": float(oms[0])})
+                           "union": u["in_use"], "batch_ms": float(bms[0]), "own_ms": float(oms[0]),
+                           "union_ms": u["union_ms"]})
         return {"grouped": bool(g.value), "groups": n.value, "grouped_ms": float(ms[0]), "per_group": groups}
 
     def profile(self, enable: bool) -> None:

@@ -35,10 +35,11 @@ def snapshot(g, step):
     return g["snaps"][steps.index(step)] if step in steps else None
 
 
-@pytest.mark.parametrize("threads", [0, 128, 256, -1])
+@pytest.mark.parametrize("threads", [0, 128, 256, -1, -2])
 def test_batch_matches_reference_and_single_runs(threads):
     """threads = 0: the autotuned launch configuration; 128 / 256: one kernel
-    of all orders per step, forced; -1: one launch per order group, forced."""
+    of all orders per step, forced; -1: one launch per order group, forced;
+    -2: every order group stepped as its union, forced."""
     from montjoie_gb300.leapfrog import MeshBatch
     gs = [load_golden(c) for c in CASES]
     batch_runs = [run_fp32(g) for g in gs]
@@ -52,8 +53,10 @@ def test_batch_matches_reference_and_single_runs(threads):
     mb.advance(30)  # one 20-step graph + 10 launches
     assert mb.info()["graph"] == 1
     assert mb.grouping()["groups"] == len({int(g["order"]) for g in gs})
-    if threads == -1:
+    if threads in (-1, -2):
         assert mb.grouping()["grouped"]
+        if threads == -2:
+            assert all(g["union"] for g in mb.grouping()["per_group"])
     elif threads:
         assert mb.tuning()["threads"] == threads and not mb.grouping()["grouped"]
     assert mb.tuning()["threads"] in (128, 256)
@@ -89,7 +92,7 @@ def test_batch_matches_reference_and_single_runs(threads):
         op.close()
 
 
-@pytest.mark.parametrize("threads", [128, 256])
+@pytest.mark.parametrize("threads", [128, 256, -2])
 @pytest.mark.parametrize("cases,n", [(["regular2_q4", "cube3_q4", "cube4_q4"], 5), (["cube2_q8", "cube2_q8"], 9)])
 def test_single_order_batch(cases, n, threads):
     """Meshes of one order run that order's kernel instance: the same states
@@ -110,6 +113,53 @@ def test_single_order_batch(cases, n, threads):
             ref = snapshot(g, lf.n_time)
             if ref is not None:
                 assert rel_l2(u, ref) < FP32_TOL
+    mb.close()
+    for op, lf in batch_runs + single_runs:
+        lf.close()
+        op.close()
+
+
+def test_union_is_bitwise_the_runs_own_kernels():
+    """Runs of every order stepped as unions (forced) give bit for bit the
+    states of the same runs advanced alone, through graph replays, plain
+    steps, odd counts and a run advanced on its own in between; the factors
+    of one run scaled after the batch was made are taken up at the next
+    advance."""
+    from montjoie_gb300.leapfrog import MeshBatch
+    gs = [load_golden(c) for c in CASES]
+    batch_runs = [run_fp32(g) for g in gs]
+    single_runs = [run_fp32(g) for g in gs]
+    mb = MeshBatch([lf for _, lf in batch_runs])
+    mb.set_config(-2)
+
+    def same():
+        for (_, lf), (_, ls) in zip(batch_runs, single_runs):
+            u0, u1 = lf.GetState()
+            v0, v1 = ls.GetState()
+            assert np.array_equal(u0, v0) and np.array_equal(u1, v1)
+            assert lf.n_time == ls.n_time
+
+    for steps, kw in ((40, {}), (7, {"graph": False}), (21, {})):
+        mb.advance(steps, **kw)
+        for _, ls in single_runs:
+            ls.Advance(steps)
+        same()
+    for k in (2, 5):  # runs advanced on their own: the batch re-reads their states
+        batch_runs[k][1].Advance(3)
+        single_runs[k][1].Advance(3)
+    mb.advance(20)
+    for _, ls in single_runs:
+        ls.Advance(20)
+    same()
+    for op, _ in (batch_runs[4], single_runs[4]):
+        op.set_element_scale(np.full(op.n_elt, 1.25))
+    mb.advance(20)
+    for _, ls in single_runs:
+        ls.Advance(20)
+    same()
+    per_group = mb.grouping()["per_group"]
+    assert all(g["union"] for g in per_group)
+    assert sum(mb.union_info(i)["n_dof"] for i in range(len(per_group))) == mb.n_dof()
     mb.close()
     for op, lf in batch_runs + single_runs:
         lf.close()
