@@ -59,6 +59,9 @@ def parse():
                     help="largest mesh of the heterogeneous batch (default 40; smaller for profiling)")
     ap.add_argument("--fp32-only", action="store_true",
                     help="profiling aid: only the FP32 set-up and timed steps of the workload (no JSON line contract)")
+    ap.add_argument("--k1-variant", default=None,
+                    help="profiling aid with --fp32-only: force the element-kernel variant E,layout (the one the "
+                         "autotuner picks unprofiled), since under a profiler its timings are distorted")
     ap.add_argument("--leg", default="all", choices=["all", "q8", "sources", "meshes", "adjoint", "order4"],
                     help="profiling aid: run one extra leg alone (no JSON line contract)")
     return ap.parse_args()
@@ -444,7 +447,9 @@ def leg_adjoint(args, torch, _lib):
     """32^3 Q4, per-element c as parameter (start
     U[1.5,2.5]), 16 sources x 64 receivers, FP32 steps, L2 misfit against
     traces of a seeded perturbed true c; gradient by the discrete adjoint with
-    sqrt(N) checkpointing.  Timed at full size; the gradient is checked on a
+    every forward state kept (or sqrt(N) checkpoints when they do not fit);
+    the sqrt(N) and binomial schedules are timed beside it and must give the
+    same gradient bit for bit.  Timed at full size; the gradient is checked on a
     small case against central differences (20 elements) and the FP64 CPU adjoint."""
     from montjoie_gb300 import mesh as M
     from montjoie_gb300.adjoint import AcousticAdjoint
@@ -463,8 +468,13 @@ def leg_adjoint(args, torch, _lib):
         i_, v_ = gaussian_source(pb.nodle, pb.jw, pb.xq, pb.n_dof, c, 2.0 / cells)
         idx.append(i_); val.append(v_); rhs.append(np.full(i_.size, s_))
     rec_idx, rec_w = receiver_weights(order, pb.verts_e, pb.nodle, rng.uniform(0.1, 0.9, size=(nrec, 3)))
-    model = AcousticAdjoint(order, pb.nodle, pb.factors, pb.n_dof, pb.mass, dt, N, S, np.concatenate(idx),
-                            np.concatenate(rhs), np.concatenate(val), pb.pulse, rec_idx, rec_w)
+    # every forward state kept when it fits in device memory (N x n_dof x S
+    # floats: 137 GB here), else sqrt(N) checkpoints
+    adj_args = (order, pb.nodle, pb.factors, pb.n_dof, pb.mass, dt, N, S, np.concatenate(idx), np.concatenate(rhs),
+                np.concatenate(val), pb.pulse, rec_idx, rec_w)
+    free_bytes = torch.cuda.mem_get_info()[0]
+    keep_all = 4.0 * pb.n_dof * S * (N + 2) < 0.8 * free_bytes
+    model = AcousticAdjoint(*adj_args, checkpoint_every=N if keep_all else 0)
     data = model.forward(c_true)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -474,8 +484,19 @@ def leg_adjoint(args, torch, _lib):
     grad = model.backward(res)
     t2 = time.perf_counter()
     J = 0.5 * float((res * res).sum())
-    sched = model.schedule()
+    sched = dict(model.schedule(), kind="every state kept" if keep_all else "sqrt(N) checkpoints")
     model.close()
+    uniform = None
+    if keep_all:  # the sqrt(N) schedule beside it
+        model_u = AcousticAdjoint(*adj_args)
+        model_u.forward(c0)
+        torch.cuda.synchronize()
+        t5 = time.perf_counter()
+        grad_u = model_u.backward(res)
+        t6 = time.perf_counter()
+        uniform = dict(model_u.schedule(), backward_seconds=t6 - t5,
+                       grad_bitwise_equal=bool(np.array_equal(grad_u, grad)))
+        model_u.close()
     # the same model with binomial checkpointing under a budget of 16 stored states
     model_rv = AcousticAdjoint(order, pb.nodle, pb.factors, pb.n_dof, pb.mass, dt, N, S, np.concatenate(idx),
                                np.concatenate(rhs), np.concatenate(val), pb.pulse, rec_idx, rec_w, snapshots=16)
@@ -490,13 +511,14 @@ def leg_adjoint(args, torch, _lib):
     # forward N steps + backward (replay ~N steps, N adjoint steps, N gradient kernels)
     dof_updates = pb.n_dof * S * N
     return {"workload": f"32^3 Q4, per-element c (start U[1.5,2.5], true c perturbed by U[-10%,10%]), {S} sources x "
-                        f"{nrec} receivers, {N} FP32 steps, L2 trace misfit, adjoint with sqrt(N) checkpoints",
+                        f"{nrec} receivers, {N} FP32 steps, L2 trace misfit, discrete adjoint",
             "n_dof": pb.n_dof, "steps": N, "loss": J, "grad_norm": float(np.linalg.norm(grad)),
             "forward_seconds": t1 - t0, "backward_seconds": t2 - t1,
             "forward_value": dof_updates / (t1 - t0), "gradient_value": dof_updates / (t2 - t0), "unit": UNIT,
-            "checkpoints_uniform": sched,
+            "schedule": sched,
+            "checkpoints_uniform": uniform,
             "checkpoints_revolve_16": dict(sched_rv, backward_seconds=t4 - t3,
-                                           grad_bitwise_equal_to_uniform=bool(np.array_equal(grad_rv, grad))),
+                                           grad_bitwise_equal=bool(np.array_equal(grad_rv, grad))),
             "fd_check_32": fd,
             "small_case_check": adjoint_small_check()}
 
@@ -609,6 +631,9 @@ def run_ours(args):
 
     # ---- FP32 chosen form, resident (value)
     op32 = pb.operator("fp32")
+    if args.k1_variant and args.fp32_only:
+        e_, lay_ = (int(v) for v in args.k1_variant.split(","))
+        op32.set_variant(e_, lay_)
     tuning32 = op32.tuning()
     lf32 = pb.integrator(op32, diagnostics=False)
     lf32.SetInitialConditionS(zeros)

@@ -139,7 +139,9 @@ int mj_op_info(const mj_op* op, int* order, int* n_elt, int* n_dof, int* precisi
  * CTA, work layout (0 compact, 1 vector lines, 2 one element per warp, 3 one
  * element per warp reading the packed connectivity: each point's dof with its
  * rank among the dof's elements, so the result slot is the dof's CSR offset
- * plus the rank and no slot array is read), grid; and the timings (ms per launch,
+ * plus the rank and no slot array is read; 4 compact with one factor stage:
+ * the next tile's factors are copied during the current tile's divergence,
+ * so a CTA holds one factor block instead of two), grid; and the timings (ms per launch,
  * or a negative occupancy score on meshes too small to time) of the
  * candidates tried (candidate_ms may be NULL, else room for 64 values). */
 int mj_op_tuning(const mj_op* op, int* tile_elems, int* vector_lines, int* grid, int* n_candidates,
@@ -148,8 +150,9 @@ int mj_op_tuning(const mj_op* op, int* tile_elems, int* vector_lines, int* grid,
 /* Forces the element-kernel variant instead of the autotuner's choice:
  * tile_elems elements per CTA and the work layout (vector_lines: 0 compact,
  * 1 vector lines, 2 one element per warp, 3 the same with packed
- * connectivity; 1, 2 and 3 are FP32 only, 2 and 3 exist for order 4, 3 for
- * meshes of fewer than 2^27 dofs each shared by at most 32 elements);
+ * connectivity, 4 compact with one factor stage; 1 to 4 are FP32 only, 2 and
+ * 3 exist for order 4, 3 for meshes of fewer than 2^27 dofs each shared by
+ * at most 32 elements);
  * MJ_ERR_ARG when no such variant exists for the order.  Integrators bound to the operator
  * keep captured CUDA graphs of the old variant until re-created. */
 int mj_op_set_variant(mj_op* op, int tile_elems, int vector_lines);
@@ -448,8 +451,12 @@ typedef struct mj_adj mj_adj;
 /* Discrete adjoint of the many-source leap-frog of `b` over nsteps steps from
  * zero initial conditions, with the forward states checkpointed every
  * checkpoint_every steps (0: ceil(sqrt(nsteps))) and replayed segment by
- * segment in the backward sweep.  No reference counterpart: the reference has
- * no time-domain adjoint.  `b` must have receivers. */
+ * segment in the backward sweep.  checkpoint_every >= nsteps keeps every
+ * forward state (nsteps x n_dof x S floats, checked against the free device
+ * memory; MJ_ERR_ARG when it does not fit): nothing is recomputed, and the
+ * gradient is bit for bit that of any other interval.  No reference
+ * counterpart: the reference has no time-domain adjoint.  `b` must have
+ * receivers. */
 int mj_adj_create(mj_lfb* b, int nsteps, int checkpoint_every, mj_adj** out);
 
 /* The same adjoint with binomial checkpointing (Griewank and Walther's

@@ -58,11 +58,33 @@ int rhs_prepare(int n, int E, int L, int* ctas) {
   return MJ_ERR_ARG;
 }
 
+// Dynamic shared memory of the ENERGY variant: the plan's bytes, then the
+// per-(element, source, z-line) sums of the element product.
 template <int N, int E, int L>
-int energy_prepare_one() {
+size_t energy_smem(int S) {
   using P = K1Plan<float, N, E, L>;
+  return P::total + sizeof(float) * (size_t)E * S * N * N;
+}
+
+template <int N, int E, int L>
+int energy_prepare_one(int S, int* ctas) {
+  using P = K1Plan<float, N, E, L>;
+  int dev = 0, optin = 0;
+  MJ_CUDA(cudaGetDevice(&dev));
+  MJ_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  const size_t bytes = energy_smem<N, E, L>(S);
+  if (bytes > (size_t)optin) {
+    set_error("adjoint gradient kernel: too many sources for its shared memory");
+    return MJ_ERR_ARG;
+  }
   MJ_CUDA(cudaFuncSetAttribute(k_local_stiffness_rhs<N, E, L, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)P::total));
+                               (int)bytes));
+  MJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas, k_local_stiffness_rhs<N, E, L, true>, P::threads,
+                                                        bytes));
+  if (*ctas < 1) {
+    set_error("adjoint gradient kernel cannot be resident");
+    return MJ_ERR_ARG;
+  }
   return MJ_OK;
 }
 
@@ -70,13 +92,16 @@ template <int N, int E, int L>
 void energy_launch_one(int grid, const float* x, const int* nodle_e, const float* fac_e, int n_tiles, int S, int* err,
                        const float* lam, double* gacc, const double* coef, cudaStream_t s) {
   using P = K1Plan<float, N, E, L>;
-  k_local_stiffness_rhs<N, E, L, true><<<grid, P::threads, P::total, s>>>(x, nodle_e, fac_e, nullptr, nullptr,
-                                                                          n_tiles, S, err, lam, gacc, coef);
+  k_local_stiffness_rhs<N, E, L, true><<<grid, P::threads, energy_smem<N, E, L>(S), s>>>(
+      x, nodle_e, fac_e, nullptr, nullptr, n_tiles, S, err, lam, gacc, coef);
 }
 
-int energy_prepare(int n, int E, int L) {
+// Sets up the ENERGY variant of (n, E, L) for S sources; *ctas: its CTAs per
+// SM (its shared memory is larger than the plain variant's, so its persistent
+// grid is sized on its own).
+int energy_prepare(int n, int E, int L, int S, int* ctas) {
 #define MJ_X(NV, EV, LV) \
-  if (n == NV && E == EV && L == LV) return energy_prepare_one<NV, EV, LV>();
+  if (n == NV && E == EV && L == LV) return energy_prepare_one<NV, EV, LV>(S, ctas);
   MJ_RHS_VARIANTS(MJ_X)
 #undef MJ_X
   set_error("no energy kernel variant for this order");
@@ -609,6 +634,8 @@ struct mj_adj {
   DevBuf slots;                      // snaps x 2 states
   DevBuf work;                       // 3 states: the current pair and the next state
   long long backward_steps = 0;      // forward steps recomputed by the backward sweep
+  bool store_all = false;            // uniform with K = N: seg keeps U^0 .. U^{N-1} from the forward sweep
+  int energy_grid = 1;               // persistent grid of the gradient kernel
 };
 
 namespace {
@@ -724,7 +751,7 @@ int adj_visit(mj_adj* a, const float* uk, int m, float*& lam1, float*& lam2, cud
                                           S);
   count_launch();
   std::swap(lam1, lam2);  // lam1 = lambda^m, lam2 = lambda^{m+1}
-  energy_launch(op->n, b->E, b->L, b->grid, uk, op->nodle_e.as<int>(), op->fac_e.as<float>(), b->n_tiles, S,
+  energy_launch(op->n, b->E, b->L, a->energy_grid, uk, op->nodle_e.as<int>(), op->fac_e.as<float>(), b->n_tiles, S,
                 op->err.as<int>(), lam1, a->grad.as<double>(), a->coef.as<double>(), s);
   count_launch();
   MJ_CUDA(cudaGetLastError());
@@ -808,7 +835,10 @@ int adj_common_init(mj_adj* a) {
   MJ_CUDA(cudaMemcpy(a->rptr.ptr, rptr.data(), sizeof(int) * rptr.size(), cudaMemcpyHostToDevice));
   MJ_CUDA(cudaMemcpy(a->rk.ptr, rk.data(), sizeof(int) * rk.size(), cudaMemcpyHostToDevice));
   MJ_CUDA(cudaMemcpy(a->rw.ptr, rw.data(), sizeof(double) * rw.size(), cudaMemcpyHostToDevice));
-  return energy_prepare(op->n, b->E, b->L);
+  int ctas = 0;
+  if (int rc = energy_prepare(op->n, b->E, b->L, b->S, &ctas)) return rc;
+  a->energy_grid = std::max(1, std::min(b->n_tiles, ctas * sm_count()));
+  return MJ_OK;
 }
 
 }  // namespace
@@ -825,11 +855,23 @@ int mj_adj_create(mj_lfb* b, int nsteps, int checkpoint_every, mj_adj** out) {
   a->N = nsteps;
   a->K = checkpoint_every > 0 ? checkpoint_every : std::max(2, (int)std::ceil(std::sqrt((double)nsteps)));
   MJ_CHECK_ARG(a->K >= 2, "mj_adj_create: checkpoint interval must be >= 2");
+  // an interval of nsteps or more keeps every forward state: one segment the
+  // forward sweep fills itself, nothing recomputed
+  a->store_all = a->K >= nsteps;
+  if (a->store_all) a->K = nsteps;
   a->J = (nsteps + a->K - 1) / a->K;
   a->rows = (size_t)b->n_dof * b->S;
+  if (a->store_all) {
+    size_t free_b = 0, total_b = 0;
+    MJ_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const double need = double(sizeof(float)) * a->rows * (a->K + 2);
+    MJ_CHECK_ARG(need < 0.9 * double(free_b),
+                 "mj_adj_create: keeping every state needs " + std::to_string(need / 1e9) + " GB, " +
+                     std::to_string(free_b / 1e9) + " GB free (use a shorter checkpoint interval)");
+  }
   MJ_CUDA(a->ckpt.alloc(sizeof(float) * a->rows * 2 * a->J));
   MJ_CUDA(a->seg.alloc(sizeof(float) * a->rows * a->K));
-  for (int j = 0; j < a->J; j++) {  // replays: U^{n0+2} .. U^{n1-1} of every segment
+  for (int j = 0; j < a->J && !a->store_all; j++) {  // replays: U^{n0+2} .. U^{n1-1} of every segment
     const int n0 = j * a->K, n1 = std::min(n0 + a->K, nsteps);
     a->backward_steps += std::max(0, n1 - n0 - 2);
   }
@@ -908,7 +950,7 @@ int mj_revolve_schedule(int nsteps, int snapshots, int capacity, int* actions, i
 int mj_adj_info(const mj_adj* a, int* revolve, int* snapshots, long long* forward_steps, size_t* device_bytes) {
   MJ_CHECK_ARG(a, "mj_adj_info: null argument");
   if (revolve) *revolve = a->revolve ? 1 : 0;
-  if (snapshots) *snapshots = a->revolve ? a->snaps : a->J;
+  if (snapshots) *snapshots = a->revolve ? a->snaps : a->store_all ? a->N : a->J;
   if (forward_steps) *forward_steps = (long long)a->N + a->backward_steps;
   if (device_bytes) *device_bytes = a->ckpt.bytes + a->seg.bytes + a->slots.bytes + a->work.bytes;
   return MJ_OK;
@@ -940,6 +982,9 @@ int mj_adj_forward(mj_adj* a, double* traces) {
       MJ_CUDA(cudaMemcpyAsync(dst, b->cur(), bytes, cudaMemcpyDeviceToDevice, s));
       MJ_CUDA(cudaMemcpyAsync(dst + a->rows, b->next(), bytes, cudaMemcpyDeviceToDevice, s));
     }
+    if (a->store_all)
+      MJ_CUDA(cudaMemcpyAsync(a->seg.as<float>() + (size_t)n * a->rows, b->cur(), bytes, cudaMemcpyDeviceToDevice,
+                              s));
     if (a->revolve && n == a->N - 1) {  // x_{N-1}, the first state the backward sweep visits
       float* w = a->work.as<float>();
       MJ_CUDA(cudaMemcpyAsync(w, b->cur(), bytes, cudaMemcpyDeviceToDevice, s));
@@ -1019,11 +1064,14 @@ int mj_adj_backward(mj_adj* a, const double* residual, const double* coef, doubl
   const float* ck = a->ckpt.as<float>();
   for (int j = a->revolve ? -1 : a->J - 1; j >= 0; j--) {
     const int n0 = j * K, n1 = std::min(n0 + K, N);
-    // replay U^{n0} .. U^{n1-1} of the segment from its checkpoint
-    MJ_CUDA(cudaMemcpyAsync(seg, ck + (size_t)j * 2 * rows, bytes, cudaMemcpyDeviceToDevice, s));
-    if (n1 - n0 >= 2)
-      MJ_CUDA(cudaMemcpyAsync(seg + rows, ck + (size_t)j * 2 * rows + rows, bytes, cudaMemcpyDeviceToDevice, s));
-    for (int n = n0; n + 2 <= n1 - 1; n++) {
+    // replay U^{n0} .. U^{n1-1} of the segment from its checkpoint (kept by
+    // the forward sweep when every state is stored)
+    if (!a->store_all) {
+      MJ_CUDA(cudaMemcpyAsync(seg, ck + (size_t)j * 2 * rows, bytes, cudaMemcpyDeviceToDevice, s));
+      if (n1 - n0 >= 2)
+        MJ_CUDA(cudaMemcpyAsync(seg + rows, ck + (size_t)j * 2 * rows + rows, bytes, cudaMemcpyDeviceToDevice, s));
+    }
+    for (int n = n0; !a->store_all && n + 2 <= n1 - 1; n++) {
       int rc = adj_forward_step(a, seg + (size_t)(n - n0) * rows, seg + (size_t)(n + 1 - n0) * rows,
                                 seg + (size_t)(n + 2 - n0) * rows, n, s);
       if (rc) return rc;

@@ -16,6 +16,7 @@ struct mj_op {
   bool vec = false;                     // work layout of the element kernel (autotuned)
   bool warp = false;                    // warp-per-element layout (FP32, order 4; autotuned)
   bool packed = false;                  // that layout with packed connectivity (nodle_pk; autotuned)
+  bool fs = false;                      // compact layout with one factor stage (FP32; autotuned)
   size_t r_len = 0;                     // element-major slots (n_elt_pad * Qp)
   size_t n_inc = 0;                     // incidences (n_elt * Q); R has n_inc + 1 entries
   mj::DevBuf nodle_e, fac_e, slot_e, R, ptr;
@@ -154,6 +155,12 @@ void k1_launch_f32(int n, int E, bool vec, int grid, const void* x, const int* n
 // packed: the variant reading the packed connectivity (nodle_e = nodle_pk,
 // slot_e = the CSR offsets ptr; see kPkDofBits).
 std::vector<int> k1_warp_tile_candidates(int n);
+// Compact layout with one factor stage (FP32, mj_k1_fs.cu): the same tile
+// sizes as the compact layout (k1_tile_candidates).
+int k1_set_gmat_fs(int n, const double* g);  // called by k1_set_gmat_f32
+int k1_prepare_fs_f32(int n, int E, int* ctas_per_sm);
+void k1_launch_fs_f32(int n, int E, int grid, const void* x, const int* nodle_e, const void* fac_e, void* R,
+                      const int* slot_e, int n_tiles, int* err, cudaStream_t s);
 int k1_prepare_w_f32(int n, int E, bool packed, int* ctas_per_sm);
 void k1_launch_w_f32(int n, int E, bool packed, int grid, const void* x, const int* nodle_e, const void* fac_e,
                      void* R, const int* slot_e, int n_tiles, int* err, cudaStream_t s);

@@ -92,6 +92,26 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
       : "memory");
 }
 
+// L2 eviction priority for data a launch reads exactly once (factors,
+// connectivity, incidence slots, the streamed vectors of the gathers): evict
+// first, so that the state vector gathered by the element kernel, and written
+// by the previous step's gather, stays in L2.
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+
+// bulk_g2s with an L2 cache policy (l2_evict_first_policy).
+__device__ __forceinline__ void bulk_g2s_hint(void* dst, const void* src, uint32_t bytes, uint64_t* bar,
+                                              uint64_t pol) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::
+          "r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar)), "l"(pol)
+      : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
@@ -249,8 +269,9 @@ __global__ void __launch_bounds__(E* N* N)
   auto issue = [&](int stage, int tile) {
     if (t == 0 && tile < n_tiles) {
       mbar_expect_tx(&bar[stage], (uint32_t)P::stage_bytes);
-      bulk_g2s(s_fac(stage), fac_e + (size_t)tile * E * 6 * Qp, (uint32_t)P::fac_bytes, &bar[stage]);
-      bulk_g2s(s_nod(stage), nodle_e + (size_t)tile * E * Qp, (uint32_t)P::nod_bytes, &bar[stage]);
+      const uint64_t pol = l2_evict_first_policy();
+      bulk_g2s_hint(s_fac(stage), fac_e + (size_t)tile * E * 6 * Qp, (uint32_t)P::fac_bytes, &bar[stage], pol);
+      bulk_g2s_hint(s_nod(stage), nodle_e + (size_t)tile * E * Qp, (uint32_t)P::nod_bytes, &bar[stage], pol);
     }
   };
   const int g = gridDim.x;
@@ -362,6 +383,195 @@ __global__ void __launch_bounds__(E* N* N)
 }
 
 // ---------------------------------------------------------------------------
+// K1, compact layout with ONE factor stage (FS).  The factors of a tile are
+// read only by the gradient half of the product, so the next tile's factors
+// are copied into the same stage while the current tile's divergence runs;
+// Nodle keeps two stages, since the next tile's u is gathered during that
+// divergence.  At high order the factors are 6/7 of a stage, so a CTA needs
+// little more than half the shared memory of k_local_stiffness and more CTAs
+// fit on an SM.  The arithmetic is that of k_local_stiffness (compact), term
+// for term, so both give the same bits.
+// ---------------------------------------------------------------------------
+template <typename Real, int N, int E>
+struct K1PlanFS {
+  static constexpr int NN = N * N;
+  static constexpr int Q = N * NN;
+  static constexpr int Qp = elem_slots(N);
+  static constexpr size_t fac_bytes = sizeof(Real) * 6 * E * Qp;
+  static constexpr size_t nod_bytes = sizeof(int) * E * Qp;
+  static constexpr size_t work_bytes = ((sizeof(Real) * 3 * E * Q + 15) / 16) * 16;
+  static constexpr size_t total = fac_bytes + 2 * nod_bytes + work_bytes + 3 * sizeof(uint64_t);
+  static constexpr int threads = E * NN;
+};
+
+template <typename Real, int N, int E, long SPIN = kSpinLimit>
+__global__ void __launch_bounds__(E* N* N)
+    k_local_stiffness_fs(const Real* __restrict__ x, const int* __restrict__ nodle_e,
+                         const Real* __restrict__ fac_e, Real* __restrict__ R, const int* __restrict__ slot_e,
+                         int n_tiles, int* __restrict__ err) {
+  using P = K1PlanFS<Real, N, E>;
+  constexpr int NN = P::NN, Q = P::Q, Qp = P::Qp;
+  const Real* __restrict__ Gm = GConst<Real>::get(N);
+  extern __shared__ __align__(128) unsigned char smem[];
+  Real* s_fac = reinterpret_cast<Real*>(smem);
+  auto s_nod = [&](int st) { return reinterpret_cast<int*>(smem + P::fac_bytes + st * P::nod_bytes); };
+  // work arrays [el][k][j][i]
+  Real* s_u = reinterpret_cast<Real*>(smem + P::fac_bytes + 2 * P::nod_bytes);
+  Real* s_vx = s_u + E * Q;
+  Real* s_vy = s_vx + E * Q;
+  // bar[0], bar[1]: the Nodle stages; bar[2]: the factor stage
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + P::fac_bytes + 2 * P::nod_bytes + P::work_bytes);
+
+  const int t = threadIdx.x;
+  const int el = t / NN;
+  const int ij = t - el * NN;
+  const int j = ij / N;
+  const int i = ij - j * N;
+  Real gci[N], gcj[N], gri[N], grj[N];
+#pragma unroll
+  for (int a = 0; a < N; a++) {
+    gci[a] = Gm[a * N + i];
+    gcj[a] = Gm[a * N + j];
+    gri[a] = Gm[i * N + a];
+    grj[a] = Gm[j * N + a];
+  }
+  const int lx = el * Q + j * N;  // + k*NN + a: x-line (el, k, j)
+  const int ly = el * Q + i;      // + k*NN + a*N: y-line (el, k, i)
+  const int pe = el * Qp + ij;
+
+  if (t == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_init(&bar[2], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  auto issue_nod = [&](int st, int tile) {
+    if (t == 0 && tile < n_tiles) {
+      mbar_expect_tx(&bar[st], (uint32_t)P::nod_bytes);
+      bulk_g2s_hint(s_nod(st), nodle_e + (size_t)tile * E * Qp, (uint32_t)P::nod_bytes, &bar[st],
+                    l2_evict_first_policy());
+    }
+  };
+  auto issue_fac = [&](int tile) {
+    if (t == 0 && tile < n_tiles) {
+      mbar_expect_tx(&bar[2], (uint32_t)P::fac_bytes);
+      bulk_g2s_hint(s_fac, fac_e + (size_t)tile * E * 6 * Qp, (uint32_t)P::fac_bytes, &bar[2],
+                    l2_evict_first_policy());
+    }
+  };
+  const int g = gridDim.x;
+  int tile = blockIdx.x;
+  issue_nod(0, tile);
+  issue_fac(tile);
+  issue_nod(1, tile + g);
+  uint32_t ph = 0u;  // bits 0, 1: parity of the next completion of Nodle stage 0, 1; bit 2: of the factor stage
+  Real u[N];
+  if (tile < n_tiles) {
+    const bool ok = mbar_wait_bounded<SPIN>(&bar[0], 0u);
+    if (__syncthreads_or(!ok)) {
+      if (t == 0) {  // report; every copy issued above may still be in flight
+        atomicExch(err, 1);
+        mbar_wait_drain(&bar[0], 0u);
+        mbar_wait_drain(&bar[2], 0u);
+        if (tile + g < n_tiles) mbar_wait_drain(&bar[1], 0u);
+      }
+      return;
+    }
+    ph ^= 1u;
+    const int* nd = s_nod(0) + pe;
+#pragma unroll
+    for (int k = 0; k < N; k++) u[k] = __ldg(x + nd[k * NN]);
+  }
+  for (int it = 0; tile < n_tiles; tile += g, ++it) {
+    const int s = it & 1;
+#pragma unroll
+    for (int k = 0; k < N; k++) s_u[lx + k * NN + i] = u[k];
+    // this tile's factors (the vote is also the barrier after staging u)
+    {
+      const bool ok = mbar_wait_bounded<SPIN>(&bar[2], (ph >> 2) & 1u);
+      if (__syncthreads_or(!ok)) {
+        if (t == 0) {  // report; this tile's factors and the next tile's Nodle may be in flight
+          atomicExch(err, 1);
+          mbar_wait_drain(&bar[2], (ph >> 2) & 1u);
+          if (tile + g < n_tiles) mbar_wait_drain(&bar[s ^ 1], (ph >> (s ^ 1)) & 1u);
+        }
+        return;
+      }
+      ph ^= 4u;
+    }
+    const Real* f = s_fac + el * 6 * Qp + ij;
+    Real vz[N];
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+      Real rx[N], ry[N];
+#pragma unroll
+      for (int a = 0; a < N; a++) {
+        rx[a] = s_u[lx + k * NN + a];
+        ry[a] = s_u[ly + k * NN + a * N];
+      }
+      Real gx = 0, gy = 0, gz = 0;
+#pragma unroll
+      for (int a = 0; a < N; a++) {
+        gz += Gm[a * N + k] * u[a];
+        gx += gci[a] * rx[a];
+        gy += gcj[a] * ry[a];
+      }
+      const Real* fk = f + k * NN;
+      const Real bxx = fk[0], bxy = fk[Qp], bxz = fk[2 * Qp];
+      const Real byy = fk[3 * Qp], byz = fk[4 * Qp], bzz = fk[5 * Qp];
+      s_vx[lx + k * NN + i] = bxx * gx + bxy * gy + bxz * gz;
+      s_vy[ly + k * NN + j * N] = bxy * gx + byy * gy + byz * gz;
+      vz[k] = bxz * gx + byz * gy + bzz * gz;
+    }
+    __syncthreads();  // the factor stage and s_u are free
+    if (t == 0) fence_proxy_async();
+    issue_fac(tile + g);  // the next tile's factors, during this divergence
+
+    // gather of the next tile's u, in flight during the divergence below
+    const int nt = tile + g;
+    if (nt < n_tiles) {
+      const int so = s ^ 1;
+      const bool ok = mbar_wait_bounded<SPIN>(&bar[so], (ph >> so) & 1u);
+      if (__syncthreads_or(!ok)) {
+        if (t == 0) {  // report; Nodle stage so and the factors just issued may be in flight
+          atomicExch(err, 1);
+          mbar_wait_drain(&bar[so], (ph >> so) & 1u);
+          mbar_wait_drain(&bar[2], (ph >> 2) & 1u);
+        }
+        return;
+      }
+      ph ^= 1u << so;
+      const int* nd = s_nod(so) + pe;
+#pragma unroll
+      for (int k = 0; k < N; k++) u[k] = __ldg(x + nd[k * NN]);
+    }
+
+    const int* st = slot_e + ((size_t)tile * E + el) * Qp + ij;
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+      Real rx[N], ry[N];
+#pragma unroll
+      for (int a = 0; a < N; a++) {
+        rx[a] = s_vx[lx + k * NN + a];
+        ry[a] = s_vy[ly + k * NN + a * N];
+      }
+      Real y = 0;
+#pragma unroll
+      for (int a = 0; a < N; a++) {
+        y += gri[a] * rx[a];
+        y += grj[a] * ry[a];
+        y += Gm[k * N + a] * vz[a];
+      }
+      R[__ldg(st + k * NN)] = y;
+    }
+    __syncthreads();  // Nodle stage s and the work arrays are free again
+    if (t == 0) fence_proxy_async();
+    issue_nod(s, tile + 2 * g);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // K1, warp-per-element layout (n*n <= 32, i.e. orders up to 4): element el
 // of the tile belongs to warp el, lane (j, i) owning the z-line (i, j, .);
 // lanes >= n*n idle.  The compact work arrays of an element are touched by
@@ -424,8 +634,9 @@ __global__ void __launch_bounds__(E * 32)
   auto issue = [&](int stage, int tile) {
     if (t == 0 && tile < n_tiles) {
       mbar_expect_tx(&bar[stage], (uint32_t)P::stage_bytes);
-      bulk_g2s(s_fac(stage), fac_e + (size_t)tile * E * 6 * Qp, (uint32_t)P::fac_bytes, &bar[stage]);
-      bulk_g2s(s_nod(stage), nodle_e + (size_t)tile * E * Qp, (uint32_t)P::nod_bytes, &bar[stage]);
+      const uint64_t pol = l2_evict_first_policy();
+      bulk_g2s_hint(s_fac(stage), fac_e + (size_t)tile * E * 6 * Qp, (uint32_t)P::fac_bytes, &bar[stage], pol);
+      bulk_g2s_hint(s_nod(stage), nodle_e + (size_t)tile * E * Qp, (uint32_t)P::nod_bytes, &bar[stage], pol);
     }
   };
   const int g = gridDim.x;
@@ -554,6 +765,12 @@ __global__ void __launch_bounds__(E * 32)
 // accumulates gacc[e] += coef[e] * sum_s sum_q lam[dof_q][s] (A_e x_s)_q,
 // i.e. lam^T A_e x summed over the right-hand sides, in FP64 (one CTA owns
 // an element per launch, so the update needs no atomics in global memory).
+// The sum has one order whatever E and L, so every tuned variant gives the
+// same bits: each (source s, z-line q) sums its points in k order (FP32
+// FMAs) into shared memory (E*S*NN floats past the plan's bytes, see
+// k1_rhs_energy_smem); after the passes, lane l of warp el adds, in FP64, the
+// sources s = l, l+32, ... with their z-lines q = 0..NN-1 in order, and a
+// fixed shuffle tree adds the lanes.
 // ---------------------------------------------------------------------------
 template <int N, int E, int L, bool ENERGY = false>
 __global__ void __launch_bounds__(E* N* N* L)
@@ -601,8 +818,9 @@ __global__ void __launch_bounds__(E* N* N* L)
   auto issue = [&](int stage, int tile) {
     if (threadIdx.x == 0 && tile < n_tiles) {
       mbar_expect_tx(&bar[stage], (uint32_t)P::stage_bytes);
-      bulk_g2s(s_fac(stage), fac_e + (size_t)tile * E * 6 * Qp, (uint32_t)P::fac_bytes, &bar[stage]);
-      bulk_g2s(s_nod(stage), nodle_e + (size_t)tile * E * Qp, (uint32_t)P::nod_bytes, &bar[stage]);
+      const uint64_t pol = l2_evict_first_policy();
+      bulk_g2s_hint(s_fac(stage), fac_e + (size_t)tile * E * 6 * Qp, (uint32_t)P::fac_bytes, &bar[stage], pol);
+      bulk_g2s_hint(s_nod(stage), nodle_e + (size_t)tile * E * Qp, (uint32_t)P::nod_bytes, &bar[stage], pol);
     }
   };
   const int g = gridDim.x;
@@ -611,9 +829,9 @@ __global__ void __launch_bounds__(E* N* N* L)
   issue(1, tile + g);
   uint32_t ph = 0u;
   const int passes = S / L;
+  float* s_ez = reinterpret_cast<float*>(smem + P::total);  // ENERGY: [el][source][z-line]
   for (int it = 0; tile < n_tiles; tile += g, ++it) {
     const int s = it & 1;
-    float energy = 0.f;
     const bool ok = mbar_wait_bounded(&bar[s], (ph >> s) & 1u);
     if (__syncthreads_or(!ok)) {
       if (threadIdx.x == 0) {  // report; stage s and, if issued, stage s^1 may have copies in flight
@@ -658,6 +876,7 @@ __global__ void __launch_bounds__(E* N* N* L)
       }
       __syncthreads();
       const int* st = slot_e + ((size_t)tile * E + el) * Qp + ij;
+      float ez = 0.f;  // ENERGY: this z-line's sum for source col
 #pragma unroll
       for (int k = 0; k < N; k++) {
         float y = 0;
@@ -667,29 +886,26 @@ __global__ void __launch_bounds__(E* N* N* L)
           y = fmaf(grj[a], s_vy[(s_line_y + k * NN + a * N) * L + lane], y);
           y = fmaf(Gm[k * N + a], vz[a], y);
         }
-        if (ENERGY) energy += y * __ldg(lam + (size_t)dofs[k] * S + col);
+        if (ENERGY) ez = fmaf(y, __ldg(lam + (size_t)dofs[k] * S + col), ez);
         else R[(size_t)__ldg(st + k * NN) * S + col] = y;
       }
+      if constexpr (ENERGY) s_ez[((size_t)el * S + col) * NN + ij] = ez;
       __syncthreads();
     }
-    if constexpr (ENERGY) {
-      // Deterministic reduction: thread partials in shared memory, then for
-      // each element one warp sums a fixed strided subset and shuffles.
-      __shared__ double s_thr[E * N * N * L];
-      s_thr[threadIdx.x] = (double)energy;
-      __syncthreads();
-      constexpr int per_elt = N * N * L;
-      const int w = threadIdx.x >> 5, lane32 = threadIdx.x & 31;
+    if constexpr (ENERGY) {  // E*NN*L >= 32*E threads: warp el sums element el
+      const int w = threadIdx.x >> 5, l32 = threadIdx.x & 31;
       if (w < E) {
         double acc = 0.0;
-        for (int t = lane32; t < per_elt; t += 32) acc += s_thr[w * per_elt + t];
+        for (int src = l32; src < S; src += 32) {
+          const float* row = s_ez + ((size_t)w * S + src) * NN;
+          for (int q = 0; q < NN; q++) acc += (double)row[q];
+        }
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-        if (lane32 == 0) {
+        if (l32 == 0) {
           const size_t e = (size_t)tile * E + w;
           gacc[e] += coef[e] * acc;
         }
       }
-      __syncthreads();
     }
     if (threadIdx.x == 0) fence_proxy_async();
     issue(s, tile + 2 * g);

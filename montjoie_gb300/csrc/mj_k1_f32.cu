@@ -4,7 +4,10 @@
 #include "mj_k1_inst.cuh"
 
 namespace mj {
-int k1_set_gmat_f32(int n, const double* g) { return set_gmat(n, g); }
+int k1_set_gmat_f32(int n, const double* g) {
+  const int rc = set_gmat(n, g);
+  return rc ? rc : k1_set_gmat_fs(n, g);  // and the one-factor-stage unit's copy
+}
 int k1_prepare_f32(int n, int E, bool vec, int* ctas) { return prepare_any(n, E, vec, ctas); }
 void k1_launch_f32(int n, int E, bool vec, int grid, const void* x, const int* nodle_e, const void* fac_e,
                    void* R, const int* slot_e, int n_tiles, int* err, cudaStream_t s) {

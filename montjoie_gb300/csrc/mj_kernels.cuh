@@ -440,11 +440,12 @@ __global__ void __launch_bounds__(kStreamThreads, 8)  // 8 CTAs per SM: 32 regis
     const uint32_t pb = (uint32_t)(((ch.d1 - ch.d0 + 1 + 3) & ~3) * 4);
     const uint32_t rb = (uint32_t)((ch.q1 - ch.q0) * 4);
     mbar_expect_tx(&bar[b], 3u * sb + pb + rb);
-    bulk_g2s(dst, u1 + ch.d0, sb, &bar[b]);
-    bulk_g2s(dst + kStreamDofs * 4, u0 + ch.d0, sb, &bar[b]);
-    bulk_g2s(dst + kStreamM, m + ch.d0, sb, &bar[b]);
-    bulk_g2s(dst + kStreamP, ptr + ch.d0, pb, &bar[b]);
-    bulk_g2s(dst + kStreamR, R + ch.q0, rb, &bar[b]);
+    const uint64_t pol = l2_evict_first_policy();  // all read once; the new state, stored, stays in L2
+    bulk_g2s_hint(dst, u1 + ch.d0, sb, &bar[b], pol);
+    bulk_g2s_hint(dst + kStreamDofs * 4, u0 + ch.d0, sb, &bar[b], pol);
+    bulk_g2s_hint(dst + kStreamM, m + ch.d0, sb, &bar[b], pol);
+    bulk_g2s_hint(dst + kStreamP, ptr + ch.d0, pb, &bar[b], pol);
+    bulk_g2s_hint(dst + kStreamR, R + ch.q0, rb, &bar[b], pol);
   };
   if (t == 0) {
     for (int b = 0; b < kStreamNB; b++) mbar_init(&bar[b], 1);

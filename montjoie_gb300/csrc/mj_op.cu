@@ -98,6 +98,12 @@ void launch_k1(mj_op* op, const void* x, cudaStream_t s) {
     count_launch();
     return;
   }
+  if (op->fs) {
+    k1_launch_fs_f32(op->n, op->E, op->grid_k1, x, op->nodle_e.as<int>(), op->fac_e.ptr, op->R.ptr,
+                     op->slot_e.as<int>(), op->n_tiles, op->err.as<int>(), s);
+    count_launch();
+    return;
+  }
   if (op->precision == MJ_FP64)
     k1_launch_f64(op->n, op->E, op->vec, op->grid_k1, x, op->nodle_e.as<int>(), op->fac_e.ptr, op->R.ptr,
                   op->slot_e.as<int>(), op->n_tiles, op->err.as<int>(), s);
@@ -129,14 +135,22 @@ int autotune_k1(mj_op* op) {
   MJ_CUDA(cudaEventCreate(&e1));
   double best = 1e300;
   int bestE = -1, bestGrid = 1;
-  bool bestVec = false, bestWarp = false, bestPacked = false;
+  bool bestVec = false, bestWarp = false, bestPacked = false, bestFs = false;
   const bool time_it = (long long)op->n_elt * op->Q >= 2000000;
-  const int n_layouts = op->precision == MJ_FP32 ? (op->nodle_pk.ptr ? 4 : 3) : 1;
-  for (int lay = 0; lay < n_layouts; lay++)
-    for (int E : (lay >= 2 ? k1_warp_tile_candidates(op->n) : cands)) {
-      const bool vec = lay == 1, warp = lay >= 2, packed = lay == 3;
+  // layouts: 0 compact, 1 vector lines, 2 one element per warp, 3 the same
+  // with packed connectivity, 4 compact with one factor stage (2-4: FP32)
+  std::vector<int> layouts = {0};
+  if (op->precision == MJ_FP32) {
+    layouts = {0, 1, 2};
+    if (op->nodle_pk.ptr) layouts.push_back(3);
+    layouts.push_back(4);
+  }
+  for (int lay : layouts)
+    for (int E : ((lay == 2 || lay == 3) ? k1_warp_tile_candidates(op->n) : cands)) {
+      const bool vec = lay == 1, warp = lay == 2 || lay == 3, packed = lay == 3, fs = lay == 4;
       int ctas = 0;
       const int rc = warp ? k1_prepare_w_f32(op->n, E, packed, &ctas)
+                     : fs ? k1_prepare_fs_f32(op->n, E, &ctas)
                           : op->precision == MJ_FP64 ? k1_prepare_f64(op->n, E, vec, &ctas)
                                                      : k1_prepare_f32(op->n, E, vec, &ctas);
       if (rc != MJ_OK) continue;
@@ -144,7 +158,8 @@ int autotune_k1(mj_op* op) {
       const int grid = std::max(1, std::min(tiles, ctas * sms));
       double ms = 0.0;
       if (time_it) {
-        op->E = E; op->vec = vec; op->warp = warp; op->packed = packed; op->grid_k1 = grid; op->n_tiles = tiles;
+        op->E = E; op->vec = vec; op->warp = warp; op->packed = packed; op->fs = fs; op->grid_k1 = grid;
+        op->n_tiles = tiles;
         launch_k1(op, x.ptr, op->stream);
         MJ_CUDA(cudaEventRecord(e0, op->stream));
         for (int rep = 0; rep < 3; rep++) launch_k1(op, x.ptr, op->stream);
@@ -155,12 +170,14 @@ int autotune_k1(mj_op* op) {
         ms = f / 3.0;
       } else {
         ms = -double(ctas) * E * op->n * op->n + (vec ? 0.5 : 0.0) + (warp ? 0.75 : 0.0) +
-             (packed ? 0.1 : 0.0);  // most resident threads first
+             (packed ? 0.1 : 0.0) + (fs ? 0.25 : 0.0);  // most resident threads first
       }
       op->tune_E.push_back(E);
       op->tune_vec.push_back(lay);
       op->tune_ms.push_back(ms);
-      if (ms < best) { best = ms; bestE = E; bestGrid = grid; bestVec = vec; bestWarp = warp; bestPacked = packed; }
+      if (ms < best) {
+        best = ms; bestE = E; bestGrid = grid; bestVec = vec; bestWarp = warp; bestPacked = packed; bestFs = fs;
+      }
     }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -172,11 +189,13 @@ int autotune_k1(mj_op* op) {
   op->vec = bestVec;
   op->warp = bestWarp;
   op->packed = bestPacked;
+  op->fs = bestFs;
   op->grid_k1 = bestGrid;
   // the chosen variant's shared-memory attribute must be the one set last
   {
     int ctas = 0;
     const int rc = bestWarp ? k1_prepare_w_f32(op->n, bestE, bestPacked, &ctas)
+                   : bestFs ? k1_prepare_fs_f32(op->n, bestE, &ctas)
                             : op->precision == MJ_FP64 ? k1_prepare_f64(op->n, bestE, bestVec, &ctas)
                                                        : k1_prepare_f32(op->n, bestE, bestVec, &ctas);
     if (rc) return rc;
@@ -620,7 +639,7 @@ int mj_op_tuning(const mj_op* op, int* tile_elems, int* vector_lines, int* grid,
                  double* candidate_ms) {
   MJ_CHECK_ARG(op, "mj_op_tuning: null operator");
   if (tile_elems) *tile_elems = op->E;
-  if (vector_lines) *vector_lines = op->packed ? 3 : op->warp ? 2 : op->vec ? 1 : 0;
+  if (vector_lines) *vector_lines = op->fs ? 4 : op->packed ? 3 : op->warp ? 2 : op->vec ? 1 : 0;
   if (grid) *grid = op->grid_k1;
   if (n_candidates) *n_candidates = (int)op->tune_ms.size();
   if (candidate_ms)
@@ -630,16 +649,18 @@ int mj_op_tuning(const mj_op* op, int* tile_elems, int* vector_lines, int* grid,
 
 int mj_op_set_variant(mj_op* op, int tile_elems, int vector_lines) {
   MJ_CHECK_ARG(op, "mj_op_set_variant: null operator");
-  MJ_CHECK_ARG(vector_lines >= 0 && vector_lines <= 3, "mj_op_set_variant: layout must be 0, 1, 2 or 3");
+  MJ_CHECK_ARG(vector_lines >= 0 && vector_lines <= 4, "mj_op_set_variant: layout must be 0, 1, 2, 3 or 4");
   MJ_CHECK_ARG(vector_lines != 3 || op->nodle_pk.ptr, "mj_op_set_variant: no packed connectivity for this operator");
-  const bool warp = vector_lines >= 2, vec = vector_lines == 1, packed = vector_lines == 3;
+  const bool warp = vector_lines == 2 || vector_lines == 3, vec = vector_lines == 1, packed = vector_lines == 3;
+  const bool fs = vector_lines == 4;
   const std::vector<int> cands = warp ? k1_warp_tile_candidates(op->n) : k1_tile_candidates(op->n);
   MJ_CHECK_ARG(std::find(cands.begin(), cands.end(), tile_elems) != cands.end(),
                "mj_op_set_variant: no element kernel with this tile size and layout for this order");
   MJ_CHECK_ARG(vector_lines == 0 || op->precision == MJ_FP32,
-               "mj_op_set_variant: vector-line and warp layouts are FP32 only");
+               "mj_op_set_variant: the vector-line, warp and one-factor-stage layouts are FP32 only");
   int ctas = 0;
   const int rc = warp ? k1_prepare_w_f32(op->n, tile_elems, packed, &ctas)
+                 : fs ? k1_prepare_fs_f32(op->n, tile_elems, &ctas)
                       : op->precision == MJ_FP64 ? k1_prepare_f64(op->n, tile_elems, false, &ctas)
                                                  : k1_prepare_f32(op->n, tile_elems, vec, &ctas);
   if (rc) return rc;
@@ -647,6 +668,7 @@ int mj_op_set_variant(mj_op* op, int tile_elems, int vector_lines) {
   op->vec = vec;
   op->warp = warp;
   op->packed = packed;
+  op->fs = fs;
   op->n_tiles = op->n_elt_pad / tile_elems;
   op->grid_k1 = std::max(1, std::min(op->n_tiles, ctas * sm_count()));
   return MJ_OK;

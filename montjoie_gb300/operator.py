@@ -124,13 +124,15 @@ class FemMatrixFreeOperator:
         _lib.check(_lib.load().mj_op_tuning(self._h, *[ctypes.byref(v) for v in vals], _lib.dptr(ms)))
         E, lay, grid, nc = (v.value for v in vals)
         return {"tile_elems": E,
-                "layout": ["compact", "vector_lines", "warp_per_element", "warp_per_element_packed"][lay],
+                "layout": ["compact", "vector_lines", "warp_per_element", "warp_per_element_packed",
+                           "compact_one_factor_stage"][lay],
                 "grid": grid, "candidate_ms": ms[:nc].tolist()}
 
     def set_variant(self, tile_elems: int, layout) -> None:
         """Forces the element-kernel variant (otherwise chosen by the autotuner):
         layout 0 / False compact, 1 / True vector lines, 2 one element per warp,
-        3 one element per warp reading the packed connectivity."""
+        3 one element per warp reading the packed connectivity, 4 compact with
+        one factor stage."""
         _lib.check(_lib.load().mj_op_set_variant(self._h, int(tile_elems), int(layout)))
 
     def device_bytes(self) -> int:

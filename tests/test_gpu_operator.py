@@ -117,20 +117,23 @@ def test_every_element_kernel_variant(case):
     """Every instantiated element-kernel variant (tile size x work layout),
     forced in turn, against the reference's MltAdd: FP64 (compact) <= 1e-12,
     FP32 (compact, vector lines, one element per warp with the slot array or
-    with the packed connectivity) <= 2e-5 relative L2; the two warp forms
-    give the same result bit for bit."""
+    with the packed connectivity, compact with one factor stage) <= 2e-5
+    relative L2; the two warp forms give the same result bit for bit, and so
+    do the two compact forms."""
     from montjoie_gb300.operator import FemMatrixFreeOperator
     g = load_golden(case)
     r = int(g["order"])
     n_dof = g["massD"].size
     from montjoie_gb300._lib import MontjoieError
-    for precision, layouts, tol in (("fp64", (0,), 1e-12), ("fp32", (0, 1, 2, 3), 2e-5)):
+    for precision, layouts, tol in (("fp64", (0,), 1e-12), ("fp32", (0, 1, 2, 3, 4), 2e-5)):
         op = FemMatrixFreeOperator(r, g["nodle"], g["bh"], n_dof, precision, gradphi=g["gradphi"])
         tried = set()
-        warp_y = {}
+        warp_y, compact_y = {}, {}
         for E in sorted(set(K1_TILES[r]) | ({1, 2, 3, 4, 5, 6, 8, 10} if r == 4 else set())):
             for vec in layouts:
-                if vec >= 2 and (r != 4 or E not in (1, 2, 3, 4, 5, 6, 8, 10)):
+                if vec in (2, 3) and (r != 4 or E not in (1, 2, 3, 4, 5, 6, 8, 10)):
+                    continue
+                if vec in (0, 4) and E not in K1_TILES[r]:
                     continue
                 try:
                     op.set_variant(E, vec)
@@ -141,9 +144,13 @@ def test_every_element_kernel_variant(case):
                 y = g["y0"].copy()
                 op.MltAddVector(float(g["alpha"]), g["x"], float(g["beta"]), y)
                 assert rel_l2(y, g["kh_y"]) < tol, (precision, E, vec)
-                if vec >= 2:
+                if vec in (2, 3):
                     warp_y.setdefault(E, []).append(y)
+                if vec in (0, 4) and precision == "fp32":
+                    compact_y.setdefault(E, []).append(y)
         assert tried == (set(layouts) if r == 4 else set(layouts) - {2, 3})
         for ys in warp_y.values():
+            assert len(ys) == 2 and np.array_equal(ys[0], ys[1])
+        for ys in compact_y.values():
             assert len(ys) == 2 and np.array_equal(ys[0], ys[1])
         op.close()
