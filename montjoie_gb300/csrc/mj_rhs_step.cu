@@ -135,7 +135,62 @@ struct RsParams {
   const float* src_val;
   float* uout;         // where U^{n+2} goes (nullptr: over U^n)
   int n_src_dof, n_pulse, S, n_tiles;
+  unsigned char zmap[kMaxNK * kMaxNK];  // z-line (j*n + i) of each thread slot of an element (rs_zline_order)
 };
+
+// Order in which the threads of an element take its n*n z-lines.  A warp
+// holds Z = 32/LB consecutive slots; each of its shared-memory line reads
+// touches one x-line per distinct row j and one y-line per distinct column i
+// among its z-lines.  Candidates: row-major, 2-D blocks, and strips of 2, 3 or
+// 4 rows walked column by column, alternate strips in reverse (snake); the one
+// with the fewest distinct rows + columns per warp, summed over the E
+// elements of a tile, is kept (row-major on ties).  Every point's arithmetic
+// is the same whichever thread does it.
+void rs_zline_order(int n, int E, int LB, unsigned char* out) {
+  const int Z = std::max(1, 32 / LB), NN = n * n;
+  auto cost = [&](const std::vector<int>& ord) {
+    int tot = 0;
+    for (int w0 = 0; w0 < E * NN; w0 += Z) {
+      std::vector<int> rows, cols;
+      for (int sl = w0; sl < std::min(w0 + Z, E * NN); sl++) {
+        const int e = sl / NN, q = ord[sl % NN];
+        rows.push_back(e * n + q / n);
+        cols.push_back(e * n + q % n);
+      }
+      std::sort(rows.begin(), rows.end());
+      std::sort(cols.begin(), cols.end());
+      tot += (int)(std::unique(rows.begin(), rows.end()) - rows.begin()) +
+             (int)(std::unique(cols.begin(), cols.end()) - cols.begin());
+    }
+    return tot;
+  };
+  std::vector<std::vector<int>> cands;
+  std::vector<int> ord;
+  for (int q = 0; q < NN; q++) ord.push_back(q);
+  cands.push_back(ord);
+  {
+    const int bw = Z >= 8 ? 4 : Z >= 2 ? 2 : 1, bh = std::max(1, Z / bw);
+    ord.clear();
+    for (int by = 0; by < n; by += bh)
+      for (int bx = 0; bx < n; bx += bw)
+        for (int y = by; y < std::min(by + bh, n); y++)
+          for (int x = bx; x < std::min(bx + bw, n); x++) ord.push_back(y * n + x);
+    cands.push_back(ord);
+  }
+  for (int bh = 2; bh <= 4; bh++) {
+    ord.clear();
+    for (int by = 0, strip = 0; by < n; by += bh, strip++)
+      for (int c = 0; c < n; c++) {
+        const int x = strip % 2 == 0 ? c : n - 1 - c;
+        for (int y = by; y < std::min(by + bh, n); y++) ord.push_back(y * n + x);
+      }
+    cands.push_back(ord);
+  }
+  size_t best = 0;
+  for (size_t c = 1; c < cands.size(); c++)
+    if (cost(cands[c]) < cost(cands[best])) best = c;
+  for (int q = 0; q < NN; q++) out[q] = (unsigned char)cands[best][q];
+}
 
 // Phase-2 work: dofs [d0, d1), contributions R rows [q0, q1).
 struct RsChunk {
@@ -177,7 +232,7 @@ __global__ void __launch_bounds__(RsPlan<N, E, LB, V>::T, rs_min_ctas(RsPlan<N, 
   const int lb = t % LB;
   const int w = t / LB;
   const int el = w / NN;
-  const int ij = w - el * NN;
+  const int ij = p.zmap[w - el * NN];  // this thread's z-line (i, j)
   const int j = ij / N;
   const int i = ij - j * N;
   float* __restrict__ cur = par == 0 ? p.ua : p.ub;        // U^n, overwritten by U^{n+2}
@@ -485,6 +540,7 @@ RsParams rs_params(mj_lfb* b, const RsVariant& v) {
   p.n_pulse = b->n_pulse;
   p.S = b->S;
   p.n_tiles = op->n_elt_pad / v.E;
+  rs_zline_order(v.n, v.E, v.LB, p.zmap);
   return p;
 }
 
