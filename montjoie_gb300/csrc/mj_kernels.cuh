@@ -392,8 +392,18 @@ __device__ __forceinline__ void stream_diag_finish(double nacc, const StreamDiag
   const int warp = t >> 5, lane = t & 31;
   if (col < where.ncols) {
     if (warp == 0) {
+      // lane l adds partials l, l+32, ... in that order; the loads of four
+      // of them are issued together so their latencies overlap
       double s = 0.0;
-      for (int q = lane; q < G; q += 32) s += __ldcg(dg.partial + q);
+      int q = lane;
+      for (; q + 3 * 32 < G; q += 4 * 32) {
+        double p[4];
+#pragma unroll
+        for (int b = 0; b < 4; b++) p[b] = __ldcg(dg.partial + q + b * 32);
+#pragma unroll
+        for (int b = 0; b < 4; b++) s += p[b];
+      }
+      for (; q < G; q += 32) s += __ldcg(dg.partial + q);
       for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
       if (lane == 0) {
         if (where.norms) where.norms[col] = s;
@@ -402,9 +412,18 @@ __device__ __forceinline__ void stream_diag_finish(double nacc, const StreamDiag
     }
     if (where.traces)
       for (int r = warp; r < dg.n_rec; r += kStreamThreads / 32) {
+        // the same order of terms; indices, then states, loaded two terms at a time
+        const int* idx = dg.rec_idx + (size_t)r * dg.n_w;
+        const double* wr = dg.rec_w + (size_t)r * dg.n_w;
         double acc = 0.0;
-        for (int q = lane; q < dg.n_w; q += 32)
-          acc += dg.rec_w[(size_t)r * dg.n_w + q] * double(__ldcg(u + dg.rec_idx[(size_t)r * dg.n_w + q]));
+        int q = lane;
+        for (; q + 32 < dg.n_w; q += 2 * 32) {
+          const int i0 = idx[q], i1 = idx[q + 32];
+          const float u0v = __ldcg(u + i0), u1v = __ldcg(u + i1);
+          acc += wr[q] * double(u0v);
+          acc += wr[q + 32] * double(u1v);
+        }
+        for (; q < dg.n_w; q += 32) acc += wr[q] * double(__ldcg(u + idx[q]));
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
         if (lane == 0) where.traces[(size_t)r * where.stride + col] = acc;
       }
