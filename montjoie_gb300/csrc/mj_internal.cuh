@@ -47,6 +47,8 @@ struct mj_lf {
   mj::DevBuf inv_mass64;     // FP64 1/D for the initial step
   mj::DevBuf norm_w;         // FP64 weights, or empty
   mj::DevBuf norm_w32;       // the same rounded to FP32 (FP32 integrators), or empty
+  bool norm_is_mass = false; // FP32: the norm weights equal the mass, so the streaming gather's fused norm takes
+                             // them as dt^2 / (dt^2/D), from the dt^2/D it stages anyway
   mj::DevBuf rec_idx, rec_w; // receivers
   mj::DevBuf ua, ub;         // state: U^n (cur) and U^{n+1} (next)
   mj::DevBuf du0, tmp;       // staging

@@ -341,7 +341,9 @@ struct DiagDev {
 // counter (zero between launches), the non-finite flag, the receivers, and
 // where to write: (dd ? *dd : direct), column where.col + col.
 struct StreamDiag {
-  const float* w32;
+  const float* w32;    // the FP32 norm weights, or NULL: weights = wdt2 / m (norm weights equal to the mass)
+  const float* m;      // dt^2/D (k_stream_diag, with w32 == NULL)
+  float wdt2;          // dt^2 in FP32 (w32 == NULL), else 0; 0 with w32 == NULL: no norm
   double* partial;
   unsigned* done;
   int* flag;
@@ -475,6 +477,7 @@ __global__ void __launch_bounds__(kStreamThreads, 8)  // 8 CTAs per SM: 32 regis
   uint32_t ph = 0u;  // bit b: parity of buffer b's next completion
   int b = 0;
   double nacc = 0.0;  // DIAG: this thread's sum of w u^2
+  constexpr int V = kStreamDofs / kStreamThreads;
   for (int c = blockIdx.x; c < n_chunks; c += G, b = (b + 1 == kStreamNB ? 0 : b + 1)) {
     const StreamChunk ch = chunks[c];
     const bool ok = mbar_wait_bounded(&bar[b], (ph >> b) & 1u);
@@ -493,7 +496,6 @@ __global__ void __launch_bounds__(kStreamThreads, 8)  // 8 CTAs per SM: 32 regis
     const float* sm = reinterpret_cast<const float*>(buf + kStreamM);
     const int* sp = reinterpret_cast<const int*>(buf + kStreamP);
     const float* sR = reinterpret_cast<const float*>(buf + kStreamR);
-    constexpr int V = kStreamDofs / kStreamThreads;
     int dls[V];
     bool on[V];
     float sums[V];
@@ -517,6 +519,7 @@ __global__ void __launch_bounds__(kStreamThreads, 8)  // 8 CTAs per SM: 32 regis
         }
         u0[d] = un;
         if (DIAG && dg.w32) wsum = stream_norm_term(__ldg(dg.w32 + d), un, wsum);
+        else if (DIAG && dg.wdt2 != 0.f) wsum = stream_norm_term(__fdiv_rn(dg.wdt2, sm[dl]), un, wsum);
       }
     }
     if (DIAG) nacc += double(wsum);
@@ -632,14 +635,17 @@ __global__ void __launch_bounds__(kStreamThreads)
   const int t = threadIdx.x, G = gridDim.x;
   constexpr int V = kStreamDofs / kStreamThreads;
   double nacc = 0.0;
-  if (dg.w32)
+  if (dg.w32 || dg.wdt2 != 0.f)
     for (int c = blockIdx.x; c < n_chunks; c += G) {
       const StreamChunk ch = chunks[c];
       float wsum = 0.f;
 #pragma unroll
       for (int v = 0; v < V; v++) {
         const int d = ch.d0 + v * kStreamThreads + t;
-        if (d < ch.d1) wsum = stream_norm_term(__ldg(dg.w32 + d), __ldg(u + d), wsum);
+        if (d < ch.d1) {
+          const float w = dg.w32 ? __ldg(dg.w32 + d) : __fdiv_rn(dg.wdt2, __ldg(dg.m + d));
+          wsum = stream_norm_term(w, __ldg(u + d), wsum);
+        }
       }
       nacc += double(wsum);
     }

@@ -870,6 +870,7 @@ int mj_lf_create(mj_op* op, const mj_lf_desc* desc, mj_lf** out) {
       std::vector<float> w32(desc->norm_weight, desc->norm_weight + n);
       MJ_CUDA(lf->norm_w32.alloc(sizeof(float) * n));
       MJ_CUDA(cudaMemcpy(lf->norm_w32.ptr, w32.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+      lf->norm_is_mass = std::equal(desc->norm_weight, desc->norm_weight + n, desc->mass);
     }
   }
   lf->n_rec = desc->n_rec;
@@ -1115,7 +1116,11 @@ void lf_step_launch(mj_lf* lf, void* cur, const void* next, int qc, cudaStream_t
 // The StreamDiag of a step whose new iterate goes to column where.col + col.
 StreamDiag lf_stream_diag(mj_lf* lf, const DiagDev* dd, DiagDev direct, int col) {
   StreamDiag g = {};
-  g.w32 = lf->norm_w32.as<float>();
+  // norm weights equal to the mass (no density): dt^2 / (dt^2/D) from the staged dt^2/D, no weight stream
+  const bool from_m = lf->norm_is_mass && lf->norm_w32.ptr;
+  g.w32 = from_m ? nullptr : lf->norm_w32.as<float>();
+  g.m = lf->minv.as<float>();
+  g.wdt2 = from_m ? (float)(lf->dt * lf->dt) : 0.f;
   g.partial = lf->stream_partial.as<double>();
   g.done = lf->diag_done.as<unsigned>();
   g.flag = lf->flag.as<int>();
