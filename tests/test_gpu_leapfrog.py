@@ -201,3 +201,27 @@ def test_fp32_streaming_gather_equals_two_kernels(case):
     assert np.array_equal(ua, ub) and np.array_equal(va, vb)
     assert np.abs(ua).max() > 0
     a.close(); b.close(); op1.close(); op2.close()
+
+
+def test_fp32_norm_with_weights_equal_to_the_mass():
+    """The fused FP32 norm takes norm weights equal to the mass from the
+    dt^2/D it stages (dt^2 / (dt^2/D)), other weights from their own FP32
+    array: both agree with the FP64 plain form's norm to 1e-6, and with each
+    other to the FP32 rounding of the weights."""
+    from montjoie_gb300.leapfrog import LeapFrogIterator
+    from montjoie_gb300.operator import FemMatrixFreeOperator
+    g = load_golden("cube4_q4")
+    n = g["massD"].size
+    mass = g["massD"]
+    other = mass.copy()
+    other[n // 2] = np.nextafter(other[n // 2], np.inf)  # not equal to the mass: its own weight array
+    norms = {}
+    for name, precision, w in (("fp64", "fp64", mass), ("from_mass", "fp32", mass), ("own", "fp32", other)):
+        op = FemMatrixFreeOperator(int(g["order"]), g["nodle"], g["bh"], n, precision, gradphi=g["gradphi"])
+        lf = LeapFrogIterator(op, float(g["dt"]), mass, g["invD"], g["src_idx"], g["src_val"], g["pulse"], w)
+        _, norms[name], _ = lf.Run(np.zeros(n), None, 120)
+        lf.close()
+        op.close()
+    ref = norms["fp64"]
+    assert rel_l2(norms["from_mass"], ref) < 1e-6 and rel_l2(norms["own"], ref) < 1e-6
+    assert rel_l2(norms["from_mass"], norms["own"]) < 1e-6
