@@ -338,6 +338,14 @@ int mj_lfb_set_fused(mj_lfb* b, int enable);
  * (candidate_ms: room for 16, may be NULL). */
 int mj_lfb_step_info(const mj_lfb* b, int* fused, int* threads, int* grid, int* n_candidates, double* candidate_ms);
 
+/* Forces the one-kernel step's variant instead of the timed choice:
+ * tile_elems elements per tile; lanes thread lanes per z-line of an element
+ * (lanes x sources_per_thread right-hand sides per pass); sources_per_thread
+ * right-hand sides held by each thread.  Every variant gives the same states
+ * bit for bit.  MJ_ERR_ARG when no such variant exists for the order or the
+ * number of right-hand sides. */
+int mj_lfb_set_step_variant(mj_lfb* b, int tile_elems, int lanes, int sources_per_thread);
+
 /* Profiling aid for the one-kernel step: with enable != 0 every step is a
  * plain launch recording per-CTA time stamps; mj_lfb_phase_ms then returns,
  * for the last step, out[0] = element phase (last CTA), out[1] = element phase

@@ -141,6 +141,7 @@ def load(build_if_missing: bool = True):
     L.mj_lfb_profile.argtypes = [_VP, ctypes.c_int]
     L.mj_lfb_phase_ms.argtypes = [_VP, _D]
     L.mj_lfb_step_info.argtypes = [_VP] + [ctypes.POINTER(ctypes.c_int)] * 4 + [_D]
+    L.mj_lfb_set_step_variant.argtypes = [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     L.mj_mb_create.argtypes = [ctypes.c_int, ctypes.POINTER(_VP), ctypes.POINTER(_VP)]
     L.mj_mb_destroy.argtypes = [_VP]
     L.mj_mb_advance.argtypes = [_VP, ctypes.c_int, ctypes.c_int]

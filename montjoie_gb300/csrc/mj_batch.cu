@@ -566,6 +566,11 @@ int mj_lfb_set_fused(mj_lfb* b, int enable) {
   return MJ_OK;
 }
 
+int mj_lfb_set_step_variant(mj_lfb* b, int tile_elems, int lanes, int sources_per_thread) {
+  MJ_CHECK_ARG(b, "mj_lfb_set_step_variant: null integrator");
+  return lfb_set_step_variant(b, tile_elems, lanes, sources_per_thread);
+}
+
 int mj_lfb_profile(mj_lfb* b, int enable) {
   MJ_CHECK_ARG(b, "mj_lfb_profile: null integrator");
   b->rs_profile = enable != 0;

@@ -208,6 +208,7 @@ int lfb_phase_ms(const mj_lfb* b, double* out);
 int lfb_fused_step_on(mj_lfb* b, float* u0, float* u1, float* out, bool sources, cudaStream_t s);
 int lfb_fused_step(mj_lfb* b, cudaStream_t s);
 int lfb_fused_check(mj_lfb* b, cudaStream_t s);
+int lfb_set_step_variant(mj_lfb* b, int E, int LB, int V);
 
 // One time step of a run with its own kernels (the ones mj_lf_advance
 // launches), on the given buffers (cur = U^n, overwritten by U^{n+2}; next =

@@ -693,6 +693,52 @@ int lfb_fused_setup(mj_lfb* b) {
   return MJ_OK;
 }
 
+// Forces the one-kernel step's variant (n of the operator, E, LB, V): its
+// chunk list and persistent grid as the creation-time timing would set them;
+// captured graphs of the previous variant are dropped.
+int lfb_set_step_variant(mj_lfb* b, int E, int LB, int V) {
+  mj_op* op = b->op;
+  const std::vector<RsVariant>& all = rs_variants();
+  int c = -1;
+  for (size_t k = 0; k < all.size(); k++)
+    if (all[k].n == op->n && all[k].E == E && all[k].LB == LB && all[k].V == V) c = (int)k;
+  if (c < 0) {
+    set_error("mj_lfb_set_step_variant: no one-kernel step variant with these parameters for this order");
+    return MJ_ERR_ARG;
+  }
+  const RsVariant& v = all[c];
+  if (b->S % (v.LB * v.V) != 0) {
+    set_error("mj_lfb_set_step_variant: the number of right-hand sides is not a multiple of the variant's pass");
+    return MJ_ERR_ARG;
+  }
+  int ctas = 0;
+  if (int rc = rs_prepare(v, &ctas)) return rc;
+  std::vector<char> is_src(op->n_dof, 0);
+  if (b->n_src) {
+    std::vector<int> si(b->n_src);
+    MJ_CUDA(cudaMemcpy(si.data(), b->src_idx.ptr, sizeof(int) * b->n_src, cudaMemcpyDeviceToHost));
+    for (int d : si) is_src[d] = 1;
+  }
+  const std::vector<RsChunk> ch = rs_chunks(b, v.half, is_src);
+  if (ch.empty() || ctas < 1) {
+    set_error("mj_lfb_set_step_variant: the variant does not fit this integrator");
+    return MJ_ERR_ARG;
+  }
+  MJ_CUDA(b->rs_chunks.alloc(sizeof(RsChunk) * ch.size()));
+  MJ_CUDA(cudaMemcpy(b->rs_chunks.ptr, ch.data(), sizeof(RsChunk) * ch.size(), cudaMemcpyHostToDevice));
+  b->rs_variant = c;
+  b->rs_threads = v.threads;
+  b->rs_grid = ctas * sm_count();
+  b->rs_n_chunks = (int)ch.size();
+  for (auto& g : b->rs_graph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+  b->fused = true;
+  return MJ_OK;
+}
+
 // mj_lfb_advance with one cooperative kernel per step.  Without traces,
 // runs of 20 steps replay a CUDA graph captured for the current step parity.
 int lfb_fused_advance(mj_lfb* b, int nsteps, double* traces, int trace_stride, bool use_graph) {

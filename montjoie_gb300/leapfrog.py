@@ -234,6 +234,13 @@ class BatchLeapFrog:
         fused, threads, grid, nc = (v.value for v in vals)
         return {"one_kernel": bool(fused), "threads": threads, "grid": grid, "candidate_ms": ms[:nc].tolist()}
 
+    def set_step_variant(self, tile_elems: int, lanes: int, sources_per_thread: int) -> None:
+        """Forces the one-kernel step's variant: tile_elems elements per tile,
+        lanes thread lanes per z-line and sources_per_thread right-hand sides
+        per thread; every variant gives the same states bit for bit."""
+        _lib.check(_lib.load().mj_lfb_set_step_variant(self._h, int(tile_elems), int(lanes),
+                                                       int(sources_per_thread)))
+
     @property
     def handle(self):
         return self._h

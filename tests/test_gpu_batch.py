@@ -109,6 +109,32 @@ def test_one_kernel_step_equals_two_kernel_step(case, S):
     b1.close(); b2.close(); op1.close(); op2.close()
 
 
+# every one-kernel step variant of order 4 (n = 5): (elements per tile, lanes
+# per z-line, sources per thread)
+Q4_STEP_VARIANTS = [(1, 4, 4), (1, 8, 4), (2, 4, 4), (1, 8, 2), (2, 2, 4)]
+
+
+@pytest.mark.parametrize("variant", Q4_STEP_VARIANTS)
+def test_every_q4_step_variant_equals_two_kernel_step(variant):
+    """Each one-kernel step variant of order 4, forced, against the two-kernel
+    step: bitwise the same states (the element products' operation order does
+    not depend on how threads and lanes are laid out)."""
+    g = load_golden("cube4_q4")
+    S = 32
+    op1, b1 = _batch(g, S)
+    op2, b2 = _batch(g, S)
+    b1.set_step_variant(*variant)
+    b2.set_fused(False)
+    b1.init(); b2.init()
+    for k, gr in ((3, False), (40, True), (5, False)):
+        b1.advance(k, graph=gr)
+        b2.advance(k, graph=gr)
+    u1, v1 = b1.state()
+    u2, v2 = b2.state()
+    assert np.array_equal(u1, u2) and np.array_equal(v1, v2)
+    b1.close(); b2.close(); op1.close(); op2.close()
+
+
 def test_one_kernel_step_traces_match_two_kernel_step():
     from montjoie_gb300.problem import receiver_weights
     g = load_golden("cube3_q4")
