@@ -513,7 +513,9 @@ int mj_adj_backward(mj_adj* a, const double* residual, const double* coef, doubl
  * (the role of MeshNumbering/NumberMap, MONTJOIE/src/Mesh/NumberMap.cxx).
  * hexes: n_elt x 8 vertex indices in reference-cube order; nodle_out:
  * n_elt x (r+1)^3 in reference local order.  Dofs are numbered in the order
- * elements first touch them.  *n_dof receives the count. */
+ * elements first touch them, each edge's, face's and element interior's
+ * interior nodes as one block when the entity is first met.  *n_dof
+ * receives the count. */
 int mj_number_hex_mesh(int order, int n_elt, int n_vert, const int32_t* hexes, int32_t* nodle_out,
                        int* n_dof);
 

@@ -306,7 +306,8 @@ int mj_number_hex_mesh(int order, int n_elt, int n_vert, const int32_t* hexes, i
     for (int j = 0; j < n; j++)
       for (int i = 0; i < n; i++) {
         const int cc[3] = {i, j, k};
-        NodeDesc nd{num[(i * n + j) * n + k], 3, 0, 0, 0, 0};
+        // interior: b = (i-1) + m((j-1) + m(k-1)), the node's place in the element's interior block
+        NodeDesc nd{num[(i * n + j) * n + k], 3, 0, (i - 1) + (r - 1) * ((j - 1) + (r - 1) * (k - 1)), 0, 0};
         int nb = 0;
         for (int d = 0; d < 3; d++) nb += (cc[d] == 0 || cc[d] == r);
         if (nb == 3) {
@@ -331,6 +332,14 @@ int mj_number_hex_mesh(int order, int n_elt, int n_vert, const int32_t* hexes, i
   auto fresh = [&](int& id) {
     if (id < 0) id = (int)next++;
     return id;
+  };
+  // an edge's or a face's interior nodes take consecutive ids, in their
+  // canonical order, when the entity is first met; so does an element's
+  // interior (every entity's dofs form one block: the gathers of an
+  // element's u touch fewer sectors)
+  auto fresh_block = [&](std::vector<int>& pool, int64_t base, int width) {
+    if (pool[base] < 0)
+      for (int t = 0; t < width; t++) pool[base + t] = (int)next++;
   };
   for (int e = 0; e < n_elt; e++) {
     const int32_t* hv = hexes + 8LL * e;
@@ -384,20 +393,34 @@ int mj_number_hex_mesh(int order, int n_elt, int n_vert, const int32_t* hexes, i
         }
     }
     int32_t* out = nodle_out + (size_t)e * Q;
+    long long ibase = -1;  // first id of this element's interior block
     for (const NodeDesc& nd : nodes) {
       int dof;
       switch (nd.kind) {
         case 0: dof = fresh(vdof[hv[nd.a]]); break;
-        case 1: dof = fresh(epool[ebase[nd.a][nd.b][nd.c] + (efwd[nd.a][nd.b][nd.c] ? nd.l : r - nd.l) - 1]); break;
+        case 1: {
+          const int64_t base = ebase[nd.a][nd.b][nd.c];
+          fresh_block(epool, base, m);
+          dof = epool[base + (efwd[nd.a][nd.b][nd.c] ? nd.l : r - nd.l) - 1];
+          break;
+        }
         case 2: {
           int p = nd.c, q = nd.l;
           if (fos[nd.a][nd.b]) p = r - p;
           if (foq[nd.a][nd.b]) q = r - q;
           const int u = fswap[nd.a][nd.b] ? q : p, v = fswap[nd.a][nd.b] ? p : q;
-          dof = fresh(fpool[fbase[nd.a][nd.b] + (u - 1) * m + (v - 1)]);
+          const int64_t base = fbase[nd.a][nd.b];
+          fresh_block(fpool, base, m * m);
+          dof = fpool[base + (u - 1) * m + (v - 1)];
           break;
         }
-        default: dof = (int)next++;
+        default: {  // interior node: its place nd.b in the element's interior block
+          if (ibase < 0) {
+            ibase = next;
+            next += (long long)m * m * m;
+          }
+          dof = (int)(ibase + nd.b);
+        }
       }
       if (next > INT32_MAX) {
         set_error("mj_number_hex_mesh: too many dofs for int32");
