@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libmontjoie_gb300.so")
 SOURCES = ["mj_op.cu", "mj_k1_f64.cu", "mj_k1_f32.cu", "mj_k1_fs.cu", "mj_setup.cu", "mj_batch.cu", "mj_static.cu",
-           "mj_multi.cu", "mj_multi_one.cu", "mj_rhs_step.cu"]
+           "mj_multi.cu", "mj_multi_one.cu", "mj_rhs_step.cu", "mj_rhs_step_en.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include"), "-I", CSRC]

@@ -733,18 +733,45 @@ struct RevolvePlanner {
   }
 };
 
-// Adjoint step m = k + 1 with U^k in `uk`: lambda^m from lambda^{m+1},
-// lambda^{m+2} and the residual of column m, then the gradient term
-// lambda^m^T A_e U^k (one kernel each).
-int adj_visit(mj_adj* a, const float* uk, int m, float*& lam1, float*& lam2, cudaStream_t s) {
+// The gradient of the misfit in the element coefficients is the sum over
+// n = 2 .. N of coef_e (A_e lambda^n)^T U^{n-1} (lambda^{N+1} = 0 and
+// U^0 = 0 add nothing).  Term n is taken where A_e lambda^n is computed
+// anyway: in adjoint step n - 1, from U^{n-1} (adj_visit with um), except the
+// last term of a run of steps, which adj_term adds.  Every schedule adds the
+// terms in the order n = N, N-1, ..., 2, each with the same FP32 sums, so all
+// give the same bits.
+
+// ENERGY kernel: gacc[e] += coef[e] * (A_e x)^T u.
+void adj_term(mj_adj* a, const float* x, const float* u, cudaStream_t s) {
+  mj_lfb* b = a->b;
+  mj_op* op = b->op;
+  energy_launch(op->n, b->E, b->L, a->energy_grid, x, op->nodle_e.as<int>(), op->fac_e.as<float>(), b->n_tiles, b->S,
+                op->err.as<int>(), u, a->grad.as<double>(), a->coef.as<double>(), s);
+  count_launch();
+}
+
+// Adjoint step m: lambda^m from lambda^{m+1}, lambda^{m+2} and the residual
+// of column m.  With um = U^m (m < N), also the gradient term n = m + 1,
+// coef_e (A_e lambda^{m+1})^T U^m: inside the one-kernel step (its EN form)
+// or by the ENERGY kernel.
+int adj_visit(mj_adj* a, const float* um, int m, float*& lam1, float*& lam2, cudaStream_t s) {
   mj_lfb* b = a->b;
   mj_op* op = b->op;
   const int S = b->S, N = a->N;
   if (b->fused) {  // lambda^m = 2 lambda^{m+1} - lambda^{m+2} + m (-A lambda^{m+1}), one kernel
-    const int rc = lfb_fused_step_on(b, lam2, lam1, lam2, false, s);
-    if (rc) return rc;
+    bool done = false;
+    if (um) {
+      const int rc = lfb_fused_step_en(b, lam2, lam1, lam2, um, a->grad.as<double>(), a->coef.as<double>(), s, &done);
+      if (rc) return rc;
+    }
+    if (!done) {
+      if (um) adj_term(a, lam1, um, s);
+      const int rc = lfb_fused_step_on(b, lam2, lam1, lam2, false, s);
+      if (rc) return rc;
+    }
   } else {
     lfb_k1(b, lam1, s);
+    if (um) adj_term(a, lam1, um, s);
     const long long total = (long long)a->rows;
     k_gather_leapfrog_rhs<<<grid_for(total), 256, 0, s>>>(b->R.as<float>(), op->ptr.as<int>(), nullptr, 0, lam2,
                                                           lam1, lam2, b->m.as<float>(), b->n_dof, S);
@@ -756,9 +783,6 @@ int adj_visit(mj_adj* a, const float* uk, int m, float*& lam1, float*& lam2, cud
                                           S);
   count_launch();
   std::swap(lam1, lam2);  // lam1 = lambda^m, lam2 = lambda^{m+1}
-  energy_launch(op->n, b->E, b->L, a->energy_grid, uk, op->nodle_e.as<int>(), op->fac_e.as<float>(), b->n_tiles, S,
-                op->err.as<int>(), lam1, a->grad.as<double>(), a->coef.as<double>(), s);
-  count_launch();
   MJ_CUDA(cudaGetLastError());
   return MJ_OK;
 }
@@ -1059,11 +1083,13 @@ int mj_adj_backward(mj_adj* a, const double* residual, const double* coef, doubl
       } else if (x.kind == RevAction::STORE) {
         MJ_CUDA(cudaMemcpyAsync(sl + (size_t)x.slot * 2 * rows, w[0], bytes, cudaMemcpyDeviceToDevice, s));
         MJ_CUDA(cudaMemcpyAsync(sl + (size_t)x.slot * 2 * rows + rows, w[1], bytes, cudaMemcpyDeviceToDevice, s));
-      } else {  // VISIT x_k: adjoint step m = k + 1 with U^k
-        const int rc = adj_visit(a, w[0], x.step + 1, lam1, lam2, s);
+      } else {  // VISIT x_k: adjoint step m = k + 1, U^m in w[1]
+        const int m = x.step + 1;
+        const int rc = adj_visit(a, m < N ? w[1] : nullptr, m, lam1, lam2, s);
         if (rc) return rc;
       }
     }
+    adj_term(a, lam1, w[0], s);  // n = 2: lambda^2 and U^1 (the last visit is x_1)
   }
   float* seg = a->seg.as<float>();
   const float* ck = a->ckpt.as<float>();
@@ -1081,11 +1107,15 @@ int mj_adj_backward(mj_adj* a, const double* residual, const double* coef, doubl
                                 seg + (size_t)(n + 2 - n0) * rows, n, s);
       if (rc) return rc;
     }
-    // adjoint steps m = n1 .. max(n0+1, 2), then the gradient term with U^{m-1}
-    for (int m = n1; m >= std::max(n0 + 1, 2); m--) {
-      const int rc = adj_visit(a, seg + (size_t)(m - 1 - n0) * rows, m, lam1, lam2, s);
+    // adjoint steps m = n1 .. lo with the gradient terms n = n1 .. lo + 1
+    // (U^{n1} was the next segment's first state: its term n1 + 1 is done),
+    // then the term n = lo with lambda^lo and U^{lo-1}
+    const int lo = std::max(n0 + 1, 2);
+    for (int m = n1; m >= lo; m--) {
+      const int rc = adj_visit(a, m < n1 ? seg + (size_t)(m - n0) * rows : nullptr, m, lam1, lam2, s);
       if (rc) return rc;
     }
+    adj_term(a, lam1, seg + (size_t)(lo - 1 - n0) * rows, s);
   }
   if (b->fused) {
     const int rc = lfb_fused_check(b, s);

@@ -119,6 +119,7 @@ struct mj_lfb {
   int rs_variant = -1, rs_grid = 0, rs_threads = 0, rs_n_chunks = 0;
   mj::DevBuf rs_chunks, rs_src_dof, rs_src_ptr, rs_src_rhs, rs_src_val, rs_sync, rs_err;
   int rs_n_src_dof = 0;
+  int rs_en_variant = -1, rs_en_grid = 0;  // the step's EN form (adjoint gradient term): for which variant, its grid
   cudaGraphExec_t rs_graph[2] = {nullptr, nullptr};
   std::vector<double> rs_tune_ms;
   std::vector<int> rs_tune_variant;
@@ -207,6 +208,8 @@ void lfb_receivers(mj_lfb* b, const float* u, int stride, int col, cudaStream_t 
 int lfb_phase_ms(const mj_lfb* b, double* out);
 int lfb_fused_step_on(mj_lfb* b, float* u0, float* u1, float* out, bool sources, cudaStream_t s);
 int lfb_fused_step(mj_lfb* b, cudaStream_t s);
+int lfb_fused_step_en(mj_lfb* b, float* u0, float* u1, float* out, const float* ue, double* gacc,
+                      const double* gcoef, cudaStream_t s, bool* done);
 int lfb_fused_check(mj_lfb* b, cudaStream_t s);
 int lfb_set_step_variant(mj_lfb* b, int E, int LB, int V);
 

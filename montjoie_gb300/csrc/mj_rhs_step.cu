@@ -24,119 +24,12 @@
 #include <memory>
 #include <vector>
 
-#include "mj_internal.cuh"
-#include "mj_k1.cuh"
-#include "mj_sync.cuh"
+#include "mj_rhs_step.cuh"
 
 namespace mj {
 namespace {
 
 constexpr int kGraphStepsRs = 20;
-
-template <int V>
-__device__ __forceinline__ void vload(const float* p, float (&r)[V]) {
-  if constexpr (V == 4) {
-    const float4 q = *reinterpret_cast<const float4*>(p);
-    r[0] = q.x; r[1] = q.y; r[2] = q.z; r[3] = q.w;
-  } else if constexpr (V == 2) {
-    const float2 q = *reinterpret_cast<const float2*>(p);
-    r[0] = q.x; r[1] = q.y;
-  } else {
-    r[0] = *p;
-  }
-}
-
-template <int V>
-__device__ __forceinline__ void vload_g(const float* p, float (&r)[V]) {
-  if constexpr (V == 4) {
-    const float4 q = __ldg(reinterpret_cast<const float4*>(p));
-    r[0] = q.x; r[1] = q.y; r[2] = q.z; r[3] = q.w;
-  } else if constexpr (V == 2) {
-    const float2 q = __ldg(reinterpret_cast<const float2*>(p));
-    r[0] = q.x; r[1] = q.y;
-  } else {
-    r[0] = __ldg(p);
-  }
-}
-
-template <int V>
-__device__ __forceinline__ void vstore(float* p, const float (&r)[V]) {
-  if constexpr (V == 4) {
-    *reinterpret_cast<float4*>(p) = make_float4(r[0], r[1], r[2], r[3]);
-  } else if constexpr (V == 2) {
-    *reinterpret_cast<float2*>(p) = make_float2(r[0], r[1]);
-  } else {
-    *p = r[0];
-  }
-}
-
-// acc[v] = fma(c, x[v], acc[v]) for the V right-hand sides of a thread, two
-// at a time by the paired FP32 FMA of sm_100+ (__ffma2_rn: each lane rounds
-// as fmaf, so the results are those of V scalar FMAs with half the issued
-// instructions); mul: acc[v] = c * x[v].
-template <int V>
-__device__ __forceinline__ void fma_v(float (&acc)[V], float c, const float (&x)[V]) {
-  if constexpr (V % 2 == 0) {
-    const float2 c2 = make_float2(c, c);
-#pragma unroll
-    for (int v = 0; v < V; v += 2) {
-      const float2 r = __ffma2_rn(c2, make_float2(x[v], x[v + 1]), make_float2(acc[v], acc[v + 1]));
-      acc[v] = r.x;
-      acc[v + 1] = r.y;
-    }
-  } else {
-#pragma unroll
-    for (int v = 0; v < V; v++) acc[v] = fmaf(c, x[v], acc[v]);
-  }
-}
-template <int V>
-__device__ __forceinline__ void mul_v(float (&acc)[V], float c, const float (&x)[V]) {
-  if constexpr (V % 2 == 0) {
-    const float2 c2 = make_float2(c, c);
-#pragma unroll
-    for (int v = 0; v < V; v += 2) {
-      const float2 r = __fmul2_rn(c2, make_float2(x[v], x[v + 1]));
-      acc[v] = r.x;
-      acc[v + 1] = r.y;
-    }
-  } else {
-#pragma unroll
-    for (int v = 0; v < V; v++) acc[v] = c * x[v];
-  }
-}
-
-template <int N, int E, int LB, int V>
-struct RsPlan {
-  static constexpr int NN = N * N, Q = N * NN, Qp = elem_slots(N);
-  static constexpr int T = E * NN * LB;  // threads
-  static constexpr int W = LB * V;       // right-hand sides per pass
-  static constexpr int kStage = (E * Qp * 28 + 127) / 128 * 128;  // factors + Nodle of a tile
-  static constexpr int kWork = (E * Q * W + 3) / 4 * 4;            // floats per work array
-  static constexpr int kArea = 2 * kStage + 3 * kWork * 4;
-  static constexpr int kSmem = kArea + 32;                         // + 4 mbarriers
-  static constexpr int kHalf = kArea / 2 / 16 * 16;                // one phase-2 chunk buffer
-  static_assert(kArea % 16 == 0, "mbarriers and buffers are aligned");
-};
-
-struct RsParams {
-  const float* fac_e;
-  const int* nodle_e;
-  const int* slot_e;
-  float* R;           // [slot][S]
-  const int* ptr;     // CSR offsets (padded)
-  float* ua;
-  float* ub;
-  const float* m;     // dt^2 / D (padded)
-  const double* pulse;
-  int* ctr;
-  const int* src_dof;  // dofs carrying sources, sorted
-  const int* src_ptr;  // their entries [src_ptr[i], src_ptr[i+1]) in
-  const int* src_rhs;  //   (right-hand side, value) pairs
-  const float* src_val;
-  float* uout;         // where U^{n+2} goes (nullptr: over U^n)
-  int n_src_dof, n_pulse, S, n_tiles;
-  unsigned char zmap[kMaxNK * kMaxNK];  // z-line (j*n + i) of each thread slot of an element (rs_zline_order)
-};
 
 // Order in which the threads of an element take its n*n z-lines.  A warp
 // holds Z = 32/LB consecutive slots; each of its shared-memory line reads
@@ -192,277 +85,7 @@ void rs_zline_order(int n, int E, int LB, unsigned char* out) {
   for (int q = 0; q < NN; q++) out[q] = (unsigned char)cands[best][q];
 }
 
-// Phase-2 work: dofs [d0, d1), contributions R rows [q0, q1).
-struct RsChunk {
-  int d0, d1, q0, q1, has_src, pad0, pad1, pad2;
-};
 
-// Byte layout of a phase-2 buffer for a chunk (all offsets 16-byte aligned):
-// u^{n+1} rows | u^n rows | R rows | dt^2/D from d0&~3 | offsets from d0&~3.
-struct RsBuf {
-  int u1, u0, r, m, p, end;
-};
-__host__ __device__ __forceinline__ RsBuf rs_buf(int d0, int d1, int q0, int q1, int S) {
-  RsBuf b;
-  const int D = d1 - d0, da = d0 & ~3;
-  b.u1 = 0;
-  b.u0 = D * S * 4;
-  b.r = 2 * D * S * 4;
-  b.m = b.r + (q1 - q0) * S * 4;
-  b.p = b.m + (((d1 + 3) & ~3) - da) * 4;
-  b.end = b.p + (((d1 + 1 + 3) & ~3) - da) * 4;
-  return b;
-}
-
-// CTAs per SM the register allocation aims at (smaller CTAs: more of them)
-__host__ __device__ constexpr int rs_min_ctas(int T) { return T <= 128 ? 4 : T <= 216 ? 3 : 1; }
-
-template <int N, int E, int LB, int V>
-__global__ void __launch_bounds__(RsPlan<N, E, LB, V>::T, rs_min_ctas(RsPlan<N, E, LB, V>::T))
-    k_rhs_step(const RsParams p, const RsChunk* __restrict__ chunks, int n_chunks, SyncState* sync, int par,
-               int* err, unsigned long long* __restrict__ stamps) {
-  using P = RsPlan<N, E, LB, V>;
-  constexpr int NN = P::NN, Q = P::Q, Qp = P::Qp, W = P::W;
-  extern __shared__ __align__(128) unsigned char smem[];
-  float* s_u = reinterpret_cast<float*>(smem + 2 * P::kStage);
-  float* s_vx = s_u + P::kWork;
-  float* s_vy = s_vx + P::kWork;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + P::kArea);
-  const int t = threadIdx.x, G = gridDim.x, S = p.S;
-  const int lb = t % LB;
-  const int w = t / LB;
-  const int el = w / NN;
-  const int ij = p.zmap[w - el * NN];  // this thread's z-line (i, j)
-  const int j = ij / N;
-  const int i = ij - j * N;
-  float* __restrict__ cur = par == 0 ? p.ua : p.ub;        // U^n, overwritten by U^{n+2}
-  const float* __restrict__ nxt = par == 0 ? p.ub : p.ua;  // U^{n+1}
-  // step counters: ctr[1-par] = ctr[par] + 1 (phase 2 reads ctr[par] only)
-  if (blockIdx.x == 0 && t == 0) p.ctr[1 - par] = p.ctr[par] + 1;
-  // optional phase time stamps of this CTA: start, phase 1 done, barrier passed, end
-  if (stamps && t == 0) stamps[4 * blockIdx.x] = global_ns();
-
-  const float* __restrict__ Gm = c_gmat32[N];
-  float gci[N], gcj[N], gri[N], grj[N];
-#pragma unroll
-  for (int a = 0; a < N; a++) {
-    gci[a] = Gm[a * N + i];
-    gcj[a] = Gm[a * N + j];
-    gri[a] = Gm[i * N + a];
-    grj[a] = Gm[j * N + a];
-  }
-  // work-array offset of point q of this thread's element and lane block
-  auto wix = [&](int q) { return ((el * Q + q) * LB + lb) * V; };
-
-  // ---- phase 1
-  auto issue = [&](int st, int tile) {
-    if (tile < p.n_tiles) {
-      unsigned char* dst = smem + st * P::kStage;
-      mbar_expect_tx(&bar[st], (uint32_t)(E * Qp * 28));
-      bulk_g2s(dst, p.fac_e + (size_t)tile * E * 6 * Qp, (uint32_t)(E * 6 * Qp * 4), &bar[st]);
-      bulk_g2s(dst + E * 6 * Qp * 4, p.nodle_e + (size_t)tile * E * Qp, (uint32_t)(E * Qp * 4), &bar[st]);
-    }
-  };
-  if (t == 0) {
-    for (int b = 0; b < 4; b++) mbar_init(&bar[b], 1);  // 0,1: tile stages; 2,3: chunk buffers
-    fence_mbar_init();
-    issue(0, blockIdx.x);
-    issue(1, blockIdx.x + G);
-  }
-  __syncthreads();
-  uint32_t ph = 0u;
-  for (int tile = blockIdx.x, it = 0; tile < p.n_tiles; tile += G, ++it) {
-    const int s = it & 1;
-    const bool ok = mbar_wait_bounded(&bar[s], (ph >> s) & 1u);
-    if (__syncthreads_or(!ok)) {
-      if (t == 0) {  // report; stage s and, if issued, stage s^1 may have copies in flight
-        atomicExch(err, 1);
-        mbar_wait_drain(&bar[s], (ph >> s) & 1u);
-        if (tile + G < p.n_tiles) mbar_wait_drain(&bar[s ^ 1], (ph >> (s ^ 1)) & 1u);
-      }
-      return;
-    }
-    ph ^= 1u << s;
-    const float* f = reinterpret_cast<const float*>(smem + s * P::kStage) + el * 6 * Qp + ij;
-    const int* nd = reinterpret_cast<const int*>(smem + s * P::kStage + E * 6 * Qp * 4) + el * Qp + ij;
-    int dofs[N];
-#pragma unroll
-    for (int k = 0; k < N; k++) dofs[k] = nd[k * NN];
-    const int* __restrict__ st = p.slot_e + ((size_t)tile * E + el) * Qp + ij;
-    for (int pass = 0; pass < S / W; pass++) {
-      const int col = pass * W + lb * V;
-      float u[N][V];
-#pragma unroll
-      for (int k = 0; k < N; k++) {
-        vload_g<V>(nxt + (size_t)dofs[k] * S + col, u[k]);
-        vstore<V>(s_u + wix(k * NN + ij), u[k]);
-      }
-      __syncthreads();
-      // the operation order of k_local_stiffness_rhs, written out as explicit
-      // FMAs so both forms round alike
-      float vz[N][V];
-#pragma unroll
-      for (int k = 0; k < N; k++) {
-        float gx[V], gy[V], gz[V];
-#pragma unroll
-        for (int v = 0; v < V; v++) gx[v] = gy[v] = gz[v] = 0.f;
-#pragma unroll
-        for (int a = 0; a < N; a++) {
-          float rx[V], ry[V];
-          vload<V>(s_u + wix(k * NN + j * N + a), rx);
-          vload<V>(s_u + wix(k * NN + a * N + i), ry);
-          fma_v<V>(gz, Gm[a * N + k], u[a]);
-          fma_v<V>(gx, gci[a], rx);
-          fma_v<V>(gy, gcj[a], ry);
-        }
-        const float* fk = f + k * NN;
-        const float bxx = fk[0], bxy = fk[Qp], bxz = fk[2 * Qp];
-        const float byy = fk[3 * Qp], byz = fk[4 * Qp], bzz = fk[5 * Qp];
-        float ox[V], oy[V];
-        mul_v<V>(ox, bxx, gx);
-        fma_v<V>(ox, bxy, gy);
-        fma_v<V>(ox, bxz, gz);
-        mul_v<V>(oy, bxy, gx);
-        fma_v<V>(oy, byy, gy);
-        fma_v<V>(oy, byz, gz);
-        mul_v<V>(vz[k], bxz, gx);
-        fma_v<V>(vz[k], byz, gy);
-        fma_v<V>(vz[k], bzz, gz);
-        vstore<V>(s_vx + wix(k * NN + ij), ox);
-        vstore<V>(s_vy + wix(k * NN + ij), oy);
-      }
-      __syncthreads();
-#pragma unroll
-      for (int k = 0; k < N; k++) {
-        float y[V];
-#pragma unroll
-        for (int v = 0; v < V; v++) y[v] = 0.f;
-#pragma unroll
-        for (int a = 0; a < N; a++) {
-          float rx[V], ry[V];
-          vload<V>(s_vx + wix(k * NN + j * N + a), rx);
-          vload<V>(s_vy + wix(k * NN + a * N + i), ry);
-          fma_v<V>(y, gri[a], rx);
-          fma_v<V>(y, grj[a], ry);
-          fma_v<V>(y, Gm[k * N + a], vz[a]);
-        }
-        vstore<V>(p.R + (size_t)__ldg(st + k * NN) * S + col, y);
-      }
-      __syncthreads();
-    }
-    if (t == 0) {
-      fence_proxy_async();
-      issue(s, tile + 2 * G);
-    }
-  }
-
-  fence_proxy_async_global();  // this thread's R stores before the bulk copies of phase 2
-  if (stamps && t == 0) stamps[4 * blockIdx.x + 1] = global_ns();
-  if (!grid_barrier(sync, err)) return;
-  if (stamps && t == 0) stamps[4 * blockIdx.x + 2] = global_ns();
-
-  // ---- phase 2
-  float* __restrict__ dst = p.uout ? p.uout : cur;
-  const int step = p.ctr[par];
-  const bool pulse_on = step < p.n_pulse;
-  const float pf = pulse_on ? (float)p.pulse[step] : 0.f;
-  const int S4 = S >> 2;
-  auto issue_chunk = [&](int c, int b) {
-    if (c >= n_chunks) return;
-    const RsChunk ch = chunks[c];
-    const RsBuf L = rs_buf(ch.d0, ch.d1, ch.q0, ch.q1, S);
-    unsigned char* dst = smem + b * P::kHalf;
-    const int da = ch.d0 & ~3;
-    mbar_expect_tx(&bar[2 + b], (uint32_t)L.end);
-    bulk_g2s(dst + L.u1, nxt + (size_t)ch.d0 * S, (uint32_t)(L.u0 - L.u1), &bar[2 + b]);
-    bulk_g2s(dst + L.u0, cur + (size_t)ch.d0 * S, (uint32_t)(L.r - L.u0), &bar[2 + b]);
-    bulk_g2s(dst + L.r, p.R + (size_t)ch.q0 * S, (uint32_t)(L.m - L.r), &bar[2 + b]);
-    bulk_g2s(dst + L.m, p.m + da, (uint32_t)(L.p - L.m), &bar[2 + b]);
-    bulk_g2s(dst + L.p, p.ptr + da, (uint32_t)(L.end - L.p), &bar[2 + b]);
-  };
-  if (t == 0) {
-    fence_proxy_async();         // phase-1 use of this shared memory is over
-    fence_proxy_async_global();  // every CTA's R stores (ordered by the barrier) before the copies
-    issue_chunk(blockIdx.x, 0);
-    issue_chunk(blockIdx.x + G, 1);
-  }
-  uint32_t ph2 = 0u;
-  for (int c = blockIdx.x, it = 0; c < n_chunks; c += G, ++it) {
-    const int b = it & 1;
-    const RsChunk ch = chunks[c];
-    const bool ok = mbar_wait_bounded(&bar[2 + b], (ph2 >> b) & 1u);
-    if (__syncthreads_or(!ok)) {
-      if (t == 0) {  // report; buffer b and, if issued, buffer b^1 may have copies in flight
-        atomicExch(err, 1);
-        mbar_wait_drain(&bar[2 + b], (ph2 >> b) & 1u);
-        if (c + G < n_chunks) mbar_wait_drain(&bar[2 + (b ^ 1)], (ph2 >> (b ^ 1)) & 1u);
-      }
-      return;
-    }
-    ph2 ^= 1u << b;
-    const unsigned char* buf = smem + b * P::kHalf;
-    const RsBuf L = rs_buf(ch.d0, ch.d1, ch.q0, ch.q1, S);
-    const float4* su1 = reinterpret_cast<const float4*>(buf + L.u1);
-    const float4* su0 = reinterpret_cast<const float4*>(buf + L.u0);
-    const float4* sR = reinterpret_cast<const float4*>(buf + L.r);
-    const float* sm = reinterpret_cast<const float*>(buf + L.m);
-    const int* sp = reinterpret_cast<const int*>(buf + L.p);
-    const int da = ch.d0 & ~3;
-    const int items = (ch.d1 - ch.d0) * S4;
-    for (int item = t; item < items; item += P::T) {
-      const int dl = item / S4;
-      const int c4 = item - dl * S4;
-      const int d = ch.d0 + dl;
-      float4 y = make_float4(0.f, 0.f, 0.f, 0.f);
-      const int qb = sp[d + 1 - da] - ch.q0;
-      for (int q = sp[d - da] - ch.q0; q < qb; q++) {
-        const float4 r = sR[q * S4 + c4];
-        y.x += r.x; y.y += r.y; y.z += r.z; y.w += r.w;
-      }
-      const float4 a1 = su1[dl * S4 + c4], a0 = su0[dl * S4 + c4];
-      const float md = sm[d - da];
-      float un[4];
-      un[0] = 2.f * a1.x - a0.x + md * (-y.x);
-      un[1] = 2.f * a1.y - a0.y + md * (-y.y);
-      un[2] = 2.f * a1.z - a0.z + md * (-y.z);
-      un[3] = 2.f * a1.w - a0.w + md * (-y.w);
-      if (ch.has_src && pulse_on) {
-        int lo = 0, hi = p.n_src_dof - 1;
-        while (lo < hi) {
-          const int mid = (lo + hi) >> 1;
-          if (__ldg(p.src_dof + mid) < d) lo = mid + 1;
-          else hi = mid;
-        }
-        if (__ldg(p.src_dof + lo) == d)
-          for (int e = __ldg(p.src_ptr + lo); e < __ldg(p.src_ptr + lo + 1); e++) {
-            const int r = __ldg(p.src_rhs + e);
-            if ((r >> 2) == c4) un[r & 3] += md * pf * __ldg(p.src_val + e);
-          }
-      }
-      *reinterpret_cast<float4*>(dst + (size_t)d * S + 4 * c4) = make_float4(un[0], un[1], un[2], un[3]);
-    }
-    __syncthreads();  // buffer b is free
-    if (t == 0) {
-      fence_proxy_async();
-      issue_chunk(c + 2 * G, b);
-    }
-  }
-  if (stamps) {
-    __syncthreads();
-    if (t == 0) stamps[4 * blockIdx.x + 3] = global_ns();
-  }
-}
-
-// ---- variants: (n, E, LB, V) per order -------------------------------------
-#define MJ_RS_VARIANTS(X)                                                                        \
-  X(2, 8, 4, 4) X(2, 4, 8, 4) X(2, 16, 2, 4)                                                     \
-  X(3, 4, 4, 4) X(3, 2, 8, 4) X(3, 8, 2, 4)                                                      \
-  X(4, 2, 4, 4) X(4, 1, 8, 4) X(4, 4, 2, 4)                                                      \
-  X(5, 1, 4, 4) X(5, 1, 8, 4) X(5, 2, 4, 4) X(5, 1, 8, 2) X(5, 2, 2, 4)                          \
-  X(6, 1, 4, 4) X(6, 1, 4, 2) X(6, 1, 8, 2)                                                      \
-  X(7, 1, 2, 4) X(7, 1, 4, 2) X(7, 1, 2, 2)                                                      \
-  X(8, 1, 2, 2) X(8, 1, 2, 4) X(8, 1, 4, 2)                                                      \
-  X(9, 1, 2, 2) X(9, 1, 1, 4) X(9, 1, 4, 2)
 
 struct RsVariant {
   int n, E, LB, V, threads, smem, half;
@@ -536,6 +159,9 @@ RsParams rs_params(mj_lfb* b, const RsVariant& v) {
   p.src_rhs = b->rs_src_rhs.as<int>();
   p.src_val = b->rs_src_val.as<float>();
   p.uout = nullptr;
+  p.ue = nullptr;
+  p.gacc = nullptr;
+  p.gcoef = nullptr;
   p.n_src_dof = b->rs_n_src_dof;
   p.n_pulse = b->n_pulse;
   p.S = b->S;
@@ -587,6 +213,7 @@ int lfb_fused_setup(mj_lfb* b) {
     float v[kMaxNK * kMaxNK];
     for (int a = 0; a < op->n * op->n; a++) v[a] = (float)op->gradphi[a];
     MJ_CUDA(cudaMemcpyToSymbol(c_gmat32, v, sizeof(float) * op->n * op->n, sizeof(float) * kMaxNK * kMaxNK * op->n));
+    if (int rc = rs_en_set_gmat(op->n, v)) return rc;
   }
   // sources grouped by dof: sorted (dof, rhs) pairs from the device copies
   std::vector<int> si(b->n_src), sr(b->n_src);
@@ -814,6 +441,37 @@ int lfb_fused_step_on(mj_lfb* b, float* u0, float* u1, float* out, bool sources,
   }
   return rs_launch(v, b->rs_grid, prm, b->rs_chunks.as<RsChunk>(), b->rs_n_chunks, b->rs_sync.as<SyncState>(), 0,
                    b->rs_err.as<int>(), s);
+}
+
+// lfb_fused_step_on without sources, in the EN form: also
+// gacc[e] += gcoef[e] * sum_s sum_q ue[dof_q][s] (A_e u1)_q.  *done = false,
+// with nothing launched, when the EN form of the step's variant does not fit
+// (its shared memory grows with S); the caller then runs the plain step and
+// the ENERGY kernel, which give the same bits.
+int lfb_fused_step_en(mj_lfb* b, float* u0, float* u1, float* out, const float* ue, double* gacc,
+                      const double* gcoef, cudaStream_t s, bool* done) {
+  *done = false;
+  const RsVariant& v = rs_variants()[b->rs_variant];
+  if (b->rs_en_variant != b->rs_variant) {
+    int ctas = 0;
+    if (int rc = rs_en_prepare(v.n, v.E, v.LB, v.V, b->S, &ctas)) return rc;
+    b->rs_en_variant = b->rs_variant;
+    b->rs_en_grid = ctas * sm_count();
+  }
+  if (b->rs_en_grid < 1) return MJ_OK;
+  RsParams prm = rs_params(b, v);
+  prm.ua = u0;
+  prm.ub = u1;
+  prm.uout = out;
+  prm.n_src_dof = 0;
+  prm.n_pulse = 0;
+  prm.ue = ue;
+  prm.gacc = gacc;
+  prm.gcoef = gcoef;
+  const int rc = rs_en_launch(v.n, v.E, v.LB, v.V, b->S, b->rs_en_grid, prm, b->rs_chunks.as<RsChunk>(),
+                              b->rs_n_chunks, b->rs_sync.as<SyncState>(), 0, b->rs_err.as<int>(), s);
+  *done = rc == MJ_OK;
+  return rc;
 }
 
 // Error flag of the one-kernel step (bounded waits), reset when set.
