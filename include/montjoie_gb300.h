@@ -503,7 +503,10 @@ int mj_adj_forward(mj_adj* a, double* traces);
  * to the traces is `residual` (same layout as traces, host).  Returns
  * grad[e] = coef[e] * sum_{n=1}^{nsteps-1} sum_s lambda^{n+1}_s^T A_e U^n_s
  * (A_e the element's stiffness as currently scaled), host arrays of n_elt.
- * With A_e = c_e^2 A_e^(1), coef[e] = -2 dt^2 / c_e gives dJ/dc_e. */
+ * With A_e = c_e^2 A_e^(1), coef[e] = -2 dt^2 / c_e gives dJ/dc_e.  Each
+ * term is evaluated as (A_e lambda^{n+1})^T U^n (A_e is symmetric) inside the
+ * adjoint step that computes A_e lambda^{n+1}, in one summation order
+ * whatever the step's variant or form and the checkpoint schedule. */
 int mj_adj_backward(mj_adj* a, const double* residual, const double* coef, double* grad);
 
 /* ---- setup helpers (geometry, numbering, mass) ------------------------ */
