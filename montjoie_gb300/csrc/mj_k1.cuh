@@ -182,6 +182,13 @@ __device__ __forceinline__ void load_line(const double* p, double (&r)[RW]) {
   }
 }
 
+// One row of the factor tensor applied to the gradient, (a, b, c) . (x, y, z),
+// in the one order every element kernel uses: fma(c, z, fma(b, y, a * x)).
+template <typename Real>
+__device__ __forceinline__ Real fac_dot(Real a, Real x, Real b, Real y, Real c, Real z) {
+  return fma(c, z, fma(b, y, a * x));
+}
+
 // Shared-memory plan of one element kernel: two stages of [factors | Nodle]
 // for a tile of E elements, work arrays, two mbarriers.  L = right-hand
 // sides handled per pass (1 for the single-RHS kernel).
@@ -329,9 +336,9 @@ __global__ void __launch_bounds__(E* N* N)
       const Real* fk = f + k * NN;
       const Real bxx = fk[0], bxy = fk[Qp], bxz = fk[2 * Qp];
       const Real byy = fk[3 * Qp], byz = fk[4 * Qp], bzz = fk[5 * Qp];
-      s_vx[lx + k * N * RW + i] = bxx * gx + bxy * gy + bxz * gz;
-      s_vy[ly + k * N * RW + j * YS] = bxy * gx + byy * gy + byz * gz;
-      vz[k] = bxz * gx + byz * gy + bzz * gz;
+      s_vx[lx + k * N * RW + i] = fac_dot(bxx, gx, bxy, gy, bxz, gz);
+      s_vy[ly + k * N * RW + j * YS] = fac_dot(bxy, gx, byy, gy, byz, gz);
+      vz[k] = fac_dot(bxz, gx, byz, gy, bzz, gz);
     }
     __syncthreads();
 
@@ -520,9 +527,9 @@ __global__ void __launch_bounds__(E* N* N)
       const Real* fk = f + k * NN;
       const Real bxx = fk[0], bxy = fk[Qp], bxz = fk[2 * Qp];
       const Real byy = fk[3 * Qp], byz = fk[4 * Qp], bzz = fk[5 * Qp];
-      s_vx[lx + k * NN + i] = bxx * gx + bxy * gy + bxz * gz;
-      s_vy[ly + k * NN + j * N] = bxy * gx + byy * gy + byz * gz;
-      vz[k] = bxz * gx + byz * gy + bzz * gz;
+      s_vx[lx + k * NN + i] = fac_dot(bxx, gx, bxy, gy, bxz, gz);
+      s_vy[ly + k * NN + j * N] = fac_dot(bxy, gx, byy, gy, byz, gz);
+      vz[k] = fac_dot(bxz, gx, byz, gy, bzz, gz);
     }
     __syncthreads();  // the factor stage and s_u are free
     if (t == 0) fence_proxy_async();
@@ -696,9 +703,9 @@ __global__ void __launch_bounds__(E * 32)
         const Real* fk = f + k * NN;
         const Real bxx = fk[0], bxy = fk[Qp], bxz = fk[2 * Qp];
         const Real byy = fk[3 * Qp], byz = fk[4 * Qp], bzz = fk[5 * Qp];
-        s_vx[lx + k * NN + i] = bxx * gx + bxy * gy + bxz * gz;
-        s_vy[ly + k * NN + j * N] = bxy * gx + byy * gy + byz * gz;
-        vz[k] = bxz * gx + byz * gy + bzz * gz;
+        s_vx[lx + k * NN + i] = fac_dot(bxx, gx, bxy, gy, bxz, gz);
+        s_vy[ly + k * NN + j * N] = fac_dot(bxy, gx, byy, gy, byz, gz);
+        vz[k] = fac_dot(bxz, gx, byz, gy, bzz, gz);
       }
     }
     __syncwarp();

@@ -220,9 +220,9 @@ __device__ __forceinline__ bool tile_run(float* R, const int* slot_e, int tile, 
       const float* fk = f + k * NN;
       const float bxx = fk[0], bxy = fk[Qp], bxz = fk[2 * Qp];
       const float byy = fk[3 * Qp], byz = fk[4 * Qp], bzz = fk[5 * Qp];
-      s_vx[lx + k * NN + i] = bxx * gx + bxy * gy + bxz * gz;
-      s_vy[ly + k * NN + j * N] = bxy * gx + byy * gy + byz * gz;
-      vz[k] = bxz * gx + byz * gy + bzz * gz;
+      s_vx[lx + k * NN + i] = fac_dot(bxx, gx, bxy, gy, bxz, gz);
+      s_vy[ly + k * NN + j * N] = fac_dot(bxy, gx, byy, gy, byz, gz);
+      vz[k] = fac_dot(bxz, gx, byz, gy, bzz, gz);
     }
   }
   __syncthreads();  // s_u is free: the next tile's u may land there
