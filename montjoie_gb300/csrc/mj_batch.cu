@@ -1011,7 +1011,8 @@ int mj_adj_forward(mj_adj* a, double* traces) {
       MJ_CUDA(cudaMemcpyAsync(dst, b->cur(), bytes, cudaMemcpyDeviceToDevice, s));
       MJ_CUDA(cudaMemcpyAsync(dst + a->rows, b->next(), bytes, cudaMemcpyDeviceToDevice, s));
     }
-    if (a->store_all)
+    // every state kept: U^0 and U^1 copied here, U^{n+2} (n + 2 < N) written by the one-kernel step itself
+    if (a->store_all && (n < 2 || !b->fused))
       MJ_CUDA(cudaMemcpyAsync(a->seg.as<float>() + (size_t)n * a->rows, b->cur(), bytes, cudaMemcpyDeviceToDevice,
                               s));
     if (a->revolve && n == a->N - 1) {  // x_{N-1}, the first state the backward sweep visits
@@ -1020,7 +1021,8 @@ int mj_adj_forward(mj_adj* a, double* traces) {
       MJ_CUDA(cudaMemcpyAsync(w + a->rows, b->next(), bytes, cudaMemcpyDeviceToDevice, s));
     }
     if (b->fused) {
-      const int rc = lfb_fused_step(b, s);
+      float* copy = a->store_all && n + 2 < a->N ? a->seg.as<float>() + (size_t)(n + 2) * a->rows : nullptr;
+      const int rc = lfb_fused_step(b, s, copy);
       if (rc) return rc;
     } else {
       lfb_step_launch(b, b->cur(), b->next(), b->step & 1, s);

@@ -207,7 +207,7 @@ int lfb_fused_advance(mj_lfb* b, int nsteps, double* traces, int trace_stride, b
 void lfb_receivers(mj_lfb* b, const float* u, int stride, int col, cudaStream_t s);
 int lfb_phase_ms(const mj_lfb* b, double* out);
 int lfb_fused_step_on(mj_lfb* b, float* u0, float* u1, float* out, bool sources, cudaStream_t s);
-int lfb_fused_step(mj_lfb* b, cudaStream_t s);
+int lfb_fused_step(mj_lfb* b, cudaStream_t s, float* copy = nullptr);
 int lfb_fused_step_en(mj_lfb* b, float* u0, float* u1, float* out, const float* ue, double* gacc,
                       const double* gcoef, cudaStream_t s, bool* done);
 int lfb_fused_check(mj_lfb* b, cudaStream_t s);

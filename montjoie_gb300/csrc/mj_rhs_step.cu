@@ -159,6 +159,7 @@ RsParams rs_params(mj_lfb* b, const RsVariant& v) {
   p.src_rhs = b->rs_src_rhs.as<int>();
   p.src_val = b->rs_src_val.as<float>();
   p.uout = nullptr;
+  p.ucopy = nullptr;
   p.ue = nullptr;
   p.gacc = nullptr;
   p.gcoef = nullptr;
@@ -478,10 +479,11 @@ int lfb_fused_step_en(mj_lfb* b, float* u0, float* u1, float* out, const float* 
 int lfb_fused_check(mj_lfb* b, cudaStream_t s) { return rs_check_err(b, s); }
 
 // One ordinary step of the one-kernel form (the integrator's own states and
-// step counter).
-int lfb_fused_step(mj_lfb* b, cudaStream_t s) {
+// step counter); copy: where a second copy of the new state goes, or nullptr.
+int lfb_fused_step(mj_lfb* b, cudaStream_t s, float* copy) {
   const RsVariant& v = rs_variants()[b->rs_variant];
-  const RsParams prm = rs_params(b, v);
+  RsParams prm = rs_params(b, v);
+  prm.ucopy = copy;
   return rs_launch(v, b->rs_grid, prm, b->rs_chunks.as<RsChunk>(), b->rs_n_chunks, b->rs_sync.as<SyncState>(),
                    b->step & 1, b->rs_err.as<int>(), s);
 }

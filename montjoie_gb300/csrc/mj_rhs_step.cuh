@@ -29,6 +29,7 @@ struct RsParams {
   const int* src_rhs;  //   (right-hand side, value) pairs
   const float* src_val;
   float* uout;         // where U^{n+2} goes (nullptr: over U^n)
+  float* ucopy;        // a second copy of U^{n+2} (a kept forward state of the adjoint), or nullptr
   // step with the gradient term (EN form): ue = U^m, one state of the
   // forward run; gacc[e] += gcoef[e] * sum_s sum_q ue[dof_q][s] (A_e U^{n+1})_q
   const float* ue;
@@ -432,7 +433,9 @@ __global__ void __launch_bounds__(RsPlan<N, E, LB, V>::T, rs_min_ctas(RsPlan<N, 
             if ((r >> 2) == c4) un[r & 3] += md * pf * __ldg(p.src_val + e);
           }
       }
-      *reinterpret_cast<float4*>(dst + (size_t)d * S + 4 * c4) = make_float4(un[0], un[1], un[2], un[3]);
+      const float4 o = make_float4(un[0], un[1], un[2], un[3]);
+      *reinterpret_cast<float4*>(dst + (size_t)d * S + 4 * c4) = o;
+      if (p.ucopy) *reinterpret_cast<float4*>(p.ucopy + (size_t)d * S + 4 * c4) = o;
     }
     __syncthreads();  // buffer b is free
     if (t == 0) {
