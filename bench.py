@@ -62,6 +62,9 @@ def parse():
     ap.add_argument("--k1-variant", default=None,
                     help="profiling aid with --fp32-only: force the element-kernel variant E,layout (the one the "
                          "autotuner picks unprofiled), since under a profiler its timings are distorted")
+    ap.add_argument("--e2e-only", action="store_true",
+                    help="profiling aid: only the FP32 set-up and the end-to-end run (diagnostics every step, "
+                         "--error-steps steps; no JSON line contract)")
     ap.add_argument("--leg", default="all", choices=["all", "q8", "sources", "meshes", "adjoint", "order4"],
                     help="profiling aid: run one extra leg alone (no JSON line contract)")
     return ap.parse_args()
@@ -631,6 +634,14 @@ def run_ours(args):
 
     # ---- FP32 chosen form, resident (value)
     op32 = pb.operator("fp32")
+    if args.e2e_only:
+        lfd = pb.integrator(op32, diagnostics=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, nd, _ = lfd.Run(zeros, None, args.error_steps)
+        print(json.dumps({"e2e_only": True, "steps": args.error_steps, "seconds": time.perf_counter() - t0,
+                          "last_norm": float(nd[-1])}))
+        return
     if args.k1_variant and args.fp32_only:
         e_, lay_ = (int(v) for v in args.k1_variant.split(","))
         op32.set_variant(e_, lay_)
