@@ -115,7 +115,8 @@ def test_mesh_batch_waits_run_out_and_next_advance_works(lowered_waits):
     from montjoie_gb300.leapfrog import MeshBatch
     runs = _batch_runs()
     mb = MeshBatch([lf for _, lf in runs])
-    mb.advance(25)  # tunes the launch configuration with the normal limits
+    mb.set_config(256)  # the one-kernel form, whose grid barrier the lowered limits make run out
+    mb.advance(25)
     u_ok = [lf.GetIterate() for _, lf in runs]
     for _, lf in runs:
         lf.SetInitialConditionS(np.zeros(lf.op.n_dof))
