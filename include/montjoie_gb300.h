@@ -284,7 +284,8 @@ typedef struct mj_lfb mj_lfb;
 
 typedef struct {
   double dt;                 /* time step */
-  int n_rhs;                 /* S independent runs (one per source), multiple of 8, <= 4096 */
+  int n_rhs;                 /* S independent runs (one per source), multiple of 8, <= 4096 (the Python
+                                BatchLeapFrog pads other counts with runs that have no source) */
   const double* mass;        /* lumped mass D (n_dof), host */
   const double* inv_mass;    /* 1/D (n_dof), host; NULL -> 1/D */
   int n_src;                 /* sparse sources: entry t adds pulse * src_val[t] at dof */

@@ -63,13 +63,15 @@ class AcousticAdjoint:
     def forward(self, c: np.ndarray) -> np.ndarray:
         """Traces (n_rec, S, N+1) of U^0..U^N for wave speed c."""
         self.set_speed(c)
-        tr = np.zeros((self.n_rec, self.S, self.N + 1))
+        S_dev = self.batch.S_dev  # runs padded to a multiple of 8 (no source, zero state)
+        tr = np.zeros((self.n_rec, S_dev, self.N + 1))
         _lib.check(_lib.load().mj_adj_forward(self._h, _lib.dptr(tr)))
-        return tr
+        return np.ascontiguousarray(tr[:, :self.S, :])
 
     def backward(self, residual: np.ndarray) -> np.ndarray:
         """dJ/dc for J with trace gradient `residual` (r - d), after forward()."""
-        res = np.ascontiguousarray(residual, dtype=np.float64).reshape(self.n_rec, self.S, self.N + 1)
+        res = np.zeros((self.n_rec, self.batch.S_dev, self.N + 1))  # padding runs: no residual
+        res[:, :self.S, :] = np.asarray(residual, dtype=np.float64).reshape(self.n_rec, self.S, self.N + 1)
         coef = -2.0 * self.dt * self.dt / self._c
         grad = np.zeros(self.n_elt)
         _lib.check(_lib.load().mj_adj_backward(self._h, _lib.dptr(res), _lib.dptr(coef), _lib.dptr(grad)))

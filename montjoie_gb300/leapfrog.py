@@ -152,12 +152,18 @@ class LeapFrogIterator:
 class BatchLeapFrog:
     """S leap-frog runs sharing one mesh and operator (FP32), each with its own
     sources and state: the reference's order-2 ModifiedEquationIterator run
-    S times, advanced together on the GPU (state n_dof x S, row-major)."""
+    S times, advanced together on the GPU (state n_dof x S, row-major).  The
+    C ABI takes S in multiples of 8; any other S >= 1 is padded to the next
+    multiple with runs that have no source and stay zero (``S_dev``), and
+    every array handed in or out has the caller's S."""
 
     def __init__(self, op: FemMatrixFreeOperator, dt: float, n_rhs: int, mass, inv_mass=None, src_idx=None,
                  src_rhs=None, src_val=None, pulse=None, rec_idx=None, rec_w=None):
         L = _lib.load()
         self.op, self.S, self.dt = op, int(n_rhs), float(dt)
+        if self.S < 1:
+            raise ValueError("at least one run")
+        self.S_dev = (self.S + 7) // 8 * 8
         n = op.n_dof
         keep = self._keep = []
 
@@ -180,39 +186,53 @@ class BatchLeapFrog:
         rec_idx, rec_w = i(rec_idx), f(rec_w)
         if mass.size != n:
             raise ValueError("mass size differs from the operator size")
+        if src_rhs is not None and src_rhs.size and (src_rhs.min() < 0 or src_rhs.max() >= self.S):
+            raise ValueError("source run index outside [0, n_rhs)")
         n_src = 0 if src_idx is None else int(src_idx.size)
         self.n_rec = 0 if rec_idx is None else int(rec_idx.shape[0])
         n_rec_w = 0 if rec_idx is None else int(rec_idx.shape[1])
-        desc = _lib.LfbDesc(self.dt, self.S, _lib.dptr(mass), _lib.dptr(inv_mass), n_src, _lib.iptr(src_idx),
+        desc = _lib.LfbDesc(self.dt, self.S_dev, _lib.dptr(mass), _lib.dptr(inv_mass), n_src, _lib.iptr(src_idx),
                             _lib.iptr(src_rhs), _lib.dptr(src_val), 0 if pulse is None else int(pulse.size),
                             _lib.dptr(pulse), self.n_rec, n_rec_w, _lib.iptr(rec_idx), _lib.dptr(rec_w))
         h = ctypes.c_void_p()
         _lib.check(L.mj_lfb_create(op.handle, ctypes.byref(desc), ctypes.byref(h)))
         self._h = h
 
-    def init(self, u0=None, du0=None) -> None:
+    def _pad(self, a):
+        """(n_dof, S) -> (n_dof, S_dev), the padding runs zero."""
         n = self.op.n_dof
-        u0 = None if u0 is None else np.ascontiguousarray(u0, dtype=np.float64).reshape(n, self.S)
-        du0 = None if du0 is None else np.ascontiguousarray(du0, dtype=np.float64).reshape(n, self.S)
+        a = np.asarray(a, dtype=np.float64).reshape(n, self.S)
+        if self.S_dev == self.S:
+            return np.ascontiguousarray(a)
+        out = np.zeros((n, self.S_dev))
+        out[:, :self.S] = a
+        return out
+
+    def init(self, u0=None, du0=None) -> None:
+        u0 = None if u0 is None else self._pad(u0)
+        du0 = None if du0 is None else self._pad(du0)
         _lib.check(_lib.load().mj_lfb_init(self._h, _lib.dptr(u0), _lib.dptr(du0)))
 
     def advance(self, nsteps: int, traces: bool = False, graph: bool = True):
         """Advances nsteps; with traces, returns the receiver values before each
         step as an (n_rec, S, nsteps) array."""
-        tr = np.zeros((self.n_rec, self.S, nsteps)) if (traces and self.n_rec) else None
+        tr = np.zeros((self.n_rec, self.S_dev, nsteps)) if (traces and self.n_rec) else None
         _lib.check(_lib.load().mj_lfb_advance(self._h, int(nsteps), _lib.dptr(tr), int(nsteps), int(bool(graph))))
-        return tr
+        return None if tr is None else np.ascontiguousarray(tr[:, :self.S, :])
 
     def state(self):
         n = self.op.n_dof
-        u, v = np.zeros((n, self.S)), np.zeros((n, self.S))
+        u, v = np.zeros((n, self.S_dev)), np.zeros((n, self.S_dev))
         _lib.check(_lib.load().mj_lfb_get_state(self._h, _lib.dptr(u), _lib.dptr(v)))
-        return u, v
+        return np.ascontiguousarray(u[:, :self.S]), np.ascontiguousarray(v[:, :self.S])
 
     def info(self):
+        """n_rhs: the caller's runs; n_rhs_device: the runs stepped (a multiple of 8)."""
         vals = [ctypes.c_int() for _ in range(5)]
         _lib.check(_lib.load().mj_lfb_info(self._h, *[ctypes.byref(v) for v in vals]))
-        return dict(zip(["n_rhs", "tile_elems", "lanes", "grid", "step"], [v.value for v in vals]))
+        out = dict(zip(["n_rhs_device", "tile_elems", "lanes", "grid", "step"], [v.value for v in vals]))
+        out["n_rhs"] = self.S
+        return out
 
     def set_fused(self, enable: bool) -> None:
         """One cooperative kernel per step (default) or two kernels per step."""
