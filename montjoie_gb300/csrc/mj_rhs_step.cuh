@@ -300,6 +300,14 @@ __global__ void __launch_bounds__(RsPlan<N, E, LB, V>::T, rs_min_ctas(RsPlan<N, 
       float ez[V];  // EN: this z-line's sums for sources col .. col+V-1
 #pragma unroll
       for (int v = 0; v < V; v++) ez[v] = 0.f;
+      // EN: this z-line's U^m values, loaded together before the loop (its R
+      // stores could alias them for the compiler, which would then issue each
+      // load only after the previous point's store)
+      float uev[EN ? N : 1][V];
+      if constexpr (EN) {
+#pragma unroll
+        for (int k = 0; k < N; k++) vload_g<V>(p.ue + (size_t)dofs[k] * S + col, uev[k]);
+      }
 #pragma unroll
       for (int k = 0; k < N; k++) {
         float y[V];
@@ -316,10 +324,8 @@ __global__ void __launch_bounds__(RsPlan<N, E, LB, V>::T, rs_min_ctas(RsPlan<N, 
         }
         vstore<V>(p.R + (size_t)__ldg(st + k * NN) * S + col, y);
         if constexpr (EN) {
-          float ue[V];
-          vload_g<V>(p.ue + (size_t)dofs[k] * S + col, ue);
 #pragma unroll
-          for (int v = 0; v < V; v++) ez[v] = fmaf(y[v], ue[v], ez[v]);
+          for (int v = 0; v < V; v++) ez[v] = fmaf(y[v], uev[k][v], ez[v]);
         }
       }
       if constexpr (EN) {
