@@ -775,9 +775,10 @@ __global__ void __launch_bounds__(E * 32)
 // The sum has one order whatever E and L, so every tuned variant gives the
 // same bits: each (source s, z-line q) sums its points in k order (FP32
 // FMAs) into shared memory (E*S*NN floats past the plan's bytes, see
-// k1_rhs_energy_smem); after the passes, lane l of warp el adds, in FP64, the
-// sources s = l, l+32, ... with their z-lines q = 0..NN-1 in order, and a
-// fixed shuffle tree adds the lanes.
+// k1_rhs_energy_smem); after the passes, lane l of warp el adds each source
+// s = l, l+32, ...: its z-lines q = 0..NN-1 in order in FP32 (FP64 adds on
+// the GB300's narrow FP64 pipe cost more than the element's other work),
+// then that sum into an FP64 accumulator; a fixed shuffle tree adds the lanes.
 // ---------------------------------------------------------------------------
 template <int N, int E, int L, bool ENERGY = false>
 __global__ void __launch_bounds__(E* N* N* L)
@@ -905,7 +906,9 @@ __global__ void __launch_bounds__(E* N* N* L)
         double acc = 0.0;
         for (int src = l32; src < S; src += 32) {
           const float* row = s_ez + ((size_t)w * S + src) * NN;
-          for (int q = 0; q < NN; q++) acc += (double)row[q];
+          float zs = 0.f;  // the element's z-lines of this source, in order, in FP32
+          for (int q = 0; q < NN; q++) zs += row[q];
+          acc += (double)zs;
         }
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
         if (l32 == 0) {

@@ -177,9 +177,10 @@ struct RsPlan {
 // of the ENERGY variant of k_local_stiffness_rhs run with x = U^{n+1} and
 // lam = ue, so both give the same bits: each (source s, z-line q) sums its
 // points in k order (FP32 FMAs) into shared memory (E*S*NN floats past the
-// plan's bytes); after a tile's passes, lane l of a warp adds, in FP64, the
-// sources s = l, l+32, ... with their z-lines q = 0..NN-1 in order, and a
-// fixed shuffle tree adds the lanes.  One CTA owns an element per launch.
+// plan's bytes); after a tile's passes, lane l of a warp adds each source
+// s = l, l+32, ...: its z-lines q = 0..NN-1 in order in FP32, then that sum
+// into an FP64 accumulator; a fixed shuffle tree adds the lanes.  One CTA owns
+// an element per launch.
 template <int N, int E, int LB, int V, bool EN = false>
 __global__ void __launch_bounds__(RsPlan<N, E, LB, V>::T, rs_min_ctas(RsPlan<N, E, LB, V>::T))
     k_rhs_step(const RsParams p, const RsChunk* __restrict__ chunks, int n_chunks, SyncState* sync, int par,
@@ -345,7 +346,9 @@ __global__ void __launch_bounds__(RsPlan<N, E, LB, V>::T, rs_min_ctas(RsPlan<N, 
           double acc = 0.0;
           for (int src = l32; src < S; src += 32) {
             const float* row = s_ez + ((size_t)e * S + src) * NN;
-            for (int q = 0; q < NN; q++) acc += (double)row[q];
+            float zs = 0.f;  // the element's z-lines of this source, in order, in FP32
+            for (int q = 0; q < NN; q++) zs += row[q];
+            acc += (double)zs;
           }
           for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
           if (l32 == 0) {
